@@ -1,0 +1,150 @@
+/*
+ * kinc_sim.h -- C ABI of the GB300 Similarity worker.
+ *
+ * This is the drop-in replacement for KINC's OpenCL Similarity worker: the
+ * object that turns one work block {start, size} of gene pairs into one
+ * result block {K, labels, correlations} per pair.  It replaces
+ *
+ *   Similarity::OpenCL::initialize(::OpenCL::Context*)     src/core/similarity_opencl.cpp:34-70
+ *   Similarity::OpenCL::makeWorker()                         src/core/similarity_opencl.cpp:24-27
+ *   Similarity::OpenCL::Worker::Worker(...)                  src/core/similarity_opencl_worker.cpp:50-86
+ *   Similarity::OpenCL::Worker::execute(const Block*)        src/core/similarity_opencl_worker.cpp:93-271
+ *
+ * and computes what Similarity::Serial::execute computes
+ * (src/core/similarity_serial.cpp:33-101) on the same inputs.
+ *
+ * Conventions: every call returns 0 on success and a non-zero KINC_SIM_E*
+ * code otherwise (no exceptions cross the ABI); kinc_sim_last_error() gives
+ * the message.  The context owns all device memory; callers own host
+ * buffers.  A context is used by one host thread at a time.
+ */
+#ifndef KINC_SIM_H
+#define KINC_SIM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KINC_SIM_OK 0
+#define KINC_SIM_EINVAL 1      /* invalid argument */
+#define KINC_SIM_ECUDA 2       /* CUDA runtime error */
+#define KINC_SIM_ENOMEM 3      /* device or host allocation failed */
+#define KINC_SIM_EKERNEL 4     /* a kernel reported an error status */
+#define KINC_SIM_EORDER 5      /* out-of-order write to a pairwise matrix */
+
+/* Work-block size the reference splits all pairs into (src/core/similarity.cpp:20). */
+#define KINC_SIM_WORK_BLOCK_SIZE 32768
+
+typedef struct kinc_sim_ctx kinc_sim_ctx;
+
+/*
+ * Analytic arguments: the Similarity CLI options (src/core/similarity_input.cpp:96-254)
+ * with the member defaults of src/core/similarity.h:58-71, plus three
+ * options of this implementation.
+ */
+typedef struct kinc_sim_params
+{
+   int32_t clus_method;   /* --clusmethod: 0 none, 1 gmm, 2 kmeans            (default 0) */
+   int32_t corr_method;   /* --corrmethod: 0 pearson, 1 spearman              (default 0) */
+   float   min_expr;      /* --minexpr                                        (default -inf) */
+   int32_t min_samples;   /* --minsamp, >= 1                                  (default 30) */
+   int32_t min_clusters;  /* --minclus, 1..64                                 (default 1) */
+   int32_t max_clusters;  /* --maxclus, 1..64                                 (default 5) */
+   int32_t criterion;     /* --crit: 0 BIC, 1 ICL                             (default 1) */
+   int32_t pre_out;       /* --preout                                         (default 0) */
+   int32_t post_out;      /* --postout                                        (default 0) */
+   float   min_corr;      /* --mincorr, 0..1                                  (default 0.5) */
+   float   max_corr;      /* --maxcorr, 0..1                                  (default 1) */
+   int32_t ksize;         /* --ksize: accepted for CLI compatibility; pairs per launch are chosen here */
+   int32_t semantics;     /* 0: the reference CPU path, including its packed-array indexing in
+                                Pearson/Spearman (default); 1: each sample's own values */
+   int32_t rand_mode;     /* 0: the process-global glibc rand() stream of a serial KINC run (default);
+                             1: the POSIX LCG reset per fit used by the OpenCL worker */
+   int32_t precision;     /* clusmethod none + pearson only: 0 per-pair FP32 (default), 1 TF32 tensor
+                             cores, 2 3xBF16 tensor cores (semantics 1 only) */
+} kinc_sim_params;
+
+/* Fill `p` with the reference defaults. */
+int kinc_sim_params_default(kinc_sim_params* p);
+
+/*
+ * Create a worker for an expression matrix `gem` (host, row-major [genes][samples]
+ * float32, NaN = missing), as Similarity::OpenCL::initialize uploads the EMX once.
+ */
+int kinc_sim_create(const float* gem, int32_t genes, int32_t samples, const kinc_sim_params* params,
+                    kinc_sim_ctx** out);
+
+void kinc_sim_destroy(kinc_sim_ctx* ctx);
+
+/* Message of the last failed call on `ctx` (or of the last failed kinc_sim_create if ctx is NULL). */
+const char* kinc_sim_last_error(const kinc_sim_ctx* ctx);
+
+/* Total pairs G(G-1)/2 and the number of 32768-pair work blocks (Similarity::size). */
+int64_t kinc_sim_total_pairs(const kinc_sim_ctx* ctx);
+int32_t kinc_sim_num_work_blocks(const kinc_sim_ctx* ctx);
+
+/*
+ * Execute the pairs [start, start + size) in linear pair order (x > y,
+ * index = x(x-1)/2 + y), writing HOST arrays:
+ *   out_K[size]                  int8   number of clusters (0 = not enough samples / all fits failed)
+ *   out_labels[size * samples]   int8   per-sample labels: cluster id >= 0, or -9 missing,
+ *                                        -6 below minexpr, -7 pre-outlier, -8 post-outlier
+ *                                        (meaningful when K > 1)
+ *   out_corr[size * max_clusters] float correlation per cluster k < K, NaN elsewhere
+ * Any output pointer may be NULL.  Blocks may be executed in any order; the
+ * position on the rand() stream is derived from `start`.
+ */
+int kinc_sim_execute_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t* out_K,
+                           int8_t* out_labels, float* out_corr);
+
+/*
+ * Same with DEVICE output arrays, stream-ordered on `stream` (a cudaStream_t,
+ * 0 = the context's own stream); returns after enqueueing.  size must be
+ * <= kinc_sim_max_device_block(ctx).
+ */
+int kinc_sim_execute_block_device(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t* d_K,
+                                  int8_t* d_labels, float* d_corr, void* stream);
+int64_t kinc_sim_max_device_block(const kinc_sim_ctx* ctx);
+
+/* Synchronise the context's stream and report any kernel error status. */
+int kinc_sim_synchronize(kinc_sim_ctx* ctx);
+
+/*
+ * Similarity::process (src/core/similarity.cpp:66-127) for one executed
+ * block, on HOST arrays from kinc_sim_execute_block: the clusters whose
+ * correlation passes !isnan(r) && mincorr <= |r| <= maxcorr, renumbered
+ * 0..c-1 per pair.  CMX items: (x, y, cluster, r) for pairs with K > 0;
+ * CCM items: (x, y, cluster, samples codes) for pairs with K > 1, the codes
+ * being labels >= 0 ? (k == label) : -label.  Capacity arguments bound the
+ * output arrays (items; codes hold cap_ccm * samples bytes).  *n_cmx and
+ * *n_ccm receive the counts.
+ */
+int kinc_sim_process_block(const kinc_sim_ctx* ctx, int64_t start, int64_t size, const int8_t* K,
+                           const int8_t* labels, const float* corr,
+                           int32_t* cmx_x, int32_t* cmx_y, int8_t* cmx_c, float* cmx_r, int64_t cap_cmx,
+                           int64_t* n_cmx,
+                           int32_t* ccm_x, int32_t* ccm_y, int8_t* ccm_c, int8_t* ccm_codes, int64_t cap_ccm,
+                           int64_t* n_ccm);
+
+/* The same filter without a context (host code only; no GPU needed): the
+ * caller passes the analytic arguments and the sample count. */
+int kinc_sim_process_pairs(const kinc_sim_params* params, int32_t samples, int64_t start, int64_t size,
+                           const int8_t* K, const int8_t* labels, const float* corr,
+                           int32_t* cmx_x, int32_t* cmx_y, int8_t* cmx_c, float* cmx_r, int64_t cap_cmx,
+                           int64_t* n_cmx,
+                           int32_t* ccm_x, int32_t* ccm_y, int8_t* ccm_c, int8_t* ccm_codes, int64_t cap_ccm,
+                           int64_t* n_ccm);
+
+/* Per-pair usable-sample counts N for [start, start+size) (diagnostics / binning checks). */
+int kinc_sim_pair_counts(kinc_sim_ctx* ctx, int64_t start, int64_t size, int32_t* out_N);
+
+/* Kernel launches made by the last kinc_sim_execute_block* call (for accounting). */
+int32_t kinc_sim_last_launch_count(const kinc_sim_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,87 @@
+"""ctypes binding of libkinc_gb300.so (include/kinc_sim.h).
+
+There is no CPU fallback: if the library is missing or cannot be loaded,
+every entry point raises.  On a machine without a GPU the library still
+loads (the CUDA runtime is linked dynamically), so symbol checks work, but
+kinc_sim_create fails with a CUDA error.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+_lib = None
+
+OK, EINVAL, ECUDA, ENOMEM, EKERNEL, EORDER = 0, 1, 2, 3, 4, 5
+WORK_BLOCK_SIZE = 32768
+
+
+class SimParams(ctypes.Structure):
+    """kinc_sim_params (include/kinc_sim.h)."""
+    _fields_ = [("clus_method", ctypes.c_int32), ("corr_method", ctypes.c_int32),
+                ("min_expr", ctypes.c_float), ("min_samples", ctypes.c_int32),
+                ("min_clusters", ctypes.c_int32), ("max_clusters", ctypes.c_int32),
+                ("criterion", ctypes.c_int32), ("pre_out", ctypes.c_int32), ("post_out", ctypes.c_int32),
+                ("min_corr", ctypes.c_float), ("max_corr", ctypes.c_float), ("ksize", ctypes.c_int32),
+                ("semantics", ctypes.c_int32), ("rand_mode", ctypes.c_int32), ("precision", ctypes.c_int32)]
+
+
+# name -> (restype, argtypes); every symbol include/kinc_sim.h declares
+_VP = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+SIGNATURES = {
+    "kinc_sim_params_default": (ctypes.c_int, [ctypes.POINTER(SimParams)]),
+    "kinc_sim_create": (ctypes.c_int, [_VP, _I32, _I32, ctypes.POINTER(SimParams), ctypes.POINTER(_VP)]),
+    "kinc_sim_destroy": (None, [_VP]),
+    "kinc_sim_last_error": (ctypes.c_char_p, [_VP]),
+    "kinc_sim_total_pairs": (_I64, [_VP]),
+    "kinc_sim_num_work_blocks": (_I32, [_VP]),
+    "kinc_sim_execute_block": (ctypes.c_int, [_VP, _I64, _I64, _VP, _VP, _VP]),
+    "kinc_sim_execute_block_device": (ctypes.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, _VP]),
+    "kinc_sim_max_device_block": (_I64, [_VP]),
+    "kinc_sim_synchronize": (ctypes.c_int, [_VP]),
+    "kinc_sim_process_block": (ctypes.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I64,
+                                              ctypes.POINTER(_I64), _VP, _VP, _VP, _VP, _I64,
+                                              ctypes.POINTER(_I64)]),
+    "kinc_sim_process_pairs": (ctypes.c_int, [ctypes.POINTER(SimParams), _I32, _I64, _I64, _VP, _VP, _VP, _VP,
+                                              _VP, _VP, _VP, _I64, ctypes.POINTER(_I64), _VP, _VP, _VP, _VP,
+                                              _I64, ctypes.POINTER(_I64)]),
+    "kinc_sim_pair_counts": (ctypes.c_int, [_VP, _I64, _I64, _VP]),
+    "kinc_sim_last_launch_count": (_I32, [_VP]),
+}
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load the native library, building it first if needed."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"native library {path} is missing; run kinc_gb300.build.build()")
+        _build.build()
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+class SimError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+def check(rc, ctx=None):
+    if rc != OK:
+        msg = load().kinc_sim_last_error(ctx)
+        raise SimError(rc, msg.decode() if msg else "")

@@ -1,0 +1,80 @@
+"""Build the native library of the package in-tree.
+
+``libkinc_gb300.so`` holds the CUDA Similarity worker and its C ABI
+(include/kinc_sim.h).  It is compiled for sm_103a only, with --fmad=false:
+the worker reproduces the reference's floating-point operation sequence and
+must not let the compiler contract a*b+c (kinc_fmath.h uses explicit fmaf).
+"""
+import os
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+OUT_DIR = os.path.join(PKG, "_lib")
+LIB = os.path.join(OUT_DIR, "libkinc_gb300.so")
+
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "-I", os.path.join(REPO, "include"), "-I", CSRC]
+
+# (source, extra flags)
+UNITS = [
+    ("kinc_sim.cu", ["--fmad=false"]),
+    ("pearson_gemm.cu", []),
+]
+
+
+def _sources():
+    return [os.path.join(CSRC, s) for s, _ in UNITS if os.path.exists(os.path.join(CSRC, s))]
+
+
+def _deps():
+    out = []
+    for d in (CSRC, os.path.join(REPO, "include")):
+        for f in os.listdir(d):
+            if f.endswith((".cu", ".cuh", ".h", ".cpp")):
+                out.append(os.path.join(d, f))
+    return out
+
+
+def up_to_date():
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(d) <= t for d in _deps())
+
+
+def build(force=False, verbose=False):
+    """Compile every CUDA unit in parallel and link the shared library."""
+    if not force and up_to_date():
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    jobs = []
+    for src, flags in UNITS:
+        path = os.path.join(CSRC, src)
+        if not os.path.exists(path):
+            continue
+        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        cmd = [NVCC, *ARCH, *COMMON, *flags, "-c", path, "-o", obj]
+        jobs.append((cmd, obj))
+
+    def run(job):
+        cmd, obj = job
+        if verbose:
+            print(" ".join(cmd))
+        subprocess.check_call(cmd)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        objs = list(ex.map(run, jobs))
+    tmp = LIB + ".tmp"
+    subprocess.check_call([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

@@ -1,0 +1,1090 @@
+/*
+ * kinc_sim.cu -- the GB300 Similarity worker behind include/kinc_sim.h.
+ *
+ * One context = one expression matrix resident in HBM plus the per-gene
+ * usable-sample bitmasks, the glibc rand() jump table and the buffers of one
+ * device block of pairs.  A device block runs as a short stream-ordered
+ * sequence of kernels:
+ *   k_count     usable-sample count N of every pair (popcount of two masks)
+ *   k_scan_*    exclusive prefix of "N >= minsamp" -> each pair's position on
+ *               the rand() stream (a serial KINC process draws rand() only for
+ *               pairs that reach the clustering loop)
+ *   k_prev      previous pair with a larger N inside the same 32768-pair work
+ *               block (what the reference's stale packed-array reads see)
+ *   k_similarity  the per-pair work (sim_device.cuh)
+ * Replaces Similarity::OpenCL::{initialize, Worker::Worker, Worker::execute}
+ * (src/core/similarity_opencl.cpp:34-70, src/core/similarity_opencl_worker.cpp:50-271).
+ */
+#include "../../include/kinc_sim.h"
+#include "sim_device.cuh"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+using namespace kinc;
+
+namespace {
+
+constexpr int WARPS_PER_BLOCK = 4;
+constexpr int SCAN_THREADS = 1024;
+
+/* ================================================================ kernels */
+
+__global__ void k_masks(const float* __restrict__ gem, int32_t G, int32_t S, int32_t W, float min_expr,
+                        uint32_t* __restrict__ umask)
+{
+   const int64_t w_total = (int64_t)G * W;
+   for ( int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < w_total;
+         t += (int64_t)gridDim.x * blockDim.x )
+   {
+      const int64_t g = t / W;
+      const int w = (int)(t % W);
+      uint32_t m = 0;
+      for ( int b = 0; b < 32; ++b )
+      {
+         const int s = w * 32 + b;
+         if ( s < S )
+         {
+            const float v = gem[g * S + s];
+            if ( !isnan(v) && !(v < min_expr) ) m |= 1u << b;
+         }
+      }
+      umask[t] = m;
+   }
+}
+
+__device__ __forceinline__ int pair_count(const uint32_t* __restrict__ umask, int W, int64_t p)
+{
+   int32_t x, y;
+   pair_xy(p, x, y);
+   const uint32_t* mx = umask + (size_t)x * W;
+   const uint32_t* my = umask + (size_t)y * W;
+   int n = 0;
+   for ( int w = 0; w < W; ++w ) n += __popc(mx[w] & my[w]);
+   return n;
+}
+
+/* N for pairs [lo, lo + count) */
+__global__ void k_count(const uint32_t* __restrict__ umask, int W, int64_t lo, int64_t count,
+                        int32_t* __restrict__ N)
+{
+   for ( int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count;
+         t += (int64_t)gridDim.x * blockDim.x )
+   {
+      N[t] = pair_count(umask, W, lo + t);
+   }
+}
+
+/* number of pairs in [0, end) with N >= min_samples, added into *acc */
+__global__ void k_count_qualifying(const uint32_t* __restrict__ umask, int W, int64_t end, int min_samples,
+                                   unsigned long long* acc)
+{
+   __shared__ unsigned long long sh[32];
+   unsigned long long c = 0;
+   for ( int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < end;
+         t += (int64_t)gridDim.x * blockDim.x )
+   {
+      c += pair_count(umask, W, t) >= min_samples;
+   }
+   for ( int o = 16; o > 0; o >>= 1 ) c += __shfl_xor_sync(0xffffffffu, c, o);
+   if ( (threadIdx.x & 31) == 0 ) sh[threadIdx.x >> 5] = c;
+   __syncthreads();
+   if ( threadIdx.x < 32 )
+   {
+      c = threadIdx.x < blockDim.x / 32 ? sh[threadIdx.x] : 0;
+      for ( int o = 16; o > 0; o >>= 1 ) c += __shfl_xor_sync(0xffffffffu, c, o);
+      if ( threadIdx.x == 0 ) atomicAdd(acc, c);
+   }
+}
+
+/* block-wide exclusive scan of one value per thread (blockDim.x == SCAN_THREADS) */
+__device__ unsigned long long block_exclusive_scan(unsigned long long v, unsigned long long* total)
+{
+   __shared__ unsigned long long warp_sums[SCAN_THREADS / 32];
+   const int lane = threadIdx.x & 31;
+   const int warp = threadIdx.x >> 5;
+   unsigned long long incl = v;
+   for ( int o = 1; o < 32; o <<= 1 )
+   {
+      const unsigned long long n = __shfl_up_sync(0xffffffffu, incl, o);
+      if ( lane >= o ) incl += n;
+   }
+   if ( lane == 31 ) warp_sums[warp] = incl;
+   __syncthreads();
+   if ( warp == 0 )
+   {
+      unsigned long long ws = lane < SCAN_THREADS / 32 ? warp_sums[lane] : 0;
+      for ( int o = 1; o < 32; o <<= 1 )
+      {
+         const unsigned long long n = __shfl_up_sync(0xffffffffu, ws, o);
+         if ( lane >= o ) ws += n;
+      }
+      warp_sums[lane] = ws;
+   }
+   __syncthreads();
+   const unsigned long long before = warp == 0 ? 0 : warp_sums[warp - 1];
+   if ( total ) *total = warp_sums[SCAN_THREADS / 32 - 1];
+   __syncthreads();
+   return before + incl - v;
+}
+
+/* per scan block: number of qualifying pairs among its SCAN_THREADS pairs */
+__global__ void k_scan_sums(const int32_t* __restrict__ N, int64_t offset, int64_t count, int min_samples,
+                            unsigned long long* __restrict__ bsum)
+{
+   const int64_t t = blockIdx.x * (int64_t)SCAN_THREADS + threadIdx.x;
+   const unsigned long long f = (t < count && N[offset + t] >= min_samples) ? 1ull : 0ull;
+   unsigned long long total;
+   block_exclusive_scan(f, &total);
+   if ( threadIdx.x == 0 ) bsum[blockIdx.x] = total;
+}
+
+/* exclusive scan of the block sums (one block, several passes), plus the base */
+__global__ void k_scan_blocks(unsigned long long* __restrict__ bsum, int nblocks,
+                              unsigned long long* __restrict__ qbase)
+{
+   unsigned long long carry = *qbase;
+   for ( int base = 0; base < nblocks; base += SCAN_THREADS )
+   {
+      const int i = base + threadIdx.x;
+      const unsigned long long v = i < nblocks ? bsum[i] : 0ull;
+      unsigned long long total;
+      const unsigned long long ex = block_exclusive_scan(v, &total);
+      if ( i < nblocks ) bsum[i] = carry + ex;
+      carry += total;
+   }
+   if ( threadIdx.x == 0 ) *qbase = carry;   /* qualifying pairs before the next block */
+}
+
+__global__ void k_scan_apply(const int32_t* __restrict__ N, int64_t offset, int64_t count, int min_samples,
+                             const unsigned long long* __restrict__ boff, uint64_t* __restrict__ qpos)
+{
+   const int64_t t = blockIdx.x * (int64_t)SCAN_THREADS + threadIdx.x;
+   const unsigned long long f = (t < count && N[offset + t] >= min_samples) ? 1ull : 0ull;
+   const unsigned long long ex = block_exclusive_scan(f, nullptr);
+   if ( t < count ) qpos[t] = boff[blockIdx.x] + ex;
+}
+
+/* previous pair (same 32768-pair work block) with a strictly larger N, by
+ * jumping along already computed links; one thread per work block.  Links
+ * are offsets from lo (-1 = none). */
+__global__ void k_prev(const int32_t* __restrict__ N, int64_t lo, int64_t end, int32_t* __restrict__ pg)
+{
+   const int64_t wb = lo / KINC_SIM_WORK_BLOCK_SIZE + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+   int64_t b0 = wb * KINC_SIM_WORK_BLOCK_SIZE;
+   int64_t b1 = (wb + 1) * KINC_SIM_WORK_BLOCK_SIZE;
+   b0 = b0 < lo ? lo : b0;
+   b1 = b1 > end ? end : b1;
+   const int64_t o0 = b0 - lo;
+   for ( int64_t o = o0; o < b1 - lo; ++o )
+   {
+      const int32_t np = N[o];
+      int64_t c = o - 1;
+      while ( c >= o0 && N[c] <= np ) c = pg[c];
+      pg[o] = c >= o0 ? (int32_t)c : -1;
+   }
+}
+
+/* The i-th usable sample (0-based) of pair c: what the reference left in its
+ * packed array at position i. */
+__device__ float2 packed_sample(const DevParams& P, const DevData& D, int64_t c, int i)
+{
+   int32_t x, y;
+   pair_xy(c, x, y);
+   const uint32_t* mx = D.umask + (size_t)x * P.W;
+   const uint32_t* my = D.umask + (size_t)y * P.W;
+   for ( int w = 0; w < P.W; ++w )
+   {
+      uint32_t m = mx[w] & my[w];
+      const int cnt = __popc(m);
+      if ( i < cnt )
+      {
+         for ( int r = 0; r < i; ++r ) m &= m - 1;
+         const int s = w * 32 + (__ffs(m) - 1);
+         return make_float2(D.gem[(size_t)x * P.S + s], D.gem[(size_t)y * P.S + s]);
+      }
+      i -= cnt;
+   }
+   return make_float2(0.f, 0.f);
+}
+
+/* Pearson::computeCluster for this lane's pair (pairwise_pearson.cpp:12-52). */
+__device__ float lane_pearson(const DevParams& P, const DevData& D, const DevBlock& B, const float2* X,
+                              const int8_t* lbl, int64_t p, int32_t x, int32_t y, int N, int8_t k)
+{
+   int n = 0;
+   float sumx = 0, sumy = 0, sumx2 = 0, sumy2 = 0, sumxy = 0;
+   if ( P.semantics == 0 )
+   {
+      /* positions i < N read the pair's own packed array at i; positions i >= N
+       * read what the last earlier pair of the work block with more than i
+       * usable samples left there (zero if none) */
+      for ( int i = 0; i < N; ++i )
+      {
+         if ( lbl[i * TILE] == k )
+         {
+            const float2 v = X[i * TILE];
+            sumx += v.x; sumy += v.y; sumx2 += v.x * v.x; sumy2 += v.y * v.y; sumxy += v.x * v.y;
+            ++n;
+         }
+      }
+      int32_t c = B.pg[p - B.lo];
+      for ( int i = N; i < P.S; ++i )
+      {
+         if ( lbl[i * TILE] != k ) continue;
+         while ( c >= 0 && B.N[c] <= i ) c = B.pg[c];
+         const float2 v = c >= 0 ? packed_sample(P, D, B.lo + c, i) : make_float2(0.f, 0.f);
+         sumx += v.x; sumy += v.y; sumx2 += v.x * v.x; sumy2 += v.y * v.y; sumxy += v.x * v.y;
+         ++n;
+      }
+   }
+   else
+   {
+      const float* g1 = D.gem + (size_t)x * P.S;
+      const float* g2 = D.gem + (size_t)y * P.S;
+      for ( int i = 0; i < P.S; ++i )
+      {
+         if ( lbl[i * TILE] == k )
+         {
+            const float vx = g1[i];
+            const float vy = g2[i];
+            sumx += vx; sumy += vy; sumx2 += vx * vx; sumy2 += vy * vy; sumxy += vx * vy;
+            ++n;
+         }
+      }
+   }
+   if ( n >= P.min_samples )
+   {
+      return (n * sumxy - sumx * sumy) / sqrtf((n * sumx2 - sumx * sumx) * (n * sumy2 - sumy * sumy));
+   }
+   return __int_as_float(0x7fc00000);
+}
+
+__device__ __forceinline__ float criterion_value(const DevParams& P, const DevData& D, int K, float logL,
+                                                 int N, float E)
+{
+   const int pp = K * (1 + 2 + 2 * 2);
+   double v = D.logn[N] * (double)pp - (double)(2.0f * logL);
+   if ( P.criterion == 1 ) v = v - (double)(2.0f * E);
+   return (float)v;
+}
+
+template <int KT>
+__device__ bool lane_fit(const DevParams& P, const float2* X, float* lpx, int8_t*& wl, int8_t*& ya,
+                         int8_t*& yb, int8_t*& yc, int N, int K, LaneRng& rng, float& logL, float& E)
+{
+   if ( P.clus == 1 )
+   {
+      return gmm_fit<KT>(X, lpx, wl, N, K, rng, P.c2, logL, E);
+   }
+   logL = kmeans_fit<KT>(X, ya, yb, yc, N, K, rng);
+   E = 0.f;
+   int8_t* t = wl;   /* the best labels become the work labels */
+   wl = yc;
+   yc = t;
+   return true;
+}
+
+/* Clustering::compute (pairwise_clustering.cpp:23-103) minus the outlier
+ * passes, for this lane's pair; labels merged into lbl. */
+__device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* X, float* lpx, int8_t* wl,
+                            int8_t* ya, int8_t* yb, int8_t* yc, int8_t* lbl, int N, LaneRng& rng)
+{
+   int bestK = 0;
+   if ( N < P.min_samples ) return 0;
+   float bestValue = INFINITY;
+   for ( int K = P.min_k; K <= P.max_k; ++K )
+   {
+      float logL = 0.f, E = 0.f;
+      bool ok;
+      switch ( K )
+      {
+      case 1: ok = lane_fit<1>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
+      case 2: ok = lane_fit<2>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
+      case 3: ok = lane_fit<3>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
+      case 4: ok = lane_fit<4>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
+      case 5: ok = lane_fit<5>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
+      case 6: ok = lane_fit<6>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
+      default: ok = lane_fit<0>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
+      }
+      if ( !ok ) continue;
+      const float value = criterion_value(P, D, K, logL, N, E);
+      if ( value < bestValue )
+      {
+         bestK = K;
+         bestValue = value;
+         for ( int i = 0, j = 0; i < N; ++i )
+         {
+            if ( lbl[i * TILE] >= 0 )
+            {
+               lbl[i * TILE] = wl[j * TILE];
+               ++j;
+            }
+         }
+      }
+   }
+   return bestK;
+}
+
+__global__ void __launch_bounds__(WARPS_PER_BLOCK * 32)
+k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
+{
+   extern __shared__ float smem[];
+   const int lane = threadIdx.x & 31;
+   const int warp = threadIdx.x >> 5;
+   const int64_t slot = blockIdx.x * (int64_t)WARPS_PER_BLOCK + warp;
+   const size_t col = (size_t)P.S * TILE;
+
+   float2* X = W.X + slot * col;
+   float* lpx = W.lpx + slot * col;
+   int8_t* lbl = W.lbl + slot * col;
+   int8_t* wl = W.wl + slot * col;
+   int8_t* ya = W.ya + slot * col;
+   int8_t* yb = W.yb + slot * col;
+   int8_t* yc = W.yc + slot * col;
+   uint32_t* ring = W.rng + slot * (size_t)(RNG_WORDS * TILE);
+   float* sbuf = smem_sort ? smem + (size_t)warp * P.sort_floats : W.sortbuf + slot * (size_t)P.sort_floats;
+
+   const int64_t ntiles = (B.size + TILE - 1) / TILE;
+   for ( ;; )
+   {
+      unsigned long long t = 0;
+      if ( lane == 0 ) t = atomicAdd(B.tiles, 1ull);
+      t = __shfl_sync(0xffffffffu, t, 0);
+      if ( (int64_t)t >= ntiles ) break;
+      const int64_t p0 = B.start + (int64_t)t * TILE;
+      const int64_t left = B.start + B.size - p0;
+      const int npairs = left < TILE ? (int)left : TILE;
+
+      /* ---- warp-cooperative: fetch, pre-outliers, rand() position, per pair */
+      int myN = 0;
+      for ( int j = 0; j < npairs; ++j )
+      {
+         const int64_t p = p0 + j;
+         int32_t x, y;
+         pair_xy(p, x, y);
+         const int n = warp_fetch(P, D, x, y, X, lbl, j, lane);
+         if ( lane == j ) myN = n;
+         if ( lane == 0 && n != B.N[p - B.lo] ) atomicCAS(B.status, ST_OK, ST_BAD_RANK);
+         if ( P.clus != 0 )
+         {
+            if ( P.pre_out )
+            {
+               warp_mark_outliers(X, n, 0, lbl, 0, -7, sbuf, j, lane);
+               warp_mark_outliers(X, n, 1, lbl, 0, -7, sbuf, j, lane);
+            }
+            if ( P.rand_mode == 0 && n >= P.min_samples )
+            {
+               const uint64_t pos = B.qpos[p - B.start] * (uint64_t)P.draws_per_pair;
+               warp_rng_jump(D, pos, ring, j, lane);
+            }
+         }
+      }
+      __syncwarp();
+
+      /* ---- lane-local: clustering */
+      int K = 1;
+      int64_t myp = p0 + lane;
+      int32_t mx = 0, my = 0;
+      if ( lane < npairs ) pair_xy(myp, mx, my);
+      if ( P.clus != 0 )
+      {
+         K = 0;
+         if ( lane < npairs )
+         {
+            LaneRng rng;
+            rng.ring = ring + lane;
+            rng.head = 0;
+            rng.mode = P.rand_mode;
+            rng.lcg = 1;
+            K = lane_cluster(P, D, X + lane, lpx + lane, wl + lane, ya + lane, yb + lane, yc + lane,
+                             lbl + lane, myN, rng);
+         }
+      }
+      __syncwarp();
+
+      /* ---- warp-cooperative: post-outliers */
+      if ( P.clus != 0 && P.post_out )
+      {
+         for ( int j = 0; j < npairs; ++j )
+         {
+            const int Kj = __shfl_sync(0xffffffffu, K, j);
+            const int nj = __shfl_sync(0xffffffffu, myN, j);
+            if ( Kj > 1 )
+            {
+               for ( int k = 0; k < Kj; ++k )
+               {
+                  warp_mark_outliers(X, nj, 0, lbl, (int8_t)k, -8, sbuf, j, lane);
+                  warp_mark_outliers(X, nj, 1, lbl, (int8_t)k, -8, sbuf, j, lane);
+               }
+            }
+         }
+      }
+
+      /* ---- correlations */
+      float* corr_row = B.outCorr ? B.outCorr + (myp - B.start) * P.max_k : nullptr;
+      if ( P.corr == 0 )
+      {
+         if ( lane < npairs && corr_row )
+         {
+            for ( int k = 0; k < P.max_k; ++k )
+            {
+               corr_row[k] = k < K ? lane_pearson(P, D, B, X + lane, lbl + lane, myp, mx, my, myN, (int8_t)k)
+                                   : __int_as_float(0x7fc00000);
+            }
+         }
+      }
+      else
+      {
+         for ( int j = 0; j < npairs; ++j )
+         {
+            const int Kj = __shfl_sync(0xffffffffu, K, j);
+            const int xj = __shfl_sync(0xffffffffu, mx, j);
+            const int yj = __shfl_sync(0xffffffffu, my, j);
+            float* row = B.outCorr ? B.outCorr + (p0 + j - B.start) * P.max_k : nullptr;
+            for ( int k = 0; k < P.max_k; ++k )
+            {
+               float r = __int_as_float(0x7fc00000);
+               if ( k < Kj ) r = warp_spearman(P, D, X, lbl, xj, yj, (int8_t)k, sbuf, j, lane);
+               if ( lane == 0 && row ) row[k] = r;
+            }
+         }
+      }
+
+      /* ---- outputs */
+      if ( lane < npairs && B.outK ) B.outK[myp - B.start] = (int8_t)K;
+      if ( B.outLabels )
+      {
+         for ( int j = 0; j < npairs; ++j )
+         {
+            int8_t* row = B.outLabels + (p0 + j - B.start) * (int64_t)P.S;
+            for ( int s = lane; s < P.S; s += 32 ) row[s] = lbl[s * TILE + j];
+         }
+      }
+      __syncwarp();
+   }
+}
+
+/* ============================================================ host side */
+
+struct DevBuf
+{
+   void* p = nullptr;
+   size_t bytes = 0;
+};
+
+}  // namespace
+
+struct kinc_sim_ctx
+{
+   kinc_sim_params params {};
+   int32_t G = 0, S = 0, W = 0;
+   DevParams dp {};
+   DevData dd {};
+   DevScratch ds {};
+   cudaStream_t stream = nullptr;
+   int grid = 0;
+   int smem_bytes = 0;
+   int smem_sort = 0;
+   int64_t max_block = 0;
+   /* device allocations */
+   float* d_gem = nullptr;
+   uint32_t* d_umask = nullptr;
+   double* d_logn = nullptr;
+   uint32_t* d_jump = nullptr;
+   uint32_t* d_rng0 = nullptr;
+   int32_t* d_N = nullptr;
+   int32_t* d_pg = nullptr;
+   uint64_t* d_qpos = nullptr;
+   unsigned long long* d_bsum = nullptr;
+   unsigned long long* d_qbase = nullptr;
+   unsigned long long* d_tiles = nullptr;
+   int* d_status = nullptr;
+   int8_t* d_K = nullptr;
+   int8_t* d_labels = nullptr;
+   float* d_corr = nullptr;
+   void* d_scratch = nullptr;
+   /* host-side tracking of the rand() position held in d_qbase */
+   int64_t q_valid_end = 0;
+   int32_t launches = 0;
+   std::string err;
+};
+
+namespace {
+
+std::string g_create_error;
+
+int fail(kinc_sim_ctx* ctx, int code, const char* fmt, ...)
+{
+   char buf[512];
+   va_list ap;
+   va_start(ap, fmt);
+   vsnprintf(buf, sizeof buf, fmt, ap);
+   va_end(ap);
+   if ( ctx ) ctx->err = buf; else g_create_error = buf;
+   return code;
+}
+
+#define CK(call)                                                                                    \
+   do                                                                                               \
+   {                                                                                                \
+      cudaError_t e_ = (call);                                                                      \
+      if ( e_ != cudaSuccess )                                                                      \
+         return fail(ctx, e_ == cudaErrorMemoryAllocation ? KINC_SIM_ENOMEM : KINC_SIM_ECUDA,       \
+                     "%s: %s", #call, cudaGetErrorString(e_));                                      \
+   } while ( 0 )
+
+/* glibc TYPE_3 rand(): state before output 0 and the jump matrices A^(2^b). */
+void glibc_rng_tables(std::vector<uint32_t>& rng0, std::vector<uint32_t>& jump)
+{
+   std::vector<int64_t> r(344);
+   r[0] = 1;
+   for ( int i = 1; i < 31; ++i )
+   {
+      const int64_t hi = r[i - 1] / 127773;
+      const int64_t lo = r[i - 1] % 127773;
+      int64_t word = 16807 * lo - 2836 * hi;
+      if ( word < 0 ) word += 2147483647;
+      r[i] = word;
+   }
+   for ( int i = 31; i < 34; ++i ) r[i] = r[i - 31];
+   for ( int i = 34; i < 344; ++i ) r[i] = (int64_t)(uint32_t)((uint32_t)r[i - 31] + (uint32_t)r[i - 3]);
+   rng0.resize(RNG_WORDS);
+   for ( int i = 0; i < RNG_WORDS; ++i ) rng0[i] = (uint32_t)r[313 + i];
+
+   /* A: s'[i] = s[i+1] (i < 30), s'[30] = s[0] + s[28]; row-major M[row][col] */
+   const int n = RNG_WORDS;
+   std::vector<uint32_t> M(n * n, 0u), T(n * n);
+   for ( int i = 0; i < n - 1; ++i ) M[i * n + i + 1] = 1u;
+   M[(n - 1) * n + 0] = 1u;
+   M[(n - 1) * n + 28] = 1u;
+   jump.assign((size_t)RNG_BITS * n * n, 0u);
+   for ( int b = 0; b < RNG_BITS; ++b )
+   {
+      for ( int row = 0; row < n; ++row )
+         for ( int c = 0; c < n; ++c ) jump[(size_t)b * n * n + c * n + row] = M[row * n + c];
+      for ( int i = 0; i < n; ++i )
+         for ( int j = 0; j < n; ++j )
+         {
+            uint32_t acc = 0;
+            for ( int k = 0; k < n; ++k ) acc += M[i * n + k] * M[k * n + j];
+            T[i * n + j] = acc;
+         }
+      M.swap(T);
+   }
+}
+
+int64_t draws_per_pair(const kinc_sim_params& p)
+{
+   if ( p.clus_method == 0 || p.rand_mode != 0 ) return 0;
+   int64_t s = 0;
+   for ( int k = p.min_clusters; k <= p.max_clusters; ++k ) s += k;
+   return p.clus_method == 2 ? 10 * s : s;
+}
+
+int next_pow2_host(int n)
+{
+   int p = 2;
+   while ( p < n ) p *= 2;
+   return p;
+}
+
+int validate(const kinc_sim_params* p, int32_t G, int32_t S, std::string& why)
+{
+   char buf[256];
+   if ( G < 2 ) { snprintf(buf, sizeof buf, "genes must be >= 2 (got %d)", G); why = buf; return 0; }
+   if ( S < 1 ) { snprintf(buf, sizeof buf, "samples must be >= 1 (got %d)", S); why = buf; return 0; }
+   if ( p->clus_method < 0 || p->clus_method > 2 ) { why = "clus_method must be 0 (none), 1 (gmm) or 2 (kmeans)"; return 0; }
+   if ( p->corr_method < 0 || p->corr_method > 1 ) { why = "corr_method must be 0 (pearson) or 1 (spearman)"; return 0; }
+   if ( p->min_samples < 1 ) { why = "min_samples must be >= 1"; return 0; }
+   if ( p->min_clusters < 1 || p->min_clusters > 64 ) { why = "min_clusters must be in 1..64"; return 0; }
+   if ( p->max_clusters < 1 || p->max_clusters > 64 ) { why = "max_clusters must be in 1..64"; return 0; }
+   if ( p->max_clusters < p->min_clusters )
+   {
+      why = "Minimum clusters must be less than or equal to maximum clusters.";
+      return 0;
+   }
+   if ( p->criterion < 0 || p->criterion > 1 ) { why = "criterion must be 0 (BIC) or 1 (ICL)"; return 0; }
+   if ( !(p->min_corr >= 0 && p->min_corr <= 1) || !(p->max_corr >= 0 && p->max_corr <= 1) )
+   {
+      why = "min_corr and max_corr must be in [0, 1]";
+      return 0;
+   }
+   if ( p->semantics < 0 || p->semantics > 1 ) { why = "semantics must be 0 or 1"; return 0; }
+   if ( p->rand_mode < 0 || p->rand_mode > 1 ) { why = "rand_mode must be 0 or 1"; return 0; }
+   if ( p->precision < 0 || p->precision > 2 ) { why = "precision must be 0, 1 or 2"; return 0; }
+   return 1;
+}
+
+}  // namespace
+
+/* ================================================================= C ABI */
+
+extern "C" int kinc_sim_params_default(kinc_sim_params* p)
+{
+   if ( !p ) return KINC_SIM_EINVAL;
+   p->clus_method = 0;
+   p->corr_method = 0;
+   p->min_expr = -std::numeric_limits<float>::infinity();
+   p->min_samples = 30;
+   p->min_clusters = 1;
+   p->max_clusters = 5;
+   p->criterion = 1;
+   p->pre_out = 0;
+   p->post_out = 0;
+   p->min_corr = 0.5f;
+   p->max_corr = 1.0f;
+   p->ksize = 4096;
+   p->semantics = 0;
+   p->rand_mode = 0;
+   p->precision = 0;
+   return KINC_SIM_OK;
+}
+
+extern "C" const char* kinc_sim_last_error(const kinc_sim_ctx* ctx)
+{
+   return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+extern "C" int64_t kinc_sim_total_pairs(const kinc_sim_ctx* ctx)
+{
+   return ctx ? (int64_t)ctx->G * (ctx->G - 1) / 2 : 0;
+}
+
+extern "C" int32_t kinc_sim_num_work_blocks(const kinc_sim_ctx* ctx)
+{
+   const int64_t total = kinc_sim_total_pairs(ctx);
+   return (int32_t)((total + KINC_SIM_WORK_BLOCK_SIZE - 1) / KINC_SIM_WORK_BLOCK_SIZE);
+}
+
+extern "C" int64_t kinc_sim_max_device_block(const kinc_sim_ctx* ctx)
+{
+   return ctx ? ctx->max_block : 0;
+}
+
+extern "C" int32_t kinc_sim_last_launch_count(const kinc_sim_ctx* ctx)
+{
+   return ctx ? ctx->launches : 0;
+}
+
+static void release(kinc_sim_ctx* c)
+{
+   void* ptrs[] = { c->d_gem, c->d_umask, c->d_logn, c->d_jump, c->d_rng0, c->d_N, c->d_pg, c->d_qpos,
+                    c->d_bsum, c->d_qbase, c->d_tiles, c->d_status, c->d_K, c->d_labels, c->d_corr,
+                    c->d_scratch };
+   for ( void* p : ptrs )
+      if ( p ) cudaFree(p);
+   if ( c->stream ) cudaStreamDestroy(c->stream);
+}
+
+extern "C" void kinc_sim_destroy(kinc_sim_ctx* ctx)
+{
+   if ( !ctx ) return;
+   release(ctx);
+   delete ctx;
+}
+
+extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples, const kinc_sim_params* params,
+                               kinc_sim_ctx** out)
+{
+   kinc_sim_ctx* ctx = nullptr;
+   if ( !out ) return fail(nullptr, KINC_SIM_EINVAL, "out is NULL");
+   *out = nullptr;
+   if ( !gem || !params ) return fail(nullptr, KINC_SIM_EINVAL, "gem and params must not be NULL");
+   std::string why;
+   if ( !validate(params, genes, samples, why) ) return fail(nullptr, KINC_SIM_EINVAL, "%s", why.c_str());
+
+   ctx = new kinc_sim_ctx();
+   ctx->params = *params;
+   ctx->G = genes;
+   ctx->S = samples;
+   ctx->W = (samples + 31) / 32;
+   const int S = samples;
+   const int W = ctx->W;
+   auto bail = [&](int code) {
+      g_create_error = ctx->err;
+      release(ctx);
+      delete ctx;
+      return code;
+   };
+#define CKC(call)                                                                                   \
+   do                                                                                               \
+   {                                                                                                \
+      cudaError_t e_ = (call);                                                                      \
+      if ( e_ != cudaSuccess )                                                                      \
+      {                                                                                             \
+         fail(ctx, e_ == cudaErrorMemoryAllocation ? KINC_SIM_ENOMEM : KINC_SIM_ECUDA, "%s: %s",    \
+              #call, cudaGetErrorString(e_));                                                       \
+         return bail(e_ == cudaErrorMemoryAllocation ? KINC_SIM_ENOMEM : KINC_SIM_ECUDA);           \
+      }                                                                                             \
+   } while ( 0 )
+
+   int dev = 0;
+   CKC(cudaGetDevice(&dev));
+   cudaDeviceProp prop;
+   CKC(cudaGetDeviceProperties(&prop, dev));
+   CKC(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+
+   /* expression matrix and masks */
+   const size_t gem_bytes = (size_t)genes * S * sizeof(float);
+   CKC(cudaMalloc(&ctx->d_gem, gem_bytes));
+   CKC(cudaMemcpyAsync(ctx->d_gem, gem, gem_bytes, cudaMemcpyHostToDevice, ctx->stream));
+   CKC(cudaMalloc(&ctx->d_umask, (size_t)genes * W * sizeof(uint32_t)));
+   k_masks<<<std::max(1, std::min(65535, (int)(((int64_t)genes * W + 255) / 256))), 256, 0, ctx->stream>>>(
+      ctx->d_gem, genes, S, W, params->min_expr, ctx->d_umask);
+   CKC(cudaGetLastError());
+
+   /* log(N) in double, N = 0..S (computeBIC's log of an int) */
+   std::vector<double> logn(S + 1);
+   for ( int n = 0; n <= S; ++n ) logn[n] = std::log((double)n);
+   CKC(cudaMalloc(&ctx->d_logn, logn.size() * sizeof(double)));
+   CKC(cudaMemcpyAsync(ctx->d_logn, logn.data(), logn.size() * sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+
+   std::vector<uint32_t> rng0, jump;
+   glibc_rng_tables(rng0, jump);
+   CKC(cudaMalloc(&ctx->d_jump, jump.size() * sizeof(uint32_t)));
+   CKC(cudaMalloc(&ctx->d_rng0, rng0.size() * sizeof(uint32_t)));
+   CKC(cudaMemcpyAsync(ctx->d_jump, jump.data(), jump.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                       ctx->stream));
+   CKC(cudaMemcpyAsync(ctx->d_rng0, rng0.data(), rng0.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                       ctx->stream));
+
+   /* device parameters */
+   DevParams& dp = ctx->dp;
+   dp.G = genes; dp.S = S; dp.W = W;
+   dp.clus = params->clus_method; dp.corr = params->corr_method;
+   dp.min_expr = params->min_expr; dp.min_samples = params->min_samples;
+   dp.min_k = params->min_clusters; dp.max_k = params->max_clusters;
+   dp.criterion = params->criterion; dp.pre_out = params->pre_out; dp.post_out = params->post_out;
+   dp.semantics = params->semantics; dp.rand_mode = params->rand_mode;
+   dp.draws_per_pair = draws_per_pair(*params);
+   dp.c2 = 2 * std::log(2.0f * M_PI);
+   dp.P2 = next_pow2_host(std::max(S, 2));
+   const bool need_sort = (params->clus_method != 0 && (params->pre_out || params->post_out))
+                          || params->corr_method == 1;
+   dp.sort_floats = params->corr_method == 1 ? 3 * dp.P2 : (need_sort ? dp.P2 : 0);
+
+   /* launch shape: sort buffers in shared memory when they fit */
+   const size_t sort_bytes_warp = (size_t)dp.sort_floats * sizeof(float);
+   ctx->smem_sort = need_sort && sort_bytes_warp * WARPS_PER_BLOCK <= 160 * 1024;
+   ctx->smem_bytes = ctx->smem_sort ? (int)(sort_bytes_warp * WARPS_PER_BLOCK) : 0;
+   if ( ctx->smem_bytes > 48 * 1024 )
+      CKC(cudaFuncSetAttribute(k_similarity, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_bytes));
+   int per_sm = 0;
+   CKC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_similarity, WARPS_PER_BLOCK * 32,
+                                                     ctx->smem_bytes));
+   per_sm = std::max(1, per_sm);
+
+   /* scratch: per warp slot, interleaved by lane */
+   const size_t col = (size_t)S * TILE;
+   const size_t slot_bytes = col * sizeof(float2) + col * sizeof(float) + 5 * col
+                             + (size_t)RNG_WORDS * TILE * sizeof(uint32_t)
+                             + (ctx->smem_sort ? 0 : sort_bytes_warp) + 256 * 8;
+   size_t free_b = 0, total_b = 0;
+   CKC(cudaMemGetInfo(&free_b, &total_b));
+   int grid = prop.multiProcessorCount * per_sm;
+   const size_t scratch_cap = free_b / 4;
+   while ( grid > prop.multiProcessorCount && (size_t)grid * WARPS_PER_BLOCK * slot_bytes > scratch_cap )
+      grid -= prop.multiProcessorCount;
+   ctx->grid = grid;
+   const size_t slots = (size_t)grid * WARPS_PER_BLOCK;
+   {
+      size_t off = 0;
+      auto take = [&](size_t bytes) {
+         const size_t o = off;
+         off += (bytes + 255) & ~(size_t)255;
+         return o;
+      };
+      const size_t oX = take(slots * col * sizeof(float2));
+      const size_t oL = take(slots * col * sizeof(float));
+      const size_t oB = take(slots * col);
+      const size_t oW = take(slots * col);
+      const size_t oA = take(slots * col);
+      const size_t oY = take(slots * col);
+      const size_t oC = take(slots * col);
+      const size_t oR = take(slots * RNG_WORDS * TILE * sizeof(uint32_t));
+      const size_t oS = take(ctx->smem_sort ? 0 : slots * sort_bytes_warp);
+      CKC(cudaMalloc(&ctx->d_scratch, off));
+      char* base = (char*)ctx->d_scratch;
+      ctx->ds.X = (float2*)(base + oX);
+      ctx->ds.lpx = (float*)(base + oL);
+      ctx->ds.lbl = (int8_t*)(base + oB);
+      ctx->ds.wl = (int8_t*)(base + oW);
+      ctx->ds.ya = (int8_t*)(base + oA);
+      ctx->ds.yb = (int8_t*)(base + oY);
+      ctx->ds.yc = (int8_t*)(base + oC);
+      ctx->ds.rng = (uint32_t*)(base + oR);
+      ctx->ds.sortbuf = ctx->smem_sort ? nullptr : (float*)(base + oS);
+   }
+
+   /* one device block of pairs */
+   const int64_t total = (int64_t)genes * (genes - 1) / 2;
+   int64_t mb = 1 << 20;
+   while ( mb > 4096 && (size_t)mb * S > ((size_t)1 << 31) ) mb >>= 1;
+   ctx->max_block = std::min<int64_t>(mb, std::max<int64_t>(total, 1));
+   const int64_t nspan = ctx->max_block + KINC_SIM_WORK_BLOCK_SIZE;
+   const int64_t nscan = (ctx->max_block + SCAN_THREADS - 1) / SCAN_THREADS;
+   CKC(cudaMalloc(&ctx->d_N, nspan * sizeof(int32_t)));
+   CKC(cudaMalloc(&ctx->d_pg, nspan * sizeof(int32_t)));
+   CKC(cudaMalloc(&ctx->d_qpos, ctx->max_block * sizeof(uint64_t)));
+   CKC(cudaMalloc(&ctx->d_bsum, (nscan + 1) * sizeof(unsigned long long)));
+   CKC(cudaMalloc(&ctx->d_qbase, sizeof(unsigned long long)));
+   CKC(cudaMalloc(&ctx->d_tiles, sizeof(unsigned long long)));
+   CKC(cudaMalloc(&ctx->d_status, sizeof(int)));
+   CKC(cudaMalloc(&ctx->d_K, ctx->max_block));
+   CKC(cudaMalloc(&ctx->d_labels, (size_t)ctx->max_block * S));
+   CKC(cudaMalloc(&ctx->d_corr, (size_t)ctx->max_block * params->max_clusters * sizeof(float)));
+   CKC(cudaMemsetAsync(ctx->d_qbase, 0, sizeof(unsigned long long), ctx->stream));
+   CKC(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
+   ctx->q_valid_end = 0;
+
+   ctx->dd.gem = ctx->d_gem;
+   ctx->dd.umask = ctx->d_umask;
+   ctx->dd.logn = ctx->d_logn;
+   ctx->dd.jump = ctx->d_jump;
+   ctx->dd.rng0 = ctx->d_rng0;
+   CKC(cudaStreamSynchronize(ctx->stream));
+   *out = ctx;
+   return KINC_SIM_OK;
+#undef CKC
+}
+
+/* enqueue one device block [start, start+size) into device outputs */
+static int enqueue_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t* d_K, int8_t* d_labels,
+                         float* d_corr, cudaStream_t st)
+{
+   const DevParams& dp = ctx->dp;
+   const int64_t end = start + size;
+   const int64_t lo = (start / KINC_SIM_WORK_BLOCK_SIZE) * KINC_SIM_WORK_BLOCK_SIZE;
+   const int64_t span = end - lo;
+   int launches = 0;
+
+   k_count<<<(int)std::min<int64_t>((span + 255) / 256, 65535), 256, 0, st>>>(ctx->d_umask, ctx->W, lo, span,
+                                                                               ctx->d_N);
+   ++launches;
+   if ( dp.clus != 0 && dp.rand_mode == 0 )
+   {
+      if ( ctx->q_valid_end != start )
+      {
+         /* rand() position of a block executed out of order: count from pair 0 */
+         CK(cudaMemsetAsync(ctx->d_qbase, 0, sizeof(unsigned long long), st));
+         if ( start > 0 )
+         {
+            k_count_qualifying<<<1024, 256, 0, st>>>(ctx->d_umask, ctx->W, start, dp.min_samples,
+                                                      ctx->d_qbase);
+            ++launches;
+         }
+      }
+      const int nscan = (int)((size + SCAN_THREADS - 1) / SCAN_THREADS);
+      const int64_t off = start - lo;
+      k_scan_sums<<<nscan, SCAN_THREADS, 0, st>>>(ctx->d_N, off, size, dp.min_samples, ctx->d_bsum);
+      k_scan_blocks<<<1, SCAN_THREADS, 0, st>>>(ctx->d_bsum, nscan, ctx->d_qbase);
+      k_scan_apply<<<nscan, SCAN_THREADS, 0, st>>>(ctx->d_N, off, size, dp.min_samples, ctx->d_bsum,
+                                                   ctx->d_qpos);
+      launches += 3;
+      ctx->q_valid_end = end;
+   }
+   if ( dp.corr == 0 && dp.semantics == 0 )
+   {
+      const int64_t nwb = (end - 1) / KINC_SIM_WORK_BLOCK_SIZE - lo / KINC_SIM_WORK_BLOCK_SIZE + 1;
+      k_prev<<<(int)((nwb + 63) / 64), 64, 0, st>>>(ctx->d_N, lo, end, ctx->d_pg);
+      ++launches;
+   }
+   CK(cudaMemsetAsync(ctx->d_tiles, 0, sizeof(unsigned long long), st));
+   DevBlock B;
+   B.start = start;
+   B.size = size;
+   B.lo = lo;
+   B.N = ctx->d_N;
+   B.pg = ctx->d_pg;
+   B.qpos = ctx->d_qpos;
+   B.outK = d_K;
+   B.outLabels = d_labels;
+   B.outCorr = d_corr;
+   B.tiles = ctx->d_tiles;
+   B.status = ctx->d_status;
+   k_similarity<<<ctx->grid, WARPS_PER_BLOCK * 32, ctx->smem_bytes, st>>>(dp, ctx->dd, ctx->ds, B,
+                                                                           ctx->smem_sort);
+   ++launches;
+   CK(cudaGetLastError());
+   ctx->launches += launches;
+   return KINC_SIM_OK;
+}
+
+static int check_range(kinc_sim_ctx* ctx, int64_t start, int64_t size)
+{
+   const int64_t total = kinc_sim_total_pairs(ctx);
+   if ( start < 0 || size < 0 || start + size > total )
+      return fail(ctx, KINC_SIM_EINVAL, "pair range [%lld, %lld) outside [0, %lld)", (long long)start,
+                  (long long)(start + size), (long long)total);
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_sim_synchronize(kinc_sim_ctx* ctx)
+{
+   if ( !ctx ) return KINC_SIM_EINVAL;
+   CK(cudaStreamSynchronize(ctx->stream));
+   int st = 0;
+   CK(cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+   if ( st != ST_OK )
+   {
+      CK(cudaMemset(ctx->d_status, 0, sizeof(int)));
+      return fail(ctx, KINC_SIM_EKERNEL, "kernel reported status %d", st);
+   }
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_sim_execute_block_device(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t* d_K,
+                                             int8_t* d_labels, float* d_corr, void* stream)
+{
+   if ( !ctx ) return KINC_SIM_EINVAL;
+   int rc = check_range(ctx, start, size);
+   if ( rc ) return rc;
+   if ( size > ctx->max_block )
+      return fail(ctx, KINC_SIM_EINVAL, "size %lld exceeds the device block limit %lld", (long long)size,
+                  (long long)ctx->max_block);
+   if ( size == 0 ) return KINC_SIM_OK;
+   ctx->launches = 0;
+   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+   return enqueue_block(ctx, start, size, d_K, d_labels, d_corr, st);
+}
+
+extern "C" int kinc_sim_execute_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t* out_K,
+                                      int8_t* out_labels, float* out_corr)
+{
+   if ( !ctx ) return KINC_SIM_EINVAL;
+   int rc = check_range(ctx, start, size);
+   if ( rc ) return rc;
+   ctx->launches = 0;
+   const int S = ctx->S;
+   const int maxK = ctx->params.max_clusters;
+   for ( int64_t done = 0; done < size; )
+   {
+      const int64_t n = std::min<int64_t>(ctx->max_block, size - done);
+      const int32_t before = ctx->launches;
+      rc = enqueue_block(ctx, start + done, n, ctx->d_K, out_labels ? ctx->d_labels : nullptr,
+                         ctx->d_corr, ctx->stream);
+      (void)before;
+      if ( rc ) return rc;
+      if ( out_K ) CK(cudaMemcpyAsync(out_K + done, ctx->d_K, n, cudaMemcpyDeviceToHost, ctx->stream));
+      if ( out_labels )
+         CK(cudaMemcpyAsync(out_labels + done * S, ctx->d_labels, (size_t)n * S, cudaMemcpyDeviceToHost,
+                            ctx->stream));
+      if ( out_corr )
+         CK(cudaMemcpyAsync(out_corr + done * maxK, ctx->d_corr, (size_t)n * maxK * sizeof(float),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+      rc = kinc_sim_synchronize(ctx);
+      if ( rc ) return rc;
+      done += n;
+   }
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_sim_pair_counts(kinc_sim_ctx* ctx, int64_t start, int64_t size, int32_t* out_N)
+{
+   if ( !ctx || !out_N ) return KINC_SIM_EINVAL;
+   int rc = check_range(ctx, start, size);
+   if ( rc ) return rc;
+   for ( int64_t done = 0; done < size; )
+   {
+      const int64_t n = std::min<int64_t>(ctx->max_block, size - done);
+      k_count<<<(int)std::min<int64_t>((n + 255) / 256, 65535), 256, 0, ctx->stream>>>(
+         ctx->d_umask, ctx->W, start + done, n, ctx->d_N);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(out_N + done, ctx->d_N, n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+      done += n;
+   }
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_sim_process_pairs(const kinc_sim_params* params, int32_t samples, int64_t start, int64_t size,
+                                      const int8_t* K, const int8_t* labels, const float* corr, int32_t* cmx_x,
+                                      int32_t* cmx_y, int8_t* cmx_c, float* cmx_r, int64_t cap_cmx,
+                                      int64_t* n_cmx, int32_t* ccm_x, int32_t* ccm_y, int8_t* ccm_c,
+                                      int8_t* ccm_codes, int64_t cap_ccm, int64_t* n_ccm)
+{
+   if ( !params || !K || !corr || samples < 1 || start < 0 || size < 0 )
+      return fail(nullptr, KINC_SIM_EINVAL, "invalid arguments to kinc_sim_process_pairs");
+   const int S = samples;
+   const int maxK = params->max_clusters;
+   const float lo = params->min_corr;
+   const float hi = params->max_corr;
+   int64_t nc = 0, nm = 0;
+   /* pair index -> (x, y) and then ++ (src/core/pairwise_index.cpp:32-57,85-94) */
+   int64_t x = 1, pos = 0;
+   while ( pos <= start ) { ++x; pos = x * (x - 1) / 2; }
+   --x;
+   int64_t y = start - x * (x - 1) / 2;
+   for ( int64_t q = 0; q < size; ++q )
+   {
+      const int Kq = K[q];
+      if ( Kq > 1 && labels && ccm_x )
+      {
+         int c = 0;
+         for ( int k = 0; k < Kq; ++k )
+         {
+            const float r = corr[q * maxK + k];
+            if ( !std::isnan(r) && lo <= std::fabs(r) && std::fabs(r) <= hi )
+            {
+               if ( nm >= cap_ccm )
+                  return fail(nullptr, KINC_SIM_EINVAL, "CCM capacity %lld exceeded", (long long)cap_ccm);
+               ccm_x[nm] = (int32_t)x;
+               ccm_y[nm] = (int32_t)y;
+               ccm_c[nm] = (int8_t)c++;
+               for ( int i = 0; i < S; ++i )
+               {
+                  const int8_t l = labels[q * S + i];
+                  ccm_codes[nm * S + i] = (int8_t)(l >= 0 ? (k == l) : -l);
+               }
+               ++nm;
+            }
+         }
+      }
+      if ( Kq > 0 && cmx_x )
+      {
+         int c = 0;
+         for ( int k = 0; k < Kq; ++k )
+         {
+            const float r = corr[q * maxK + k];
+            if ( !std::isnan(r) && lo <= std::fabs(r) && std::fabs(r) <= hi )
+            {
+               if ( nc >= cap_cmx )
+                  return fail(nullptr, KINC_SIM_EINVAL, "CMX capacity %lld exceeded", (long long)cap_cmx);
+               cmx_x[nc] = (int32_t)x;
+               cmx_y[nc] = (int32_t)y;
+               cmx_c[nc] = (int8_t)c++;
+               cmx_r[nc] = r;
+               ++nc;
+            }
+         }
+      }
+      if ( ++y >= x ) { y = 0; ++x; }
+   }
+   if ( n_cmx ) *n_cmx = nc;
+   if ( n_ccm ) *n_ccm = nm;
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_sim_process_block(const kinc_sim_ctx* cctx, int64_t start, int64_t size, const int8_t* K,
+                                      const int8_t* labels, const float* corr, int32_t* cmx_x, int32_t* cmx_y,
+                                      int8_t* cmx_c, float* cmx_r, int64_t cap_cmx, int64_t* n_cmx,
+                                      int32_t* ccm_x, int32_t* ccm_y, int8_t* ccm_c, int8_t* ccm_codes,
+                                      int64_t cap_ccm, int64_t* n_ccm)
+{
+   kinc_sim_ctx* ctx = const_cast<kinc_sim_ctx*>(cctx);
+   if ( !ctx ) return KINC_SIM_EINVAL;
+   const int rc = kinc_sim_process_pairs(&ctx->params, ctx->S, start, size, K, labels, corr, cmx_x, cmx_y, cmx_c,
+                                         cmx_r, cap_cmx, n_cmx, ccm_x, ccm_y, ccm_c, ccm_codes, cap_ccm, n_ccm);
+   if ( rc ) ctx->err = g_create_error;
+   return rc;
+}

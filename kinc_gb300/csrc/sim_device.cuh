@@ -1,0 +1,728 @@
+/*
+ * sim_device.cuh -- device code of the GB300 Similarity worker.
+ *
+ * Execution model.  One warp owns a tile of 32 gene pairs at a time (a
+ * persistent grid pulls tiles from an atomic queue).  Work whose result does
+ * not depend on evaluation order -- fetching and compacting the pair,
+ * Tukey quartiles (order statistics), the Spearman bitonic network -- runs
+ * warp-cooperatively, one pair after another, with the pair's data staged in
+ * shared memory.  Work whose result depends on the order of floating-point
+ * operations -- every EM / Lloyd / Pearson sum, which the reference
+ * accumulates sequentially in sample order -- runs one pair per lane, each
+ * lane repeating the reference's exact operation sequence on its own pair.
+ * Per-pair arrays live in global scratch interleaved by lane ([i][32]), so
+ * lane-parallel passes are coalesced.  The whole translation unit is built
+ * with --fmad=false so no a*b+c is contracted; kinc_fmath.h supplies exp/log.
+ *
+ * Reference semantics restated here (paths relative to the KINC tree):
+ *   fetchPair                 src/core/similarity_serial.cpp:108-141
+ *   Clustering::compute       src/core/pairwise_clustering.cpp:23-103
+ *   markOutliers              src/core/pairwise_clustering.cpp:110-148
+ *   computeBIC / computeICL   src/core/pairwise_clustering.cpp:155-172
+ *   GMM::fit and helpers      src/core/pairwise_gmm.cpp:11-445
+ *   KMeans::fit               src/core/pairwise_kmeans.cpp:12-127
+ *   Pearson::computeCluster   src/core/pairwise_pearson.cpp:12-52
+ *   Spearman::computeCluster  src/core/pairwise_spearman.cpp:27-166
+ */
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "kinc_fmath.h"
+
+namespace kinc {
+
+constexpr int TILE = 32;            /* pairs per warp tile */
+constexpr int RNG_WORDS = 31;       /* glibc TYPE_3 state words */
+constexpr int RNG_BITS = 48;        /* jump table covers positions < 2^48 */
+
+/* status codes a kernel may raise (first one wins) */
+constexpr int ST_OK = 0;
+constexpr int ST_BAD_RANK = 1;      /* fetched N disagrees with the pre-pass count */
+
+struct DevParams
+{
+   int32_t G, S, W;                 /* genes, samples, 32-bit mask words per gene */
+   int32_t clus, corr;
+   float min_expr;
+   int32_t min_samples, min_k, max_k, criterion, pre_out, post_out;
+   int32_t semantics, rand_mode;
+   int64_t draws_per_pair;          /* glibc draws one qualifying pair consumes */
+   double c2;                       /* D * log(2 pi), D = 2, in double */
+   int32_t P2;                      /* next power of two >= max(S, 2) */
+   int32_t sort_floats;             /* floats of sort buffer per warp */
+};
+
+struct DevData
+{
+   const float* gem;                /* [G][S] */
+   const uint32_t* umask;           /* [G][W] usable: !isnan && !(v < minexpr) */
+   const double* logn;              /* [S+1] log((double)N) */
+   const uint32_t* jump;            /* [RNG_BITS][31][31] A^(2^b), [b][col][row] */
+   const uint32_t* rng0;            /* [31] state before output 0 */
+};
+
+struct DevScratch
+{
+   float2* X;                       /* per warp slot: [S][32] */
+   float* lpx;                      /* per warp slot: [S][32] */
+   int8_t* lbl;                     /* per warp slot: [S][32] */
+   int8_t* wl;                      /* per warp slot: [S][32] work labels */
+   int8_t* ya;                      /* per warp slot: [S][32] K-means */
+   int8_t* yb;
+   int8_t* yc;
+   uint32_t* rng;                   /* per warp slot: [31][32] */
+   float* sortbuf;                  /* per warp slot: sort_floats, used when not in shared memory */
+};
+
+struct DevBlock
+{
+   int64_t start, size;             /* pairs of this launch */
+   int64_t lo;                      /* first pair covered by N[] / pg[] (start of its work block) */
+   const int32_t* N;                /* [p - lo] */
+   const int32_t* pg;               /* [p - lo]: previous pair in the work block with larger N, or -1 */
+   const uint64_t* qpos;            /* [p - start]: qualifying pairs before p (rand position / draws) */
+   int8_t* outK;                    /* [p - start] */
+   int8_t* outLabels;               /* [p - start][S] */
+   float* outCorr;                  /* [p - start][max_k] */
+   unsigned long long* tiles;       /* tile queue counter */
+   int* status;
+};
+
+/* ------------------------------------------------------------- helpers */
+
+__device__ __forceinline__ void pair_xy(int64_t p, int32_t& x, int32_t& y)
+{
+   /* inverse of p = x(x-1)/2 + y, x > y >= 0 (src/core/pairwise_index.cpp:32-57) */
+   int64_t xx = (int64_t)((1.0 + sqrt(1.0 + 8.0 * (double)p)) * 0.5);
+   while ( xx * (xx - 1) / 2 > p ) --xx;
+   while ( (xx + 1) * xx / 2 <= p ) ++xx;
+   x = (int32_t)xx;
+   y = (int32_t)(p - xx * (xx - 1) / 2);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+   unsigned m;
+   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+   return m;
+}
+
+__device__ __forceinline__ int next_pow2(int n)
+{
+   int p = 2;
+   while ( p < n ) p *= 2;
+   return p;
+}
+
+/* Spearman::bitonicSort network (pairwise_spearman.cpp:109-134) executed by a
+ * warp: every stage's compare-exchanges touch disjoint slots, so running them
+ * in parallel performs exactly the reference's sequence of swaps. */
+__device__ void warp_bitonic(int size, float* key, float* extra, int lane)
+{
+   const int bsize = size / 2;
+   for ( int ob = 2; ob <= size; ob *= 2 )
+   {
+      const int half = ob / 2;
+      for ( int ib = ob; ib >= 2; ib /= 2 )
+      {
+         const int t = ib / 2;
+         for ( int i = lane; i < bsize; i += 32 )
+         {
+            const bool desc = (i / half) & 1;
+            const int a = (i / t) * ib + (i % t);
+            const int b = a + t;
+            const float ka = key[a];
+            const float kb = key[b];
+            if ( (ka > kb && !desc) || (ka < kb && desc) )
+            {
+               key[a] = kb;
+               key[b] = ka;
+               if ( extra )
+               {
+                  const float ea = extra[a];
+                  extra[a] = extra[b];
+                  extra[b] = ea;
+               }
+            }
+         }
+         __syncwarp();
+      }
+   }
+}
+
+/* ----------------------------------------------------------- rand() */
+
+/* glibc rand() from a 31-word lagged-Fibonacci state kept in scratch,
+ * interleaved by lane; head = index of the oldest word. */
+struct LaneRng
+{
+   uint32_t* ring;
+   int head;
+   int mode;
+   uint64_t lcg;
+
+   __device__ __forceinline__ int32_t next()
+   {
+      if ( mode == 0 )
+      {
+         int h28 = head + 28;
+         if ( h28 >= RNG_WORDS ) h28 -= RNG_WORDS;
+         const uint32_t v = ring[head * TILE] + ring[h28 * TILE];
+         ring[head * TILE] = v;
+         head = head + 1 == RNG_WORDS ? 0 : head + 1;
+         return (int32_t)(v >> 1);
+      }
+      lcg = lcg * 1103515245ull + 12345ull;
+      return (int32_t)((uint32_t)(lcg / 65536ull) % 32768u);
+   }
+};
+
+/* Jump the glibc state to output position `pos` (warp-cooperative: lane r < 31
+ * holds word r) and store it interleaved for lane `slot`. */
+__device__ void warp_rng_jump(const DevData& D, uint64_t pos, uint32_t* ring, int slot, int lane)
+{
+   uint32_t s = lane < RNG_WORDS ? D.rng0[lane] : 0u;
+   for ( int b = 0; b < RNG_BITS && pos; ++b, pos >>= 1 )
+   {
+      if ( !(pos & 1) ) continue;
+      const uint32_t* M = D.jump + (size_t)b * RNG_WORDS * RNG_WORDS;
+      uint32_t acc = 0;
+      for ( int c = 0; c < RNG_WORDS; ++c )
+      {
+         const uint32_t sc = __shfl_sync(0xffffffffu, s, c);
+         if ( lane < RNG_WORDS ) acc += M[c * RNG_WORDS + lane] * sc;
+      }
+      s = acc;
+   }
+   if ( lane < RNG_WORDS ) ring[lane * TILE + slot] = s;
+}
+
+/* ------------------------------------------------------ warp-coop steps */
+
+/* fetchPair for pair (x, y) into column `j` of the tile's interleaved arrays. */
+__device__ int warp_fetch(const DevParams& P, const DevData& D, int32_t x, int32_t y, float2* X,
+                          int8_t* lbl, int j, int lane)
+{
+   const float* g1 = D.gem + (size_t)x * P.S;
+   const float* g2 = D.gem + (size_t)y * P.S;
+   int n = 0;
+   for ( int base = 0; base < P.S; base += 32 )
+   {
+      const int s = base + lane;
+      bool use = false;
+      float v1 = 0.f, v2 = 0.f;
+      if ( s < P.S )
+      {
+         v1 = g1[s];
+         v2 = g2[s];
+         const bool nanb = isnan(v1) || isnan(v2);
+         const bool low = v1 < P.min_expr || v2 < P.min_expr;
+         lbl[s * TILE + j] = nanb ? (int8_t)-9 : (low ? (int8_t)-6 : (int8_t)0);
+         use = !nanb && !low;
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, use);
+      if ( use ) X[(n + __popc(bal & lanemask_lt())) * TILE + j] = make_float2(v1, v2);
+      n += __popc(bal);
+   }
+   __syncwarp();
+   return n;
+}
+
+/* Clustering::markOutliers on column j of the tile (labels by sample position
+ * i < N, values from the packed array at i, as in the reference). */
+__device__ void warp_mark_outliers(const float2* X, int N, int col, int8_t* lbl, int8_t cluster,
+                                   int8_t marker, float* buf, int j, int lane)
+{
+   int n = 0;
+   for ( int base = 0; base < N; base += 32 )
+   {
+      const int i = base + lane;
+      bool sel = false;
+      float v = 0.f;
+      if ( i < N )
+      {
+         const int8_t l = lbl[i * TILE + j];
+         sel = l == cluster || l == marker;
+         if ( sel )
+         {
+            const float2 xv = X[i * TILE + j];
+            v = col == 0 ? xv.x : xv.y;
+         }
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, sel);
+      if ( sel ) buf[n + __popc(bal & lanemask_lt())] = v;
+      n += __popc(bal);
+   }
+   if ( n == 0 )
+   {
+      __syncwarp();
+      return;
+   }
+   const int np2 = next_pow2(n);
+   for ( int i = n + lane; i < np2; i += 32 ) buf[i] = __int_as_float(0x7f800000);
+   __syncwarp();
+   warp_bitonic(np2, buf, nullptr, lane);
+   const float Q1 = buf[n * 1 / 4];
+   const float Q3 = buf[n * 3 / 4];
+   const float T_min = Q1 - 1.5f * (Q3 - Q1);
+   const float T_max = Q3 + 1.5f * (Q3 - Q1);
+   __syncwarp();
+   for ( int i = lane; i < N; i += 32 )
+   {
+      if ( lbl[i * TILE + j] == cluster )
+      {
+         const float2 xv = X[i * TILE + j];
+         const float v = col == 0 ? xv.x : xv.y;
+         if ( v < T_min || T_max < v ) lbl[i * TILE + j] = marker;
+      }
+   }
+   __syncwarp();
+}
+
+/* Spearman::computeCluster for column j, cluster k. */
+__device__ float warp_spearman(const DevParams& P, const DevData& D, const float2* X, const int8_t* lbl,
+                               int32_t x, int32_t y, int8_t k, float* buf, int j, int lane)
+{
+   float* sx = buf;
+   float* sy = buf + P.P2;
+   float* sr = buf + 2 * P.P2;
+   const float* g1 = D.gem + (size_t)x * P.S;
+   const float* g2 = D.gem + (size_t)y * P.S;
+   int n = 0;
+   int jw = 0;
+   for ( int base = 0; base < P.S; base += 32 )
+   {
+      const int i = base + lane;
+      const int8_t l = i < P.S ? lbl[i * TILE + j] : (int8_t)-1;
+      const bool nonneg = l >= 0;
+      const bool incl = l == k;
+      const unsigned bn = __ballot_sync(0xffffffffu, nonneg);
+      const unsigned bi = __ballot_sync(0xffffffffu, incl);
+      if ( incl )
+      {
+         const int slot = n + __popc(bi & lanemask_lt());
+         float2 v;
+         if ( P.semantics == 0 )
+         {
+            v = X[(jw + __popc(bn & lanemask_lt())) * TILE + j];
+         }
+         else
+         {
+            v = make_float2(g1[i], g2[i]);
+         }
+         sx[slot] = v.x;
+         sy[slot] = v.y;
+         sr[slot] = (float)(slot + 1);
+      }
+      n += __popc(bi);
+      jw += __popc(bn);
+   }
+   if ( n < P.min_samples )
+   {
+      __syncwarp();
+      return __int_as_float(0x7fc00000);
+   }
+   const int np2 = next_pow2(n);
+   for ( int i = n + lane; i < np2; i += 32 )
+   {
+      sx[i] = __int_as_float(0x7f800000);
+      sy[i] = __int_as_float(0x7f800000);
+      sr[i] = 0.f;
+   }
+   __syncwarp();
+   warp_bitonic(np2, sx, sy, lane);
+   warp_bitonic(np2, sy, sr, lane);
+   uint32_t diff = 0;
+   for ( int i = lane; i < n; i += 32 )
+   {
+      const int tmp = (int)((float)(i + 1) - sr[i]);
+      diff += (uint32_t)(tmp * tmp);
+   }
+   for ( int o = 16; o > 0; o >>= 1 ) diff += __shfl_xor_sync(0xffffffffu, diff, o);
+   __syncwarp();
+   const int32_t denom = (int32_t)((uint32_t)n * ((uint32_t)n * (uint32_t)n - 1u));
+   return (float)(1.0 - 6.0 * (double)(int32_t)diff / (double)denom);
+}
+
+/* ------------------------------------------------------ lane-local fits */
+
+__device__ __forceinline__ float log_mvn(float x0, float x1, float m0, float m1, float a, float b, float c,
+                                         float nrm)
+{
+   /* calcLogMvNorm (pairwise_gmm.cpp:54-77) with the symmetric inverse [a b; b c] */
+   const float xm0 = x0 - m0;
+   const float xm1 = x1 - m1;
+   const float b0 = a * xm0 + b * xm1;
+   const float b1 = b * xm0 + c * xm1;
+   const float dot = xm0 * b0 + xm1 * b1;
+   return nrm - 0.5f * dot;
+}
+
+/* matrixInverse + prepareCovariance (pairwise_linalg.cpp:163-173, pairwise_gmm.cpp:31-47) */
+__device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, double c2, float& a, float& b,
+                                            float& c, float& nrm)
+{
+   const float det = s00 * s11 - s01 * s01;
+   a = s11 / det;
+   b = -s01 / det;
+   c = s00 / det;
+   if ( det <= 0 ) return false;
+   nrm = (float)(-0.5 * (c2 + (double)kinc_logf(det)));
+   return true;
+}
+
+/*
+ * GMM::fit for one pair on this lane (pairwise_gmm.cpp:367-445).  KT > 0
+ * fixes K at compile time; KT == 0 handles any K <= 64 from local memory.
+ * Per EM iteration it makes three passes over the samples: E (log-densities,
+ * per-sample log-sum-exp, logL, and the per-component maxima calcLogGammaK
+ * needs), M1 (per-component log-sum-exp of the responsibilities, and the mean
+ * sums) and M2 (covariance sums around the new means).  loggamma is never
+ * stored: M1/M2 recompute it bit-identically from the pre-update parameters
+ * and the stored per-sample log p(x).  Each accumulator is still summed in
+ * sample order, so every value equals the reference's.
+ */
+template <int KT>
+__device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn, LaneRng& rng, double c2,
+                        float& out_logL, float& out_E)
+{
+   constexpr int KA = KT > 0 ? KT : 64;
+   constexpr int UF = KT > 0 ? KT : 1;
+   const int K = KT > 0 ? KT : Kdyn;
+   float m0[KA], m1[KA], ia[KA], ib[KA], ic[KA], nrm[KA], logpi[KA];
+   float om0[KA], om1[KA], oa[KA], ob[KA], oc[KA], onrm[KA];
+
+   if ( rng.mode == 1 ) rng.lcg = 1;
+   {
+      float a0, b0, c0, n0;
+      prepare_cov(1.f, 0.f, 1.f, c2, a0, b0, c0, n0);
+      const float lp0 = kinc_logf(1.0f / K);
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k )
+      {
+         if ( k >= K ) break;
+         const int ii = rng.next() % N;
+         const float2 xv = X[ii * TILE];
+         m0[k] = xv.x;
+         m1[k] = xv.y;
+         ia[k] = a0; ib[k] = b0; ic[k] = c0; nrm[k] = n0;
+         logpi[k] = lp0;
+      }
+   }
+
+   float prevL = -INFINITY;
+   float curL = -INFINITY;
+   bool converged = false;
+   for ( int t = 0; t < 100; ++t )
+   {
+      /* ---- E step */
+      float logL = 0.0f;
+      float maxG[KA];
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k )
+      {
+         if ( k >= K ) break;
+         maxG[k] = -INFINITY;
+      }
+      for ( int i = 0; i < N; ++i )
+      {
+         const float2 xv = X[i * TILE];
+         float lg[KA];
+         float m = -INFINITY;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) break;
+            lg[k] = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]);
+            const float lp = logpi[k] + lg[k];
+            if ( lp > m ) m = lp;
+         }
+         float sum = 0.0f;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) break;
+            sum += kinc_expf((logpi[k] + lg[k]) - m);
+         }
+         const float logpx = m + kinc_logf(sum);
+         logL += logpx;
+         lpx[i * TILE] = logpx;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) break;
+            const float v = lg[k] + (-logpx);
+            if ( v > maxG[k] ) maxG[k] = v;
+         }
+      }
+      prevL = curL;
+      curL = logL;
+      if ( fabsf(curL - prevL) < 1e-8f )
+      {
+         converged = true;
+         break;
+      }
+
+      /* ---- M step, pass 1: logGamma sums and mean sums */
+      float sG[KA], a0[KA], a1[KA];
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k )
+      {
+         if ( k >= K ) break;
+         om0[k] = m0[k]; om1[k] = m1[k]; oa[k] = ia[k]; ob[k] = ib[k]; oc[k] = ic[k]; onrm[k] = nrm[k];
+         sG[k] = 0.f; a0[k] = 0.f; a1[k] = 0.f;
+      }
+      for ( int i = 0; i < N; ++i )
+      {
+         const float2 xv = X[i * TILE];
+         const float logpx = lpx[i * TILE];
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) break;
+            const float lgk = log_mvn(xv.x, xv.y, om0[k], om1[k], oa[k], ob[k], oc[k], onrm[k]) + (-logpx);
+            sG[k] += kinc_expf(lgk - maxG[k]);
+            const float g = kinc_expf(lgk);
+            a0[k] += g * xv.x;
+            a1[k] += g * xv.y;
+         }
+      }
+      float Gam[KA];
+      {
+         float logGamma[KA];
+         float mx = -INFINITY;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) break;
+            logGamma[k] = maxG[k] + kinc_logf(sG[k]);
+            const float arg = logpi[k] + logGamma[k];
+            if ( arg > mx ) mx = arg;
+         }
+         float s = 0.f;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) break;
+            s += kinc_expf((logpi[k] + logGamma[k]) - mx);
+         }
+         const float lgs = mx + kinc_logf(s);
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) break;
+            logpi[k] += logGamma[k] - lgs;
+            Gam[k] = kinc_expf(logGamma[k]);
+            const float sc = 1.0f / Gam[k];
+            m0[k] = a0[k] * sc;
+            m1[k] = a1[k] * sc;
+         }
+      }
+
+      /* ---- M step, pass 2: covariance sums around the new means */
+      float s00[KA], s01[KA], s11[KA];
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k )
+      {
+         if ( k >= K ) break;
+         s00[k] = 0.f; s01[k] = 0.f; s11[k] = 0.f;
+      }
+      for ( int i = 0; i < N; ++i )
+      {
+         const float2 xv = X[i * TILE];
+         const float logpx = lpx[i * TILE];
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) break;
+            const float lgk = log_mvn(xv.x, xv.y, om0[k], om1[k], oa[k], ob[k], oc[k], onrm[k]) + (-logpx);
+            const float g = kinc_expf(lgk);
+            const float xm0 = xv.x - m0[k];
+            const float xm1 = xv.y - m1[k];
+            s00[k] += g * (xm0 * xm0);
+            s01[k] += g * (xm0 * xm1);
+            s11[k] += g * (xm1 * xm1);
+         }
+      }
+      bool ok = true;
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k )
+      {
+         if ( k >= K ) break;
+         const float sc = 1.0f / Gam[k];
+         ok = prepare_cov(s00[k] * sc, s01[k] * sc, s11[k] * sc, c2, ia[k], ib[k], ic[k], nrm[k]) && ok;
+      }
+      if ( !ok ) return false;
+   }
+
+   /* ---- calcLabels + calcEntropy on what the reference's loggamma array holds:
+    * log(gamma/pi) of the last E step if EM converged, exp of it (from the
+    * pre-update parameters of the last iteration) if it ran out of iterations */
+   out_logL = curL;
+   float E = 0.f;
+   for ( int i = 0; i < N; ++i )
+   {
+      const float2 xv = X[i * TILE];
+      const float logpx = lpx[i * TILE];
+      int max_k = -1;
+      float max_g = -INFINITY;
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k )
+      {
+         if ( k >= K ) break;
+         float v;
+         if ( converged )
+         {
+            v = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
+         }
+         else
+         {
+            v = kinc_expf(log_mvn(xv.x, xv.y, om0[k], om1[k], oa[k], ob[k], oc[k], onrm[k]) + (-logpx));
+         }
+         if ( max_g < v )
+         {
+            max_k = k;
+            max_g = v;
+         }
+      }
+      wl[i * TILE] = (int8_t)max_k;
+      E += max_k >= 0 ? kinc_logf(max_g) : __int_as_float(0x7fc00000);
+   }
+   out_E = E;
+   return true;
+}
+
+/* vectorDiffNorm (pairwise_linalg.cpp:97-104) */
+__device__ __forceinline__ float diff_norm(float x0, float x1, float m0, float m1)
+{
+   float dist = 0;
+   dist += (x0 - m0) * (x0 - m0);
+   dist += (x1 - m1) * (x1 - m1);
+   return sqrtf(dist);
+}
+
+/* KMeans::fit for one pair on this lane (pairwise_kmeans.cpp:12-99).  The
+ * best run's labels end up in *best (a pointer into the three buffers). */
+template <int KT>
+__device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*& best, int N, int Kdyn,
+                            LaneRng& rng)
+{
+   constexpr int KA = KT > 0 ? KT : 64;
+   constexpr int UF = KT > 0 ? KT : 1;
+   const int K = KT > 0 ? KT : Kdyn;
+   float bestLogL = -INFINITY;
+   if ( rng.mode == 1 ) rng.lcg = 1;
+   for ( int init = 0; init < 10; ++init )
+   {
+      float mu0[KA], mu1[KA];
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k )
+      {
+         if ( k >= K ) break;
+         const int ii = rng.next() % N;
+         const float2 xv = X[ii * TILE];
+         mu0[k] = xv.x;
+         mu1[k] = xv.y;
+      }
+      int8_t* ya = cur;
+      int8_t* yb = nxt;
+      for ( int i = 0; i < N; ++i )
+      {
+         ya[i * TILE] = 0;
+         yb[i * TILE] = 0;
+      }
+      for ( int t = 0; t < 300; ++t )
+      {
+         bool same = true;
+         for ( int i = 0; i < N; ++i )
+         {
+            const float2 xv = X[i * TILE];
+            int min_k = -1;
+            float min_d = 0.f;
+#pragma unroll UF
+            for ( int k = 0; k < KA; ++k )
+            {
+               if ( k >= K ) break;
+               const float d = diff_norm(xv.x, xv.y, mu0[k], mu1[k]);
+               if ( min_k == -1 || d < min_d )
+               {
+                  min_k = k;
+                  min_d = d;
+               }
+            }
+            yb[i * TILE] = (int8_t)min_k;
+            same = same && (ya[i * TILE] == (int8_t)min_k);
+         }
+         if ( same ) break;
+         int8_t* tmp = ya;
+         ya = yb;
+         yb = tmp;
+         float s0[KA], s1[KA];
+         int nk[KA];
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) break;
+            s0[k] = 0.f; s1[k] = 0.f; nk[k] = 0;
+         }
+         for ( int i = 0; i < N; ++i )
+         {
+            const float2 xv = X[i * TILE];
+            const int8_t l = ya[i * TILE];
+#pragma unroll UF
+            for ( int k = 0; k < KA; ++k )
+            {
+               if ( k >= K ) break;
+               if ( l == k )
+               {
+                  s0[k] += xv.x;
+                  s1[k] += xv.y;
+                  nk[k]++;
+               }
+            }
+         }
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) break;
+            const float sc = 1.0f / nk[k];
+            mu0[k] = s0[k] * sc;
+            mu1[k] = s1[k] * sc;
+         }
+      }
+      /* computeLogLikelihood: one accumulator, cluster-major order */
+      float S = 0.f;
+      for ( int k = 0; k < K; ++k )
+      {
+         float c0 = 0.f, c1 = 0.f;
+#pragma unroll UF
+         for ( int kk = 0; kk < KA; ++kk )
+         {
+            if ( kk >= K ) break;
+            if ( kk == k ) { c0 = mu0[kk]; c1 = mu1[kk]; }
+         }
+         for ( int i = 0; i < N; ++i )
+         {
+            if ( ya[i * TILE] != k ) continue;
+            const float2 xv = X[i * TILE];
+            const float d = diff_norm(xv.x, xv.y, c0, c1);
+            S += d * d;
+         }
+      }
+      const float logL = -S;
+      /* keep the buffers distinct: cur/nxt are this run's, best the kept one */
+      if ( bestLogL < logL )
+      {
+         bestLogL = logL;
+         int8_t* old = best;
+         best = ya;
+         cur = (ya == cur) ? old : cur;
+         nxt = (ya == nxt) ? old : nxt;
+      }
+   }
+   return bestLogL;
+}
+
+} /* namespace kinc */

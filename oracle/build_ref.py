@@ -1,0 +1,87 @@
+"""Build recipe for the checkers under oracle/ (TEST INFRASTRUCTURE ONLY).
+
+* ``oracle/_build/libkinc_oracle.so`` -- the plain-C restatement
+  (kinc_oracle.c).  Builds anywhere (x86 container or the Arm GPU host).
+* ``oracle/_ref/libkinc_ref{0,1,2}.so`` -- KINC's own CPU Pairwise:: sources,
+  compiled unmodified from the KINC source tree with the stand-in ACE header
+  in ref_shim/ and the restated serial driver ref_driver.cpp.  Only built when
+  the KINC tree is present (``KINC_REFERENCE_DIR``, default /root/reference).
+  The suffix is the math resolution (ref_shim/ace/core/core.h): 0 = the
+  portable kinc_expf/kinc_logf the GPU uses, 1 = glibc float expf/logf,
+  2 = the C library's double functions.
+
+Everything is compiled with -ffp-contract=off so that x86 and Arm hosts give
+identical results (GCC contracts a*b+c into FMA on Arm by default).
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+REF_DIR = os.environ.get("KINC_REFERENCE_DIR", "/root/reference")
+REF_SOURCES = ["pairwise_linalg.cpp", "pairwise_clustering.cpp", "pairwise_gmm.cpp",
+               "pairwise_kmeans.cpp", "pairwise_correlation.cpp", "pairwise_pearson.cpp",
+               "pairwise_spearman.cpp"]
+FP_FLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC"]
+
+
+def _newer(target, sources):
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(s) <= t for s in sources)
+
+
+def build_oracle():
+    out_dir = os.path.join(HERE, "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libkinc_oracle.so")
+    srcs = [os.path.join(HERE, "kinc_oracle.c"), os.path.join(HERE, "kinc_oracle.h"),
+            os.path.join(REPO, "kinc_gb300", "csrc", "kinc_fmath.h")]
+    if _newer(out, srcs):
+        return out
+    cmd = ["gcc", "-std=c99", "-shared", *FP_FLAGS, "-o", out, srcs[0], "-lm", "-lpthread"]
+    subprocess.check_call(cmd)
+    return out
+
+
+def reference_available():
+    return os.path.isfile(os.path.join(REF_DIR, "src", "core", "pairwise_gmm.cpp"))
+
+
+def build_ref(math_mode=0):
+    """Compile the KINC Pairwise:: sources where they lie; returns the .so path or None."""
+    if not reference_available():
+        return None
+    core = os.path.join(REF_DIR, "src", "core")
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, f"libkinc_ref{math_mode}.so")
+    srcs = [os.path.join(core, s) for s in REF_SOURCES] + [os.path.join(HERE, "ref_driver.cpp")]
+    deps = srcs + [os.path.join(HERE, "ref_shim", "ace", "core", "core.h"),
+                   os.path.join(HERE, "ref_shim", "pre.h"),
+                   os.path.join(REPO, "kinc_gb300", "csrc", "kinc_fmath.h")]
+    if _newer(out, deps):
+        return out
+    cmd = ["g++", "-std=c++14", "-shared", *FP_FLAGS, "-w",
+           f"-DKINC_REF_MATH={math_mode}",
+           "-DCCMATRIX_H", "-DCORRELATIONMATRIX_H", "-DEXPRESSIONMATRIX_H",
+           "-include", os.path.join(HERE, "ref_shim", "pre.h"),
+           "-I", os.path.join(HERE, "ref_shim"), "-I", core,
+           "-I", os.path.join(REPO, "kinc_gb300", "csrc"),
+           "-o", out, *srcs]
+    subprocess.check_call(cmd)
+    return out
+
+
+def build_all():
+    paths = [build_oracle()]
+    for m in (0, 1, 2):
+        paths.append(build_ref(m))
+    return paths
+
+
+if __name__ == "__main__":
+    for p in build_all():
+        print(p if p else "reference tree not present: oracle/_ref not built", file=sys.stdout)

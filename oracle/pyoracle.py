@@ -1,0 +1,205 @@
+"""ctypes bindings for the CPU checkers (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+arm may import this module.  It wraps:
+
+* the C restatement (``libkinc_oracle.so``, built from kinc_oracle.c), and
+* KINC's own Pairwise:: sources compiled by build_ref.py
+  (``oracle/_ref/libkinc_ref{0,1,2}.so``), when the KINC tree was available
+  to build them.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_ref
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+class KoParams(ctypes.Structure):
+    _fields_ = [("clus_method", ctypes.c_int32), ("corr_method", ctypes.c_int32),
+                ("min_expr", ctypes.c_float), ("min_samples", ctypes.c_int32),
+                ("min_clusters", ctypes.c_int32), ("max_clusters", ctypes.c_int32),
+                ("criterion", ctypes.c_int32), ("pre_out", ctypes.c_int32),
+                ("post_out", ctypes.c_int32), ("min_corr", ctypes.c_float),
+                ("max_corr", ctypes.c_float), ("semantics", ctypes.c_int32),
+                ("rand_mode", ctypes.c_int32)]
+
+
+class KoRand(ctypes.Structure):
+    _fields_ = [("r", ctypes.c_uint32 * 34), ("head", ctypes.c_int32), ("drawn", ctypes.c_uint64)]
+
+
+_lib = None
+_ref = {}
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_ref.build_oracle()
+        L = ctypes.CDLL(path)
+        P = ctypes.POINTER
+        L.ko_rand_seed.argtypes = [P(KoRand), ctypes.c_uint32]
+        L.ko_rand_next.argtypes = [P(KoRand)]
+        L.ko_rand_next.restype = ctypes.c_int32
+        L.ko_rand_skip.argtypes = [P(KoRand), ctypes.c_uint64]
+        L.ko_libc_rand.argtypes = [ctypes.c_uint32, ctypes.c_int32, P(ctypes.c_int32)]
+        L.ko_draws_per_pair.argtypes = [P(KoParams)]
+        L.ko_draws_per_pair.restype = ctypes.c_int64
+        L.ko_count_qualifying.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, P(KoParams),
+                                          ctypes.c_int64]
+        L.ko_count_qualifying.restype = ctypes.c_int64
+        L.ko_run_block.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, P(KoParams), P(KoRand),
+                                   ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p]
+        L.ko_run_block.restype = ctypes.c_int
+        L.ko_run_segments_parallel.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, P(KoParams),
+                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_int32, ctypes.c_int32, P(ctypes.c_double)]
+        L.ko_run_segments_parallel.restype = ctypes.c_int64
+        L.ko_process_block.argtypes = [ctypes.c_int32, P(KoParams), ctypes.c_int64, ctypes.c_int64,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + \
+            [ctypes.c_void_p] * 8 + [P(ctypes.c_int64)]
+        L.ko_process_block.restype = ctypes.c_int64
+        L.ko_pearson_fp64.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                      ctypes.c_float, ctypes.c_int32]
+        L.ko_pearson_fp64.restype = ctypes.c_double
+        _lib = L
+    return _lib
+
+
+def ref_lib(math_mode=0):
+    """KINC's compiled Pairwise:: sources, or None if the KINC tree is absent."""
+    if math_mode not in _ref:
+        path = build_ref.build_ref(math_mode)
+        if path is None:
+            _ref[math_mode] = None
+        else:
+            L = ctypes.CDLL(path)
+            L.kinc_ref_run_block.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + \
+                [ctypes.c_int, ctypes.c_int, ctypes.c_float] + [ctypes.c_int] * 6 + \
+                [ctypes.c_int64, ctypes.c_int64, ctypes.c_uint64] + [ctypes.c_void_p] * 4
+            L.kinc_ref_run_block.restype = ctypes.c_int
+            _ref[math_mode] = L
+    return _ref[math_mode]
+
+
+DEFAULTS = dict(clus_method=0, corr_method=0, min_expr=float("-inf"), min_samples=30, min_clusters=1,
+                max_clusters=5, criterion=1, pre_out=0, post_out=0, min_corr=0.5, max_corr=1.0,
+                semantics=0, rand_mode=0)
+
+
+def params(**kw):
+    d = dict(DEFAULTS)
+    d.update(kw)
+    p = KoParams()
+    for k, v in d.items():
+        setattr(p, k, v)
+    return p
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def rand_position(gem, p, start):
+    """Draws a fresh serial KINC process has taken from rand() before pair `start`."""
+    L = lib()
+    G, S = gem.shape
+    per = L.ko_draws_per_pair(ctypes.byref(p))
+    if per == 0 or start == 0:
+        return 0
+    return per * L.ko_count_qualifying(_ptr(gem), G, S, ctypes.byref(p), start)
+
+
+def run_block(gem, p, start, size, rand_pos=None):
+    """The C restatement of Similarity::Serial::execute over [start, start+size)."""
+    L = lib()
+    gem = np.ascontiguousarray(gem, dtype=np.float32)
+    G, S = gem.shape
+    K = np.zeros(size, np.int8)
+    labels = np.zeros((size, S), np.int8)
+    corr = np.zeros((size, p.max_clusters), np.float32)
+    N = np.zeros(size, np.int32)
+    g = KoRand()
+    L.ko_rand_seed(ctypes.byref(g), 1)
+    pos = rand_position(gem, p, start) if rand_pos is None else rand_pos
+    L.ko_rand_skip(ctypes.byref(g), pos)
+    rc = L.ko_run_block(_ptr(gem), G, S, ctypes.byref(p), ctypes.byref(g), start, size, _ptr(K), _ptr(labels),
+                        _ptr(corr), _ptr(N))
+    if rc != 0:
+        raise ValueError("oracle rejected the arguments")
+    return K, labels, corr, N
+
+
+def run_ref(gem, p, start, size, math_mode=0, rand_pos=None):
+    """KINC's own models over [start, start+size), or None when not built."""
+    R = ref_lib(math_mode)
+    if R is None:
+        return None
+    gem = np.ascontiguousarray(gem, dtype=np.float32)
+    G, S = gem.shape
+    K = np.zeros(size, np.int8)
+    labels = np.zeros((size, S), np.int8)
+    corr = np.zeros((size, p.max_clusters), np.float32)
+    N = np.zeros(size, np.int32)
+    pos = rand_position(gem, p, start) if rand_pos is None else rand_pos
+    R.kinc_ref_run_block(_ptr(gem), G, S, p.clus_method, p.corr_method, p.min_expr, p.min_samples,
+                         p.min_clusters, p.max_clusters, p.criterion, p.pre_out, p.post_out, start, size, pos,
+                         _ptr(K), _ptr(labels), _ptr(corr), _ptr(N))
+    return K, labels, corr, N
+
+
+def process_block(S, p, start, K, labels, corr):
+    """Similarity::process restated: (cmx items, ccm items) as dicts of arrays."""
+    L = lib()
+    size = len(K)
+    cap = size * p.max_clusters
+    cx, cy, cc, cr = (np.zeros(cap, np.int32), np.zeros(cap, np.int32), np.zeros(cap, np.int8),
+                      np.zeros(cap, np.float32))
+    mx, my, mc, codes = (np.zeros(cap, np.int32), np.zeros(cap, np.int32), np.zeros(cap, np.int8),
+                         np.zeros((cap, S), np.int8))
+    n_ccm = ctypes.c_int64(0)
+    n_cmx = L.ko_process_block(S, ctypes.byref(p), start, size, _ptr(np.ascontiguousarray(K)),
+                               _ptr(np.ascontiguousarray(labels)), _ptr(np.ascontiguousarray(corr)),
+                               _ptr(cx), _ptr(cy), _ptr(cc), _ptr(cr), _ptr(mx), _ptr(my), _ptr(mc), _ptr(codes),
+                               ctypes.byref(n_ccm))
+    m = n_ccm.value
+    return (dict(x=cx[:n_cmx], y=cy[:n_cmx], c=cc[:n_cmx], r=cr[:n_cmx]),
+            dict(x=mx[:m], y=my[:m], c=mc[:m], codes=codes[:m]))
+
+
+def run_segments_parallel(gem, p, starts, sizes, threads):
+    """Time the restatement over segments with POSIX threads; returns (pairs, seconds)."""
+    L = lib()
+    gem = np.ascontiguousarray(gem, dtype=np.float32)
+    G, S = gem.shape
+    starts = np.ascontiguousarray(starts, dtype=np.int64)
+    sizes = np.ascontiguousarray(sizes, dtype=np.int64)
+    pos = np.array([rand_position(gem, p, int(s)) for s in starts], dtype=np.uint64)
+    secs = ctypes.c_double(0)
+    done = L.ko_run_segments_parallel(_ptr(gem), G, S, ctypes.byref(p), _ptr(starts), _ptr(sizes), _ptr(pos),
+                                      len(starts), threads, ctypes.byref(secs))
+    return done, secs.value
+
+
+def pearson_fp64(gem, x, y, min_expr=float("-inf"), min_samples=30):
+    gem = np.ascontiguousarray(gem, dtype=np.float32)
+    return lib().ko_pearson_fp64(_ptr(gem), gem.shape[1], x, y, min_expr, min_samples)
+
+
+def libc_rand(n, seed=1):
+    out = (ctypes.c_int32 * n)()
+    lib().ko_libc_rand(seed, n, out)
+    return np.frombuffer(out, dtype=np.int32).copy()
+
+
+def rand_stream(n, seed=1, skip=0):
+    L = lib()
+    g = KoRand()
+    L.ko_rand_seed(ctypes.byref(g), seed)
+    L.ko_rand_skip(ctypes.byref(g), skip)
+    return np.array([L.ko_rand_next(ctypes.byref(g)) for _ in range(n)], dtype=np.int32)

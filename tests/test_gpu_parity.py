@@ -1,0 +1,50 @@
+"""GPU parity: the CUDA worker against the oracle (the C restatement of the
+reference's serial path, itself pinned to KINC's compiled Pairwise:: code by
+test_oracle.py).  Integer outputs (K, N, labels) and correlations must match
+bit for bit: the worker repeats the reference's float operation sequence."""
+import numpy as np
+import pytest
+
+from kinc_gb300 import Similarity, synthetic
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # name, workload, genes, samples, start, size, gpu args, oracle args
+    ("gmm_spearman_bic_outliers", 2, 60, 120, 0, 1770,
+     dict(clusmethod="gmm", corrmethod="spearman", crit="BIC", preout=True, postout=True),
+     dict(clus_method=1, corr_method=1, criterion=0, pre_out=1, post_out=1)),
+    ("gmm_pearson_icl", 2, 60, 120, 100, 900,
+     dict(clusmethod="gmm", corrmethod="pearson", crit="ICL"),
+     dict(clus_method=1, corr_method=0, criterion=1)),
+    ("kmeans_pearson_bic", 4, 50, 160, 0, 1225,
+     dict(clusmethod="kmeans", corrmethod="pearson", crit="BIC", maxclus=3),
+     dict(clus_method=2, corr_method=0, criterion=0, max_clusters=3)),
+    ("none_pearson", 1, 300, 50, 0, 44850, dict(), dict()),
+    ("none_spearman", 1, 200, 70, 0, 19900, dict(corrmethod="spearman"), dict(corr_method=1)),
+    ("gmm_pearson_fixed_lcg", 2, 50, 100, 0, 1225,
+     dict(clusmethod="gmm", corrmethod="pearson", crit="BIC", semantics="fixed", rand="lcg", postout=True),
+     dict(clus_method=1, corr_method=0, criterion=0, semantics=1, rand_mode=1, post_out=1)),
+]
+
+
+def _corr_equal(a, b):
+    return np.array_equal(np.nan_to_num(a, nan=9.0), np.nan_to_num(b, nan=9.0))
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_gpu_matches_oracle(case):
+    name, wl, G, S, start, size, gargs, oargs = case
+    gem = synthetic.generate(wl, genes=G, samples=S)
+    sim = Similarity(gem, **gargs)
+    sim.initialize()
+    size = min(size, sim.total_pairs() - start)
+    res = sim.execute(None, start=start, size=size)
+    sim.close()
+    K, labels, corr, N = pyoracle.run_block(gem, pyoracle.params(**oargs), start, size)
+    assert np.array_equal(res.K, K), f"K differs on {(res.K != K).sum()} pairs"
+    multi = K > 1
+    assert np.array_equal(res.labels[multi], labels[multi])
+    diff = np.abs(np.nan_to_num(res.corr, nan=9.0) - np.nan_to_num(corr, nan=9.0))
+    assert _corr_equal(res.corr, corr), f"max |dr| {diff.max()} on {(diff > 0).sum()} entries"
