@@ -1,0 +1,330 @@
+"""Similarity benchmark: gene pairs/sec on the GMM(k<=5) + Spearman workload.
+
+Workload (the headline configuration): expression matrix 5,000 genes x 1,000
+samples float32, 10% NaN, 10 planted mixture modules (kinc_gb300.synthetic
+workload 2); clusmethod gmm, minclus 1, maxclus 5, crit BIC, preout + postout,
+minsamp 30, corrmethod spearman.  A "step" is one device block of pairs
+(--block, default 131,072 = 4 of KINC's 32,768-pair work blocks) taken in
+pair order; warm-up and timed steps walk consecutive blocks, so every timed
+pair is distinct.  Under torchrun every rank takes its own disjoint range of
+blocks (weak scaling, no collective on the data path).
+
+Lines printed by rank 0 (one JSON object):
+  value    pairs/s with the matrix already resident in HBM, timed with CUDA
+           events on the worker's stream (max over ranks);
+  e2e      the same through the C ABI with host buffers: kinc_sim_create
+           (host->device upload of the matrix) + kinc_sim_execute_block into
+           pinned host arrays (device->host K, labels, correlations);
+  roofline the similarity kernel's algorithmic FP32 rate;
+  cpu_baseline  the oracle (C restatement of KINC's serial path) on the host
+           cores over a bounded sample.
+--impl reference runs that CPU path as the timed arm instead.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOAD = dict(workload=2, clusmethod="gmm", corrmethod="spearman", minclus=1, maxclus=5, crit="BIC",
+                preout=True, postout=True, minsamp=30)
+ORACLE_ARGS = dict(clus_method=1, corr_method=1, min_clusters=1, max_clusters=5, criterion=0, pre_out=1,
+                   post_out=1, min_samples=30)
+# algorithmic cost of one GMM unit (sample, component, EM iteration): 40 FP32 flops
+FLOPS_PER_UNIT = 40
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.out = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.out.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(gem, threads, pairs_per_thread, seed):
+    """Time the oracle on `threads` segments of consecutive pairs, each starting
+    at a seeded random work-block boundary; returns (pairs/s, pairs, seconds)."""
+    from oracle import pyoracle
+    G = gem.shape[0]
+    total = G * (G - 1) // 2
+    nblocks = (total + 32767) // 32768
+    rng = np.random.default_rng(seed)
+    blocks = rng.choice(nblocks - 1, size=threads, replace=threads > nblocks - 1)
+    starts = blocks.astype(np.int64) * 32768
+    sizes = np.full(threads, pairs_per_thread, np.int64)
+    p = pyoracle.params(**ORACLE_ARGS)
+    done, secs = pyoracle.run_segments_parallel(gem, p, starts, sizes, threads)
+    return done / secs, int(done), secs
+
+
+def run_reference(args, gem):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    ppt = args.ref_pairs_per_thread
+    for i in range(args.warmup):
+        cpu_sample(gem, threads, ppt, seed=1000 + i)
+    tot_pairs, tot_secs = 0, 0.0
+    for i in range(args.steps):
+        _, n, s = cpu_sample(gem, threads, ppt, seed=2000 + i)
+        tot_pairs += n
+        tot_secs += s
+    value = tot_pairs / tot_secs
+    line = {
+        "impl": "reference", "metric": "gene pairs/sec", "value": value, "unit": "pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic (seeded; no public dataset)",
+        "config": config_dict(args, gem),
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": f"{threads} threads x {ppt} consecutive pairs from seeded random work blocks "
+                                   f"per step, oracle C restatement of KINC's serial path"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args, gem):
+    G, S = gem.shape
+    return {"workload": "GMM k<=5 + Spearman, GEM 5000x1000 float32, 10% NaN, 10 planted modules; "
+                        "BIC, preout+postout, minsamp 30",
+            "genes": G, "samples": S, "pairs_per_step": args.block, "global_batch": args.block,
+            "clusmethod": "gmm", "corrmethod": "spearman", "minclus": 1, "maxclus": 5, "crit": "BIC",
+            "semantics": "reference CPU path (bit-exact)", "l2": "256 MiB memset between steps"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--block", type=int, default=131072)
+    ap.add_argument("--ref-pairs-per-thread", type=int, default=24)
+    ap.add_argument("--cpu-pairs-per-thread", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+
+    from kinc_gb300 import synthetic
+    gem = synthetic.generate(WORKLOAD["workload"])
+
+    if args.impl == "reference":
+        if int(os.environ.get("WORLD_SIZE", "1")) > 1 and int(os.environ.get("RANK", "0")) != 0:
+            return
+        run_reference(args, gem)
+        return
+
+    import ctypes
+
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from kinc_gb300 import Similarity, _native
+    L = _native.load()
+    sim_args = {k: v for k, v in WORKLOAD.items() if k != "workload"}
+    G, S = gem.shape
+    total = G * (G - 1) // 2
+    B = args.block
+    nsteps = args.warmup + args.steps
+    per_rank = nsteps * B
+    if per_rank * world > total:
+        raise SystemExit(f"{world} ranks x {nsteps} steps x {B} pairs exceeds the {total} pairs of the workload")
+    base = rank * per_rank
+
+    sim = Similarity(gem, **sim_args)
+    sim.initialize()
+    ctx = sim._ctx
+    maxk = sim.params.max_clusters
+    dK = torch.empty(B, dtype=torch.int8, device="cuda")
+    dL = torch.empty((B, S), dtype=torch.int8, device="cuda")
+    dC = torch.empty((B, maxk), dtype=torch.float32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    vp = ctypes.c_void_p
+
+    def step(i):
+        flush.zero_()
+        rc = L.kinc_sim_execute_block_device(ctx, base + i * B, B, vp(dK.data_ptr()), vp(dL.data_ptr()),
+                                             vp(dC.data_ptr()), vp(stream.cuda_stream))
+        _native.check(rc, ctx)
+        return L.kinc_sim_last_launch_count(ctx)
+
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            step(i)
+        torch.cuda.synchronize()
+        counters = (ctypes.c_uint64 * 4)()
+        _native.check(L.kinc_sim_work_counters(ctx, counters, 1), ctx)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        launches = 0
+        for i in range(args.warmup, nsteps):
+            launches += step(i)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        ms = ev0.elapsed_time(ev1)
+        _native.check(L.kinc_sim_synchronize(ctx), ctx)
+        _native.check(L.kinc_sim_work_counters(ctx, counters, 1), ctx)
+    units, fits = int(counters[0]), int(counters[1])
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+    ms_max = float(t.item())
+    value = world * args.steps * B / (ms_max / 1e3)
+    sim.close()
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        hK = torch.empty(B, dtype=torch.int8, pin_memory=True)
+        hL = torch.empty((B, S), dtype=torch.int8, pin_memory=True)
+        hC = torch.empty((B, maxk), dtype=torch.float32, pin_memory=True)
+        gem_pinned = torch.from_numpy(gem).pin_memory()
+        e2e_steps = max(1, min(args.steps, 3))
+        e2e_base = base + args.warmup * B
+        params = _native.SimParams()
+        params_src = Similarity(gem, **sim_args).params
+        ctypes.memmove(ctypes.byref(params), ctypes.byref(params_src), ctypes.sizeof(params))
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c2 = ctypes.c_void_p()
+        _native.check(L.kinc_sim_create(vp(gem_pinned.data_ptr()), G, S, ctypes.byref(params), ctypes.byref(c2)))
+        for i in range(e2e_steps):
+            rc = L.kinc_sim_execute_block(c2, e2e_base + i * B, B, vp(hK.data_ptr()), vp(hL.data_ptr()),
+                                          vp(hC.data_ptr()))
+            _native.check(rc, c2)
+        L.kinc_sim_destroy(c2)
+        secs = time.perf_counter() - t0
+        tt = torch.tensor([secs], dtype=torch.float64, device="cuda")
+        if world > 1:
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        secs = float(tt.item())
+        e2e = {"value": world * e2e_steps * B / secs, "unit": "pairs/s",
+               "h2d_bytes_per_step": int(gem.nbytes // e2e_steps),
+               "d2h_bytes_per_step": int(B * (1 + S + 4 * maxk)),
+               "steps": e2e_steps,
+               "includes": "kinc_sim_create (matrix upload) + execute_block into pinned host arrays + destroy"}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    # ---- roofline of the similarity kernel (algorithmic FP32 flops of the EM units)
+    peaks_path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    sm_max = 2070.0
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as fh:
+            sm_max = float(json.load(fh).get("sm_max_mhz", sm_max))
+    props = torch.cuda.get_device_properties(local)
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    achieved = units * FLOPS_PER_UNIT / (ms / 1e3) / 1e12
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "k_similarity_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            tj = json.load(fh)
+        traffic = tj.get("bytes_per_pair", 0) * B * args.steps / max(1, args.steps)
+    roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak, "traffic": traffic,
+                "peak_source": f"nominal FP32 FMA rate: {props.multi_processor_count} SMs x 128 lanes x 2 flops x "
+                               f"{sm_max:.0f} MHz (MEASURED_PEAKS.json holds no FP32 figure)",
+                "kernel": "k_similarity", "units": units, "flops_per_unit": FLOPS_PER_UNIT, "fits": fits}
+
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, n, s = cpu_sample(gem, threads, args.cpu_pairs_per_thread, seed=7)
+        cpu = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port",
+               "sample": f"{n} pairs: {threads} threads x {args.cpu_pairs_per_thread} consecutive pairs from "
+                         f"seeded random work blocks, {s:.1f} s"}
+
+    line = {"metric": "gene pairs/sec", "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded; no public dataset)",
+            "config": config_dict(args, gem), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+            "cpu_baseline": cpu, "clocks": clk}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -143,6 +143,11 @@ int kinc_sim_pair_counts(kinc_sim_ctx* ctx, int64_t start, int64_t size, int32_t
 /* Kernel launches made by the last kinc_sim_execute_block* call (for accounting). */
 int32_t kinc_sim_last_launch_count(const kinc_sim_ctx* ctx);
 
+/* Work done since the last reset: out[0] = clustering model units (sum over
+ * fits of iterations x N x K), out[1] = fits run, out[2..3] reserved.
+ * Synchronises the context's stream. */
+int kinc_sim_work_counters(kinc_sim_ctx* ctx, uint64_t* out, int reset);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,6 +49,7 @@ SIGNATURES = {
                                               _I64, ctypes.POINTER(_I64)]),
     "kinc_sim_pair_counts": (ctypes.c_int, [_VP, _I64, _I64, _VP]),
     "kinc_sim_last_launch_count": (_I32, [_VP]),
+    "kinc_sim_work_counters": (ctypes.c_int, [_VP, _VP, ctypes.c_int]),
 }
 
 

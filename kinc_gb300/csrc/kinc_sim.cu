@@ -279,13 +279,14 @@ __device__ __forceinline__ float criterion_value(const DevParams& P, const DevDa
 
 template <int KT>
 __device__ bool lane_fit(const DevParams& P, const float2* X, float* lpx, int8_t*& wl, int8_t*& ya,
-                         int8_t*& yb, int8_t*& yc, int N, int K, LaneRng& rng, float& logL, float& E)
+                         int8_t*& yb, int8_t*& yc, int N, int K, LaneRng& rng, float& logL, float& E,
+                         unsigned long long& units)
 {
    if ( P.clus == 1 )
    {
-      return gmm_fit<KT>(X, lpx, wl, N, K, rng, P.c2, logL, E);
+      return gmm_fit<KT>(X, lpx, wl, N, K, rng, P.c2, logL, E, units);
    }
-   logL = kmeans_fit<KT>(X, ya, yb, yc, N, K, rng);
+   logL = kmeans_fit<KT>(X, ya, yb, yc, N, K, rng, units);
    E = 0.f;
    int8_t* t = wl;   /* the best labels become the work labels */
    wl = yc;
@@ -296,7 +297,8 @@ __device__ bool lane_fit(const DevParams& P, const float2* X, float* lpx, int8_t
 /* Clustering::compute (pairwise_clustering.cpp:23-103) minus the outlier
  * passes, for this lane's pair; labels merged into lbl. */
 __device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* X, float* lpx, int8_t* wl,
-                            int8_t* ya, int8_t* yb, int8_t* yc, int8_t* lbl, int N, LaneRng& rng)
+                            int8_t* ya, int8_t* yb, int8_t* yc, int8_t* lbl, int N, LaneRng& rng,
+                            unsigned long long& units, unsigned long long& fits)
 {
    int bestK = 0;
    if ( N < P.min_samples ) return 0;
@@ -307,14 +309,15 @@ __device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* 
       bool ok;
       switch ( K )
       {
-      case 1: ok = lane_fit<1>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
-      case 2: ok = lane_fit<2>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
-      case 3: ok = lane_fit<3>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
-      case 4: ok = lane_fit<4>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
-      case 5: ok = lane_fit<5>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
-      case 6: ok = lane_fit<6>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
-      default: ok = lane_fit<0>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E); break;
+      case 1: ok = lane_fit<1>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units); break;
+      case 2: ok = lane_fit<2>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units); break;
+      case 3: ok = lane_fit<3>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units); break;
+      case 4: ok = lane_fit<4>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units); break;
+      case 5: ok = lane_fit<5>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units); break;
+      case 6: ok = lane_fit<6>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units); break;
+      default: ok = lane_fit<0>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units); break;
       }
+      ++fits;
       if ( !ok ) continue;
       const float value = criterion_value(P, D, K, logL, N, E);
       if ( value < bestValue )
@@ -392,6 +395,7 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
 
       /* ---- lane-local: clustering */
       int K = 1;
+      unsigned long long units = 0, fits = 0;
       int64_t myp = p0 + lane;
       int32_t mx = 0, my = 0;
       if ( lane < npairs ) pair_xy(myp, mx, my);
@@ -406,7 +410,17 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
             rng.mode = P.rand_mode;
             rng.lcg = 1;
             K = lane_cluster(P, D, X + lane, lpx + lane, wl + lane, ya + lane, yb + lane, yc + lane,
-                             lbl + lane, myN, rng);
+                             lbl + lane, myN, rng, units, fits);
+         }
+         for ( int o = 16; o > 0; o >>= 1 )
+         {
+            units += __shfl_xor_sync(0xffffffffu, units, o);
+            fits += __shfl_xor_sync(0xffffffffu, fits, o);
+         }
+         if ( lane == 0 && B.work )
+         {
+            atomicAdd(&B.work[0], units);
+            atomicAdd(&B.work[1], fits);
          }
       }
       __syncwarp();
@@ -507,6 +521,7 @@ struct kinc_sim_ctx
    unsigned long long* d_bsum = nullptr;
    unsigned long long* d_qbase = nullptr;
    unsigned long long* d_tiles = nullptr;
+   unsigned long long* d_work = nullptr;
    int* d_status = nullptr;
    int8_t* d_K = nullptr;
    int8_t* d_labels = nullptr;
@@ -675,10 +690,21 @@ extern "C" int32_t kinc_sim_last_launch_count(const kinc_sim_ctx* ctx)
    return ctx ? ctx->launches : 0;
 }
 
+extern "C" int kinc_sim_work_counters(kinc_sim_ctx* ctx, uint64_t* out, int reset)
+{
+   if ( !ctx || !out ) return KINC_SIM_EINVAL;
+   CK(cudaStreamSynchronize(ctx->stream));
+   unsigned long long w[4];
+   CK(cudaMemcpy(w, ctx->d_work, sizeof w, cudaMemcpyDeviceToHost));
+   for ( int i = 0; i < 4; ++i ) out[i] = w[i];
+   if ( reset ) CK(cudaMemset(ctx->d_work, 0, sizeof w));
+   return KINC_SIM_OK;
+}
+
 static void release(kinc_sim_ctx* c)
 {
    void* ptrs[] = { c->d_gem, c->d_umask, c->d_logn, c->d_jump, c->d_rng0, c->d_N, c->d_pg, c->d_qpos,
-                    c->d_bsum, c->d_qbase, c->d_tiles, c->d_status, c->d_K, c->d_labels, c->d_corr,
+                    c->d_bsum, c->d_qbase, c->d_tiles, c->d_work, c->d_status, c->d_K, c->d_labels, c->d_corr,
                     c->d_scratch };
    for ( void* p : ptrs )
       if ( p ) cudaFree(p);
@@ -839,6 +865,8 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    CKC(cudaMalloc(&ctx->d_bsum, (nscan + 1) * sizeof(unsigned long long)));
    CKC(cudaMalloc(&ctx->d_qbase, sizeof(unsigned long long)));
    CKC(cudaMalloc(&ctx->d_tiles, sizeof(unsigned long long)));
+   CKC(cudaMalloc(&ctx->d_work, 4 * sizeof(unsigned long long)));
+   CKC(cudaMemsetAsync(ctx->d_work, 0, 4 * sizeof(unsigned long long), ctx->stream));
    CKC(cudaMalloc(&ctx->d_status, sizeof(int)));
    CKC(cudaMalloc(&ctx->d_K, ctx->max_block));
    CKC(cudaMalloc(&ctx->d_labels, (size_t)ctx->max_block * S));
@@ -912,6 +940,7 @@ static int enqueue_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t*
    B.outCorr = d_corr;
    B.tiles = ctx->d_tiles;
    B.status = ctx->d_status;
+   B.work = ctx->d_work;
    k_similarity<<<ctx->grid, WARPS_PER_BLOCK * 32, ctx->smem_bytes, st>>>(dp, ctx->dd, ctx->ds, B,
                                                                            ctx->smem_sort);
    ++launches;

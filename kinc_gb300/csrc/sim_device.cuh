@@ -88,6 +88,8 @@ struct DevBlock
    float* outCorr;                  /* [p - start][max_k] */
    unsigned long long* tiles;       /* tile queue counter */
    int* status;
+   unsigned long long* work;        /* [0] model units: sum over fits of iterations x N x K;
+                                       [1] fits run */
 };
 
 /* ------------------------------------------------------------- helpers */
@@ -386,7 +388,7 @@ __device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, dou
  */
 template <int KT>
 __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn, LaneRng& rng, double c2,
-                        float& out_logL, float& out_E)
+                        float& out_logL, float& out_E, unsigned long long& units)
 {
    constexpr int KA = KT > 0 ? KT : 64;
    constexpr int UF = KT > 0 ? KT : 1;
@@ -417,6 +419,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
    bool converged = false;
    for ( int t = 0; t < 100; ++t )
    {
+      units += (unsigned long long)N * K;
       /* ---- E step */
       float logL = 0.0f;
       float maxG[KA];
@@ -607,7 +610,7 @@ __device__ __forceinline__ float diff_norm(float x0, float x1, float m0, float m
  * best run's labels end up in *best (a pointer into the three buffers). */
 template <int KT>
 __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*& best, int N, int Kdyn,
-                            LaneRng& rng)
+                            LaneRng& rng, unsigned long long& units)
 {
    constexpr int KA = KT > 0 ? KT : 64;
    constexpr int UF = KT > 0 ? KT : 1;
@@ -635,6 +638,7 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
       }
       for ( int t = 0; t < 300; ++t )
       {
+         units += (unsigned long long)N * K;
          bool same = true;
          for ( int i = 0; i < N; ++i )
          {

@@ -864,7 +864,14 @@ int ko_run_block(const float* gem, int32_t G, int32_t S, const ko_params* p, ko_
    {
       const float* g1 = gem + (int64_t)x * S;
       const float* g2 = gem + (int64_t)y * S;
-      const int N = fetch_pair(gem, S, x, y, p->min_expr, w.X, w.labels);
+      int N;
+      if ( q > 0 && (start + q) % 32768 == 0 )
+      {
+         /* a new work block: Serial::execute starts from fresh zeroed arrays */
+         memset(w.X, 0, (size_t)S * sizeof(v2));
+         memset(w.labels, 0, (size_t)S);
+      }
+      N = fetch_pair(gem, S, x, y, p->min_expr, w.X, w.labels);
       int K = 1;
       int k;
       if ( p->clus_method != 0 )

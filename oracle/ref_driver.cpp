@@ -11,7 +11,9 @@
  * The models are the reference's: Pairwise::GMM, Pairwise::KMeans,
  * Pairwise::Pearson, Pairwise::Spearman.  rand() is the C library's, reset
  * with srand(1) and advanced by `rand_skip` draws, which puts it where a
- * fresh serial KINC process would be at the block start.
+ * fresh serial KINC process would be at the block start.  A call may span
+ * several work blocks; the workspaces are renewed at each block boundary as
+ * they are when ACE calls Serial::execute once per block.
  */
 #include "pairwise_gmm.h"
 #include "pairwise_kmeans.h"
@@ -108,6 +110,12 @@ extern "C" int kinc_ref_run_block(const float* gem, int G, int S, int clus_metho
    decode(start, x, y);
    for ( int64_t q = 0; q < size; ++q )
    {
+      if ( q > 0 && (start + q) % 32768 == 0 )
+      {
+         /* Similarity::Serial::execute runs once per work block with fresh workspaces */
+         X = QVector<Pairwise::Vector2>(S);
+         labels = QVector<qint8>(S);
+      }
       int numSamples = fetchPair(gem, S, x, y, min_expr, X, labels);
       qint8 K { 1 };
       if ( clus )

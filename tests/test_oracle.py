@@ -138,3 +138,14 @@ def test_process_matches_reference_rules():
         c = cmx["c"][key == k]
         assert np.array_equal(c, np.arange(len(c)))
     assert set(np.unique(ccm["codes"])) <= {0, 1, 6, 7, 8, 9}
+
+
+def test_work_block_boundary_renews_packed_array():
+    """Serial::execute runs once per 32768-pair work block with fresh arrays:
+    a call spanning two blocks equals the two blocks run separately."""
+    gem = synthetic.generate(1, genes=260, samples=36)
+    p = pyoracle.params()
+    both = pyoracle.run_block(gem, p, 32000, 1600)
+    first = pyoracle.run_block(gem, p, 32000, 768)
+    second = pyoracle.run_block(gem, p, 32768, 832)
+    assert same_corr(both[2][:768], first[2]) and same_corr(both[2][768:], second[2])
