@@ -23,6 +23,9 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 # (source, extra flags)
 UNITS = [
     ("kinc_sim.cu", ["--fmad=false"]),
+    ("sim_none.cu", ["--fmad=false"]),
+    ("sim_gmm.cu", ["--fmad=false"]),
+    ("sim_kmeans.cu", ["--fmad=false"]),
     ("pearson_gemm.cu", []),
 ]
 

@@ -80,8 +80,8 @@ KINC_HD float kinc_u2f(uint32_t u)
 #endif
 }
 
-/* e^x, single precision. */
-KINC_HD float kinc_expf(float x)
+/* slow path of kinc_expf: NaN, overflow, underflow and subnormal results */
+KINC_HD float kinc_expf_tail(float x, float n, float p)
 {
    if ( !(x == x) )
    {
@@ -95,21 +95,6 @@ KINC_HD float kinc_expf(float x)
    {
       return 0.0f;
    }
-
-   const float n = KINC_RINTF(x * KINC_F_LOG2E);
-   float r = KINC_FMAF(-n, KINC_F_LN2_HI, x);
-   r = KINC_FMAF(-n, KINC_F_LN2_LO, r);
-
-   /* 1 + r + r^2/2! + ... + r^7/7! */
-   float p = 1.98412698412698412698e-4f;                /* 1/5040 */
-   p = KINC_FMAF(p, r, 1.38888888888888888889e-3f);     /* 1/720 */
-   p = KINC_FMAF(p, r, 8.33333333333333333333e-3f);     /* 1/120 */
-   p = KINC_FMAF(p, r, 4.16666666666666666667e-2f);     /* 1/24 */
-   p = KINC_FMAF(p, r, 1.66666666666666666667e-1f);     /* 1/6 */
-   p = KINC_FMAF(p, r, 0.5f);
-   p = KINC_FMAF(p, r, 1.0f);
-   p = KINC_FMAF(p, r, 1.0f);
-
    const int in = (int)n;
    if ( in >= -126 && in <= 127 )
    {
@@ -124,36 +109,36 @@ KINC_HD float kinc_expf(float x)
    return (p * kinc_u2f((uint32_t)(in + 64 + 127) << 23)) * kinc_u2f((uint32_t)(-64 + 127) << 23);
 }
 
-/* natural logarithm, single precision. */
-KINC_HD float kinc_logf(float x)
+/* e^x, single precision. */
+KINC_HD float kinc_expf(float x)
 {
-   if ( !(x == x) )
-   {
-      return x + x;
-   }
-   if ( x < 0.0f )
-   {
-      return kinc_u2f(0x7fc00000u);
-   }
-   if ( x == 0.0f )
-   {
-      return kinc_u2f(0xff800000u);
-   }
-   if ( x == kinc_u2f(0x7f800000u) )
-   {
-      return x;
-   }
+   const float n = KINC_RINTF(x * KINC_F_LOG2E);
+   float r = KINC_FMAF(-n, KINC_F_LN2_HI, x);
+   r = KINC_FMAF(-n, KINC_F_LN2_LO, r);
 
-   uint32_t b = kinc_f2u(x);
-   int e = 0;
-   if ( b < 0x00800000u )
+   /* 1 + r + r^2/2! + ... + r^7/7! */
+   float p = 1.98412698412698412698e-4f;                /* 1/5040 */
+   p = KINC_FMAF(p, r, 1.38888888888888888889e-3f);     /* 1/720 */
+   p = KINC_FMAF(p, r, 8.33333333333333333333e-3f);     /* 1/120 */
+   p = KINC_FMAF(p, r, 4.16666666666666666667e-2f);     /* 1/24 */
+   p = KINC_FMAF(p, r, 1.66666666666666666667e-1f);     /* 1/6 */
+   p = KINC_FMAF(p, r, 0.5f);
+   p = KINC_FMAF(p, r, 1.0f);
+   p = KINC_FMAF(p, r, 1.0f);
+
+   /* |x| <= 87 keeps n in [-126, 126]: 2^n is a normal float and the product
+    * rounds once (NaN fails the comparison and takes the tail) */
+   if ( x <= 87.0f && x >= -87.0f )
    {
-      /* subnormal: scale into the normal range first (exact) */
-      x = x * 8388608.0f;
-      b = kinc_f2u(x);
-      e = -23;
+      return p * kinc_u2f((uint32_t)((int)n + 127) << 23);
    }
-   e += (int)(b >> 23) - 127;
+   return kinc_expf_tail(x, n, p);
+}
+
+/* natural logarithm of the positive normal float with bits b, times 2^eoff */
+KINC_HD float kinc_logf_normal(uint32_t b, int eoff)
+{
+   int e = (int)(b >> 23) - 127 + eoff;
    float m = kinc_u2f((b & 0x007fffffu) | 0x3f800000u);
    if ( m > KINC_F_SQRT2 )
    {
@@ -177,6 +162,34 @@ KINC_HD float kinc_logf(float x)
    const float small = KINC_FMAF(s, hfsq + R, ef * KINC_F_LN2_LO);
    const float logm = f - (hfsq - small);
    return KINC_FMAF(ef, KINC_F_LN2_HI, logm);
+}
+
+/* natural logarithm, single precision. */
+KINC_HD float kinc_logf(float x)
+{
+   const uint32_t b = kinc_f2u(x);
+   if ( b - 0x00800000u < 0x7f000000u )
+   {
+      return kinc_logf_normal(b, 0);
+   }
+   if ( !(x == x) )
+   {
+      return x + x;
+   }
+   if ( x < 0.0f )
+   {
+      return kinc_u2f(0x7fc00000u);
+   }
+   if ( x == 0.0f )
+   {
+      return kinc_u2f(0xff800000u);
+   }
+   if ( x == kinc_u2f(0x7f800000u) )
+   {
+      return x;
+   }
+   /* subnormal: scale into the normal range first (exact) */
+   return kinc_logf_normal(kinc_f2u(x * 8388608.0f), -23);
 }
 
 #endif

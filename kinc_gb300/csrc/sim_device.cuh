@@ -121,7 +121,7 @@ __device__ __forceinline__ int next_pow2(int n)
 /* Spearman::bitonicSort network (pairwise_spearman.cpp:109-134) executed by a
  * warp: every stage's compare-exchanges touch disjoint slots, so running them
  * in parallel performs exactly the reference's sequence of swaps. */
-__device__ void warp_bitonic(int size, float* key, float* extra, int lane)
+__device__ inline void warp_bitonic(int size, float* key, float* extra, int lane)
 {
    const int bsize = size / 2;
    for ( int ob = 2; ob <= size; ob *= 2 )
@@ -183,7 +183,7 @@ struct LaneRng
 
 /* Jump the glibc state to output position `pos` (warp-cooperative: lane r < 31
  * holds word r) and store it interleaved for lane `slot`. */
-__device__ void warp_rng_jump(const DevData& D, uint64_t pos, uint32_t* ring, int slot, int lane)
+__device__ inline void warp_rng_jump(const DevData& D, uint64_t pos, uint32_t* ring, int slot, int lane)
 {
    uint32_t s = lane < RNG_WORDS ? D.rng0[lane] : 0u;
    for ( int b = 0; b < RNG_BITS && pos; ++b, pos >>= 1 )
@@ -204,7 +204,7 @@ __device__ void warp_rng_jump(const DevData& D, uint64_t pos, uint32_t* ring, in
 /* ------------------------------------------------------ warp-coop steps */
 
 /* fetchPair for pair (x, y) into column `j` of the tile's interleaved arrays. */
-__device__ int warp_fetch(const DevParams& P, const DevData& D, int32_t x, int32_t y, float2* X,
+__device__ inline int warp_fetch(const DevParams& P, const DevData& D, int32_t x, int32_t y, float2* X,
                           int8_t* lbl, int j, int lane)
 {
    const float* g1 = D.gem + (size_t)x * P.S;
@@ -234,7 +234,7 @@ __device__ int warp_fetch(const DevParams& P, const DevData& D, int32_t x, int32
 
 /* Clustering::markOutliers on column j of the tile (labels by sample position
  * i < N, values from the packed array at i, as in the reference). */
-__device__ void warp_mark_outliers(const float2* X, int N, int col, int8_t* lbl, int8_t cluster,
+__device__ inline void warp_mark_outliers(const float2* X, int N, int col, int8_t* lbl, int8_t cluster,
                                    int8_t marker, float* buf, int j, int lane)
 {
    int n = 0;
@@ -284,7 +284,7 @@ __device__ void warp_mark_outliers(const float2* X, int N, int col, int8_t* lbl,
 }
 
 /* Spearman::computeCluster for column j, cluster k. */
-__device__ float warp_spearman(const DevParams& P, const DevData& D, const float2* X, const int8_t* lbl,
+__device__ inline float warp_spearman(const DevParams& P, const DevData& D, const float2* X, const int8_t* lbl,
                                int32_t x, int32_t y, int8_t k, float* buf, int j, int lane)
 {
    float* sx = buf;
@@ -382,9 +382,13 @@ __device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, dou
  * per-sample log-sum-exp, logL, and the per-component maxima calcLogGammaK
  * needs), M1 (per-component log-sum-exp of the responsibilities, and the mean
  * sums) and M2 (covariance sums around the new means).  loggamma is never
- * stored: M1/M2 recompute it bit-identically from the pre-update parameters
- * and the stored per-sample log p(x).  Each accumulator is still summed in
- * sample order, so every value equals the reference's.
+ * stored: M1/M2 recompute it bit-identically from the parameters of the E
+ * step (the inverse covariances and normalisers only change after M2, the new
+ * means are held apart until then) and the stored per-sample log p(x).  Each
+ * accumulator is still summed in sample order, so every value equals the
+ * reference's.  The update of the last iteration is only checked (a
+ * non-positive determinant still fails the fit), since the reference labels
+ * samples with that iteration's E-step responsibilities.
  */
 template <int KT>
 __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn, LaneRng& rng, double c2,
@@ -394,7 +398,6 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
    constexpr int UF = KT > 0 ? KT : 1;
    const int K = KT > 0 ? KT : Kdyn;
    float m0[KA], m1[KA], ia[KA], ib[KA], ic[KA], nrm[KA], logpi[KA];
-   float om0[KA], om1[KA], oa[KA], ob[KA], oc[KA], onrm[KA];
 
    if ( rng.mode == 1 ) rng.lcg = 1;
    {
@@ -429,9 +432,11 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
          if ( k >= K ) break;
          maxG[k] = -INFINITY;
       }
+      float2 xn = X[0];
       for ( int i = 0; i < N; ++i )
       {
-         const float2 xv = X[i * TILE];
+         const float2 xv = xn;
+         if ( i + 1 < N ) xn = X[(i + 1) * TILE];
          float lg[KA];
          float m = -INFINITY;
 #pragma unroll UF
@@ -469,31 +474,37 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
       }
 
       /* ---- M step, pass 1: logGamma sums and mean sums */
-      float sG[KA], a0[KA], a1[KA];
-#pragma unroll UF
-      for ( int k = 0; k < KA; ++k )
+      float nm0[KA], nm1[KA], Gam[KA];
       {
-         if ( k >= K ) break;
-         om0[k] = m0[k]; om1[k] = m1[k]; oa[k] = ia[k]; ob[k] = ib[k]; oc[k] = ic[k]; onrm[k] = nrm[k];
-         sG[k] = 0.f; a0[k] = 0.f; a1[k] = 0.f;
-      }
-      for ( int i = 0; i < N; ++i )
-      {
-         const float2 xv = X[i * TILE];
-         const float logpx = lpx[i * TILE];
+         float sG[KA];
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
             if ( k >= K ) break;
-            const float lgk = log_mvn(xv.x, xv.y, om0[k], om1[k], oa[k], ob[k], oc[k], onrm[k]) + (-logpx);
-            sG[k] += kinc_expf(lgk - maxG[k]);
-            const float g = kinc_expf(lgk);
-            a0[k] += g * xv.x;
-            a1[k] += g * xv.y;
+            sG[k] = 0.f; nm0[k] = 0.f; nm1[k] = 0.f;
          }
-      }
-      float Gam[KA];
-      {
+         xn = X[0];
+         float ln = lpx[0];
+         for ( int i = 0; i < N; ++i )
+         {
+            const float2 xv = xn;
+            const float logpx = ln;
+            if ( i + 1 < N )
+            {
+               xn = X[(i + 1) * TILE];
+               ln = lpx[(i + 1) * TILE];
+            }
+#pragma unroll UF
+            for ( int k = 0; k < KA; ++k )
+            {
+               if ( k >= K ) break;
+               const float lgk = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
+               sG[k] += kinc_expf(lgk - maxG[k]);
+               const float g = kinc_expf(lgk);
+               nm0[k] += g * xv.x;
+               nm1[k] += g * xv.y;
+            }
+         }
          float logGamma[KA];
          float mx = -INFINITY;
 #pragma unroll UF
@@ -519,8 +530,8 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
             logpi[k] += logGamma[k] - lgs;
             Gam[k] = kinc_expf(logGamma[k]);
             const float sc = 1.0f / Gam[k];
-            m0[k] = a0[k] * sc;
-            m1[k] = a1[k] * sc;
+            nm0[k] = nm0[k] * sc;
+            nm1[k] = nm1[k] * sc;
          }
       }
 
@@ -532,37 +543,51 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
          if ( k >= K ) break;
          s00[k] = 0.f; s01[k] = 0.f; s11[k] = 0.f;
       }
+      xn = X[0];
+      float ln = lpx[0];
       for ( int i = 0; i < N; ++i )
       {
-         const float2 xv = X[i * TILE];
-         const float logpx = lpx[i * TILE];
+         const float2 xv = xn;
+         const float logpx = ln;
+         if ( i + 1 < N )
+         {
+            xn = X[(i + 1) * TILE];
+            ln = lpx[(i + 1) * TILE];
+         }
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
             if ( k >= K ) break;
-            const float lgk = log_mvn(xv.x, xv.y, om0[k], om1[k], oa[k], ob[k], oc[k], onrm[k]) + (-logpx);
+            const float lgk = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
             const float g = kinc_expf(lgk);
-            const float xm0 = xv.x - m0[k];
-            const float xm1 = xv.y - m1[k];
+            const float xm0 = xv.x - nm0[k];
+            const float xm1 = xv.y - nm1[k];
             s00[k] += g * (xm0 * xm0);
             s01[k] += g * (xm0 * xm1);
             s11[k] += g * (xm1 * xm1);
          }
       }
       bool ok = true;
+      const bool last = t == 99;
 #pragma unroll UF
       for ( int k = 0; k < KA; ++k )
       {
          if ( k >= K ) break;
          const float sc = 1.0f / Gam[k];
-         ok = prepare_cov(s00[k] * sc, s01[k] * sc, s11[k] * sc, c2, ia[k], ib[k], ic[k], nrm[k]) && ok;
+         float a, b, c, n;
+         ok = prepare_cov(s00[k] * sc, s01[k] * sc, s11[k] * sc, c2, a, b, c, n) && ok;
+         if ( !last )
+         {
+            m0[k] = nm0[k]; m1[k] = nm1[k];
+            ia[k] = a; ib[k] = b; ic[k] = c; nrm[k] = n;
+         }
       }
       if ( !ok ) return false;
    }
 
    /* ---- calcLabels + calcEntropy on what the reference's loggamma array holds:
-    * log(gamma/pi) of the last E step if EM converged, exp of it (from the
-    * pre-update parameters of the last iteration) if it ran out of iterations */
+    * log(gamma/pi) of the last E step if EM converged, exp of it if it ran out
+    * of iterations (the parameters still are that E step's in both cases) */
    out_logL = curL;
    float E = 0.f;
    for ( int i = 0; i < N; ++i )
@@ -575,15 +600,8 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
       for ( int k = 0; k < KA; ++k )
       {
          if ( k >= K ) break;
-         float v;
-         if ( converged )
-         {
-            v = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
-         }
-         else
-         {
-            v = kinc_expf(log_mvn(xv.x, xv.y, om0[k], om1[k], oa[k], ob[k], oc[k], onrm[k]) + (-logpx));
-         }
+         float v = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
+         if ( !converged ) v = kinc_expf(v);
          if ( max_g < v )
          {
             max_k = k;

@@ -1,0 +1,354 @@
+/*
+ * sim_kernel.cuh -- the per-pair Similarity kernel, specialised by
+ * clustering method (CLUS: 0 none, 1 GMM, 2 K-means) and by the largest
+ * cluster count compiled with static register arrays (KS = 3 or 5: every
+ * fit keeps its per-component state in registers, the host picks KS >=
+ * maxclus; KS = 0: the generic local-memory form for any maxclus <= 64).
+ * Each specialisation is instantiated in its own translation unit
+ * (sim_none.cu, sim_gmm.cu, sim_kmeans.cu) so the register budget of one
+ * does not constrain the others.  Blocks of 4 warps are limited to 128
+ * registers per thread so 16 warps stay resident per SM.
+ */
+#pragma once
+
+#include "sim_device.cuh"
+
+namespace kinc {
+
+constexpr int WARPS_PER_BLOCK = 4;
+#ifndef KINC_MIN_BLOCKS
+#define KINC_MIN_BLOCKS 4
+#endif
+
+/* The i-th usable sample (0-based) of pair c: what the reference left in its
+ * packed array at position i. */
+__device__ inline float2 packed_sample(const DevParams& P, const DevData& D, int64_t c, int i)
+{
+   int32_t x, y;
+   pair_xy(c, x, y);
+   const uint32_t* mx = D.umask + (size_t)x * P.W;
+   const uint32_t* my = D.umask + (size_t)y * P.W;
+   for ( int w = 0; w < P.W; ++w )
+   {
+      uint32_t m = mx[w] & my[w];
+      const int cnt = __popc(m);
+      if ( i < cnt )
+      {
+         for ( int r = 0; r < i; ++r ) m &= m - 1;
+         const int s = w * 32 + (__ffs(m) - 1);
+         return make_float2(D.gem[(size_t)x * P.S + s], D.gem[(size_t)y * P.S + s]);
+      }
+      i -= cnt;
+   }
+   return make_float2(0.f, 0.f);
+}
+
+/* Pearson::computeCluster for this lane's pair (pairwise_pearson.cpp:12-52). */
+__device__ inline float lane_pearson(const DevParams& P, const DevData& D, const DevBlock& B, const float2* X,
+                                     const int8_t* lbl, int64_t p, int32_t x, int32_t y, int N, int8_t k)
+{
+   int n = 0;
+   float sumx = 0, sumy = 0, sumx2 = 0, sumy2 = 0, sumxy = 0;
+   if ( P.semantics == 0 )
+   {
+      /* positions i < N read the pair's own packed array at i; positions i >= N
+       * read what the last earlier pair of the work block with more than i
+       * usable samples left there (zero if none) */
+      for ( int i = 0; i < N; ++i )
+      {
+         if ( lbl[i * TILE] == k )
+         {
+            const float2 v = X[i * TILE];
+            sumx += v.x; sumy += v.y; sumx2 += v.x * v.x; sumy2 += v.y * v.y; sumxy += v.x * v.y;
+            ++n;
+         }
+      }
+      int32_t c = B.pg[p - B.lo];
+      for ( int i = N; i < P.S; ++i )
+      {
+         if ( lbl[i * TILE] != k ) continue;
+         while ( c >= 0 && B.N[c] <= i ) c = B.pg[c];
+         const float2 v = c >= 0 ? packed_sample(P, D, B.lo + c, i) : make_float2(0.f, 0.f);
+         sumx += v.x; sumy += v.y; sumx2 += v.x * v.x; sumy2 += v.y * v.y; sumxy += v.x * v.y;
+         ++n;
+      }
+   }
+   else
+   {
+      const float* g1 = D.gem + (size_t)x * P.S;
+      const float* g2 = D.gem + (size_t)y * P.S;
+      for ( int i = 0; i < P.S; ++i )
+      {
+         if ( lbl[i * TILE] == k )
+         {
+            const float vx = g1[i];
+            const float vy = g2[i];
+            sumx += vx; sumy += vy; sumx2 += vx * vx; sumy2 += vy * vy; sumxy += vx * vy;
+            ++n;
+         }
+      }
+   }
+   if ( n >= P.min_samples )
+   {
+      return (n * sumxy - sumx * sumy) / sqrtf((n * sumx2 - sumx * sumx) * (n * sumy2 - sumy * sumy));
+   }
+   return __int_as_float(0x7fc00000);
+}
+
+/* computeBIC / computeICL (pairwise_clustering.cpp:155-172): log of the int N
+ * is double, 2*logL is float, the difference is double, the result float. */
+__device__ __forceinline__ float criterion_value(const DevParams& P, const DevData& D, int K, float logL, int N,
+                                                 float E)
+{
+   const int pp = K * (1 + 2 + 2 * 2);
+   double v = D.logn[N] * (double)pp - (double)(2.0f * logL);
+   if ( P.criterion == 1 ) v = v - (double)(2.0f * E);
+   return (float)v;
+}
+
+template <int CLUS, int KT>
+__device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, float* lpx, int8_t*& wl,
+                                         int8_t*& ya, int8_t*& yb, int8_t*& yc, int N, int K, LaneRng& rng,
+                                         float& logL, float& E, unsigned long long& units)
+{
+   if ( CLUS == 1 )
+   {
+      return gmm_fit<KT>(X, lpx, wl, N, K, rng, P.c2, logL, E, units);
+   }
+   logL = kmeans_fit<KT>(X, ya, yb, yc, N, K, rng, units);
+   E = 0.f;
+   int8_t* t = wl;   /* the best labels become the work labels */
+   wl = yc;
+   yc = t;
+   return true;
+}
+
+/* Clustering::compute (pairwise_clustering.cpp:23-103) minus the outlier
+ * passes, for this lane's pair; labels merged into lbl. */
+template <int CLUS, int KS>
+__device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* X, float* lpx, int8_t* wl,
+                            int8_t* ya, int8_t* yb, int8_t* yc, int8_t* lbl, int N, LaneRng& rng,
+                            unsigned long long& units, unsigned long long& fits)
+{
+   int bestK = 0;
+   if ( N < P.min_samples ) return 0;
+   float bestValue = INFINITY;
+   for ( int K = P.min_k; K <= P.max_k; ++K )
+   {
+      float logL = 0.f, E = 0.f;
+      bool ok;
+      if ( KS == 0 ) ok = lane_fit<CLUS, 0>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      else if ( K == 1 ) ok = lane_fit<CLUS, 1>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      else if ( K == 2 ) ok = lane_fit<CLUS, 2>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      else if ( K == 3 || KS < 4 ) ok = lane_fit<CLUS, 3>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      else if ( K == 4 ) ok = lane_fit<CLUS, (KS >= 4 ? 4 : 3)>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E,
+                                                                units);
+      else ok = lane_fit<CLUS, (KS >= 5 ? 5 : 3)>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      ++fits;
+      if ( !ok ) continue;
+      const float value = criterion_value(P, D, K, logL, N, E);
+      if ( value < bestValue )
+      {
+         bestK = K;
+         bestValue = value;
+         for ( int i = 0, j = 0; i < N; ++i )
+         {
+            if ( lbl[i * TILE] >= 0 )
+            {
+               lbl[i * TILE] = wl[j * TILE];
+               ++j;
+            }
+         }
+      }
+   }
+   return bestK;
+}
+
+template <int CLUS, int KS>
+__global__ void __launch_bounds__(WARPS_PER_BLOCK * 32, KINC_MIN_BLOCKS)
+k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
+{
+   extern __shared__ float smem[];
+   const int lane = threadIdx.x & 31;
+   const int warp = threadIdx.x >> 5;
+   const int64_t slot = blockIdx.x * (int64_t)WARPS_PER_BLOCK + warp;
+   const size_t col = (size_t)P.S * TILE;
+
+   float2* X = W.X + slot * col;
+   float* lpx = W.lpx + slot * col;
+   int8_t* lbl = W.lbl + slot * col;
+   int8_t* wl = W.wl + slot * col;
+   int8_t* ya = W.ya + slot * col;
+   int8_t* yb = W.yb + slot * col;
+   int8_t* yc = W.yc + slot * col;
+   uint32_t* ring = W.rng + slot * (size_t)(RNG_WORDS * TILE);
+   float* sbuf = smem_sort ? smem + (size_t)warp * P.sort_floats : W.sortbuf + slot * (size_t)P.sort_floats;
+
+   const int64_t ntiles = (B.size + TILE - 1) / TILE;
+   for ( ;; )
+   {
+      unsigned long long t = 0;
+      if ( lane == 0 ) t = atomicAdd(B.tiles, 1ull);
+      t = __shfl_sync(0xffffffffu, t, 0);
+      if ( (int64_t)t >= ntiles ) break;
+      const int64_t p0 = B.start + (int64_t)t * TILE;
+      const int64_t left = B.start + B.size - p0;
+      const int npairs = left < TILE ? (int)left : TILE;
+
+      /* ---- warp-cooperative: fetch, pre-outliers, rand() position, per pair */
+      int myN = 0;
+      for ( int j = 0; j < npairs; ++j )
+      {
+         const int64_t p = p0 + j;
+         int32_t x, y;
+         pair_xy(p, x, y);
+         const int n = warp_fetch(P, D, x, y, X, lbl, j, lane);
+         if ( lane == j ) myN = n;
+         if ( lane == 0 && n != B.N[p - B.lo] ) atomicCAS(B.status, ST_OK, ST_BAD_RANK);
+         if ( CLUS != 0 )
+         {
+            if ( P.pre_out )
+            {
+               warp_mark_outliers(X, n, 0, lbl, 0, -7, sbuf, j, lane);
+               warp_mark_outliers(X, n, 1, lbl, 0, -7, sbuf, j, lane);
+            }
+            if ( P.rand_mode == 0 && n >= P.min_samples )
+            {
+               const uint64_t pos = B.qpos[p - B.start] * (uint64_t)P.draws_per_pair;
+               warp_rng_jump(D, pos, ring, j, lane);
+            }
+         }
+      }
+      __syncwarp();
+
+      /* ---- lane-local: clustering */
+      int K = 1;
+      const int64_t myp = p0 + lane;
+      int32_t mx = 0, my = 0;
+      if ( lane < npairs ) pair_xy(myp, mx, my);
+      if ( CLUS != 0 )
+      {
+         unsigned long long units = 0, fits = 0;
+         K = 0;
+         if ( lane < npairs )
+         {
+            LaneRng rng;
+            rng.ring = ring + lane;
+            rng.head = 0;
+            rng.mode = P.rand_mode;
+            rng.lcg = 1;
+            K = lane_cluster<CLUS, KS>(P, D, X + lane, lpx + lane, wl + lane, ya + lane, yb + lane, yc + lane,
+                                       lbl + lane, myN, rng, units, fits);
+         }
+         for ( int o = 16; o > 0; o >>= 1 )
+         {
+            units += __shfl_xor_sync(0xffffffffu, units, o);
+            fits += __shfl_xor_sync(0xffffffffu, fits, o);
+         }
+         if ( lane == 0 && B.work )
+         {
+            atomicAdd(&B.work[0], units);
+            atomicAdd(&B.work[1], fits);
+         }
+      }
+      __syncwarp();
+
+      /* ---- warp-cooperative: post-outliers */
+      if ( CLUS != 0 && P.post_out )
+      {
+         for ( int j = 0; j < npairs; ++j )
+         {
+            const int Kj = __shfl_sync(0xffffffffu, K, j);
+            const int nj = __shfl_sync(0xffffffffu, myN, j);
+            if ( Kj > 1 )
+            {
+               for ( int k = 0; k < Kj; ++k )
+               {
+                  warp_mark_outliers(X, nj, 0, lbl, (int8_t)k, -8, sbuf, j, lane);
+                  warp_mark_outliers(X, nj, 1, lbl, (int8_t)k, -8, sbuf, j, lane);
+               }
+            }
+         }
+      }
+
+      /* ---- correlations */
+      if ( P.corr == 0 )
+      {
+         if ( lane < npairs && B.outCorr )
+         {
+            float* corr_row = B.outCorr + (myp - B.start) * P.max_k;
+            for ( int k = 0; k < P.max_k; ++k )
+            {
+               corr_row[k] = k < K ? lane_pearson(P, D, B, X + lane, lbl + lane, myp, mx, my, myN, (int8_t)k)
+                                   : __int_as_float(0x7fc00000);
+            }
+         }
+      }
+      else
+      {
+         for ( int j = 0; j < npairs; ++j )
+         {
+            const int Kj = __shfl_sync(0xffffffffu, K, j);
+            const int xj = __shfl_sync(0xffffffffu, mx, j);
+            const int yj = __shfl_sync(0xffffffffu, my, j);
+            float* row = B.outCorr ? B.outCorr + (p0 + j - B.start) * P.max_k : nullptr;
+            for ( int k = 0; k < P.max_k; ++k )
+            {
+               float r = __int_as_float(0x7fc00000);
+               if ( k < Kj ) r = warp_spearman(P, D, X, lbl, xj, yj, (int8_t)k, sbuf, j, lane);
+               if ( lane == 0 && row ) row[k] = r;
+            }
+         }
+      }
+
+      /* ---- outputs */
+      if ( lane < npairs && B.outK ) B.outK[myp - B.start] = (int8_t)K;
+      if ( B.outLabels )
+      {
+         for ( int j = 0; j < npairs; ++j )
+         {
+            int8_t* row = B.outLabels + (p0 + j - B.start) * (int64_t)P.S;
+            for ( int s = lane; s < P.S; s += 32 ) row[s] = lbl[s * TILE + j];
+         }
+      }
+      __syncwarp();
+   }
+}
+
+/* host-side handle of one specialisation */
+struct SimKernel
+{
+   const void* fn;
+   int clus;
+   int ks;
+};
+
+template <int CLUS, int KS>
+inline SimKernel sim_kernel_handle()
+{
+   return SimKernel { (const void*)&k_similarity<CLUS, KS>, CLUS, KS };
+}
+
+template <int CLUS, int KS>
+inline cudaError_t sim_kernel_launch(int grid, int smem, cudaStream_t st, const DevParams& P, const DevData& D,
+                                     const DevScratch& W, const DevBlock& B, int smem_sort)
+{
+   k_similarity<CLUS, KS><<<grid, WARPS_PER_BLOCK * 32, smem, st>>>(P, D, W, B, smem_sort);
+   return cudaGetLastError();
+}
+
+/* defined in sim_none.cu / sim_gmm.cu / sim_kmeans.cu */
+SimKernel sim_kernel_select(int clus, int max_k);
+cudaError_t sim_kernel_launch_any(const SimKernel& k, int grid, int smem, cudaStream_t st, const DevParams& P,
+                                  const DevData& D, const DevScratch& W, const DevBlock& B, int smem_sort);
+SimKernel sim_kernel_none();
+SimKernel sim_kernel_gmm(int max_k);
+SimKernel sim_kernel_kmeans(int max_k);
+cudaError_t sim_launch_none(const SimKernel& k, int grid, int smem, cudaStream_t st, const DevParams& P,
+                            const DevData& D, const DevScratch& W, const DevBlock& B, int smem_sort);
+cudaError_t sim_launch_gmm(const SimKernel& k, int grid, int smem, cudaStream_t st, const DevParams& P,
+                           const DevData& D, const DevScratch& W, const DevBlock& B, int smem_sort);
+cudaError_t sim_launch_kmeans(const SimKernel& k, int grid, int smem, cudaStream_t st, const DevParams& P,
+                              const DevData& D, const DevScratch& W, const DevBlock& B, int smem_sort);
+
+} /* namespace kinc */
