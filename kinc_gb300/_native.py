@@ -54,7 +54,8 @@ SIGNATURES = {
 
 
 def library_path():
-    return _build.LIB
+    """The library to load: KINC_GB300_LIB overrides the in-tree build (A/B runs)."""
+    return os.environ.get("KINC_GB300_LIB", _build.LIB)
 
 
 def load(build_if_missing=True):
@@ -62,7 +63,7 @@ def load(build_if_missing=True):
     global _lib
     if _lib is not None:
         return _lib
-    path = _build.LIB
+    path = library_path()
     if not os.path.exists(path):
         if not build_if_missing:
             raise RuntimeError(f"native library {path} is missing; run kinc_gb300.build.build()")

@@ -17,7 +17,8 @@
  * a*b+c on their own (host: -ffp-contract=off; device: --fmad=false).
  *
  * Methods (written from the mathematics, not from any vendor library):
- *   exp:  Cody-Waite argument reduction x = n*ln2 + r with a two-part ln2
+ *   exp:  n = rint(x/ln2) by the 1.5*2^23 shifter; Cody-Waite argument
+ *         reduction x = n*ln2 + r with a two-part ln2
  *         whose leading part has 16 significant bits (so n*LN2_HI and
  *         x - n*LN2_HI are exact for |n| <= 2^8), |r| <= ln2/2; then the
  *         degree-7 Taylor polynomial of e^r by Horner's rule in fused
@@ -44,13 +45,11 @@
 #include <cstring>
 #include <cmath>
 #define KINC_FMAF(a, b, c) ::fmaf((a), (b), (c))
-#define KINC_RINTF(a) ::rintf(a)
 #else
 #include <stdint.h>
 #include <string.h>
 #include <math.h>
 #define KINC_FMAF(a, b, c) fmaf((a), (b), (c))
-#define KINC_RINTF(a) rintf(a)
 #endif
 
 #define KINC_F_LOG2E 1.44269502162933349609375f      /* float nearest to 1/ln2 */
@@ -112,7 +111,15 @@ KINC_HD float kinc_expf_tail(float x, float n, float p)
 /* e^x, single precision. */
 KINC_HD float kinc_expf(float x)
 {
-   const float n = KINC_RINTF(x * KINC_F_LOG2E);
+   /* n = rint(x / ln2): adding and removing 1.5 * 2^23 rounds to the nearest
+    * integer (ties to even) for |x / ln2| < 2^22, which covers every x that
+    * reaches the scaling below; the sum's low mantissa bits hold n itself */
+#ifdef __CUDA_ARCH__
+   const float shifted = __fadd_rn(__fmul_rn(x, KINC_F_LOG2E), 12582912.0f);   /* never contracted */
+#else
+   const float shifted = x * KINC_F_LOG2E + 12582912.0f;   /* hosts build with -ffp-contract=off */
+#endif
+   const float n = shifted - 12582912.0f;
    float r = KINC_FMAF(-n, KINC_F_LN2_HI, x);
    r = KINC_FMAF(-n, KINC_F_LN2_LO, r);
 
@@ -128,9 +135,10 @@ KINC_HD float kinc_expf(float x)
 
    /* |x| <= 87 keeps n in [-126, 126]: 2^n is a normal float and the product
     * rounds once (NaN fails the comparison and takes the tail) */
-   if ( x <= 87.0f && x >= -87.0f )
+   if ( (x < 0.0f ? -x : x) <= 87.0f )
    {
-      return p * kinc_u2f((uint32_t)((int)n + 127) << 23);
+      /* bits(shifted) - bits(1.5 * 2^23) = n; 2^n has exponent field n + 127 */
+      return p * kinc_u2f((kinc_f2u(shifted) - 0x4b400000u + 127u) << 23);
    }
    return kinc_expf_tail(x, n, p);
 }

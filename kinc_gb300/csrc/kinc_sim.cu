@@ -521,7 +521,9 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
 
    /* scratch: per warp slot, interleaved by lane */
    const size_t col = (size_t)S * TILE;
-   const size_t slot_bytes = col * sizeof(float2) + col * sizeof(float) + 5 * col
+   dp.gam_k = (KINC_STORE_GAMMA && params->clus_method == 1)
+                 ? (params->max_clusters <= 3 ? 3 : params->max_clusters <= 5 ? 5 : 0) : 0;
+   const size_t slot_bytes = col * sizeof(float2) + col * sizeof(float) * (1 + dp.gam_k) + 5 * col
                              + (size_t)RNG_WORDS * TILE * sizeof(uint32_t)
                              + (ctx->smem_sort ? 0 : sort_bytes_warp) + 256 * 8;
    size_t free_b = 0, total_b = 0;
@@ -541,6 +543,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
       };
       const size_t oX = take(slots * col * sizeof(float2));
       const size_t oL = take(slots * col * sizeof(float));
+      const size_t oG = take(slots * col * sizeof(float) * dp.gam_k);
       const size_t oB = take(slots * col);
       const size_t oW = take(slots * col);
       const size_t oA = take(slots * col);
@@ -552,6 +555,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
       char* base = (char*)ctx->d_scratch;
       ctx->ds.X = (float2*)(base + oX);
       ctx->ds.lpx = (float*)(base + oL);
+      ctx->ds.gam = dp.gam_k ? (float*)(base + oG) : nullptr;
       ctx->ds.lbl = (int8_t*)(base + oB);
       ctx->ds.wl = (int8_t*)(base + oW);
       ctx->ds.ya = (int8_t*)(base + oA);

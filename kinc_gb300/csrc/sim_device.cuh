@@ -34,6 +34,16 @@
 namespace kinc {
 
 constexpr int TILE = 32;            /* pairs per warp tile */
+#ifndef KINC_SAMPLE_UNROLL
+#define KINC_SAMPLE_UNROLL 1
+#endif
+constexpr int SAMPLE_UNROLL = KINC_SAMPLE_UNROLL;   /* unroll factor of the EM sample loops */
+#ifndef KINC_STATIC_K
+#define KINC_STATIC_K 1             /* 1: one compiled fit per K (K known to the compiler); 0: one fit for all K <= KS */
+#endif
+#ifndef KINC_STORE_GAMMA
+#define KINC_STORE_GAMMA 0          /* 1: keep the M1 responsibilities for M2 instead of recomputing them */
+#endif
 constexpr int RNG_WORDS = 31;       /* glibc TYPE_3 state words */
 constexpr int RNG_BITS = 48;        /* jump table covers positions < 2^48 */
 
@@ -52,6 +62,7 @@ struct DevParams
    double c2;                       /* D * log(2 pi), D = 2, in double */
    int32_t P2;                      /* next power of two >= max(S, 2) */
    int32_t sort_floats;             /* floats of sort buffer per warp */
+   int32_t gam_k;                   /* components per sample in DevScratch::gam (0: none) */
 };
 
 struct DevData
@@ -67,6 +78,7 @@ struct DevScratch
 {
    float2* X;                       /* per warp slot: [S][32] */
    float* lpx;                      /* per warp slot: [S][32] */
+   float* gam;                      /* per warp slot: [S][gam_k][32] GMM responsibilities */
    int8_t* lbl;                     /* per warp slot: [S][32] */
    int8_t* wl;                      /* per warp slot: [S][32] work labels */
    int8_t* ya;                      /* per warp slot: [S][32] K-means */
@@ -376,8 +388,7 @@ __device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, dou
 }
 
 /*
- * GMM::fit for one pair on this lane (pairwise_gmm.cpp:367-445).  KT > 0
- * fixes K at compile time; KT == 0 handles any K <= 64 from local memory.
+ * GMM::fit for one pair on this lane (pairwise_gmm.cpp:367-445).
  * Per EM iteration it makes three passes over the samples: E (log-densities,
  * per-sample log-sum-exp, logL, and the per-component maxima calcLogGammaK
  * needs), M1 (per-component log-sum-exp of the responsibilities, and the mean
@@ -391,12 +402,17 @@ __device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, dou
  * samples with that iteration's E-step responsibilities.
  */
 template <int KT>
-__device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn, LaneRng& rng, double c2,
-                        float& out_logL, float& out_E, unsigned long long& units)
+__device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int N, int Kr, LaneRng& rng,
+                        double c2, float& out_logL, float& out_E, unsigned long long& units)
 {
+   const int K = (KINC_STATIC_K && KT > 0) ? KT : Kr;
+   /* KT > 0: up to KT components in registers (K <= KT at run time);
+    * KT == 0: any K <= 64 from local memory.  M2 recomputes the
+    * responsibilities of M1 unless KINC_STORE_GAMMA keeps them in
+    * gam[(i*KT + k)*32] */
    constexpr int KA = KT > 0 ? KT : 64;
    constexpr int UF = KT > 0 ? KT : 1;
-   const int K = KT > 0 ? KT : Kdyn;
+   constexpr bool STORE_G = KT > 0 && KINC_STORE_GAMMA;
    float m0[KA], m1[KA], ia[KA], ib[KA], ic[KA], nrm[KA], logpi[KA];
 
    if ( rng.mode == 1 ) rng.lcg = 1;
@@ -407,7 +423,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
       for ( int k = 0; k < KA; ++k )
       {
-         if ( k >= K ) break;
+         if ( k >= K ) continue;
          const int ii = rng.next() % N;
          const float2 xv = X[ii * TILE];
          m0[k] = xv.x;
@@ -429,10 +445,11 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
       for ( int k = 0; k < KA; ++k )
       {
-         if ( k >= K ) break;
+         if ( k >= K ) continue;
          maxG[k] = -INFINITY;
       }
       float2 xn = X[0];
+      #pragma unroll SAMPLE_UNROLL
       for ( int i = 0; i < N; ++i )
       {
          const float2 xv = xn;
@@ -442,7 +459,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
-            if ( k >= K ) break;
+            if ( k >= K ) continue;
             lg[k] = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]);
             const float lp = logpi[k] + lg[k];
             if ( lp > m ) m = lp;
@@ -451,7 +468,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
-            if ( k >= K ) break;
+            if ( k >= K ) continue;
             sum += kinc_expf((logpi[k] + lg[k]) - m);
          }
          const float logpx = m + kinc_logf(sum);
@@ -460,7 +477,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
-            if ( k >= K ) break;
+            if ( k >= K ) continue;
             const float v = lg[k] + (-logpx);
             if ( v > maxG[k] ) maxG[k] = v;
          }
@@ -480,11 +497,12 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
-            if ( k >= K ) break;
+            if ( k >= K ) continue;
             sG[k] = 0.f; nm0[k] = 0.f; nm1[k] = 0.f;
          }
          xn = X[0];
          float ln = lpx[0];
+         #pragma unroll SAMPLE_UNROLL
          for ( int i = 0; i < N; ++i )
          {
             const float2 xv = xn;
@@ -497,10 +515,11 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
             for ( int k = 0; k < KA; ++k )
             {
-               if ( k >= K ) break;
+               if ( k >= K ) continue;
                const float lgk = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
                sG[k] += kinc_expf(lgk - maxG[k]);
                const float g = kinc_expf(lgk);
+               if ( STORE_G ) gam[(i * KA + k) * TILE] = g;
                nm0[k] += g * xv.x;
                nm1[k] += g * xv.y;
             }
@@ -510,7 +529,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
-            if ( k >= K ) break;
+            if ( k >= K ) continue;
             logGamma[k] = maxG[k] + kinc_logf(sG[k]);
             const float arg = logpi[k] + logGamma[k];
             if ( arg > mx ) mx = arg;
@@ -519,14 +538,14 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
-            if ( k >= K ) break;
+            if ( k >= K ) continue;
             s += kinc_expf((logpi[k] + logGamma[k]) - mx);
          }
          const float lgs = mx + kinc_logf(s);
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
-            if ( k >= K ) break;
+            if ( k >= K ) continue;
             logpi[k] += logGamma[k] - lgs;
             Gam[k] = kinc_expf(logGamma[k]);
             const float sc = 1.0f / Gam[k];
@@ -540,11 +559,12 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
       for ( int k = 0; k < KA; ++k )
       {
-         if ( k >= K ) break;
+         if ( k >= K ) continue;
          s00[k] = 0.f; s01[k] = 0.f; s11[k] = 0.f;
       }
       xn = X[0];
       float ln = lpx[0];
+      #pragma unroll SAMPLE_UNROLL
       for ( int i = 0; i < N; ++i )
       {
          const float2 xv = xn;
@@ -557,9 +577,17 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
-            if ( k >= K ) break;
-            const float lgk = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
-            const float g = kinc_expf(lgk);
+            if ( k >= K ) continue;
+            float g;
+            if ( STORE_G )
+            {
+               g = gam[(i * KA + k) * TILE];
+            }
+            else
+            {
+               const float lgk = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
+               g = kinc_expf(lgk);
+            }
             const float xm0 = xv.x - nm0[k];
             const float xm1 = xv.y - nm1[k];
             s00[k] += g * (xm0 * xm0);
@@ -572,7 +600,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
       for ( int k = 0; k < KA; ++k )
       {
-         if ( k >= K ) break;
+         if ( k >= K ) continue;
          const float sc = 1.0f / Gam[k];
          float a, b, c, n;
          ok = prepare_cov(s00[k] * sc, s01[k] * sc, s11[k] * sc, c2, a, b, c, n) && ok;
@@ -599,7 +627,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, int8_t* wl, int N, int Kdyn
 #pragma unroll UF
       for ( int k = 0; k < KA; ++k )
       {
-         if ( k >= K ) break;
+         if ( k >= K ) continue;
          float v = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
          if ( !converged ) v = kinc_expf(v);
          if ( max_g < v )
@@ -627,12 +655,14 @@ __device__ __forceinline__ float diff_norm(float x0, float x1, float m0, float m
 /* KMeans::fit for one pair on this lane (pairwise_kmeans.cpp:12-99).  The
  * best run's labels end up in *best (a pointer into the three buffers). */
 template <int KT>
-__device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*& best, int N, int Kdyn,
+__device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*& best, int N, int Kr,
                             LaneRng& rng, unsigned long long& units)
 {
+   const int K = (KINC_STATIC_K && KT > 0) ? KT : Kr;
+   /* KT > 0: up to KT centroids in registers (K <= KT at run time);
+    * KT == 0: any K <= 64 from local memory */
    constexpr int KA = KT > 0 ? KT : 64;
    constexpr int UF = KT > 0 ? KT : 1;
-   const int K = KT > 0 ? KT : Kdyn;
    float bestLogL = -INFINITY;
    if ( rng.mode == 1 ) rng.lcg = 1;
    for ( int init = 0; init < 10; ++init )
@@ -641,7 +671,7 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
 #pragma unroll UF
       for ( int k = 0; k < KA; ++k )
       {
-         if ( k >= K ) break;
+         if ( k >= K ) continue;
          const int ii = rng.next() % N;
          const float2 xv = X[ii * TILE];
          mu0[k] = xv.x;
@@ -666,7 +696,7 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
 #pragma unroll UF
             for ( int k = 0; k < KA; ++k )
             {
-               if ( k >= K ) break;
+               if ( k >= K ) continue;
                const float d = diff_norm(xv.x, xv.y, mu0[k], mu1[k]);
                if ( min_k == -1 || d < min_d )
                {
@@ -686,7 +716,7 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
-            if ( k >= K ) break;
+            if ( k >= K ) continue;
             s0[k] = 0.f; s1[k] = 0.f; nk[k] = 0;
          }
          for ( int i = 0; i < N; ++i )
@@ -696,7 +726,7 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
 #pragma unroll UF
             for ( int k = 0; k < KA; ++k )
             {
-               if ( k >= K ) break;
+               if ( k >= K ) continue;
                if ( l == k )
                {
                   s0[k] += xv.x;
@@ -708,7 +738,7 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
-            if ( k >= K ) break;
+            if ( k >= K ) continue;
             const float sc = 1.0f / nk[k];
             mu0[k] = s0[k] * sc;
             mu1[k] = s1[k] * sc;
@@ -722,7 +752,7 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
 #pragma unroll UF
          for ( int kk = 0; kk < KA; ++kk )
          {
-            if ( kk >= K ) break;
+            if ( kk >= K ) continue;
             if ( kk == k ) { c0 = mu0[kk]; c1 = mu1[kk]; }
          }
          for ( int i = 0; i < N; ++i )

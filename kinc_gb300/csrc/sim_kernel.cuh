@@ -2,8 +2,9 @@
  * sim_kernel.cuh -- the per-pair Similarity kernel, specialised by
  * clustering method (CLUS: 0 none, 1 GMM, 2 K-means) and by the largest
  * cluster count compiled with static register arrays (KS = 3 or 5: every
- * fit keeps its per-component state in registers, the host picks KS >=
- * maxclus; KS = 0: the generic local-memory form for any maxclus <= 64).
+ * fit, whatever its K <= KS, runs the same code with its per-component state
+ * in registers, the host picks KS >= maxclus; KS = 0: the generic
+ * local-memory form for any maxclus <= 64).
  * Each specialisation is instantiated in its own translation unit
  * (sim_none.cu, sim_gmm.cu, sim_kmeans.cu) so the register budget of one
  * does not constrain the others.  Blocks of 4 warps are limited to 128
@@ -107,13 +108,13 @@ __device__ __forceinline__ float criterion_value(const DevParams& P, const DevDa
 }
 
 template <int CLUS, int KT>
-__device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, float* lpx, int8_t*& wl,
-                                         int8_t*& ya, int8_t*& yb, int8_t*& yc, int N, int K, LaneRng& rng,
-                                         float& logL, float& E, unsigned long long& units)
+__device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, float* lpx, float* gam,
+                                         int8_t*& wl, int8_t*& ya, int8_t*& yb, int8_t*& yc, int N, int K,
+                                         LaneRng& rng, float& logL, float& E, unsigned long long& units)
 {
    if ( CLUS == 1 )
    {
-      return gmm_fit<KT>(X, lpx, wl, N, K, rng, P.c2, logL, E, units);
+      return gmm_fit<KT>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units);
    }
    logL = kmeans_fit<KT>(X, ya, yb, yc, N, K, rng, units);
    E = 0.f;
@@ -126,7 +127,8 @@ __device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, fl
 /* Clustering::compute (pairwise_clustering.cpp:23-103) minus the outlier
  * passes, for this lane's pair; labels merged into lbl. */
 template <int CLUS, int KS>
-__device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* X, float* lpx, int8_t* wl,
+__device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* X, float* lpx, float* gam,
+                            int8_t* wl,
                             int8_t* ya, int8_t* yb, int8_t* yc, int8_t* lbl, int N, LaneRng& rng,
                             unsigned long long& units, unsigned long long& fits)
 {
@@ -137,13 +139,13 @@ __device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* 
    {
       float logL = 0.f, E = 0.f;
       bool ok;
-      if ( KS == 0 ) ok = lane_fit<CLUS, 0>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units);
-      else if ( K == 1 ) ok = lane_fit<CLUS, 1>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units);
-      else if ( K == 2 ) ok = lane_fit<CLUS, 2>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units);
-      else if ( K == 3 || KS < 4 ) ok = lane_fit<CLUS, 3>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units);
-      else if ( K == 4 ) ok = lane_fit<CLUS, (KS >= 4 ? 4 : 3)>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E,
-                                                                units);
-      else ok = lane_fit<CLUS, (KS >= 5 ? 5 : 3)>(P, X, lpx, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      if ( !KINC_STATIC_K || KS == 0 )
+         ok = lane_fit<CLUS, KS>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      else if ( K == 1 ) ok = lane_fit<CLUS, 1>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      else if ( K == 2 ) ok = lane_fit<CLUS, 2>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      else if ( K == 3 || KS < 4 ) ok = lane_fit<CLUS, 3>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      else if ( K == 4 ) ok = lane_fit<CLUS, 4>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
+      else ok = lane_fit<CLUS, 5>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
       ++fits;
       if ( !ok ) continue;
       const float value = criterion_value(P, D, K, logL, N, E);
@@ -176,6 +178,7 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
 
    float2* X = W.X + slot * col;
    float* lpx = W.lpx + slot * col;
+   float* gam = W.gam ? W.gam + slot * col * P.gam_k : nullptr;
    int8_t* lbl = W.lbl + slot * col;
    int8_t* wl = W.wl + slot * col;
    int8_t* ya = W.ya + slot * col;
@@ -237,8 +240,8 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
             rng.head = 0;
             rng.mode = P.rand_mode;
             rng.lcg = 1;
-            K = lane_cluster<CLUS, KS>(P, D, X + lane, lpx + lane, wl + lane, ya + lane, yb + lane, yc + lane,
-                                       lbl + lane, myN, rng, units, fits);
+            K = lane_cluster<CLUS, KS>(P, D, X + lane, lpx + lane, gam ? gam + lane : nullptr, wl + lane,
+                                       ya + lane, yb + lane, yc + lane, lbl + lane, myN, rng, units, fits);
          }
          for ( int o = 16; o > 0; o >>= 1 )
          {
