@@ -148,6 +148,32 @@ int32_t kinc_sim_last_launch_count(const kinc_sim_ctx* ctx);
  * Synchronises the context's stream. */
 int kinc_sim_work_counters(kinc_sim_ctx* ctx, uint64_t* out, int reset);
 
+/*
+ * Allocation-free form of kinc_sim_execute_block_device, for callers that may
+ * not allocate device memory: hosts that give the whole device to their own
+ * pool allocator and forbid raw cudaMalloc (which also synchronises the
+ * device), or that run this step where allocating is not allowed.  No
+ * counterpart in the reference.
+ *
+ * The caller passes the expression matrix already on the device (d_gem,
+ * row-major [genes][samples] float32) and device outputs laid out as in
+ * kinc_sim_execute_block.  All working memory is a 64 MiB static device array
+ * inside the library, which every GPU that loads the library holds until the
+ * process exits.  Limits: samples <= 4096 and size <= 262144 pairs per call,
+ * and the per-gene masks, per-pair arrays and at least one 4-warp block of
+ * working space must fit in the 64 MiB; larger requests are rejected with
+ * KINC_SIM_EINVAL and a message from kinc_sim_last_error(NULL).  precision must be 0.
+ *
+ * The first call on a device looks up the array's device address and uploads
+ * the rand() jump table; make that first call before any stream capture.
+ * Every call shares the one array, so calls that overlap on the GPU race:
+ * the function serialises host callers and waits for its own work on
+ * `stream` (a cudaStream_t, 0 = default stream) before returning.
+ */
+int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes, int32_t samples,
+                                   const kinc_sim_params* params, int64_t start, int64_t size, int8_t* d_K,
+                                   int8_t* d_labels, float* d_corr, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

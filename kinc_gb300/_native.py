@@ -50,6 +50,8 @@ SIGNATURES = {
     "kinc_sim_pair_counts": (ctypes.c_int, [_VP, _I64, _I64, _VP]),
     "kinc_sim_last_launch_count": (_I32, [_VP]),
     "kinc_sim_work_counters": (ctypes.c_int, [_VP, _VP, ctypes.c_int]),
+    "kinc_sim_execute_block_noalloc": (ctypes.c_int, [_VP, _I32, _I32, ctypes.POINTER(SimParams), _I64, _I64,
+                                                      _VP, _VP, _VP, _VP]),
 }
 
 

@@ -26,6 +26,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -836,4 +837,296 @@ extern "C" int kinc_sim_process_block(const kinc_sim_ctx* cctx, int64_t start, i
                                          cmx_r, cap_cmx, n_cmx, ccm_x, ccm_y, ccm_c, ccm_codes, cap_ccm, n_ccm);
    if ( rc ) ctx->err = g_create_error;
    return rc;
+}
+
+/* ======================================================= allocation-free
+ *
+ * kinc_sim_execute_block_noalloc: the same work as kinc_sim_execute_block_device
+ * for callers that may not allocate device memory -- hosts that hand the
+ * whole device to their own pool allocator and forbid raw cudaMalloc (which
+ * also synchronises the device), or that run this step inside a region where
+ * allocation is not allowed.  The caller passes its device expression matrix
+ * and device outputs; everything else lives in the file-scope arrays below,
+ * which every GPU that loads this library holds until the process exits.
+ */
+namespace {
+
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)64 << 20;   /* 64 MiB of working memory */
+constexpr int64_t NOALLOC_MAX_PAIRS = (int64_t)1 << 18;      /* pairs per call */
+constexpr int NOALLOC_MAX_SAMPLES = 4096;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+static __device__ __align__(256) uint32_t g_noalloc_jump[RNG_BITS * RNG_WORDS * RNG_WORDS];
+static __device__ __align__(256) uint32_t g_noalloc_rng0[RNG_WORDS];
+
+struct NoallocDevice
+{
+   bool ready;
+   unsigned char* scratch;     /* device address of g_noalloc_scratch on this device */
+   uint32_t* jump;
+   uint32_t* rng0;
+};
+
+NoallocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
+uint32_t g_noalloc_host_jump[RNG_BITS * RNG_WORDS * RNG_WORDS];
+uint32_t g_noalloc_host_rng0[RNG_WORDS];
+double g_noalloc_host_logn[NOALLOC_MAX_SAMPLES + 1];
+bool g_noalloc_tables = false;
+std::mutex g_noalloc_mutex;
+
+/* error messages are written into reserved capacity, so reporting one does not allocate */
+struct NoallocErrorReserve
+{
+   NoallocErrorReserve() { g_create_error.reserve(1024); }
+} g_noalloc_error_reserve;
+
+/* the glibc rand() tables of glibc_rng_tables, computed into fixed storage */
+void noalloc_rng_tables()
+{
+   int64_t r[344];
+   r[0] = 1;
+   for ( int i = 1; i < 31; ++i )
+   {
+      const int64_t hi = r[i - 1] / 127773;
+      const int64_t lo = r[i - 1] % 127773;
+      int64_t word = 16807 * lo - 2836 * hi;
+      if ( word < 0 ) word += 2147483647;
+      r[i] = word;
+   }
+   for ( int i = 31; i < 34; ++i ) r[i] = r[i - 31];
+   for ( int i = 34; i < 344; ++i ) r[i] = (int64_t)(uint32_t)((uint32_t)r[i - 31] + (uint32_t)r[i - 3]);
+   for ( int i = 0; i < RNG_WORDS; ++i ) g_noalloc_host_rng0[i] = (uint32_t)r[313 + i];
+   const int n = RNG_WORDS;
+   static uint32_t M[RNG_WORDS * RNG_WORDS], T[RNG_WORDS * RNG_WORDS];
+   for ( int i = 0; i < n * n; ++i ) M[i] = 0u;
+   for ( int i = 0; i < n - 1; ++i ) M[i * n + i + 1] = 1u;
+   M[(n - 1) * n + 0] = 1u;
+   M[(n - 1) * n + 28] = 1u;
+   for ( int b = 0; b < RNG_BITS; ++b )
+   {
+      for ( int row = 0; row < n; ++row )
+         for ( int c = 0; c < n; ++c ) g_noalloc_host_jump[(size_t)b * n * n + c * n + row] = M[row * n + c];
+      for ( int i = 0; i < n; ++i )
+         for ( int j = 0; j < n; ++j )
+         {
+            uint32_t acc = 0;
+            for ( int k = 0; k < n; ++k ) acc += M[i * n + k] * M[k * n + j];
+            T[i * n + j] = acc;
+         }
+      for ( int i = 0; i < n * n; ++i ) M[i] = T[i];
+   }
+}
+
+/* the argument checks of validate(), with static messages (nothing allocated) */
+const char* noalloc_check(const kinc_sim_params* p, int32_t G, int32_t S)
+{
+   if ( G < 2 ) return "genes must be >= 2";
+   if ( S < 1 ) return "samples must be >= 1";
+   if ( p->clus_method < 0 || p->clus_method > 2 ) return "clus_method must be 0 (none), 1 (gmm) or 2 (kmeans)";
+   if ( p->corr_method < 0 || p->corr_method > 1 ) return "corr_method must be 0 (pearson) or 1 (spearman)";
+   if ( p->min_samples < 1 ) return "min_samples must be >= 1";
+   if ( p->min_clusters < 1 || p->min_clusters > 64 ) return "min_clusters must be in 1..64";
+   if ( p->max_clusters < 1 || p->max_clusters > 64 ) return "max_clusters must be in 1..64";
+   if ( p->max_clusters < p->min_clusters ) return "Minimum clusters must be less than or equal to maximum clusters.";
+   if ( p->criterion < 0 || p->criterion > 1 ) return "criterion must be 0 (BIC) or 1 (ICL)";
+   if ( !(p->min_corr >= 0 && p->min_corr <= 1) || !(p->max_corr >= 0 && p->max_corr <= 1) )
+      return "min_corr and max_corr must be in [0, 1]";
+   if ( p->semantics < 0 || p->semantics > 1 ) return "semantics must be 0 or 1";
+   if ( p->rand_mode < 0 || p->rand_mode > 1 ) return "rand_mode must be 0 or 1";
+   if ( p->precision != 0 ) return "the allocation-free entry point runs the per-pair FP32 path only (precision 0)";
+   return nullptr;
+}
+
+}  // namespace
+
+extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes, int32_t samples,
+                                              const kinc_sim_params* params, int64_t start, int64_t size,
+                                              int8_t* d_K, int8_t* d_labels, float* d_corr, void* stream)
+{
+   kinc_sim_ctx* ctx = nullptr;   /* errors go to kinc_sim_last_error(NULL) */
+   if ( !d_gem || !params ) return fail(nullptr, KINC_SIM_EINVAL, "d_gem and params must not be NULL");
+   const char* bad = noalloc_check(params, genes, samples);
+   if ( bad ) return fail(nullptr, KINC_SIM_EINVAL, "%s", bad);
+   if ( samples > NOALLOC_MAX_SAMPLES )
+      return fail(nullptr, KINC_SIM_EINVAL, "samples %d exceeds the allocation-free limit of %d", samples,
+                  NOALLOC_MAX_SAMPLES);
+   if ( size < 0 || size > NOALLOC_MAX_PAIRS )
+      return fail(nullptr, KINC_SIM_EINVAL, "size %lld exceeds the allocation-free limit of %lld pairs per call",
+                  (long long)size, (long long)NOALLOC_MAX_PAIRS);
+   const int64_t total = (int64_t)genes * (genes - 1) / 2;
+   if ( start < 0 || start + size > total )
+      return fail(nullptr, KINC_SIM_EINVAL, "pair range [%lld, %lld) outside [0, %lld)", (long long)start,
+                  (long long)(start + size), (long long)total);
+   if ( size == 0 ) return KINC_SIM_OK;
+
+   int dev = 0;
+   CK(cudaGetDevice(&dev));
+   if ( dev < 0 || dev >= NOALLOC_MAX_DEVICES )
+      return fail(nullptr, KINC_SIM_EINVAL, "device %d beyond the supported %d", dev, NOALLOC_MAX_DEVICES);
+   cudaStream_t st = (cudaStream_t)stream;
+   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+
+   /* set-up, once per device, with that device current */
+   NoallocDevice& nd = g_noalloc_dev[dev];
+   if ( !nd.ready )
+   {
+      void* p = nullptr;
+      CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+      nd.scratch = (unsigned char*)p;
+      CK(cudaGetSymbolAddress(&p, g_noalloc_jump));
+      nd.jump = (uint32_t*)p;
+      CK(cudaGetSymbolAddress(&p, g_noalloc_rng0));
+      nd.rng0 = (uint32_t*)p;
+      if ( !g_noalloc_tables )
+      {
+         noalloc_rng_tables();
+         g_noalloc_tables = true;
+      }
+      CK(cudaMemcpyToSymbol(g_noalloc_jump, g_noalloc_host_jump, sizeof g_noalloc_host_jump));
+      CK(cudaMemcpyToSymbol(g_noalloc_rng0, g_noalloc_host_rng0, sizeof g_noalloc_host_rng0));
+      nd.ready = true;
+   }
+
+   /* device parameters, as kinc_sim_create derives them */
+   const int S = samples;
+   const int W = (S + 31) / 32;
+   DevParams dp {};
+   dp.G = genes; dp.S = S; dp.W = W;
+   dp.clus = params->clus_method; dp.corr = params->corr_method;
+   dp.min_expr = params->min_expr; dp.min_samples = params->min_samples;
+   dp.min_k = params->min_clusters; dp.max_k = params->max_clusters;
+   dp.criterion = params->criterion; dp.pre_out = params->pre_out; dp.post_out = params->post_out;
+   dp.semantics = params->semantics; dp.rand_mode = params->rand_mode;
+   dp.draws_per_pair = draws_per_pair(*params);
+   dp.c2 = 2 * std::log(2.0f * M_PI);
+   dp.P2 = next_pow2_host(std::max(S, 2));
+   const bool need_sort = (params->clus_method != 0 && (params->pre_out || params->post_out))
+                          || params->corr_method == 1;
+   dp.sort_floats = params->corr_method == 1 ? 3 * dp.P2 : (need_sort ? dp.P2 : 0);
+   dp.gam_k = 0;
+   const size_t sort_bytes_warp = (size_t)dp.sort_floats * sizeof(float);
+   const int smem_sort = need_sort && sort_bytes_warp * WARPS_PER_BLOCK <= 160 * 1024;
+   const int smem_bytes = smem_sort ? (int)(sort_bytes_warp * WARPS_PER_BLOCK) : 0;
+   const SimKernel kern = params->clus_method == 0 ? sim_kernel_none()
+                        : params->clus_method == 1 ? sim_kernel_gmm(params->max_clusters)
+                                                   : sim_kernel_kmeans(params->max_clusters);
+   if ( smem_bytes > 48 * 1024 )
+      CK(cudaFuncSetAttribute(kern.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
+
+   /* carve the static array: fixed parts first, then as many warp slots as fit */
+   size_t off = 0;
+   auto take = [&](size_t bytes) {
+      const size_t o = off;
+      off += (bytes + 255) & ~(size_t)255;
+      return o;
+   };
+   const int64_t lo = (start / KINC_SIM_WORK_BLOCK_SIZE) * KINC_SIM_WORK_BLOCK_SIZE;
+   const int64_t end = start + size;
+   const int64_t span = end - lo;
+   const int nscan = (int)((size + SCAN_THREADS - 1) / SCAN_THREADS);
+   const size_t oMask = take((size_t)genes * W * sizeof(uint32_t));
+   const size_t oLogn = take((size_t)(S + 1) * sizeof(double));
+   const size_t oN = take((size_t)span * sizeof(int32_t));
+   const size_t oPg = take((size_t)span * sizeof(int32_t));
+   const size_t oQ = take((size_t)size * sizeof(uint64_t));
+   const size_t oBsum = take((size_t)(nscan + 1) * sizeof(unsigned long long));
+   const size_t oSmall = take(8 * sizeof(unsigned long long));
+   const size_t col = (size_t)S * TILE;
+   const size_t slot_bytes = ((col * sizeof(float2) + 255) & ~(size_t)255) + ((col * sizeof(float) + 255) & ~(size_t)255)
+                             + 5 * ((col + 255) & ~(size_t)255)
+                             + (((size_t)RNG_WORDS * TILE * sizeof(uint32_t) + 255) & ~(size_t)255)
+                             + (smem_sort ? 0 : ((sort_bytes_warp + 255) & ~(size_t)255));
+   if ( off >= NOALLOC_SCRATCH_BYTES || (NOALLOC_SCRATCH_BYTES - off) / slot_bytes < (size_t)WARPS_PER_BLOCK )
+      return fail(nullptr, KINC_SIM_EINVAL,
+                  "%d genes x %d samples and %lld pairs do not fit the %zu-byte allocation-free scratch",
+                  genes, samples, (long long)size, NOALLOC_SCRATCH_BYTES);
+   const size_t nslots = ((NOALLOC_SCRATCH_BYTES - off) / slot_bytes) / WARPS_PER_BLOCK * WARPS_PER_BLOCK;
+   unsigned char* base = nd.scratch;
+   DevScratch ds {};
+   {
+      size_t o = off;
+      auto carve = [&](size_t bytes) {
+         unsigned char* p = base + o;
+         o += (bytes + 255) & ~(size_t)255;
+         return p;
+      };
+      ds.X = (float2*)carve(nslots * col * sizeof(float2));
+      ds.lpx = (float*)carve(nslots * col * sizeof(float));
+      ds.gam = nullptr;
+      ds.lbl = (int8_t*)carve(nslots * col);
+      ds.wl = (int8_t*)carve(nslots * col);
+      ds.ya = (int8_t*)carve(nslots * col);
+      ds.yb = (int8_t*)carve(nslots * col);
+      ds.yc = (int8_t*)carve(nslots * col);
+      ds.rng = (uint32_t*)carve(nslots * RNG_WORDS * TILE * sizeof(uint32_t));
+      ds.sortbuf = smem_sort ? nullptr : (float*)carve(nslots * sort_bytes_warp);
+      if ( o > NOALLOC_SCRATCH_BYTES )
+         return fail(nullptr, KINC_SIM_EINVAL, "allocation-free scratch layout overflow");
+   }
+   uint32_t* d_umask = (uint32_t*)(base + oMask);
+   double* d_logn = (double*)(base + oLogn);
+   int32_t* d_N = (int32_t*)(base + oN);
+   int32_t* d_pg = (int32_t*)(base + oPg);
+   uint64_t* d_qpos = (uint64_t*)(base + oQ);
+   unsigned long long* d_bsum = (unsigned long long*)(base + oBsum);
+   unsigned long long* small = (unsigned long long*)(base + oSmall);
+   unsigned long long* d_qbase = small + 0;
+   unsigned long long* d_tiles = small + 1;
+   unsigned long long* d_work = small + 2;      /* 4 words */
+   int* d_status = (int*)(small + 6);
+
+   /* every call shares the array: clear what must start at zero */
+   CK(cudaMemsetAsync(small, 0, 8 * sizeof(unsigned long long), st));
+   for ( int n = 0; n <= S; ++n ) g_noalloc_host_logn[n] = std::log((double)n);
+   CK(cudaMemcpyAsync(d_logn, g_noalloc_host_logn, (size_t)(S + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
+   k_masks<<<std::max(1, std::min(65535, (int)(((int64_t)genes * W + 255) / 256))), 256, 0, st>>>(
+      d_gem, genes, S, W, params->min_expr, d_umask);
+   k_count<<<(int)std::min<int64_t>((span + 255) / 256, 65535), 256, 0, st>>>(d_umask, W, lo, span, d_N);
+   if ( dp.clus != 0 && dp.rand_mode == 0 )
+   {
+      if ( start > 0 )
+         k_count_qualifying<<<1024, 256, 0, st>>>(d_umask, W, start, dp.min_samples, d_qbase);
+      const int64_t offq = start - lo;
+      k_scan_sums<<<nscan, SCAN_THREADS, 0, st>>>(d_N, offq, size, dp.min_samples, d_bsum);
+      k_scan_blocks<<<1, SCAN_THREADS, 0, st>>>(d_bsum, nscan, d_qbase);
+      k_scan_apply<<<nscan, SCAN_THREADS, 0, st>>>(d_N, offq, size, dp.min_samples, d_bsum, d_qpos);
+   }
+   if ( dp.corr == 0 && dp.semantics == 0 )
+   {
+      const int64_t nwb = (end - 1) / KINC_SIM_WORK_BLOCK_SIZE - lo / KINC_SIM_WORK_BLOCK_SIZE + 1;
+      k_prev<<<(int)((nwb + 63) / 64), 64, 0, st>>>(d_N, lo, end, d_pg);
+   }
+   CK(cudaGetLastError());
+   DevData dd {};
+   dd.gem = d_gem;
+   dd.umask = d_umask;
+   dd.logn = d_logn;
+   dd.jump = nd.jump;
+   dd.rng0 = nd.rng0;
+   DevBlock B {};
+   B.start = start;
+   B.size = size;
+   B.lo = lo;
+   B.N = d_N;
+   B.pg = d_pg;
+   B.qpos = d_qpos;
+   B.outK = d_K;
+   B.outLabels = d_labels;
+   B.outCorr = d_corr;
+   B.tiles = d_tiles;
+   B.status = d_status;
+   B.work = d_work;
+   const int grid = (int)(nslots / WARPS_PER_BLOCK);
+   cudaError_t e = kern.clus == 0 ? sim_launch_none(kern, grid, smem_bytes, st, dp, dd, ds, B, smem_sort)
+                 : kern.clus == 1 ? sim_launch_gmm(kern, grid, smem_bytes, st, dp, dd, ds, B, smem_sort)
+                                  : sim_launch_kmeans(kern, grid, smem_bytes, st, dp, dd, ds, B, smem_sort);
+   CK(e);
+
+   /* the scratch is shared by every call: finish before the next one reuses it */
+   CK(cudaStreamSynchronize(st));
+   int status = 0;
+   CK(cudaMemcpy(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost));
+   if ( status != ST_OK ) return fail(nullptr, KINC_SIM_EKERNEL, "kernel reported status %d", status);
+   return KINC_SIM_OK;
 }
