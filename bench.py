@@ -301,7 +301,7 @@ def main():
     if os.path.exists(tpath):
         with open(tpath) as fh:
             tj = json.load(fh)
-        traffic = tj.get("bytes_per_pair", 0) * B * args.steps / max(1, args.steps)
+        traffic = tj.get("bytes_per_pair", 0) * B   # DRAM bytes of one launch (one step), scaled from the capture
     roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak, "traffic": traffic,
                 "peak_source": f"nominal FP32 FMA rate: {props.multi_processor_count} SMs x 128 lanes x 2 flops x "
