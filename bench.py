@@ -145,6 +145,91 @@ def run_reference(args, gem):
     print(json.dumps(line), flush=True)
 
 
+def dense_leg(L, vp, check_pairs=1000000):
+    """Pearson without clustering on the dense 20,000 x 2,000 workload (kinc_gb300.synthetic workload 3:
+    rank-50 factors + noise, per-gene NaN rate ~U(0,0.2)): all 199,990,000 pairs with the tcgen05 tensor-core
+    form (TF32 and 3xBF16) and a 1,048,576-pair block with the plain per-pair FP32 kernel, both
+    device-resident and timed with CUDA events; max |r - r_fp64| over a seeded random subset."""
+    import ctypes
+
+    import torch
+
+    from kinc_gb300 import Similarity, _native, synthetic
+    from oracle import pyoracle
+    gem = synthetic.generate(3)
+    G, S = gem.shape
+    total = G * (G - 1) // 2
+    rng = np.random.default_rng(20260103)
+    idx = np.sort(rng.choice(total, size=min(check_pairs, total), replace=False))
+    x, y = pyoracle.pair_xy(idx)
+    ref = pyoracle.pearson_fp64_pairs(gem, x, y)
+    ok = ~np.isnan(ref)
+    out = {"workload": "Pearson, no clustering, GEM 20000x2000 float32, rank-50 factors + N(0,0.5) noise, "
+                       "per-gene NaN rate ~U(0,0.2), pairwise-complete (semantics fixed)",
+           "pairs": total, "fp64_check_pairs": int(len(idx))}
+    stream = torch.cuda.Stream()
+    for prec in ("tf32", "3xbf16", "fp32"):
+        sim = Similarity(gem, semantics="fixed", precision=prec, maxclus=1)
+        sim.initialize()
+        ctx = sim._ctx
+        mb = L.kinc_sim_max_device_block(ctx)
+        n_run = total if prec != "fp32" else min(1 << 20, total)
+        chunk = min(mb, n_run)
+        dK = torch.empty(chunk, dtype=torch.int8, device="cuda")
+        dC = torch.empty((chunk, 1), dtype=torch.float32, device="cuda")
+        dL = torch.empty((chunk, S), dtype=torch.int8, device="cuda") if prec == "fp32" else None
+        got = np.empty(n_run, np.float32)
+
+        def run(keep):
+            for s0 in range(0, n_run, chunk):
+                n = min(chunk, n_run - s0)
+                rc = L.kinc_sim_execute_block_device(ctx, s0, n, vp(dK.data_ptr()),
+                                                     vp(dL.data_ptr()) if dL is not None else None,
+                                                     vp(dC.data_ptr()), vp(stream.cuda_stream))
+                _native.check(rc, ctx)
+                if keep:
+                    stream.synchronize()
+                    got[s0:s0 + n] = dC[:n, 0].cpu().numpy()
+        with torch.cuda.stream(stream):
+            run(True)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            reps = 3 if prec != "fp32" else 1
+            e0.record(stream)
+            for _ in range(reps):
+                run(False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        _native.check(L.kinc_sim_synchronize(ctx), ctx)
+        sim.close()
+        entry = {"pairs_timed": int(n_run), "ms": ms, "pairs_per_s": n_run / (ms / 1e3)}
+        sel = idx < n_run
+        if sel.any():
+            g = got[idx[sel]].astype(np.float64)
+            m = ok[sel]
+            entry["max_abs_err_vs_fp64"] = float(np.abs(g[m] - ref[sel][m]).max())
+            entry["fp64_pairs_compared"] = int(m.sum())
+        if prec != "fp32":
+            useful = 12.0 * S * n_run / (ms / 1e3) / 1e12
+            entry["useful_tflops"] = useful
+        out[prec] = entry
+    peaks = os.path.join(REPO, "MEASURED_PEAKS.json")
+    bf16 = 1893.1
+    if os.path.exists(peaks):
+        with open(peaks) as fh:
+            bf16 = float(json.load(fh).get("bf16_tflops", bf16))
+    out["tf32"]["frac_of_tf32_peak"] = out["tf32"]["useful_tflops"] / (bf16 / 2)
+    out["3xbf16"]["executed_tflops"] = 2 * out["3xbf16"]["useful_tflops"]
+    out["3xbf16"]["frac_of_bf16_peak"] = out["3xbf16"]["executed_tflops"] / bf16
+    out["peak_note"] = (f"TF32 dense peak taken as half the measured bf16 burst ({bf16:.0f} TFLOP/s, "
+                        "MEASURED_PEAKS.json); 3xBF16 executes 2x the useful flops of the TF32 form")
+    out["speedup_tf32_vs_fp32_per_pair"] = out["tf32"]["pairs_per_s"] / out["fp32"]["pairs_per_s"]
+    out["speedup_3xbf16_vs_fp32_per_pair"] = out["3xbf16"]["pairs_per_s"] / out["fp32"]["pairs_per_s"]
+    return out
+
+
 def config_dict(args, gem):
     G, S = gem.shape
     return {"workload": "GMM k<=5 + Spearman, GEM 5000x1000 float32, 10% NaN, 10 planted modules; "
@@ -165,6 +250,8 @@ def main():
     ap.add_argument("--cpu-pairs-per-thread", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-dense", action="store_true")
+    ap.add_argument("--dense-check-pairs", type=int, default=1000000)
     args = ap.parse_args()
 
     from kinc_gb300 import synthetic
@@ -308,6 +395,8 @@ def main():
                                f"{sm_max:.0f} MHz (MEASURED_PEAKS.json holds no FP32 figure)",
                 "kernel": "k_similarity", "units": units, "flops_per_unit": FLOPS_PER_UNIT, "fits": fits}
 
+    tensor_core = None if args.no_dense else dense_leg(L, vp, args.dense_check_pairs)
+
     cpu = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -320,7 +409,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded; no public dataset)",
             "config": config_dict(args, gem), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-            "cpu_baseline": cpu, "clocks": clk}
+            "cpu_baseline": cpu, "clocks": clk, "tensor_core": tensor_core}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

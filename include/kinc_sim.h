@@ -62,8 +62,9 @@ typedef struct kinc_sim_params
                                 Pearson/Spearman (default); 1: each sample's own values */
    int32_t rand_mode;     /* 0: the process-global glibc rand() stream of a serial KINC run (default);
                              1: the POSIX LCG reset per fit used by the OpenCL worker */
-   int32_t precision;     /* clusmethod none + pearson only: 0 per-pair FP32 (default), 1 TF32 tensor
-                             cores, 2 3xBF16 tensor cores (semantics 1 only) */
+   int32_t precision;     /* clusmethod none + pearson + semantics 1 only: 0 per-pair FP32 (default),
+                             1 TF32 tensor cores, 2 3xBF16 tensor cores (pairwise-complete Pearson as a
+                             masked contraction; labels are not written) */
 } kinc_sim_params;
 
 /* Fill `p` with the reference defaults. */

@@ -17,6 +17,7 @@
  */
 #include "../../include/kinc_sim.h"
 #include "sim_kernel.cuh"
+#include "pearson_tc.h"
 
 #include <cuda_runtime.h>
 
@@ -212,6 +213,8 @@ struct kinc_sim_ctx
    DevScratch ds {};
    cudaStream_t stream = nullptr;
    SimKernel kern {};
+   TcState tc;                      /* tensor-core Pearson form (precision != 0) */
+   bool use_tc = false;
    int grid = 0;
    int smem_bytes = 0;
    int smem_sort = 0;
@@ -343,6 +346,12 @@ int validate(const kinc_sim_params* p, int32_t G, int32_t S, std::string& why)
    if ( p->semantics < 0 || p->semantics > 1 ) { why = "semantics must be 0 or 1"; return 0; }
    if ( p->rand_mode < 0 || p->rand_mode > 1 ) { why = "rand_mode must be 0 or 1"; return 0; }
    if ( p->precision < 0 || p->precision > 2 ) { why = "precision must be 0, 1 or 2"; return 0; }
+   if ( p->precision != 0 && (p->clus_method != 0 || p->corr_method != 0 || p->semantics != 1) )
+   {
+      why = "precision TF32/3xBF16 is the tensor-core pairwise-complete Pearson: it needs clus_method none, "
+            "corr_method pearson and semantics 1 (each sample's own values)";
+      return 0;
+   }
    return 1;
 }
 
@@ -415,6 +424,7 @@ static void release(kinc_sim_ctx* c)
                     c->d_scratch };
    for ( void* p : ptrs )
       if ( p ) cudaFree(p);
+   tc_release(c->tc);
    if ( c->stream ) cudaStreamDestroy(c->stream);
 }
 
@@ -566,16 +576,17 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
       ctx->ds.sortbuf = ctx->smem_sort ? nullptr : (float*)(base + oS);
    }
 
-   /* one device block of pairs */
+   /* one device block of pairs (the tensor-core form writes no labels, so its blocks can be far larger) */
    const int64_t total = (int64_t)genes * (genes - 1) / 2;
    int64_t mb = 1 << 20;
    while ( mb > 4096 && (size_t)mb * S > ((size_t)1 << 31) ) mb >>= 1;
+   if ( params->precision != 0 ) mb = (int64_t)1 << 27;
    ctx->max_block = std::min<int64_t>(mb, std::max<int64_t>(total, 1));
-   const int64_t nspan = ctx->max_block + KINC_SIM_WORK_BLOCK_SIZE;
+   const int64_t nspan = (params->precision != 0 ? 4096 : ctx->max_block) + KINC_SIM_WORK_BLOCK_SIZE;
    const int64_t nscan = (ctx->max_block + SCAN_THREADS - 1) / SCAN_THREADS;
    CKC(cudaMalloc(&ctx->d_N, nspan * sizeof(int32_t)));
    CKC(cudaMalloc(&ctx->d_pg, nspan * sizeof(int32_t)));
-   CKC(cudaMalloc(&ctx->d_qpos, ctx->max_block * sizeof(uint64_t)));
+   CKC(cudaMalloc(&ctx->d_qpos, (params->precision != 0 ? 4096 : ctx->max_block) * sizeof(uint64_t)));
    CKC(cudaMalloc(&ctx->d_bsum, (nscan + 1) * sizeof(unsigned long long)));
    CKC(cudaMalloc(&ctx->d_qbase, sizeof(unsigned long long)));
    CKC(cudaMalloc(&ctx->d_tiles, sizeof(unsigned long long)));
@@ -583,12 +594,25 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    CKC(cudaMemsetAsync(ctx->d_work, 0, 4 * sizeof(unsigned long long), ctx->stream));
    CKC(cudaMalloc(&ctx->d_status, sizeof(int)));
    CKC(cudaMalloc(&ctx->d_K, ctx->max_block));
-   CKC(cudaMalloc(&ctx->d_labels, (size_t)ctx->max_block * S));
+   if ( params->precision == 0 ) CKC(cudaMalloc(&ctx->d_labels, (size_t)ctx->max_block * S));
    CKC(cudaMalloc(&ctx->d_corr, (size_t)ctx->max_block * params->max_clusters * sizeof(float)));
    CKC(cudaMemsetAsync(ctx->d_qbase, 0, sizeof(unsigned long long), ctx->stream));
    CKC(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
    ctx->q_valid_end = 0;
 
+   if ( params->precision != 0 )
+   {
+      char msg[256] = { 0 };
+      cudaError_t e = tc_prepare(ctx->tc, ctx->d_gem, genes, S, params->min_expr, params->precision, ctx->stream,
+                                 msg, sizeof msg);
+      if ( e != cudaSuccess )
+      {
+         fail(ctx, e == cudaErrorMemoryAllocation ? KINC_SIM_ENOMEM : KINC_SIM_ECUDA, "tensor-core set-up: %s %s",
+              cudaGetErrorString(e), msg);
+         return bail(e == cudaErrorMemoryAllocation ? KINC_SIM_ENOMEM : KINC_SIM_ECUDA);
+      }
+      ctx->use_tc = true;
+   }
    ctx->dd.gem = ctx->d_gem;
    ctx->dd.umask = ctx->d_umask;
    ctx->dd.logn = ctx->d_logn;
@@ -605,6 +629,14 @@ static int enqueue_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t*
                          float* d_corr, cudaStream_t st)
 {
    const DevParams& dp = ctx->dp;
+   if ( ctx->use_tc )
+   {
+      int launches = 0;
+      CK(tc_enqueue(ctx->tc, ctx->G, ctx->S, dp.min_samples, dp.max_k, start, size, d_K, d_corr, ctx->d_status, st,
+                    &launches));
+      ctx->launches += launches;
+      return KINC_SIM_OK;
+   }
    const int64_t end = start + size;
    const int64_t lo = (start / KINC_SIM_WORK_BLOCK_SIZE) * KINC_SIM_WORK_BLOCK_SIZE;
    const int64_t span = end - lo;
@@ -721,12 +753,12 @@ extern "C" int kinc_sim_execute_block(kinc_sim_ctx* ctx, int64_t start, int64_t 
    {
       const int64_t n = std::min<int64_t>(ctx->max_block, size - done);
       const int32_t before = ctx->launches;
-      rc = enqueue_block(ctx, start + done, n, ctx->d_K, out_labels ? ctx->d_labels : nullptr,
+      rc = enqueue_block(ctx, start + done, n, ctx->d_K, (out_labels && ctx->d_labels) ? ctx->d_labels : nullptr,
                          ctx->d_corr, ctx->stream);
       (void)before;
       if ( rc ) return rc;
       if ( out_K ) CK(cudaMemcpyAsync(out_K + done, ctx->d_K, n, cudaMemcpyDeviceToHost, ctx->stream));
-      if ( out_labels )
+      if ( out_labels && ctx->d_labels )
          CK(cudaMemcpyAsync(out_labels + done * S, ctx->d_labels, (size_t)n * S, cudaMemcpyDeviceToHost,
                             ctx->stream));
       if ( out_corr )

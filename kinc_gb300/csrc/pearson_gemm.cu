@@ -1,0 +1,620 @@
+/*
+ * pearson_gemm.cu -- pairwise-complete Pearson for clusmethod none as a dense
+ * masked contraction on the tcgen05 tensor cores (precision TF32 or 3xBF16).
+ *
+ * For genes x, y with usable-sample masks m and centred values a (a = v - mean
+ * over the gene's usable samples, 0 where unusable), every sum Pearson needs
+ * over the samples both genes have is a product of two [genes][samples]
+ * operands:
+ *     n   = M  . M^T      Sxy = A . A^T
+ *     Sx  = A  . M^T      Sy  = M . A^T
+ *     Sxx = A2 . M^T      Syy = M . A2^T       (A2 = a^2)
+ * Centring by the gene mean changes no correlation (r is shift invariant per
+ * gene) but removes the cancellation that would otherwise swamp TF32.  One CTA
+ * computes a 128 x 64 tile of pairs: TMA streams 128-byte-swizzled K-chunks of
+ * the operands into a 3-stage shared-memory ring, one thread issues the
+ * tcgen05.mma instructions (M=128, N=64) into six accumulators held in TMEM
+ * (6 x 64 of the 512 columns), and the four warps read them back with
+ * tcgen05.ld and form r = (n Sxy - Sx Sy) / sqrt((n Sxx - Sx^2)(n Syy - Sy^2))
+ * with error-compensated products.  3xBF16 splits a = hi + lo and sums
+ * hi.hi + hi.lo + lo.hi (the mask is exact in BF16).
+ *
+ * The result is the mathematically pairwise-complete Pearson (each sample's own
+ * values), i.e. semantics "fixed"; KINC's packed-array indexing is not a
+ * contraction.  Every wait on an mbarrier is bounded: on expiry the kernel
+ * records an error, drains its own copies (bounded), frees its TMEM and returns.
+ */
+#include "../../include/kinc_sim.h"
+#include "pearson_tc.h"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+
+namespace kinc_tc {
+
+constexpr int BM = 128;               /* pair-tile rows (genes x) */
+constexpr int BN = 64;                /* pair-tile columns (genes y) */
+constexpr int NACC = 6;               /* Sxy, Sx, Sy, Sxx, Syy, n */
+constexpr int TMEM_COLS = 512;
+constexpr int STAGES = 3;
+constexpr int THREADS = 128;
+constexpr long long WAIT_CYCLES = 4ll << 30;  /* ~2 s of SM clock before a wait gives up */
+
+constexpr int ST_TIMEOUT = 10;        /* an mbarrier wait expired */
+
+/* per precision: element type, elements per K-chunk row, swizzle, operands per side */
+template <int MODE> struct Cfg;
+template <> struct Cfg<1>             /* TF32: A, A2, M as fp32 rounded to tf32 */
+{
+   static constexpr int ELEM = 4;
+   static constexpr int BK = 32;      /* 128-byte rows, SWIZZLE_128B */
+   static constexpr int ROWB = 128;
+   static constexpr int NMAT = 3;
+   static constexpr int UMMA_K = 8;
+   static constexpr uint32_t A_FMT = 2, B_FMT = 2;   /* tf32 */
+   static constexpr uint64_t LAYOUT = 2;              /* SWIZZLE_128B */
+};
+template <> struct Cfg<2>             /* 3xBF16: A_hi, A_lo, A2_hi, A2_lo, M as bf16 */
+{
+   static constexpr int ELEM = 2;
+   static constexpr int BK = 32;      /* 64-byte rows, SWIZZLE_64B */
+   static constexpr int ROWB = 64;
+   static constexpr int NMAT = 5;
+   static constexpr int UMMA_K = 16;
+   static constexpr uint32_t A_FMT = 1, B_FMT = 1;   /* bf16 */
+   static constexpr uint64_t LAYOUT = 4;              /* SWIZZLE_64B */
+};
+
+template <int MODE>
+struct Layout
+{
+   static constexpr int XMAT = BM * Cfg<MODE>::ROWB;          /* bytes of one x-side operand chunk */
+   static constexpr int YMAT = BN * Cfg<MODE>::ROWB;
+   static constexpr int STAGE = Cfg<MODE>::NMAT * (XMAT + YMAT);
+   static constexpr int RING = STAGES * STAGE;
+   static constexpr int SMEM = RING + 1024 /* alignment slack */ + 256 /* barriers */;
+};
+
+/* ---------------------------------------------------------------- PTX */
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+   return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+/* bounded wait for phase `parity` of an mbarrier; false on expiry */
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+   const long long t0 = clock64();
+   for ( ;; )
+   {
+      uint32_t ok;
+      asm volatile("{\n\t.reg .pred p;\n\t"
+                   "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                   "selp.u32 %0, 1, 0, p;\n\t}"
+                   : "=r"(ok)
+                   : "r"(bar), "r"(parity)
+                   : "memory");
+      if ( ok ) return true;
+      if ( clock64() - t0 > WAIT_CYCLES ) return false;
+   }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar)
+{
+   asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+                "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+                : "memory");
+}
+
+/* shared-memory matrix descriptor: K-major, swizzled rows of ROWB bytes, 8-row atoms */
+template <int MODE>
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
+{
+   const uint64_t sbo = (uint64_t)(8 * Cfg<MODE>::ROWB) >> 4;
+   uint64_t d = 0;
+   d |= (uint64_t)((addr >> 4) & 0x3fff);       /* start address */
+   d |= (uint64_t)0 << 16;                        /* leading byte offset: unused for swizzled K-major */
+   d |= (sbo & 0x3fff) << 32;                     /* stride byte offset: next 8-row group */
+   d |= (uint64_t)1 << 46;                        /* descriptor version */
+   d |= Cfg<MODE>::LAYOUT << 61;                  /* swizzle mode */
+   return d;
+}
+
+/* instruction descriptor: D f32, A/B format, both K-major, N = BN, M = BM */
+template <int MODE>
+__host__ __device__ constexpr uint32_t instr_desc()
+{
+   return (1u << 4)                                /* D format f32 */
+          | (Cfg<MODE>::A_FMT << 7) | (Cfg<MODE>::B_FMT << 10)
+          | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+template <int MODE>
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate)
+{
+   constexpr uint32_t idesc = instr_desc<MODE>();
+   if ( MODE == 1 )
+   {
+      asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                   "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                   "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+   }
+   else
+   {
+      asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                   "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                   "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+   }
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+{
+   uint32_t r[16];
+   asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15},"
+                " [%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr));
+   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+   for ( int i = 0; i < 16; ++i ) v[i] = __uint_as_float(r[i]);
+}
+
+/* ------------------------------------------------------------ kernels */
+
+/* Operands per gene (one warp per gene): mean over usable samples in fp64,
+ * centred values rounded to the tensor-core format, zero where unusable or
+ * beyond S (padding to Sp columns and Gp rows). */
+template <int MODE>
+__global__ void k_tc_prep(const float* __restrict__ gem, int G, int S, int Gp, int Sp, float min_expr,
+                          void* __restrict__ ops)
+{
+   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+   const int lane = threadIdx.x & 31;
+   if ( warp >= Gp ) return;
+   const size_t plane = (size_t)Gp * Sp;
+   double sum = 0.0;
+   int n = 0;
+   if ( warp < G )
+   {
+      for ( int s = lane; s < S; s += 32 )
+      {
+         const float v = gem[(size_t)warp * S + s];
+         if ( !isnan(v) && !(v < min_expr) )
+         {
+            sum += v;
+            ++n;
+         }
+      }
+   }
+   for ( int o = 16; o > 0; o >>= 1 )
+   {
+      sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      n += __shfl_xor_sync(0xffffffffu, n, o);
+   }
+   const double mean = n > 0 ? sum / n : 0.0;
+   for ( int s = lane; s < Sp; s += 32 )
+   {
+      float a = 0.f, m = 0.f;
+      if ( warp < G && s < S )
+      {
+         const float v = gem[(size_t)warp * S + s];
+         if ( !isnan(v) && !(v < min_expr) )
+         {
+            a = (float)((double)v - mean);
+            m = 1.f;
+         }
+      }
+      const float a2 = a * a;
+      const size_t o = (size_t)warp * Sp + s;
+      if ( MODE == 1 )
+      {
+         float* f = (float*)ops;
+         uint32_t t;
+         asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(a));
+         f[o] = __uint_as_float(t);
+         asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(t) : "f"(a2));
+         f[plane + o] = __uint_as_float(t);
+         f[2 * plane + o] = m;
+      }
+      else
+      {
+         __nv_bfloat16* h = (__nv_bfloat16*)ops;
+         const __nv_bfloat16 ahi = __float2bfloat16_rn(a);
+         const __nv_bfloat16 alo = __float2bfloat16_rn(a - __bfloat162float(ahi));
+         const __nv_bfloat16 qhi = __float2bfloat16_rn(a2);
+         const __nv_bfloat16 qlo = __float2bfloat16_rn(a2 - __bfloat162float(qhi));
+         h[o] = ahi;
+         h[plane + o] = alo;
+         h[2 * plane + o] = qhi;
+         h[3 * plane + o] = qlo;
+         h[4 * plane + o] = __float2bfloat16_rn(m);
+      }
+   }
+}
+
+struct TcArgs
+{
+   int I0;                            /* first row tile (blockIdx.y = I - I0, blockIdx.x = J) */
+   int64_t xb;                        /* last row of the pair range */
+   int G;
+   int min_samples;
+   int max_k;
+   int64_t start, end;                /* pairs written: [start, end) */
+   float* out_corr;                   /* [p - start][max_k], column 0 */
+   int* status;
+   int kchunks;
+};
+
+/* error-compensated a*b - c*d in fp32 (the products' rounding errors recovered by fma) */
+__device__ __forceinline__ float diff_of_products(float a, float b, float c, float d)
+{
+   const float cd = c * d;
+   const float err = fmaf(-c, d, cd);
+   const float dop = fmaf(a, b, -cd);
+   return dop + err;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant__ TcMaps maps, TcArgs args)
+{
+   using C = Cfg<MODE>;
+   using L = Layout<MODE>;
+   extern __shared__ __align__(1024) unsigned char smem_raw[];
+   /* 1024-byte aligned ring (swizzle atoms), barriers after it */
+   unsigned char* ring = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+   uint64_t* bars = (uint64_t*)(ring + L::RING);
+   uint32_t* tmem_holder = (uint32_t*)(bars + 2 * STAGES + 1);
+   __shared__ int s_fail;
+
+   const int I = args.I0 + (int)blockIdx.y;
+   const int J = (int)blockIdx.x;
+   /* tiles entirely on or above the diagonal (y >= x) or past the range hold no pair */
+   const int64_t rowmax = (int64_t)(I + 1) * BM - 1;
+   const int64_t xmax = rowmax < args.xb ? rowmax : args.xb;
+   if ( (int64_t)J * BN >= xmax ) return;
+   /* a CTA that failed earlier in this launch stops the rest from starting */
+   if ( *(volatile int*)args.status != 0 ) return;
+   const int warp = threadIdx.x >> 5;
+   const int lane = threadIdx.x & 31;
+
+   const uint32_t full0 = smem_u32(&bars[0]);
+   const uint32_t empty0 = smem_u32(&bars[STAGES]);
+   const uint32_t done = smem_u32(&bars[2 * STAGES]);
+
+   if ( threadIdx.x == 0 )
+   {
+      s_fail = 0;
+      for ( int s = 0; s < STAGES; ++s )
+      {
+         mbar_init(full0 + 8 * s, 1);
+         mbar_init(empty0 + 8 * s, 1);
+      }
+      mbar_init(done, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+   }
+   if ( warp == 0 )
+   {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                   "r"(TMEM_COLS));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+   }
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   const uint32_t tmem = *tmem_holder;
+
+   const int K = args.kchunks;
+   int issued = 0;                      /* TMA chunks issued (producer) */
+   if ( warp == 0 && lane == 0 )
+   {
+      /* ---- producer: TMA into the ring */
+      for ( int kc = 0; kc < K; ++kc )
+      {
+         const int s = kc % STAGES;
+         if ( kc >= STAGES && !mbar_wait(empty0 + 8 * s, ((kc / STAGES) - 1) & 1) )
+         {
+            atomicExch(&s_fail, 1);
+            break;
+         }
+         if ( *(volatile int*)&s_fail ) break;
+         const uint32_t stage = smem_u32(ring + s * L::STAGE);
+         mbar_expect_tx(full0 + 8 * s, L::STAGE);
+         for ( int m = 0; m < C::NMAT; ++m )
+         {
+            tma_load_2d(stage + m * L::XMAT, &maps.x[m], kc * C::BK, I * BM, full0 + 8 * s);
+            tma_load_2d(stage + C::NMAT * L::XMAT + m * L::YMAT, &maps.y[m], kc * C::BK, J * BN, full0 + 8 * s);
+         }
+         ++issued;
+      }
+   }
+   else if ( warp == 1 && lane == 0 )
+   {
+      /* ---- MMA issuer */
+      for ( int kc = 0; kc < K; ++kc )
+      {
+         const int s = kc % STAGES;
+         if ( !mbar_wait(full0 + 8 * s, (kc / STAGES) & 1) )
+         {
+            atomicExch(&s_fail, 1);
+            break;
+         }
+         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+         const uint32_t stage = smem_u32(ring + s * L::STAGE);
+         const uint32_t ysb = stage + C::NMAT * L::XMAT;
+         for ( int ks = 0; ks < C::BK / C::UMMA_K; ++ks )
+         {
+            const uint32_t koff = ks * C::UMMA_K * C::ELEM;   /* byte step along K inside the row */
+            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+            if ( MODE == 1 )
+            {
+               /* x side: 0 A, 1 A2, 2 M; y side likewise */
+               const uint64_t xa = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
+               const uint64_t xq = smem_desc<MODE>(stage + 1 * L::XMAT + koff);
+               const uint64_t xm = smem_desc<MODE>(stage + 2 * L::XMAT + koff);
+               const uint64_t ya = smem_desc<MODE>(ysb + 0 * L::YMAT + koff);
+               const uint64_t yq = smem_desc<MODE>(ysb + 1 * L::YMAT + koff);
+               const uint64_t ym = smem_desc<MODE>(ysb + 2 * L::YMAT + koff);
+               mma<MODE>(tmem + 0 * BN, xa, ya, acc);   /* Sxy */
+               mma<MODE>(tmem + 1 * BN, xa, ym, acc);   /* Sx */
+               mma<MODE>(tmem + 2 * BN, xm, ya, acc);   /* Sy */
+               mma<MODE>(tmem + 3 * BN, xq, ym, acc);   /* Sxx */
+               mma<MODE>(tmem + 4 * BN, xm, yq, acc);   /* Syy */
+               mma<MODE>(tmem + 5 * BN, xm, ym, acc);   /* n */
+            }
+            else
+            {
+               /* 0 A_hi, 1 A_lo, 2 A2_hi, 3 A2_lo, 4 M */
+               uint64_t xd[5], yd[5];
+#pragma unroll
+               for ( int m = 0; m < 5; ++m )
+               {
+                  xd[m] = smem_desc<MODE>(stage + m * L::XMAT + koff);
+                  yd[m] = smem_desc<MODE>(ysb + m * L::YMAT + koff);
+               }
+               mma<MODE>(tmem + 0 * BN, xd[0], yd[0], acc);   /* Sxy: hi.hi + hi.lo + lo.hi */
+               mma<MODE>(tmem + 0 * BN, xd[0], yd[1], 1u);
+               mma<MODE>(tmem + 0 * BN, xd[1], yd[0], 1u);
+               mma<MODE>(tmem + 1 * BN, xd[0], yd[4], acc);   /* Sx */
+               mma<MODE>(tmem + 1 * BN, xd[1], yd[4], 1u);
+               mma<MODE>(tmem + 2 * BN, xd[4], yd[0], acc);   /* Sy */
+               mma<MODE>(tmem + 2 * BN, xd[4], yd[1], 1u);
+               mma<MODE>(tmem + 3 * BN, xd[2], yd[4], acc);   /* Sxx */
+               mma<MODE>(tmem + 3 * BN, xd[3], yd[4], 1u);
+               mma<MODE>(tmem + 4 * BN, xd[4], yd[2], acc);   /* Syy */
+               mma<MODE>(tmem + 4 * BN, xd[4], yd[3], 1u);
+               mma<MODE>(tmem + 5 * BN, xd[4], yd[4], acc);   /* n */
+            }
+         }
+         mma_commit(empty0 + 8 * s);      /* frees the stage when these MMAs have read it */
+      }
+      mma_commit(done);                   /* all accumulators final */
+   }
+   __syncwarp();
+
+   /* ---- epilogue: every warp reads its 32 TMEM lanes (tile rows) */
+   bool ok = mbar_wait(done, 0);
+   if ( !ok ) atomicExch(&s_fail, 1);
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   if ( ok && !*(volatile int*)&s_fail )
+   {
+      const int row = warp * 32 + lane;
+      const int64_t x = (int64_t)I * BM + row;
+      const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+      const int64_t pbase = x * (x - 1) / 2;
+      for ( int c = 0; c < BN / 16; ++c )
+      {
+         float v[NACC][16];
+#pragma unroll
+         for ( int a = 0; a < NACC; ++a ) tmem_ld16(lane_base + a * BN + c * 16, v[a]);
+         if ( x < args.G )
+         {
+#pragma unroll
+            for ( int jj = 0; jj < 16; ++jj )
+            {
+               const int64_t y = (int64_t)J * BN + c * 16 + jj;
+               if ( y >= x ) continue;
+               const int64_t p = pbase + y;
+               if ( p < args.start || p >= args.end ) continue;
+               const float sxy = v[0][jj], sx = v[1][jj], sy = v[2][jj], sxx = v[3][jj], syy = v[4][jj];
+               const float n = v[5][jj];
+               float r = __int_as_float(0x7fc00000);
+               if ( n >= (float)args.min_samples && n > 0.f )
+               {
+                  const float num = diff_of_products(n, sxy, sx, sy);
+                  const float dx = diff_of_products(n, sxx, sx, sx);
+                  const float dy = diff_of_products(n, syy, sy, sy);
+                  r = num * rsqrtf(dx) * rsqrtf(dy);
+               }
+               args.out_corr[(p - args.start) * args.max_k] = r;
+            }
+         }
+      }
+   }
+
+   /* ---- teardown: on failure drain this CTA's copies (bounded), then free TMEM */
+   __syncthreads();
+   if ( *(volatile int*)&s_fail )
+   {
+      if ( threadIdx.x == 0 )
+      {
+         atomicCAS(args.status, 0, ST_TIMEOUT);
+         for ( int kc = (issued > STAGES ? issued - STAGES : 0); kc < issued; ++kc )
+         {
+            mbar_wait(full0 + 8 * (kc % STAGES), (kc / STAGES) & 1);
+         }
+      }
+      __syncthreads();
+   }
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   if ( warp == 0 )
+   {
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+   }
+}
+
+/* K = 1 and NaN beyond column 0 for the pairs of the range (clusmethod none) */
+__global__ void k_tc_fill(int64_t size, int max_k, int8_t* __restrict__ K, float* __restrict__ corr)
+{
+   for ( int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < size; t += (int64_t)gridDim.x * blockDim.x )
+   {
+      if ( K ) K[t] = 1;
+      for ( int k = 1; k < max_k; ++k ) corr[t * max_k + k] = __int_as_float(0x7fc00000);
+   }
+}
+
+/* ---------------------------------------------------------------- host */
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn()
+{
+   static EncodeTiledFn fn = nullptr;
+   if ( !fn )
+   {
+      void* p = nullptr;
+      cudaDriverEntryPointQueryResult q;
+      if ( cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess
+           && q == cudaDriverEntryPointSuccess )
+         fn = (EncodeTiledFn)p;
+   }
+   return fn;
+}
+
+}  // namespace kinc_tc
+
+using namespace kinc_tc;
+
+/* prepare operands and tensor maps; returns a CUDA error or cudaSuccess */
+cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_expr, int mode, cudaStream_t st,
+                       char* err, size_t errlen)
+{
+   t.mode = mode;
+   t.Gp = (G + BM - 1) / BM * BM;
+   t.Sp = (S + 63) / 64 * 64;
+   const int elem = mode == 1 ? 4 : 2;
+   const int nmat = mode == 1 ? 3 : 5;
+   const size_t plane = (size_t)t.Gp * t.Sp * elem;
+   cudaError_t e = cudaMalloc(&t.ops, plane * nmat);
+   if ( e != cudaSuccess ) return e;
+   const int blocks = (t.Gp * 32 + 255) / 256;
+   if ( mode == 1 )
+   {
+      k_tc_prep<1><<<blocks, 256, 0, st>>>(d_gem, G, S, t.Gp, t.Sp, min_expr, t.ops);
+   }
+   else
+   {
+      k_tc_prep<2><<<blocks, 256, 0, st>>>(d_gem, G, S, t.Gp, t.Sp, min_expr, t.ops);
+   }
+   e = cudaGetLastError();
+   if ( e != cudaSuccess ) return e;
+   EncodeTiledFn enc = encode_fn();
+   if ( !enc )
+   {
+      snprintf(err, errlen, "cuTensorMapEncodeTiled is not available");
+      return cudaErrorNotSupported;
+   }
+   const int bk = 32;
+   for ( int m = 0; m < nmat; ++m )
+   {
+      char* base = (char*)t.ops + m * plane;
+      const cuuint64_t dims[2] = { (cuuint64_t)t.Sp, (cuuint64_t)t.Gp };
+      const cuuint64_t strides[1] = { (cuuint64_t)t.Sp * elem };
+      const cuuint32_t estr[2] = { 1, 1 };
+      const CUtensorMapDataType dt = mode == 1 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+      const CUtensorMapSwizzle sw = mode == 1 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+      const cuuint32_t boxx[2] = { (cuuint32_t)bk, (cuuint32_t)BM };
+      const cuuint32_t boxy[2] = { (cuuint32_t)bk, (cuuint32_t)BN };
+      CUresult r1 = enc(&t.maps.x[m], dt, 2, base, dims, strides, boxx, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      CUresult r2 = enc(&t.maps.y[m], dt, 2, base, dims, strides, boxy, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if ( r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS )
+      {
+         snprintf(err, errlen, "cuTensorMapEncodeTiled failed (%d, %d)", (int)r1, (int)r2);
+         return cudaErrorInvalidValue;
+      }
+   }
+   return cudaSuccess;
+}
+
+void tc_release(TcState& t)
+{
+   if ( t.ops ) cudaFree(t.ops);
+   t.ops = nullptr;
+}
+
+/* enqueue the pairs [start, start+size): K = 1, corr[.][0] = r, NaN elsewhere */
+cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int64_t start, int64_t size,
+                       int8_t* d_K, float* d_corr, int* d_status, cudaStream_t st, int* launches)
+{
+   const int64_t end = start + size;
+   /* rows touched by the range */
+   auto row_of = [](int64_t p) {
+      int64_t x = (int64_t)((1.0 + sqrt(1.0 + 8.0 * (double)p)) * 0.5);
+      while ( x * (x - 1) / 2 > p ) --x;
+      while ( (x + 1) * x / 2 <= p ) ++x;
+      return x;
+   };
+   const int64_t xa = row_of(start);
+   const int64_t xb = row_of(end - 1);
+   const int Ia = (int)(xa / BM), Ib = (int)(xb / BM);
+   const int Jn = (int)((xb + BN - 1) / BN);
+   if ( Jn < 1 ) return cudaSuccess;
+   k_tc_fill<<<(int)std::min<int64_t>((size + 255) / 256, 65535), 256, 0, st>>>(size, max_k, d_K, d_corr);
+   TcArgs a;
+   a.I0 = Ia;
+   a.xb = xb;
+   a.G = G;
+   a.min_samples = min_samples;
+   a.max_k = max_k;
+   a.start = start;
+   a.end = end;
+   a.out_corr = d_corr;
+   a.status = d_status;
+   a.kchunks = t.Sp / 32;
+   if ( t.mode == 1 )
+   {
+      const int smem = Layout<1>::SMEM;
+      cudaFuncSetAttribute(k_pearson_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      k_pearson_tc<1><<<dim3((unsigned)Jn, (unsigned)(Ib - Ia + 1)), THREADS, smem, st>>>(t.maps, a);
+   }
+   else
+   {
+      const int smem = Layout<2>::SMEM;
+      cudaFuncSetAttribute(k_pearson_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      k_pearson_tc<2><<<dim3((unsigned)Jn, (unsigned)(Ib - Ia + 1)), THREADS, smem, st>>>(t.maps, a);
+   }
+   if ( launches ) *launches += 2;
+   (void)S;
+   return cudaGetLastError();
+}

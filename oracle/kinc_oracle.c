@@ -1166,3 +1166,47 @@ double ko_pearson_fp64(const float* gem, int32_t S, int32_t x, int32_t y, float 
    }
    return sxy / sqrt(sxx * syy);
 }
+
+typedef struct
+{
+   const float* gem;
+   int32_t S;
+   const int32_t* xs;
+   const int32_t* ys;
+   int64_t lo, hi;
+   float min_expr;
+   int32_t min_samples;
+   double* out;
+} fp64_job;
+
+static void* fp64_worker(void* p)
+{
+   fp64_job* j = (fp64_job*)p;
+   int64_t i;
+   for ( i = j->lo; i < j->hi; ++i )
+   {
+      j->out[i] = ko_pearson_fp64(j->gem, j->S, j->xs[i], j->ys[i], j->min_expr, j->min_samples);
+   }
+   return NULL;
+}
+
+void ko_pearson_fp64_batch(const float* gem, int32_t S, const int32_t* xs, const int32_t* ys, int64_t n,
+                           float min_expr, int32_t min_samples, double* out, int32_t threads)
+{
+   pthread_t th[256];
+   fp64_job jobs[256];
+   int32_t t;
+   if ( threads < 1 ) threads = 1;
+   if ( threads > 256 ) threads = 256;
+   for ( t = 0; t < threads; ++t )
+   {
+      jobs[t].gem = gem; jobs[t].S = S; jobs[t].xs = xs; jobs[t].ys = ys;
+      jobs[t].lo = n * t / threads; jobs[t].hi = n * (t + 1) / threads;
+      jobs[t].min_expr = min_expr; jobs[t].min_samples = min_samples; jobs[t].out = out;
+      pthread_create(&th[t], NULL, fp64_worker, &jobs[t]);
+   }
+   for ( t = 0; t < threads; ++t )
+   {
+      pthread_join(th[t], NULL);
+   }
+}

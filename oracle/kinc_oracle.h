@@ -99,6 +99,10 @@ int64_t ko_process_block(int32_t S, const ko_params* p, int64_t start, int64_t s
 double ko_pearson_fp64(const float* gem, int32_t S, int32_t x, int32_t y, float min_expr,
                        int32_t min_samples);
 
+/* the same for n pairs (xs[i], ys[i]) with `threads` POSIX threads */
+void ko_pearson_fp64_batch(const float* gem, int32_t S, const int32_t* xs, const int32_t* ys, int64_t n,
+                           float min_expr, int32_t min_samples, double* out, int32_t threads);
+
 #ifdef __cplusplus
 }
 #endif

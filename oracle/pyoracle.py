@@ -67,6 +67,9 @@ def lib():
         L.ko_pearson_fp64.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                       ctypes.c_float, ctypes.c_int32]
         L.ko_pearson_fp64.restype = ctypes.c_double
+        L.ko_pearson_fp64_batch.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_int64, ctypes.c_float, ctypes.c_int32, ctypes.c_void_p,
+                                            ctypes.c_int32]
         _lib = L
     return _lib
 
@@ -189,6 +192,26 @@ def run_segments_parallel(gem, p, starts, sizes, threads):
 def pearson_fp64(gem, x, y, min_expr=float("-inf"), min_samples=30):
     gem = np.ascontiguousarray(gem, dtype=np.float32)
     return lib().ko_pearson_fp64(_ptr(gem), gem.shape[1], x, y, min_expr, min_samples)
+
+
+def pearson_fp64_pairs(gem, xs, ys, min_expr=float("-inf"), min_samples=30):
+    """FP64 pairwise-complete Pearson for the pairs (xs[i], ys[i])."""
+    gem = np.ascontiguousarray(gem, dtype=np.float32)
+    xs = np.ascontiguousarray(xs, dtype=np.int32)
+    ys = np.ascontiguousarray(ys, dtype=np.int32)
+    out = np.empty(len(xs), np.float64)
+    lib().ko_pearson_fp64_batch(_ptr(gem), gem.shape[1], _ptr(xs), _ptr(ys), len(xs), min_expr, min_samples,
+                                _ptr(out), os.cpu_count() or 1)
+    return out
+
+
+def pair_xy(p):
+    """Vectorised linear pair index -> (x, y), x > y."""
+    p = np.asarray(p, dtype=np.int64)
+    x = ((1 + np.sqrt(1 + 8 * p.astype(np.float64))) // 2).astype(np.int64)
+    x -= (x * (x - 1) // 2 > p)
+    x += ((x + 1) * x // 2 <= p)
+    return x, p - x * (x - 1) // 2
 
 
 def libc_rand(n, seed=1):

@@ -1,0 +1,60 @@
+"""Tensor-core masked Pearson (precision TF32 / 3xBF16, clusmethod none):
+maximum |r| error against the FP64 pairwise-complete oracle, and agreement
+with the plain per-pair FP32 kernel on the same pairs (semantics fixed)."""
+import numpy as np
+import pytest
+
+from kinc_gb300 import Similarity, synthetic
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+# max |r - r_fp64| allowed per precision
+TOL = {"3xbf16": 1e-4, "tf32": 2e-3}
+
+
+def _dense(genes, samples, seed=5):
+    return synthetic.generate(3, genes=genes, samples=samples, seed=seed)
+
+
+@pytest.mark.parametrize("precision", ["tf32", "3xbf16"])
+@pytest.mark.parametrize("shape", [(300, 500), (257, 130)])
+def test_tensor_core_pearson_vs_fp64(precision, shape):
+    G, S = shape
+    gem = _dense(G, S)
+    sim = Similarity(gem, semantics="fixed", precision=precision)
+    sim.initialize()
+    total = sim.total_pairs()
+    res = sim.execute(None, start=0, size=total)
+    sim.close()
+    assert np.all(res.K == 1)
+    x, y = pyoracle.pair_xy(np.arange(total))
+    ref = pyoracle.pearson_fp64_pairs(gem, x, y)
+    got = res.corr[:, 0].astype(np.float64)
+    both = ~np.isnan(ref)
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
+    err = np.abs(got[both] - ref[both]).max()
+    assert err <= TOL[precision], f"max |dr| {err}"
+
+
+@pytest.mark.parametrize("precision", ["tf32", "3xbf16"])
+def test_tensor_core_partial_range_matches_full(precision):
+    gem = _dense(200, 96, seed=9)
+    sim = Similarity(gem, semantics="fixed", precision=precision)
+    sim.initialize()
+    full = sim.execute(None, start=0, size=sim.total_pairs())
+    part = sim.execute(None, start=12345, size=4321)
+    sim.close()
+    assert np.array_equal(np.nan_to_num(part.corr[:, 0], nan=9), np.nan_to_num(full.corr[12345:16666, 0], nan=9))
+
+
+def test_plain_fp32_fixed_semantics_vs_fp64():
+    gem = _dense(120, 300)
+    sim = Similarity(gem, semantics="fixed")
+    sim.initialize()
+    res = sim.execute(None, start=0, size=sim.total_pairs())
+    sim.close()
+    x, y = pyoracle.pair_xy(np.arange(sim.total_pairs()))
+    ref = pyoracle.pearson_fp64_pairs(gem, x, y)
+    both = ~np.isnan(ref)
+    assert np.abs(res.corr[both, 0] - ref[both]).max() < 1e-4
