@@ -1,0 +1,86 @@
+/*
+ * kinc_pairwise_matrix.h -- KINC's pairwise matrix files (CCM cluster
+ * matrix, CMX correlation matrix) and expression matrix (EMX) data, plus the
+ * ordered block-by-block runner that writes them.
+ *
+ * Byte layout of a pairwise matrix (the data section KINC's classes write
+ * through their stream):
+ *   header, 30 bytes         src/core/pairwise_matrix.h:32-40, src/core/pairwise_matrix.cpp:12-57
+ *     i32 geneSize, i32 maxClusterSize, i32 dataSize, i64 pairSize, i64 clusterSize, i16 offset
+ *   sub-header, `offset` bytes
+ *     CCM: i32 sampleSize          src/core/ccmatrix.h:21-23
+ *     CMX: i8 correlationSize      src/core/correlationmatrix.h:21-23
+ *   items, each 9 + dataSize bytes, in strictly increasing indent order
+ *     i32 x, i32 y, i8 cluster     src/core/pairwise_matrix.cpp:122-151
+ *     CCM payload: (sampleSize+1)/2 bytes, sample 2i in the low nibble, 2i+1 in the high nibble
+ *                                  src/core/ccmatrix.cpp:223-243, dataSize src/core/ccmatrix.cpp:126
+ *     CMX payload: correlationSize float32   src/core/correlationmatrix.cpp:231-242
+ * EMX: i32 geneSize, i32 sampleSize, then float32 [gene][sample]   src/core/expressionmatrix.cpp:21-37
+ *
+ * The reference writes through ACE's stream class, which is not part of the
+ * KINC tree; its byte order is a parameter here (big-endian, the Qt stream
+ * default, unless little_endian is set).  Gene/sample names, which ACE keeps
+ * as metadata, are not part of these files.
+ */
+#ifndef KINC_PAIRWISE_MATRIX_H
+#define KINC_PAIRWISE_MATRIX_H
+
+#include <stdint.h>
+
+#include "kinc_sim.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KINC_PM_CCM 1
+#define KINC_PM_CMX 2
+
+typedef struct kinc_pm kinc_pm;
+
+/* Pairwise::Matrix::initialize + writeNewData: a new CCM (subsize = samples) or
+ * CMX (subsize = correlations per cluster) file. */
+int kinc_pm_create(const char* path, int32_t type, int32_t genes, int32_t max_clusters, int32_t subsize,
+                   int32_t little_endian, kinc_pm** out);
+
+/* Append n items already in pair order: (x[i], y[i], c[i]) and the payload of
+ * item i at payload + i*stride (CCM: samples int8 codes 0/1/6/7/8/9, packed to
+ * nibbles here; CMX: subsize float32).  Matrix::write's rule holds: each indent
+ * (x(x-1)/2 + y)*64 + c must exceed the last one written, else KINC_SIM_EORDER.
+ * pairSize counts the distinct (x, y) pairs written. */
+int kinc_pm_write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y, const int8_t* c,
+                        const void* payload);
+
+/* Matrix::finish: rewrite the header counts and close. */
+int kinc_pm_close(kinc_pm* m);
+
+/* Open an existing file for reading; reports its header. */
+int kinc_pm_open(const char* path, int32_t type, int32_t little_endian, kinc_pm** out, int32_t* genes,
+                 int32_t* max_clusters, int32_t* subsize, int64_t* pairs, int64_t* clusters);
+
+/* Read items [first, first+n): CCM payloads unpacked to one int8 code per sample. */
+int kinc_pm_read_items(kinc_pm* m, int64_t first, int64_t n, int32_t* x, int32_t* y, int8_t* c, void* payload);
+
+/* EMX data section. */
+int kinc_emx_write(const char* path, const float* gem, int32_t genes, int32_t samples, int32_t little_endian);
+int kinc_emx_read_header(const char* path, int32_t little_endian, int32_t* genes, int32_t* samples);
+int kinc_emx_read(const char* path, int32_t little_endian, float* gem, int64_t capacity);
+
+/* Message of the last failed kinc_pm_* / kinc_emx_* / kinc_sim_run_to_files call on this thread. */
+const char* kinc_pm_last_error(void);
+
+/*
+ * The analytic's block loop (ACE's serial runner + Similarity::process,
+ * src/core/similarity.cpp:17-39,66-127) on the worker: work blocks
+ * [first_block, first_block + nblocks) are executed in order, filtered and
+ * appended to the CCM and CMX files (either path may be NULL).  nblocks < 0
+ * means all remaining blocks.  The files are created and finished here.
+ */
+int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, const char* cmx_path, int32_t little_endian,
+                          int64_t first_block, int64_t nblocks);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -82,6 +82,9 @@ void kinc_sim_destroy(kinc_sim_ctx* ctx);
 /* Message of the last failed call on `ctx` (or of the last failed kinc_sim_create if ctx is NULL). */
 const char* kinc_sim_last_error(const kinc_sim_ctx* ctx);
 
+/* The context's arguments and matrix shape (any output may be NULL). */
+int kinc_sim_get_params(const kinc_sim_ctx* ctx, kinc_sim_params* params, int32_t* genes, int32_t* samples);
+
 /* Total pairs G(G-1)/2 and the number of 32768-pair work blocks (Similarity::size). */
 int64_t kinc_sim_total_pairs(const kinc_sim_ctx* ctx);
 int32_t kinc_sim_num_work_blocks(const kinc_sim_ctx* ctx);

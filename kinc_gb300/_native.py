@@ -50,6 +50,21 @@ SIGNATURES = {
     "kinc_sim_pair_counts": (ctypes.c_int, [_VP, _I64, _I64, _VP]),
     "kinc_sim_last_launch_count": (_I32, [_VP]),
     "kinc_sim_work_counters": (ctypes.c_int, [_VP, _VP, ctypes.c_int]),
+    "kinc_sim_get_params": (ctypes.c_int, [_VP, ctypes.POINTER(SimParams), ctypes.POINTER(_I32),
+                                           ctypes.POINTER(_I32)]),
+    # include/kinc_pairwise_matrix.h
+    "kinc_pm_create": (ctypes.c_int, [ctypes.c_char_p, _I32, _I32, _I32, _I32, _I32, ctypes.POINTER(_VP)]),
+    "kinc_pm_write_items": (ctypes.c_int, [_VP, _I64, _VP, _VP, _VP, _VP]),
+    "kinc_pm_close": (ctypes.c_int, [_VP]),
+    "kinc_pm_open": (ctypes.c_int, [ctypes.c_char_p, _I32, _I32, ctypes.POINTER(_VP), ctypes.POINTER(_I32),
+                                    ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I64),
+                                    ctypes.POINTER(_I64)]),
+    "kinc_pm_read_items": (ctypes.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, _VP]),
+    "kinc_emx_write": (ctypes.c_int, [ctypes.c_char_p, _VP, _I32, _I32, _I32]),
+    "kinc_emx_read_header": (ctypes.c_int, [ctypes.c_char_p, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
+    "kinc_emx_read": (ctypes.c_int, [ctypes.c_char_p, _I32, _VP, _I64]),
+    "kinc_pm_last_error": (ctypes.c_char_p, []),
+    "kinc_sim_run_to_files": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_char_p, _I32, _I64, _I64]),
     "kinc_sim_execute_block_noalloc": (ctypes.c_int, [_VP, _I32, _I32, ctypes.POINTER(SimParams), _I64, _I64,
                                                       _VP, _VP, _VP, _VP]),
 }

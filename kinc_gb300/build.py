@@ -27,6 +27,7 @@ UNITS = [
     ("sim_gmm.cu", ["--fmad=false"]),
     ("sim_kmeans.cu", ["--fmad=false"]),
     ("pearson_gemm.cu", []),
+    ("pairwise_file.cpp", []),
 ]
 
 
@@ -60,7 +61,7 @@ def build(force=False, verbose=False):
         path = os.path.join(CSRC, src)
         if not os.path.exists(path):
             continue
-        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         cmd = [NVCC, *ARCH, *COMMON, *flags, "-c", path, "-o", obj]
         jobs.append((cmd, obj))
 

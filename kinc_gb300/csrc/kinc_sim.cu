@@ -385,6 +385,15 @@ extern "C" const char* kinc_sim_last_error(const kinc_sim_ctx* ctx)
    return ctx ? ctx->err.c_str() : g_create_error.c_str();
 }
 
+extern "C" int kinc_sim_get_params(const kinc_sim_ctx* ctx, kinc_sim_params* params, int32_t* genes, int32_t* samples)
+{
+   if ( !ctx ) return KINC_SIM_EINVAL;
+   if ( params ) *params = ctx->params;
+   if ( genes ) *genes = ctx->G;
+   if ( samples ) *samples = ctx->S;
+   return KINC_SIM_OK;
+}
+
 extern "C" int64_t kinc_sim_total_pairs(const kinc_sim_ctx* ctx)
 {
    return ctx ? (int64_t)ctx->G * (ctx->G - 1) / 2 : 0;

@@ -1,0 +1,422 @@
+/*
+ * pairwise_file.cpp -- CCM / CMX pairwise matrix files, EMX data, and the
+ * ordered block runner (include/kinc_pairwise_matrix.h).
+ *
+ * Restates the on-disk behaviour of Pairwise::Matrix (src/core/pairwise_matrix.cpp:12-151,251-273),
+ * CCMatrix::Pair::writeCluster/readCluster (src/core/ccmatrix.cpp:223-270),
+ * CorrelationMatrix::Pair::writeCluster/readCluster (src/core/correlationmatrix.cpp:231-260) and
+ * ExpressionMatrix's data section (src/core/expressionmatrix.cpp:21-37).
+ */
+#include "../../include/kinc_pairwise_matrix.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+thread_local std::string t_err;
+
+int pm_fail(int code, const char* fmt, ...)
+{
+   char buf[512];
+   va_list ap;
+   va_start(ap, fmt);
+   vsnprintf(buf, sizeof buf, fmt, ap);
+   va_end(ap);
+   t_err = buf;
+   return code;
+}
+
+constexpr int HEADER = 30;      /* Matrix::_headerSize */
+constexpr int ITEM_HEADER = 9;  /* Matrix::_itemHeaderSize */
+constexpr int MAX_CLUSTER_SIZE = 64;
+
+/* byte-order-aware scalar I/O */
+struct Endian
+{
+   bool little;
+
+   template <class T>
+   void put(std::vector<unsigned char>& out, T v) const
+   {
+      unsigned char b[sizeof(T)];
+      memcpy(b, &v, sizeof(T));
+      const bool host_little = true;   /* x86-64 and aarch64 builds are little-endian */
+      if ( little != host_little )
+         for ( size_t i = 0; i < sizeof(T) / 2; ++i ) std::swap(b[i], b[sizeof(T) - 1 - i]);
+      out.insert(out.end(), b, b + sizeof(T));
+   }
+
+   template <class T>
+   T get(const unsigned char* p) const
+   {
+      unsigned char b[sizeof(T)];
+      memcpy(b, p, sizeof(T));
+      if ( !little )
+         for ( size_t i = 0; i < sizeof(T) / 2; ++i ) std::swap(b[i], b[sizeof(T) - 1 - i]);
+      T v;
+      memcpy(&v, b, sizeof(T));
+      return v;
+   }
+};
+
+}  // namespace
+
+struct kinc_pm
+{
+   FILE* f = nullptr;
+   bool writing = false;
+   int type = 0;
+   Endian e {};
+   int32_t genes = 0, max_clusters = 0, subsize = 0, data_size = 0;
+   int16_t offset = 0;
+   int64_t pairs = 0, clusters = 0;
+   int64_t last_indent = -1;
+   int64_t last_pair = -1;
+   std::vector<unsigned char> buf;
+};
+
+namespace {
+
+int32_t data_size_of(int type, int32_t subsize)
+{
+   return type == KINC_PM_CCM ? (subsize + 1) / 2 : subsize * (int32_t)sizeof(float);
+}
+
+int16_t offset_of(int type)
+{
+   return type == KINC_PM_CCM ? 4 : 1;   /* CCMatrix / CorrelationMatrix DATA_OFFSET */
+}
+
+int write_header(kinc_pm* m)
+{
+   std::vector<unsigned char> h;
+   m->e.put<int32_t>(h, m->genes);
+   m->e.put<int32_t>(h, m->max_clusters);
+   m->e.put<int32_t>(h, m->data_size);
+   m->e.put<int64_t>(h, m->pairs);
+   m->e.put<int64_t>(h, m->clusters);
+   m->e.put<int16_t>(h, m->offset);
+   if ( m->type == KINC_PM_CCM ) m->e.put<int32_t>(h, m->subsize);
+   else m->e.put<int8_t>(h, (int8_t)m->subsize);
+   if ( fseek(m->f, 0, SEEK_SET) != 0 || fwrite(h.data(), 1, h.size(), m->f) != h.size() )
+      return pm_fail(KINC_SIM_ECUDA, "cannot write the pairwise matrix header");
+   return KINC_SIM_OK;
+}
+
+}  // namespace
+
+extern "C" const char* kinc_pm_last_error(void)
+{
+   return t_err.c_str();
+}
+
+extern "C" int kinc_pm_create(const char* path, int32_t type, int32_t genes, int32_t max_clusters, int32_t subsize,
+                              int32_t little_endian, kinc_pm** out)
+{
+   if ( !path || !out ) return pm_fail(KINC_SIM_EINVAL, "path and out must not be NULL");
+   *out = nullptr;
+   if ( type != KINC_PM_CCM && type != KINC_PM_CMX ) return pm_fail(KINC_SIM_EINVAL, "type must be CCM or CMX");
+   /* Matrix::initialize (src/core/pairwise_matrix.cpp:69-117) */
+   if ( genes < 1 ) return pm_fail(KINC_SIM_EINVAL, "Gene names metadata is not an array or is empty.");
+   if ( max_clusters < 1 || subsize < 1 )
+      return pm_fail(KINC_SIM_EINVAL, "An integer argument given is less than the minimum.");
+   if ( max_clusters > MAX_CLUSTER_SIZE )
+      return pm_fail(KINC_SIM_EINVAL, "The max cluster size cannot be larger than MAX_CLUSTER_SIZE.");
+   if ( type == KINC_PM_CMX && subsize > 127 ) return pm_fail(KINC_SIM_EINVAL, "correlationSize must fit in int8");
+   kinc_pm* m = new kinc_pm();
+   m->f = fopen(path, "w+b");
+   if ( !m->f )
+   {
+      delete m;
+      return pm_fail(KINC_SIM_EINVAL, "cannot open %s for writing", path);
+   }
+   m->writing = true;
+   m->type = type;
+   m->e.little = little_endian != 0;
+   m->genes = genes;
+   m->max_clusters = max_clusters;
+   m->subsize = subsize;
+   m->data_size = data_size_of(type, subsize);
+   m->offset = offset_of(type);
+   int rc = write_header(m);
+   if ( rc )
+   {
+      fclose(m->f);
+      delete m;
+      return rc;
+   }
+   *out = m;
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_pm_write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y, const int8_t* c,
+                                   const void* payload)
+{
+   if ( !m || !m->writing ) return pm_fail(KINC_SIM_EINVAL, "Attempting to write data to uninitialized object.");
+   if ( n < 0 || (n > 0 && (!x || !y || !c || !payload)) ) return pm_fail(KINC_SIM_EINVAL, "invalid item arrays");
+   m->buf.clear();
+   const size_t item = ITEM_HEADER + (size_t)m->data_size;
+   /* validate the whole batch first so a rejected batch leaves the file as it was */
+   {
+      int64_t last = m->last_indent;
+      for ( int64_t i = 0; i < n; ++i )
+      {
+         if ( x[i] < 1 || y[i] < 0 || x[i] <= y[i] || x[i] >= m->genes )
+            return pm_fail(KINC_SIM_EINVAL, "Cannot initialize pairwise index (%d, %d).", x[i], y[i]);
+         if ( c[i] < 0 || c[i] >= MAX_CLUSTER_SIZE || c[i] >= m->max_clusters )
+            return pm_fail(KINC_SIM_EINVAL, "Cluster %d is outside limits.", c[i]);
+         const int64_t pair = (int64_t)x[i] * (x[i] - 1) / 2 + y[i];
+         const int64_t indent = pair * MAX_CLUSTER_SIZE + c[i];
+         if ( indent <= last )
+            return pm_fail(KINC_SIM_EORDER, "Attempting to write indent %lld when last written is %lld.",
+                           (long long)(pair * MAX_CLUSTER_SIZE), (long long)last);
+         last = indent;
+      }
+   }
+   m->buf.reserve((size_t)n * item);
+   for ( int64_t i = 0; i < n; ++i )
+   {
+      const int64_t pair = (int64_t)x[i] * (x[i] - 1) / 2 + y[i];
+      const int64_t indent = pair * MAX_CLUSTER_SIZE + c[i];
+      m->e.put<int32_t>(m->buf, x[i]);
+      m->e.put<int32_t>(m->buf, y[i]);
+      m->e.put<int8_t>(m->buf, c[i]);
+      if ( m->type == KINC_PM_CCM )
+      {
+         const int8_t* codes = (const int8_t*)payload + (size_t)i * m->subsize;
+         for ( int s = 0; s < m->subsize; s += 2 )
+         {
+            int8_t v = (int8_t)(codes[s] & 0x0F);
+            if ( s + 1 < m->subsize ) v = (int8_t)(v | (int8_t)(codes[s + 1] << 4));
+            m->buf.push_back((unsigned char)v);
+         }
+      }
+      else
+      {
+         const float* r = (const float*)payload + (size_t)i * m->subsize;
+         for ( int k = 0; k < m->subsize; ++k ) m->e.put<float>(m->buf, r[k]);
+      }
+      if ( pair != m->last_pair )
+      {
+         ++m->pairs;
+         m->last_pair = pair;
+      }
+      ++m->clusters;
+      m->last_indent = indent;
+   }
+   const long pos = (long)(HEADER + m->offset) + (long)((m->clusters - n) * (int64_t)item);
+   if ( fseek(m->f, pos, SEEK_SET) != 0 || fwrite(m->buf.data(), 1, m->buf.size(), m->f) != m->buf.size() )
+      return pm_fail(KINC_SIM_ECUDA, "write failed");
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_pm_close(kinc_pm* m)
+{
+   if ( !m ) return KINC_SIM_EINVAL;
+   int rc = KINC_SIM_OK;
+   if ( m->writing ) rc = write_header(m);
+   if ( m->f ) fclose(m->f);
+   delete m;
+   return rc;
+}
+
+extern "C" int kinc_pm_open(const char* path, int32_t type, int32_t little_endian, kinc_pm** out, int32_t* genes,
+                            int32_t* max_clusters, int32_t* subsize, int64_t* pairs, int64_t* clusters)
+{
+   if ( !path || !out ) return pm_fail(KINC_SIM_EINVAL, "path and out must not be NULL");
+   *out = nullptr;
+   kinc_pm* m = new kinc_pm();
+   m->f = fopen(path, "rb");
+   if ( !m->f )
+   {
+      delete m;
+      return pm_fail(KINC_SIM_EINVAL, "cannot open %s", path);
+   }
+   m->type = type;
+   m->e.little = little_endian != 0;
+   unsigned char h[HEADER + 4];
+   const size_t want = HEADER + (type == KINC_PM_CCM ? 4 : 1);
+   if ( fread(h, 1, want, m->f) != want )
+   {
+      fclose(m->f);
+      delete m;
+      return pm_fail(KINC_SIM_EINVAL, "%s: truncated header", path);
+   }
+   m->genes = m->e.get<int32_t>(h);
+   m->max_clusters = m->e.get<int32_t>(h + 4);
+   m->data_size = m->e.get<int32_t>(h + 8);
+   m->pairs = m->e.get<int64_t>(h + 12);
+   m->clusters = m->e.get<int64_t>(h + 20);
+   m->offset = m->e.get<int16_t>(h + 28);
+   m->subsize = type == KINC_PM_CCM ? m->e.get<int32_t>(h + 30) : (int32_t)(int8_t)h[30];
+   if ( m->offset != offset_of(type) || m->data_size != data_size_of(type, m->subsize) )
+   {
+      fclose(m->f);
+      delete m;
+      return pm_fail(KINC_SIM_EINVAL, "%s: not a %s file with this byte order", path,
+                     type == KINC_PM_CCM ? "CCM" : "CMX");
+   }
+   if ( genes ) *genes = m->genes;
+   if ( max_clusters ) *max_clusters = m->max_clusters;
+   if ( subsize ) *subsize = m->subsize;
+   if ( pairs ) *pairs = m->pairs;
+   if ( clusters ) *clusters = m->clusters;
+   *out = m;
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_pm_read_items(kinc_pm* m, int64_t first, int64_t n, int32_t* x, int32_t* y, int8_t* c,
+                                  void* payload)
+{
+   if ( !m || m->writing ) return pm_fail(KINC_SIM_EINVAL, "not opened for reading");
+   if ( first < 0 || n < 0 || first + n > m->clusters ) return pm_fail(KINC_SIM_EINVAL, "item range out of bounds");
+   const size_t item = ITEM_HEADER + (size_t)m->data_size;
+   std::vector<unsigned char> b((size_t)n * item);
+   const long pos = (long)(HEADER + m->offset) + (long)(first * (int64_t)item);
+   if ( n > 0 && (fseek(m->f, pos, SEEK_SET) != 0 || fread(b.data(), 1, b.size(), m->f) != b.size()) )
+      return pm_fail(KINC_SIM_EINVAL, "truncated items");
+   for ( int64_t i = 0; i < n; ++i )
+   {
+      const unsigned char* p = b.data() + (size_t)i * item;
+      if ( x ) x[i] = m->e.get<int32_t>(p);
+      if ( y ) y[i] = m->e.get<int32_t>(p + 4);
+      if ( c ) c[i] = (int8_t)p[8];
+      if ( !payload ) continue;
+      if ( m->type == KINC_PM_CCM )
+      {
+         int8_t* codes = (int8_t*)payload + (size_t)i * m->subsize;
+         for ( int s = 0; s < m->subsize; ++s )
+         {
+            const unsigned char v = p[ITEM_HEADER + s / 2];
+            codes[s] = (int8_t)((s % 2 == 0) ? (v & 0x0F) : ((v >> 4) & 0x0F));
+         }
+      }
+      else
+      {
+         float* r = (float*)payload + (size_t)i * m->subsize;
+         for ( int k = 0; k < m->subsize; ++k ) r[k] = m->e.get<float>(p + ITEM_HEADER + 4 * k);
+      }
+   }
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_emx_write(const char* path, const float* gem, int32_t genes, int32_t samples,
+                              int32_t little_endian)
+{
+   if ( !path || !gem || genes < 1 || samples < 1 ) return pm_fail(KINC_SIM_EINVAL, "invalid EMX arguments");
+   FILE* f = fopen(path, "wb");
+   if ( !f ) return pm_fail(KINC_SIM_EINVAL, "cannot open %s for writing", path);
+   Endian e { little_endian != 0 };
+   std::vector<unsigned char> b;
+   e.put<int32_t>(b, genes);
+   e.put<int32_t>(b, samples);
+   b.reserve(8 + (size_t)genes * samples * 4);
+   for ( int64_t i = 0; i < (int64_t)genes * samples; ++i ) e.put<float>(b, gem[i]);
+   const bool ok = fwrite(b.data(), 1, b.size(), f) == b.size();
+   fclose(f);
+   return ok ? KINC_SIM_OK : pm_fail(KINC_SIM_EINVAL, "write failed");
+}
+
+extern "C" int kinc_emx_read_header(const char* path, int32_t little_endian, int32_t* genes, int32_t* samples)
+{
+   FILE* f = path ? fopen(path, "rb") : nullptr;
+   if ( !f ) return pm_fail(KINC_SIM_EINVAL, "cannot open EMX %s", path ? path : "(null)");
+   unsigned char h[8];
+   const bool ok = fread(h, 1, 8, f) == 8;
+   fclose(f);
+   if ( !ok ) return pm_fail(KINC_SIM_EINVAL, "%s: truncated EMX header", path);
+   Endian e { little_endian != 0 };
+   const int32_t g = e.get<int32_t>(h), s = e.get<int32_t>(h + 4);
+   if ( g < 1 || s < 1 ) return pm_fail(KINC_SIM_EINVAL, "%s: corrupt EMX header (%d genes, %d samples)", path, g, s);
+   if ( genes ) *genes = g;
+   if ( samples ) *samples = s;
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_emx_read(const char* path, int32_t little_endian, float* gem, int64_t capacity)
+{
+   int32_t g = 0, s = 0;
+   int rc = kinc_emx_read_header(path, little_endian, &g, &s);
+   if ( rc ) return rc;
+   if ( !gem || capacity < (int64_t)g * s ) return pm_fail(KINC_SIM_EINVAL, "EMX buffer too small");
+   FILE* f = fopen(path, "rb");
+   if ( !f ) return pm_fail(KINC_SIM_EINVAL, "cannot open EMX %s", path);
+   std::vector<unsigned char> b((size_t)g * s * 4);
+   const bool ok = fseek(f, 8, SEEK_SET) == 0 && fread(b.data(), 1, b.size(), f) == b.size();
+   fclose(f);
+   if ( !ok ) return pm_fail(KINC_SIM_EINVAL, "%s: truncated EMX data", path);
+   Endian e { little_endian != 0 };
+   for ( int64_t i = 0; i < (int64_t)g * s; ++i ) gem[i] = e.get<float>(b.data() + 4 * i);
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, const char* cmx_path,
+                                     int32_t little_endian, int64_t first_block, int64_t nblocks)
+{
+   kinc_sim_params p;
+   int32_t G = 0, S = 0;
+   if ( !ctx || kinc_sim_get_params(ctx, &p, &G, &S) != KINC_SIM_OK ) return pm_fail(KINC_SIM_EINVAL, "no context");
+   const int64_t total = kinc_sim_total_pairs(ctx);
+   const int64_t nb = kinc_sim_num_work_blocks(ctx);
+   if ( first_block < 0 || first_block > nb ) return pm_fail(KINC_SIM_EINVAL, "first_block out of range");
+   const int64_t last = nblocks < 0 ? nb : std::min<int64_t>(nb, first_block + nblocks);
+   const int maxK = p.max_clusters;
+   kinc_pm* ccm = nullptr;
+   kinc_pm* cmx = nullptr;
+   int rc = KINC_SIM_OK;
+   if ( ccm_path && (rc = kinc_pm_create(ccm_path, KINC_PM_CCM, G, maxK, S, little_endian, &ccm)) ) return rc;
+   if ( cmx_path && (rc = kinc_pm_create(cmx_path, KINC_PM_CMX, G, maxK, 1, little_endian, &cmx)) )
+   {
+      kinc_pm_close(ccm);
+      return rc;
+   }
+   const int64_t B = KINC_SIM_WORK_BLOCK_SIZE;
+   int8_t* K = nullptr;
+   int8_t* labels = nullptr;
+   float* corr = nullptr;
+   cudaError_t e1 = cudaMallocHost((void**)&K, B);
+   cudaError_t e2 = cudaMallocHost((void**)&labels, (size_t)B * S);
+   cudaError_t e3 = cudaMallocHost((void**)&corr, (size_t)B * maxK * sizeof(float));
+   std::vector<int32_t> cx(B * maxK), cy(B * maxK), mx(B * maxK), my(B * maxK);
+   std::vector<int8_t> cc(B * maxK), mc(B * maxK);
+   std::vector<float> cr(B * maxK);
+   std::vector<int8_t> codes(ccm ? (size_t)B * maxK * S : 1);
+   if ( e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess )
+      rc = pm_fail(KINC_SIM_ENOMEM, "cannot allocate pinned host buffers");
+   for ( int64_t b = first_block; rc == KINC_SIM_OK && b < last; ++b )
+   {
+      /* Similarity::makeWork (src/core/similarity.cpp:30-39) */
+      const int64_t start = b * B;
+      const int64_t size = std::min<int64_t>(total - start, B);
+      rc = kinc_sim_execute_block(ctx, start, size, K, ccm ? labels : nullptr, corr);
+      if ( rc )
+      {
+         t_err = kinc_sim_last_error(ctx);
+         break;
+      }
+      int64_t n_cmx = 0, n_ccm = 0;
+      rc = kinc_sim_process_pairs(&p, S, start, size, K, labels, corr, cx.data(), cy.data(), cc.data(), cr.data(),
+                                  (int64_t)cx.size(), &n_cmx, ccm ? mx.data() : nullptr, my.data(), mc.data(),
+                                  codes.data(), ccm ? (int64_t)mx.size() : 0, &n_ccm);
+      if ( rc )
+      {
+         t_err = kinc_sim_last_error(nullptr);
+         break;
+      }
+      if ( ccm && (rc = kinc_pm_write_items(ccm, n_ccm, mx.data(), my.data(), mc.data(), codes.data())) ) break;
+      if ( cmx && (rc = kinc_pm_write_items(cmx, n_cmx, cx.data(), cy.data(), cc.data(), cr.data())) ) break;
+   }
+   if ( K ) cudaFreeHost(K);
+   if ( labels ) cudaFreeHost(labels);
+   if ( corr ) cudaFreeHost(corr);
+   const int rc1 = ccm ? kinc_pm_close(ccm) : KINC_SIM_OK;
+   const int rc2 = cmx ? kinc_pm_close(cmx) : KINC_SIM_OK;
+   return rc ? rc : (rc1 ? rc1 : rc2);
+}

@@ -1,0 +1,69 @@
+"""KINC's pairwise matrix files (CCM cluster matrix, CMX correlation matrix)
+and expression matrix (EMX) data section, read and written by the native
+library (include/kinc_pairwise_matrix.h)."""
+import ctypes
+
+import numpy as np
+
+from . import _native
+
+CCM, CMX = 1, 2
+
+
+def _check(rc):
+    if rc != _native.OK:
+        raise _native.SimError(rc, _native.load().kinc_pm_last_error().decode())
+
+
+def write(path, kind, genes, max_clusters, subsize, x, y, c, payload, little_endian=False):
+    """Write a CCM (payload int8 codes [n][samples]) or CMX (payload float32 [n][subsize]) file."""
+    L = _native.load()
+    h = ctypes.c_void_p()
+    _check(L.kinc_pm_create(str(path).encode(), kind, genes, max_clusters, subsize, int(little_endian),
+                            ctypes.byref(h)))
+    try:
+        x = np.ascontiguousarray(x, np.int32)
+        y = np.ascontiguousarray(y, np.int32)
+        c = np.ascontiguousarray(c, np.int8)
+        payload = np.ascontiguousarray(payload, np.int8 if kind == CCM else np.float32)
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        _check(L.kinc_pm_write_items(h, len(x), vp(x), vp(y), vp(c), vp(payload)))
+    finally:
+        _check(L.kinc_pm_close(h))
+
+
+def read(path, kind, little_endian=False):
+    """Read a CCM/CMX file: dict(genes, max_clusters, subsize, pairs, x, y, c, payload)."""
+    L = _native.load()
+    h = ctypes.c_void_p()
+    g, k, s = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    pairs, clusters = ctypes.c_int64(), ctypes.c_int64()
+    _check(L.kinc_pm_open(str(path).encode(), kind, int(little_endian), ctypes.byref(h), ctypes.byref(g),
+                          ctypes.byref(k), ctypes.byref(s), ctypes.byref(pairs), ctypes.byref(clusters)))
+    try:
+        n = clusters.value
+        x = np.empty(n, np.int32)
+        y = np.empty(n, np.int32)
+        c = np.empty(n, np.int8)
+        payload = np.empty((n, s.value), np.int8 if kind == CCM else np.float32)
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        _check(L.kinc_pm_read_items(h, 0, n, vp(x), vp(y), vp(c), vp(payload)))
+    finally:
+        L.kinc_pm_close(h)
+    return dict(genes=g.value, max_clusters=k.value, subsize=s.value, pairs=pairs.value, x=x, y=y, c=c,
+                payload=payload)
+
+
+def write_emx(path, gem, little_endian=False):
+    gem = np.ascontiguousarray(gem, np.float32)
+    _check(_native.load().kinc_emx_write(str(path).encode(), gem.ctypes.data_as(ctypes.c_void_p), gem.shape[0],
+                                         gem.shape[1], int(little_endian)))
+
+
+def read_emx(path, little_endian=False):
+    L = _native.load()
+    g, s = ctypes.c_int32(), ctypes.c_int32()
+    _check(L.kinc_emx_read_header(str(path).encode(), int(little_endian), ctypes.byref(g), ctypes.byref(s)))
+    gem = np.empty((g.value, s.value), np.float32)
+    _check(L.kinc_emx_read(str(path).encode(), int(little_endian), gem.ctypes.data_as(ctypes.c_void_p), gem.size))
+    return gem

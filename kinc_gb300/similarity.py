@@ -230,9 +230,18 @@ class Similarity:
             matrix.write_pair(int(x[i]), int(y[i]), payloads[i:j])
             i = j
 
-    def run(self):
-        """Run every work block in order and return (ccm, cmx)."""
+    def run(self, ccm_path=None, cmx_path=None, little_endian=False):
+        """Run every work block in order.  With file paths, the native runner writes the CCM/CMX
+        files (include/kinc_pairwise_matrix.h); otherwise the items are kept in memory and
+        (ccm, cmx) PairwiseMatrix objects are returned."""
         self.initialize()
+        if ccm_path is not None or cmx_path is not None:
+            L = _native.load()
+            rc = L.kinc_sim_run_to_files(self._ctx, str(ccm_path).encode() if ccm_path else None,
+                                         str(cmx_path).encode() if cmx_path else None, int(little_endian), 0, -1)
+            if rc != _native.OK:
+                raise _native.SimError(rc, L.kinc_pm_last_error().decode())
+            return ccm_path, cmx_path
         for b in range(self.size()):
             self.process(self.execute(self.make_work(b)))
         return self.ccm, self.cmx

@@ -1,0 +1,115 @@
+"""CCM / CMX pairwise matrix files and EMX data (include/kinc_pairwise_matrix.h),
+following the reference's round-trip tests (tests/testclustermatrix.cpp,
+tests/testcorrelationmatrix.cpp, tests/testexpressionmatrix.cpp): random
+contents written, read back and compared field by field.  Host code only."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from kinc_gb300 import _native, pairwise_matrix as pm
+
+
+def _random_items(rng, genes, max_clusters, samples):
+    xs, ys, cs, codes, corr = [], [], [], [], []
+    for x in range(1, genes):
+        for y in range(x):
+            k = int(rng.integers(0, max_clusters + 1))
+            for c in range(k):
+                xs.append(x)
+                ys.append(y)
+                cs.append(c)
+                codes.append(rng.choice([0, 1, 6, 7, 8, 9], size=samples))
+                corr.append(rng.uniform(-1, 1))
+    return (np.array(xs), np.array(ys), np.array(cs), np.array(codes, np.int8).reshape(-1, samples),
+            np.array(corr, np.float32).reshape(-1, 1))
+
+
+@pytest.mark.parametrize("little", [False, True])
+def test_cluster_matrix_round_trip(tmp_path, native, little):
+    rng = np.random.default_rng(1)
+    genes, maxk, samples = 10, 5, 5
+    x, y, c, codes, _ = _random_items(rng, genes, maxk, samples)
+    path = tmp_path / "a.ccm"
+    pm.write(path, pm.CCM, genes, maxk, samples, x, y, c, codes, little_endian=little)
+    got = pm.read(path, pm.CCM, little_endian=little)
+    assert (got["genes"], got["max_clusters"], got["subsize"]) == (genes, maxk, samples)
+    assert got["pairs"] == len({(a, b) for a, b in zip(x, y)})
+    assert np.array_equal(got["x"], x) and np.array_equal(got["y"], y) and np.array_equal(got["c"], c)
+    assert np.array_equal(got["payload"], codes)
+    # 30-byte header + 4-byte sample count + items of 9 + (5+1)/2 bytes
+    assert os.path.getsize(path) == 30 + 4 + len(x) * (9 + 3)
+    with open(path, "rb") as fh:
+        head = fh.read(34)
+    fmt = "<iiiqqhi" if little else ">iiiqqhi"
+    assert struct.unpack(fmt, head) == (genes, maxk, 3, got["pairs"], len(x), 4, samples)
+
+
+def test_cluster_matrix_nibbles(tmp_path, native):
+    codes = np.array([[9, 1, 0, 7, 8]], np.int8)
+    path = tmp_path / "n.ccm"
+    pm.write(path, pm.CCM, 4, 2, 5, [3], [1], [0], codes)
+    with open(path, "rb") as fh:
+        raw = fh.read()
+    item = raw[34:]
+    assert struct.unpack(">iib", item[:9]) == (3, 1, 0)
+    assert item[9:] == bytes([0x19, 0x70, 0x08])     # low nibble = even sample
+
+
+@pytest.mark.parametrize("little", [False, True])
+def test_correlation_matrix_round_trip(tmp_path, native, little):
+    rng = np.random.default_rng(2)
+    genes, maxk = 10, 5
+    x, y, c, _, corr = _random_items(rng, genes, maxk, 3)
+    path = tmp_path / "a.cmx"
+    pm.write(path, pm.CMX, genes, maxk, 1, x, y, c, corr, little_endian=little)
+    got = pm.read(path, pm.CMX, little_endian=little)
+    assert np.array_equal(got["payload"], corr)
+    assert np.array_equal(got["x"], x) and np.array_equal(got["c"], c)
+    assert os.path.getsize(path) == 30 + 1 + len(x) * (9 + 4)
+
+
+def test_wrong_byte_order_is_detected(tmp_path, native):
+    path = tmp_path / "b.cmx"
+    pm.write(path, pm.CMX, 5, 3, 1, [2], [0], [0], np.array([[0.7]], np.float32))
+    with pytest.raises(_native.SimError):
+        pm.read(path, pm.CMX, little_endian=True)
+
+
+def test_order_and_index_errors(tmp_path, native):
+    path = tmp_path / "c.cmx"
+    with pytest.raises(_native.SimError) as e:
+        pm.write(path, pm.CMX, 6, 3, 1, [3, 2], [1, 0], [0, 0], np.zeros((2, 1), np.float32))
+    assert e.value.code == _native.EORDER
+    with pytest.raises(_native.SimError):
+        pm.write(path, pm.CMX, 6, 3, 1, [2], [2], [0], np.zeros((1, 1), np.float32))
+    with pytest.raises(_native.SimError):
+        pm.write(path, pm.CMX, 6, 3, 1, [2], [1], [3], np.zeros((1, 1), np.float32))
+    with pytest.raises(_native.SimError):
+        pm.write(path, pm.CMX, 6, 65, 1, [], [], [], np.zeros((0, 1), np.float32))
+
+
+@pytest.mark.parametrize("little", [False, True])
+def test_expression_matrix_round_trip(tmp_path, native, little):
+    rng = np.random.default_rng(3)
+    gem = rng.normal(8, 2, size=(10, 5)).astype(np.float32)
+    gem[rng.random(gem.shape) < 0.2] = np.nan
+    path = tmp_path / "a.emx"
+    pm.write_emx(path, gem, little_endian=little)
+    got = pm.read_emx(path, little_endian=little)
+    assert np.array_equal(np.isnan(got), np.isnan(gem))
+    assert np.array_equal(got[~np.isnan(gem)], gem[~np.isnan(gem)])
+    assert os.path.getsize(path) == 8 + gem.size * 4
+
+
+def test_truncated_expression_matrix(tmp_path, native):
+    path = tmp_path / "t.emx"
+    with open(path, "wb") as fh:
+        fh.write(struct.pack(">ii", 10, 5) + b"\0" * 12)
+    with pytest.raises(_native.SimError, match="truncated"):
+        pm.read_emx(path)
+    with open(path, "wb") as fh:
+        fh.write(b"\0\0")
+    with pytest.raises(_native.SimError, match="truncated EMX header"):
+        pm.read_emx(path)

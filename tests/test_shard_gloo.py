@@ -1,0 +1,87 @@
+"""Multi-process sharding of the Similarity path on CPU: world_size 2 over
+gloo.  Each rank runs its contiguous range of work blocks (on the oracle --
+the per-pair computation is the same on every worker), the item lists are
+gathered to rank 0 and merged in rank order, and the result equals a
+single-process run.  No GPU is involved."""
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from kinc_gb300 import shard, synthetic
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _items(gem, start, size, kw):
+    from oracle import pyoracle
+    p = pyoracle.params(**kw)
+    if size == 0:
+        return {"x": [], "y": [], "c": [], "r": []}, {"x": [], "y": [], "c": [], "codes": []}
+    K, labels, corr, _ = pyoracle.run_block(gem, p, start, size)
+    cmx, ccm = pyoracle.process_block(gem.shape[1], p, start, K, labels, corr)
+    return ({k: v.tolist() for k, v in cmx.items()},
+            {"x": ccm["x"].tolist(), "y": ccm["y"].tolist(), "c": ccm["c"].tolist(),
+             "codes": [row.tobytes() for row in ccm["codes"]]})
+
+
+def _worker(rank, world, port, genes, samples, kw, q):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    gem = synthetic.generate(2, genes=genes, samples=samples)
+    sh = shard.shard_pairs(genes, world, rank, block=128)
+    mine = _items(gem, sh.start, sh.size, kw)
+    gathered = [None] * world
+    dist.all_gather_object(gathered, (sh.start, sh.size, mine))
+    if rank == 0:
+        q.put(gathered)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("kw", [dict(clus_method=1, corr_method=0, criterion=0, post_out=1),
+                                dict(clus_method=0, corr_method=1)])
+def test_two_ranks_equal_one(kw):
+    import torch.multiprocessing as mp
+    genes, samples, world = 28, 60, 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, world, port, genes, samples, kw, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    gathered = q.get(timeout=300)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    # shards are contiguous, disjoint and cover every pair
+    ranges = [(g[0], g[1]) for g in gathered]
+    assert ranges[0][0] == 0 and ranges[0][0] + ranges[0][1] == ranges[1][0]
+    assert ranges[1][0] + ranges[1][1] == shard.total_pairs(genes)
+    cmx = shard.merge_items([g[2][0] for g in gathered])
+    ccm = shard.merge_items([g[2][1] for g in gathered])
+    gem = synthetic.generate(2, genes=genes, samples=samples)
+    one_cmx, one_ccm = _items(gem, 0, shard.total_pairs(genes), kw)
+    for k in one_cmx:
+        assert list(cmx[k]) == list(one_cmx[k]), k
+    for k in one_ccm:
+        assert list(ccm[k]) == list(one_ccm[k]), k
+
+
+def test_shards_cover_all_pairs():
+    for genes in (2, 3, 100, 5000):
+        for world in (1, 2, 3, 8):
+            shards = [shard.shard_pairs(genes, world, r) for r in range(world)]
+            assert shards[0].start == 0
+            assert all(a.end == b.start for a, b in zip(shards, shards[1:]))
+            assert shards[-1].end == shard.total_pairs(genes)
+            assert all(s.start % shard.WORK_BLOCK_SIZE == 0 for s in shards if s.size)
