@@ -51,6 +51,11 @@ int kinc_pm_create(const char* path, int32_t type, int32_t genes, int32_t max_cl
 int kinc_pm_write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y, const int8_t* c,
                         const void* payload);
 
+/* The same with CCM payloads already packed ((samples + 1) / 2 bytes per item, as
+ * kinc_sim_compact_block_device writes them); CMX payloads as above. */
+int kinc_pm_write_items_packed(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y, const int8_t* c,
+                               const void* payload);
+
 /* Matrix::finish: rewrite the header counts and close. */
 int kinc_pm_close(kinc_pm* m);
 

@@ -132,6 +132,20 @@ int kinc_sim_process_block(const kinc_sim_ctx* ctx, int64_t start, int64_t size,
                            int32_t* ccm_x, int32_t* ccm_y, int8_t* ccm_c, int8_t* ccm_codes, int64_t cap_ccm,
                            int64_t* n_ccm);
 
+/*
+ * The same filter on the GPU for a block executed with kinc_sim_execute_block_device,
+ * stream-ordered: DEVICE inputs d_K, d_labels (NULL: no CCM items), d_corr; DEVICE outputs
+ * with room for cap_cmx / cap_ccm items (any output array may be NULL).  CCM payloads are
+ * written packed, (samples + 1) / 2 bytes per item with sample 2i in the low nibble, as the
+ * CCM file stores them.  d_counts[0] / d_counts[1] receive the numbers of CMX / CCM items,
+ * even when they exceed the capacities (items beyond them are dropped).
+ */
+int kinc_sim_compact_block_device(kinc_sim_ctx* ctx, int64_t start, int64_t size, const int8_t* d_K,
+                                  const int8_t* d_labels, const float* d_corr,
+                                  int32_t* cmx_x, int32_t* cmx_y, int8_t* cmx_c, float* cmx_r, int64_t cap_cmx,
+                                  int32_t* ccm_x, int32_t* ccm_y, int8_t* ccm_c, uint8_t* ccm_packed,
+                                  int64_t cap_ccm, uint64_t* d_counts, void* stream);
+
 /* The same filter without a context (host code only; no GPU needed): the
  * caller passes the analytic arguments and the sample count. */
 int kinc_sim_process_pairs(const kinc_sim_params* params, int32_t samples, int64_t start, int64_t size,

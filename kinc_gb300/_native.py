@@ -56,6 +56,9 @@ SIGNATURES = {
     "kinc_pm_create": (ctypes.c_int, [ctypes.c_char_p, _I32, _I32, _I32, _I32, _I32, ctypes.POINTER(_VP)]),
     "kinc_pm_write_items": (ctypes.c_int, [_VP, _I64, _VP, _VP, _VP, _VP]),
     "kinc_pm_close": (ctypes.c_int, [_VP]),
+    "kinc_pm_write_items_packed": (ctypes.c_int, [_VP, _I64, _VP, _VP, _VP, _VP]),
+    "kinc_sim_compact_block_device": (ctypes.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _I64, _VP,
+                                                     _VP, _VP, _VP, _I64, _VP, _VP]),
     "kinc_pm_open": (ctypes.c_int, [ctypes.c_char_p, _I32, _I32, ctypes.POINTER(_VP), ctypes.POINTER(_I32),
                                     ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I64),
                                     ctypes.POINTER(_I64)]),

@@ -27,6 +27,7 @@ UNITS = [
     ("sim_gmm.cu", ["--fmad=false"]),
     ("sim_kmeans.cu", ["--fmad=false"]),
     ("pearson_gemm.cu", []),
+    ("compact.cu", []),
     ("pairwise_file.cpp", []),
 ]
 

@@ -33,6 +33,14 @@
 
 using namespace kinc;
 
+/* compact.cu */
+size_t compact_scratch_words(int64_t size);
+cudaError_t compact_enqueue(int64_t start, int64_t size, int max_k, int S, const int8_t* d_K,
+                            const int8_t* d_labels, const float* d_corr, float lo, float hi,
+                            unsigned long long* d_scratch, int64_t cap_cmx, int64_t cap_ccm, int32_t* cmx_x,
+                            int32_t* cmx_y, int8_t* cmx_c, float* cmx_r, int32_t* ccm_x, int32_t* ccm_y,
+                            int8_t* ccm_c, uint8_t* ccm_nibbles, unsigned long long* d_counts, cudaStream_t st);
+
 namespace {
 
 constexpr int SCAN_THREADS = 1024;
@@ -232,6 +240,7 @@ struct kinc_sim_ctx
    unsigned long long* d_qbase = nullptr;
    unsigned long long* d_tiles = nullptr;
    unsigned long long* d_work = nullptr;
+   unsigned long long* d_compact = nullptr;   /* per-chunk counters of the device process() */
    int* d_status = nullptr;
    int8_t* d_K = nullptr;
    int8_t* d_labels = nullptr;
@@ -429,7 +438,7 @@ extern "C" int kinc_sim_work_counters(kinc_sim_ctx* ctx, uint64_t* out, int rese
 static void release(kinc_sim_ctx* c)
 {
    void* ptrs[] = { c->d_gem, c->d_umask, c->d_logn, c->d_jump, c->d_rng0, c->d_N, c->d_pg, c->d_qpos,
-                    c->d_bsum, c->d_qbase, c->d_tiles, c->d_work, c->d_status, c->d_K, c->d_labels, c->d_corr,
+                    c->d_bsum, c->d_qbase, c->d_tiles, c->d_work, c->d_compact, c->d_status, c->d_K, c->d_labels, c->d_corr,
                     c->d_scratch };
    for ( void* p : ptrs )
       if ( p ) cudaFree(p);
@@ -600,6 +609,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    CKC(cudaMalloc(&ctx->d_qbase, sizeof(unsigned long long)));
    CKC(cudaMalloc(&ctx->d_tiles, sizeof(unsigned long long)));
    CKC(cudaMalloc(&ctx->d_work, 4 * sizeof(unsigned long long)));
+   CKC(cudaMalloc(&ctx->d_compact, compact_scratch_words(ctx->max_block) * sizeof(unsigned long long)));
    CKC(cudaMemsetAsync(ctx->d_work, 0, 4 * sizeof(unsigned long long), ctx->stream));
    CKC(cudaMalloc(&ctx->d_status, sizeof(int)));
    CKC(cudaMalloc(&ctx->d_K, ctx->max_block));
@@ -777,6 +787,28 @@ extern "C" int kinc_sim_execute_block(kinc_sim_ctx* ctx, int64_t start, int64_t 
       if ( rc ) return rc;
       done += n;
    }
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_sim_compact_block_device(kinc_sim_ctx* ctx, int64_t start, int64_t size, const int8_t* d_K,
+                                             const int8_t* d_labels, const float* d_corr, int32_t* cmx_x,
+                                             int32_t* cmx_y, int8_t* cmx_c, float* cmx_r, int64_t cap_cmx,
+                                             int32_t* ccm_x, int32_t* ccm_y, int8_t* ccm_c, uint8_t* ccm_packed,
+                                             int64_t cap_ccm, uint64_t* d_counts, void* stream)
+{
+   if ( !ctx || !d_K || !d_corr || !d_counts ) return KINC_SIM_EINVAL;
+   int rc = check_range(ctx, start, size);
+   if ( rc ) return rc;
+   if ( size > ctx->max_block )
+      return fail(ctx, KINC_SIM_EINVAL, "size %lld exceeds the device block limit %lld", (long long)size,
+                  (long long)ctx->max_block);
+   if ( size == 0 ) return cudaMemsetAsync(d_counts, 0, 2 * sizeof(uint64_t),
+                                           stream ? (cudaStream_t)stream : ctx->stream) == cudaSuccess
+                             ? KINC_SIM_OK : KINC_SIM_ECUDA;
+   cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+   CK(compact_enqueue(start, size, ctx->params.max_clusters, ctx->S, d_K, d_labels, d_corr, ctx->params.min_corr,
+                      ctx->params.max_corr, ctx->d_compact, cap_cmx, cap_ccm, cmx_x, cmx_y, cmx_c, cmx_r, ccm_x,
+                      ccm_y, ccm_c, ccm_packed, (unsigned long long*)d_counts, st));
    return KINC_SIM_OK;
 }
 

@@ -156,8 +156,23 @@ extern "C" int kinc_pm_create(const char* path, int32_t type, int32_t genes, int
    return KINC_SIM_OK;
 }
 
+static int write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y, const int8_t* c,
+                       const void* payload, bool packed);
+
 extern "C" int kinc_pm_write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y, const int8_t* c,
                                    const void* payload)
+{
+   return write_items(m, n, x, y, c, payload, false);
+}
+
+extern "C" int kinc_pm_write_items_packed(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y,
+                                          const int8_t* c, const void* payload)
+{
+   return write_items(m, n, x, y, c, payload, true);
+}
+
+static int write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y, const int8_t* c,
+                       const void* payload, bool packed)
 {
    if ( !m || !m->writing ) return pm_fail(KINC_SIM_EINVAL, "Attempting to write data to uninitialized object.");
    if ( n < 0 || (n > 0 && (!x || !y || !c || !payload)) ) return pm_fail(KINC_SIM_EINVAL, "invalid item arrays");
@@ -188,7 +203,12 @@ extern "C" int kinc_pm_write_items(kinc_pm* m, int64_t n, const int32_t* x, cons
       m->e.put<int32_t>(m->buf, x[i]);
       m->e.put<int32_t>(m->buf, y[i]);
       m->e.put<int8_t>(m->buf, c[i]);
-      if ( m->type == KINC_PM_CCM )
+      if ( m->type == KINC_PM_CCM && packed )
+      {
+         const unsigned char* b = (const unsigned char*)payload + (size_t)i * m->data_size;
+         m->buf.insert(m->buf.end(), b, b + m->data_size);
+      }
+      else if ( m->type == KINC_PM_CCM )
       {
          const int8_t* codes = (const int8_t*)payload + (size_t)i * m->subsize;
          for ( int s = 0; s < m->subsize; s += 2 )
@@ -366,56 +386,111 @@ extern "C" int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, co
    const int64_t total = kinc_sim_total_pairs(ctx);
    const int64_t nb = kinc_sim_num_work_blocks(ctx);
    if ( first_block < 0 || first_block > nb ) return pm_fail(KINC_SIM_EINVAL, "first_block out of range");
-   const int64_t last = nblocks < 0 ? nb : std::min<int64_t>(nb, first_block + nblocks);
+   const int64_t last_block = nblocks < 0 ? nb : std::min<int64_t>(nb, first_block + nblocks);
+   const int64_t pair0 = first_block * KINC_SIM_WORK_BLOCK_SIZE;
+   const int64_t pair1 = std::min<int64_t>(total, last_block * KINC_SIM_WORK_BLOCK_SIZE);
    const int maxK = p.max_clusters;
+   const bool want_ccm = ccm_path != nullptr && p.clus_method != 0;
    kinc_pm* ccm = nullptr;
    kinc_pm* cmx = nullptr;
    int rc = KINC_SIM_OK;
    if ( ccm_path && (rc = kinc_pm_create(ccm_path, KINC_PM_CCM, G, maxK, S, little_endian, &ccm)) ) return rc;
    if ( cmx_path && (rc = kinc_pm_create(cmx_path, KINC_PM_CMX, G, maxK, 1, little_endian, &cmx)) )
    {
-      kinc_pm_close(ccm);
+      if ( ccm ) kinc_pm_close(ccm);
       return rc;
    }
-   const int64_t B = KINC_SIM_WORK_BLOCK_SIZE;
-   int8_t* K = nullptr;
-   int8_t* labels = nullptr;
-   float* corr = nullptr;
-   cudaError_t e1 = cudaMallocHost((void**)&K, B);
-   cudaError_t e2 = cudaMallocHost((void**)&labels, (size_t)B * S);
-   cudaError_t e3 = cudaMallocHost((void**)&corr, (size_t)B * maxK * sizeof(float));
-   std::vector<int32_t> cx(B * maxK), cy(B * maxK), mx(B * maxK), my(B * maxK);
-   std::vector<int8_t> cc(B * maxK), mc(B * maxK);
-   std::vector<float> cr(B * maxK);
-   std::vector<int8_t> codes(ccm ? (size_t)B * maxK * S : 1);
-   if ( e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess )
-      rc = pm_fail(KINC_SIM_ENOMEM, "cannot allocate pinned host buffers");
-   for ( int64_t b = first_block; rc == KINC_SIM_OK && b < last; ++b )
+   /* device blocks of whole work blocks; items are filtered and compacted on the GPU and only
+    * the kept ones are copied back (Similarity::process, src/core/similarity.cpp:66-127) */
+   const int64_t B = std::max<int64_t>(KINC_SIM_WORK_BLOCK_SIZE,
+                                       kinc_sim_max_device_block(ctx) / KINC_SIM_WORK_BLOCK_SIZE * KINC_SIM_WORK_BLOCK_SIZE);
+   const int64_t Bn = std::min<int64_t>(B, std::max<int64_t>(pair1 - pair0, 1));
+   const int nbytes = (S + 1) / 2;
+   int64_t cap = Bn * maxK;
+   cudaStream_t st = nullptr;
+   int8_t *dK = nullptr, *dL = nullptr, *dCc = nullptr, *dMc = nullptr;
+   float *dC = nullptr, *dCr = nullptr;
+   int32_t *dCx = nullptr, *dCy = nullptr, *dMx = nullptr, *dMy = nullptr;
+   uint8_t* dMp = nullptr;
+   uint64_t* dCount = nullptr;
+   int32_t *hx = nullptr, *hy = nullptr;
+   int8_t* hc = nullptr;
+   void* hp = nullptr;
+   uint64_t* hCount = nullptr;
+   bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
+   ok = ok && cudaMalloc(&dK, Bn) == cudaSuccess;
+   ok = ok && cudaMalloc(&dC, (size_t)Bn * maxK * sizeof(float)) == cudaSuccess;
+   ok = ok && (!want_ccm || cudaMalloc(&dL, (size_t)Bn * S) == cudaSuccess);
+   ok = ok && cudaMalloc(&dCount, 2 * sizeof(uint64_t)) == cudaSuccess;
+   ok = ok && cudaMallocHost(&hCount, 2 * sizeof(uint64_t)) == cudaSuccess;
+   /* item buffers grow on demand (cap starts at every cluster of the block passing) */
+   auto alloc_items = [&](int64_t n) {
+      cudaFree(dCx); cudaFree(dCy); cudaFree(dCc); cudaFree(dCr); cudaFree(dMx); cudaFree(dMy); cudaFree(dMc);
+      cudaFree(dMp); cudaFreeHost(hx); cudaFreeHost(hy); cudaFreeHost(hc); cudaFreeHost(hp);
+      dCx = dCy = dMx = dMy = nullptr; dCc = dMc = nullptr; dCr = nullptr; dMp = nullptr;
+      hx = hy = nullptr; hc = nullptr; hp = nullptr;
+      bool good = cudaMalloc(&dCx, n * 4) == cudaSuccess && cudaMalloc(&dCy, n * 4) == cudaSuccess
+                  && cudaMalloc(&dCc, n) == cudaSuccess && cudaMalloc(&dCr, n * 4) == cudaSuccess
+                  && cudaMallocHost(&hx, n * 4) == cudaSuccess && cudaMallocHost(&hy, n * 4) == cudaSuccess
+                  && cudaMallocHost(&hc, n) == cudaSuccess
+                  && cudaMallocHost(&hp, (size_t)n * std::max<int>(nbytes, 4)) == cudaSuccess;
+      if ( good && want_ccm )
+         good = cudaMalloc(&dMx, n * 4) == cudaSuccess && cudaMalloc(&dMy, n * 4) == cudaSuccess
+                && cudaMalloc(&dMc, n) == cudaSuccess && cudaMalloc(&dMp, (size_t)n * nbytes) == cudaSuccess;
+      return good;
+   };
+   cap = std::min<int64_t>(cap, (int64_t)1 << 24);
+   ok = ok && alloc_items(cap);
+   if ( !ok ) rc = pm_fail(KINC_SIM_ENOMEM, "cannot allocate the runner's buffers");
+   for ( int64_t start = pair0; rc == KINC_SIM_OK && start < pair1; start += Bn )
    {
-      /* Similarity::makeWork (src/core/similarity.cpp:30-39) */
-      const int64_t start = b * B;
-      const int64_t size = std::min<int64_t>(total - start, B);
-      rc = kinc_sim_execute_block(ctx, start, size, K, ccm ? labels : nullptr, corr);
-      if ( rc )
+      const int64_t size = std::min<int64_t>(Bn, pair1 - start);
+      rc = kinc_sim_execute_block_device(ctx, start, size, dK, dL, dC, st);
+      if ( rc ) { t_err = kinc_sim_last_error(ctx); break; }
+      for ( int attempt = 0; attempt < 2 && rc == KINC_SIM_OK; ++attempt )
       {
-         t_err = kinc_sim_last_error(ctx);
-         break;
+         rc = kinc_sim_compact_block_device(ctx, start, size, dK, dL, dC, dCx, dCy, dCc, dCr, cap, dMx, dMy, dMc,
+                                            dMp, want_ccm ? cap : 0, dCount, st);
+         if ( rc ) { t_err = kinc_sim_last_error(ctx); break; }
+         if ( cudaMemcpyAsync(hCount, dCount, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess
+              || cudaStreamSynchronize(st) != cudaSuccess )
+         {
+            rc = pm_fail(KINC_SIM_ECUDA, "device process failed: %s", kinc_sim_last_error(ctx));
+            break;
+         }
+         rc = kinc_sim_synchronize(ctx);
+         if ( rc ) { t_err = kinc_sim_last_error(ctx); break; }
+         const int64_t need = (int64_t)std::max(hCount[0], hCount[1]);
+         if ( need <= cap ) break;
+         cap = need;
+         if ( !alloc_items(cap) ) rc = pm_fail(KINC_SIM_ENOMEM, "cannot grow the item buffers to %lld", (long long)cap);
       }
-      int64_t n_cmx = 0, n_ccm = 0;
-      rc = kinc_sim_process_pairs(&p, S, start, size, K, labels, corr, cx.data(), cy.data(), cc.data(), cr.data(),
-                                  (int64_t)cx.size(), &n_cmx, ccm ? mx.data() : nullptr, my.data(), mc.data(),
-                                  codes.data(), ccm ? (int64_t)mx.size() : 0, &n_ccm);
-      if ( rc )
+      if ( rc ) break;
+      const int64_t n_cmx = (int64_t)hCount[0], n_ccm = want_ccm ? (int64_t)hCount[1] : 0;
+      if ( ccm && n_ccm > 0 )
       {
-         t_err = kinc_sim_last_error(nullptr);
-         break;
+         bool good = cudaMemcpyAsync(hx, dMx, n_ccm * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                     && cudaMemcpyAsync(hy, dMy, n_ccm * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                     && cudaMemcpyAsync(hc, dMc, n_ccm, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                     && cudaMemcpyAsync(hp, dMp, (size_t)n_ccm * nbytes, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                     && cudaStreamSynchronize(st) == cudaSuccess;
+         if ( !good ) { rc = pm_fail(KINC_SIM_ECUDA, "copy of CCM items failed"); break; }
+         if ( (rc = kinc_pm_write_items_packed(ccm, n_ccm, hx, hy, hc, hp)) ) break;
       }
-      if ( ccm && (rc = kinc_pm_write_items(ccm, n_ccm, mx.data(), my.data(), mc.data(), codes.data())) ) break;
-      if ( cmx && (rc = kinc_pm_write_items(cmx, n_cmx, cx.data(), cy.data(), cc.data(), cr.data())) ) break;
+      if ( cmx && n_cmx > 0 )
+      {
+         bool good = cudaMemcpyAsync(hx, dCx, n_cmx * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                     && cudaMemcpyAsync(hy, dCy, n_cmx * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                     && cudaMemcpyAsync(hc, dCc, n_cmx, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                     && cudaMemcpyAsync(hp, dCr, n_cmx * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                     && cudaStreamSynchronize(st) == cudaSuccess;
+         if ( !good ) { rc = pm_fail(KINC_SIM_ECUDA, "copy of CMX items failed"); break; }
+         if ( (rc = kinc_pm_write_items(cmx, n_cmx, hx, hy, hc, hp)) ) break;
+      }
    }
-   if ( K ) cudaFreeHost(K);
-   if ( labels ) cudaFreeHost(labels);
-   if ( corr ) cudaFreeHost(corr);
+   alloc_items(0);
+   cudaFree(dK); cudaFree(dC); cudaFree(dL); cudaFree(dCount); cudaFreeHost(hCount);
+   if ( st ) cudaStreamDestroy(st);
    const int rc1 = ccm ? kinc_pm_close(ccm) : KINC_SIM_OK;
    const int rc2 = cmx ? kinc_pm_close(cmx) : KINC_SIM_OK;
    return rc ? rc : (rc1 ? rc1 : rc2);

@@ -11,18 +11,21 @@ import pytest
 from kinc_gb300 import _native, synthetic
 from oracle import pyoracle
 
-HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "kinc_sim.h")
+INCLUDE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
 
 
 def declared_symbols():
-    text = open(HEADER).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(kinc_sim_\w+)\s*\(", text)))
+    names = set()
+    for f in sorted(os.listdir(INCLUDE)):
+        if f.endswith(".h"):
+            text = re.sub(r"/\*.*?\*/", "", open(os.path.join(INCLUDE, f)).read(), flags=re.S)
+            names |= set(re.findall(r"\b(kinc_(?:sim|pm|emx)_\w+)\s*\(", text))
+    return sorted(names)
 
 
 def test_library_exports_every_declared_symbol(native):
     names = declared_symbols()
-    assert len(names) >= 12
+    assert len(names) >= 25
     for n in names:
         assert hasattr(native, n), n
         assert n in _native.SIGNATURES, n
