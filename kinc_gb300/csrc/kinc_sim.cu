@@ -25,6 +25,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <mutex>
@@ -202,6 +203,49 @@ __global__ void k_prev(const int32_t* __restrict__ N, int64_t lo, int64_t end, i
    }
 }
 
+/* counting sort of a block's pairs by usable-sample count, largest first, so a
+ * warp's 32 pairs have similar trip counts and the heaviest tiles start first */
+constexpr int BIN_THREADS = 256;
+constexpr int MAX_BINS = 4096;
+
+__global__ void k_bin_hist(const int32_t* __restrict__ N, int64_t off, int64_t size, int shift, int nbins,
+                           unsigned int* __restrict__ hist)
+{
+   __shared__ unsigned int h[MAX_BINS];
+   for ( int i = threadIdx.x; i < nbins; i += blockDim.x ) h[i] = 0;
+   __syncthreads();
+   for ( int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < size; t += (int64_t)gridDim.x * blockDim.x )
+   {
+      atomicAdd(&h[N[off + t] >> shift], 1u);
+   }
+   __syncthreads();
+   for ( int i = threadIdx.x; i < nbins; i += blockDim.x )
+      if ( h[i] ) atomicAdd(&hist[i], h[i]);
+}
+
+/* exclusive scan in descending bin order (one thread; nbins <= 4096) */
+__global__ void k_bin_offsets(unsigned int* __restrict__ hist, int nbins)
+{
+   if ( threadIdx.x != 0 ) return;
+   unsigned int run = 0;
+   for ( int b = nbins - 1; b >= 0; --b )
+   {
+      const unsigned int c = hist[b];
+      hist[b] = run;
+      run += c;
+   }
+}
+
+__global__ void k_bin_scatter(const int32_t* __restrict__ N, int64_t off, int64_t size, int shift,
+                              unsigned int* __restrict__ cursor, int32_t* __restrict__ order)
+{
+   for ( int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < size; t += (int64_t)gridDim.x * blockDim.x )
+   {
+      const unsigned int pos = atomicAdd(&cursor[N[off + t] >> shift], 1u);
+      order[pos] = (int32_t)t;
+   }
+}
+
 /* ============================================================ host side */
 
 struct DevBuf
@@ -241,6 +285,9 @@ struct kinc_sim_ctx
    unsigned long long* d_tiles = nullptr;
    unsigned long long* d_work = nullptr;
    unsigned long long* d_compact = nullptr;   /* per-chunk counters of the device process() */
+   int32_t* d_order = nullptr;                /* binned tile order of the current block */
+   unsigned int* d_bins = nullptr;
+   int bin_shift = 0, nbins = 1;
    int* d_status = nullptr;
    int8_t* d_K = nullptr;
    int8_t* d_labels = nullptr;
@@ -438,7 +485,7 @@ extern "C" int kinc_sim_work_counters(kinc_sim_ctx* ctx, uint64_t* out, int rese
 static void release(kinc_sim_ctx* c)
 {
    void* ptrs[] = { c->d_gem, c->d_umask, c->d_logn, c->d_jump, c->d_rng0, c->d_N, c->d_pg, c->d_qpos,
-                    c->d_bsum, c->d_qbase, c->d_tiles, c->d_work, c->d_compact, c->d_status, c->d_K, c->d_labels, c->d_corr,
+                    c->d_bsum, c->d_qbase, c->d_tiles, c->d_work, c->d_compact, c->d_order, c->d_bins, c->d_status, c->d_K, c->d_labels, c->d_corr,
                     c->d_scratch };
    for ( void* p : ptrs )
       if ( p ) cudaFree(p);
@@ -610,6 +657,15 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    CKC(cudaMalloc(&ctx->d_tiles, sizeof(unsigned long long)));
    CKC(cudaMalloc(&ctx->d_work, 4 * sizeof(unsigned long long)));
    CKC(cudaMalloc(&ctx->d_compact, compact_scratch_words(ctx->max_block) * sizeof(unsigned long long)));
+   /* KINC_SIM_TILE_ORDER=natural keeps the pair order in tiles (for comparisons) */
+   const char* order_env = getenv("KINC_SIM_TILE_ORDER");
+   if ( params->precision == 0 && !(order_env && strcmp(order_env, "natural") == 0) )
+   {
+      while ( (S >> ctx->bin_shift) + 1 > MAX_BINS ) ++ctx->bin_shift;
+      ctx->nbins = (S >> ctx->bin_shift) + 1;
+      CKC(cudaMalloc(&ctx->d_order, ctx->max_block * sizeof(int32_t)));
+      CKC(cudaMalloc(&ctx->d_bins, ctx->nbins * sizeof(unsigned int)));
+   }
    CKC(cudaMemsetAsync(ctx->d_work, 0, 4 * sizeof(unsigned long long), ctx->stream));
    CKC(cudaMalloc(&ctx->d_status, sizeof(int)));
    CKC(cudaMalloc(&ctx->d_K, ctx->max_block));
@@ -692,6 +748,16 @@ static int enqueue_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t*
       k_prev<<<(int)((nwb + 63) / 64), 64, 0, st>>>(ctx->d_N, lo, end, ctx->d_pg);
       ++launches;
    }
+   if ( ctx->d_order && size > TILE )
+   {
+      const int64_t off = start - lo;
+      const int g = (int)std::min<int64_t>((size + BIN_THREADS - 1) / BIN_THREADS, 1024);
+      CK(cudaMemsetAsync(ctx->d_bins, 0, ctx->nbins * sizeof(unsigned int), st));
+      k_bin_hist<<<g, BIN_THREADS, 0, st>>>(ctx->d_N, off, size, ctx->bin_shift, ctx->nbins, ctx->d_bins);
+      k_bin_offsets<<<1, 32, 0, st>>>(ctx->d_bins, ctx->nbins);
+      k_bin_scatter<<<g, BIN_THREADS, 0, st>>>(ctx->d_N, off, size, ctx->bin_shift, ctx->d_bins, ctx->d_order);
+      launches += 3;
+   }
    CK(cudaMemsetAsync(ctx->d_tiles, 0, sizeof(unsigned long long), st));
    DevBlock B;
    B.start = start;
@@ -700,6 +766,7 @@ static int enqueue_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t*
    B.N = ctx->d_N;
    B.pg = ctx->d_pg;
    B.qpos = ctx->d_qpos;
+   B.order = (ctx->d_order && size > TILE) ? ctx->d_order : nullptr;
    B.outK = d_K;
    B.outLabels = d_labels;
    B.outCorr = d_corr;
@@ -1184,6 +1251,7 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    B.N = d_N;
    B.pg = d_pg;
    B.qpos = d_qpos;
+   B.order = nullptr;
    B.outK = d_K;
    B.outLabels = d_labels;
    B.outCorr = d_corr;

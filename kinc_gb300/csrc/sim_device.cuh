@@ -95,6 +95,7 @@ struct DevBlock
    const int32_t* N;                /* [p - lo] */
    const int32_t* pg;               /* [p - lo]: previous pair in the work block with larger N, or -1 */
    const uint64_t* qpos;            /* [p - start]: qualifying pairs before p (rand position / draws) */
+   const int32_t* order;            /* tile slot -> p - start (pairs binned by N, largest first); NULL: identity */
    int8_t* outK;                    /* [p - start] */
    int8_t* outLabels;               /* [p - start][S] */
    float* outCorr;                  /* [p - start][max_k] */
@@ -653,14 +654,19 @@ __device__ __forceinline__ float diff_norm(float x0, float x1, float m0, float m
 }
 
 /* KMeans::fit for one pair on this lane (pairwise_kmeans.cpp:12-99).  The
- * best run's labels end up in *best (a pointer into the three buffers). */
+ * best run's labels end up in *best (a pointer into the three buffers).
+ * Each Lloyd iteration is one pass: the reference's mean update of an
+ * iteration sums the samples under exactly the labels that iteration's
+ * assignment produced, in sample order, so those sums are accumulated during
+ * the assignment (and dropped when the labels did not change).  The first
+ * iteration compares against the all-zero initial labels without reading them. */
 template <int KT>
 __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*& best, int N, int Kr,
                             LaneRng& rng, unsigned long long& units)
 {
-   const int K = (KINC_STATIC_K && KT > 0) ? KT : Kr;
    /* KT > 0: up to KT centroids in registers (K <= KT at run time);
     * KT == 0: any K <= 64 from local memory */
+   const int K = (KINC_STATIC_K && KT > 0) ? KT : Kr;
    constexpr int KA = KT > 0 ? KT : 64;
    constexpr int UF = KT > 0 ? KT : 1;
    float bestLogL = -INFINITY;
@@ -677,20 +683,27 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
          mu0[k] = xv.x;
          mu1[k] = xv.y;
       }
-      int8_t* ya = cur;
-      int8_t* yb = nxt;
-      for ( int i = 0; i < N; ++i )
-      {
-         ya[i * TILE] = 0;
-         yb[i * TILE] = 0;
-      }
+      int8_t* ya = cur;     /* labels of the previous iteration */
+      int8_t* yb = nxt;     /* labels being assigned */
+      bool first = true;    /* ya is the all-zero initial vector, not yet written */
+      bool converged = false;
       for ( int t = 0; t < 300; ++t )
       {
          units += (unsigned long long)N * K;
          bool same = true;
+         float s0[KA], s1[KA];
+         int nk[KA];
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            s0[k] = 0.f; s1[k] = 0.f; nk[k] = 0;
+         }
+         float2 xn = X[0];
          for ( int i = 0; i < N; ++i )
          {
-            const float2 xv = X[i * TILE];
+            const float2 xv = xn;
+            if ( i + 1 < N ) xn = X[(i + 1) * TILE];
             int min_k = -1;
             float min_d = 0.f;
 #pragma unroll UF
@@ -705,29 +718,13 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
                }
             }
             yb[i * TILE] = (int8_t)min_k;
-            same = same && (ya[i * TILE] == (int8_t)min_k);
-         }
-         if ( same ) break;
-         int8_t* tmp = ya;
-         ya = yb;
-         yb = tmp;
-         float s0[KA], s1[KA];
-         int nk[KA];
-#pragma unroll UF
-         for ( int k = 0; k < KA; ++k )
-         {
-            if ( k >= K ) continue;
-            s0[k] = 0.f; s1[k] = 0.f; nk[k] = 0;
-         }
-         for ( int i = 0; i < N; ++i )
-         {
-            const float2 xv = X[i * TILE];
-            const int8_t l = ya[i * TILE];
+            const int8_t prev = first ? (int8_t)0 : ya[i * TILE];
+            same = same && (prev == (int8_t)min_k);
 #pragma unroll UF
             for ( int k = 0; k < KA; ++k )
             {
                if ( k >= K ) continue;
-               if ( l == k )
+               if ( k == min_k )
                {
                   s0[k] += xv.x;
                   s1[k] += xv.y;
@@ -735,6 +732,15 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
                }
             }
          }
+         if ( same )
+         {
+            converged = true;
+            break;
+         }
+         int8_t* tmp = ya;
+         ya = yb;
+         yb = tmp;
+         first = false;
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
@@ -744,6 +750,8 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
             mu1[k] = s1[k] * sc;
          }
       }
+      /* the labels: the unchanged assignment (in yb) if converged, else the last one (ya) */
+      int8_t* lab = converged ? yb : ya;
       /* computeLogLikelihood: one accumulator, cluster-major order */
       float S = 0.f;
       for ( int k = 0; k < K; ++k )
@@ -757,7 +765,7 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
          }
          for ( int i = 0; i < N; ++i )
          {
-            if ( ya[i * TILE] != k ) continue;
+            if ( lab[i * TILE] != k ) continue;
             const float2 xv = X[i * TILE];
             const float d = diff_norm(xv.x, xv.y, c0, c1);
             S += d * d;
@@ -769,9 +777,9 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
       {
          bestLogL = logL;
          int8_t* old = best;
-         best = ya;
-         cur = (ya == cur) ? old : cur;
-         nxt = (ya == nxt) ? old : nxt;
+         best = lab;
+         cur = (lab == cur) ? old : cur;
+         nxt = (lab == nxt) ? old : nxt;
       }
    }
    return bestLogL;

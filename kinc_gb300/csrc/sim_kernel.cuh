@@ -21,28 +21,43 @@ constexpr int WARPS_PER_BLOCK = 4;
 #define KINC_MIN_BLOCKS 4
 #endif
 
-/* The i-th usable sample (0-based) of pair c: what the reference left in its
- * packed array at position i. */
-__device__ inline float2 packed_sample(const DevParams& P, const DevData& D, int64_t c, int i)
+/* What the reference left in its packed array at position i by pair c: the
+ * i-th usable sample (0-based) of c.  Reads come with increasing i for the
+ * same or an earlier pair, so the word scan resumes where the last one ended
+ * while c is unchanged. */
+struct PackedCursor
 {
-   int32_t x, y;
-   pair_xy(c, x, y);
-   const uint32_t* mx = D.umask + (size_t)x * P.W;
-   const uint32_t* my = D.umask + (size_t)y * P.W;
-   for ( int w = 0; w < P.W; ++w )
+   int64_t c = -1;
+   int w = 0;          /* current mask word */
+   int before = 0;     /* usable samples in words < w */
+   int32_t x = 0, y = 0;
+
+   __device__ float2 at(const DevParams& P, const DevData& D, int64_t pc, int i)
    {
-      uint32_t m = mx[w] & my[w];
-      const int cnt = __popc(m);
-      if ( i < cnt )
+      if ( pc != c )
       {
-         for ( int r = 0; r < i; ++r ) m &= m - 1;
-         const int s = w * 32 + (__ffs(m) - 1);
-         return make_float2(D.gem[(size_t)x * P.S + s], D.gem[(size_t)y * P.S + s]);
+         c = pc;
+         w = 0;
+         before = 0;
+         pair_xy(pc, x, y);
       }
-      i -= cnt;
+      const uint32_t* mx = D.umask + (size_t)x * P.W;
+      const uint32_t* my = D.umask + (size_t)y * P.W;
+      for ( ; w < P.W; ++w )
+      {
+         uint32_t m = mx[w] & my[w];
+         const int cnt = __popc(m);
+         if ( i < before + cnt )
+         {
+            for ( int r = 0; r < i - before; ++r ) m &= m - 1;
+            const int s = w * 32 + (__ffs(m) - 1);
+            return make_float2(D.gem[(size_t)x * P.S + s], D.gem[(size_t)y * P.S + s]);
+         }
+         before += cnt;
+      }
+      return make_float2(0.f, 0.f);
    }
-   return make_float2(0.f, 0.f);
-}
+};
 
 /* Pearson::computeCluster for this lane's pair (pairwise_pearson.cpp:12-52). */
 __device__ inline float lane_pearson(const DevParams& P, const DevData& D, const DevBlock& B, const float2* X,
@@ -65,11 +80,12 @@ __device__ inline float lane_pearson(const DevParams& P, const DevData& D, const
          }
       }
       int32_t c = B.pg[p - B.lo];
+      PackedCursor cur;
       for ( int i = N; i < P.S; ++i )
       {
          if ( lbl[i * TILE] != k ) continue;
          while ( c >= 0 && B.N[c] <= i ) c = B.pg[c];
-         const float2 v = c >= 0 ? packed_sample(P, D, B.lo + c, i) : make_float2(0.f, 0.f);
+         const float2 v = c >= 0 ? cur.at(P, D, B.lo + c, i) : make_float2(0.f, 0.f);
          sumx += v.x; sumy += v.y; sumx2 += v.x * v.x; sumy2 += v.y * v.y; sumxy += v.x * v.y;
          ++n;
       }
@@ -194,15 +210,18 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
       if ( lane == 0 ) t = atomicAdd(B.tiles, 1ull);
       t = __shfl_sync(0xffffffffu, t, 0);
       if ( (int64_t)t >= ntiles ) break;
-      const int64_t p0 = B.start + (int64_t)t * TILE;
-      const int64_t left = B.start + B.size - p0;
+      const int64_t slot0 = (int64_t)t * TILE;
+      const int64_t left = B.size - slot0;
       const int npairs = left < TILE ? (int)left : TILE;
+      /* this lane's pair: tile slots map to pairs through the binned order */
+      int64_t myp = B.start + slot0 + lane;
+      if ( B.order && lane < npairs ) myp = B.start + B.order[slot0 + lane];
 
       /* ---- warp-cooperative: fetch, pre-outliers, rand() position, per pair */
       int myN = 0;
       for ( int j = 0; j < npairs; ++j )
       {
-         const int64_t p = p0 + j;
+         const int64_t p = __shfl_sync(0xffffffffu, myp, j);
          int32_t x, y;
          pair_xy(p, x, y);
          const int n = warp_fetch(P, D, x, y, X, lbl, j, lane);
@@ -226,7 +245,6 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
 
       /* ---- lane-local: clustering */
       int K = 1;
-      const int64_t myp = p0 + lane;
       int32_t mx = 0, my = 0;
       if ( lane < npairs ) pair_xy(myp, mx, my);
       if ( CLUS != 0 )
@@ -294,7 +312,8 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
             const int Kj = __shfl_sync(0xffffffffu, K, j);
             const int xj = __shfl_sync(0xffffffffu, mx, j);
             const int yj = __shfl_sync(0xffffffffu, my, j);
-            float* row = B.outCorr ? B.outCorr + (p0 + j - B.start) * P.max_k : nullptr;
+            const int64_t pj = __shfl_sync(0xffffffffu, myp, j);
+            float* row = B.outCorr ? B.outCorr + (pj - B.start) * P.max_k : nullptr;
             for ( int k = 0; k < P.max_k; ++k )
             {
                float r = __int_as_float(0x7fc00000);
@@ -310,7 +329,8 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
       {
          for ( int j = 0; j < npairs; ++j )
          {
-            int8_t* row = B.outLabels + (p0 + j - B.start) * (int64_t)P.S;
+            const int64_t pj = __shfl_sync(0xffffffffu, myp, j);
+            int8_t* row = B.outLabels + (pj - B.start) * (int64_t)P.S;
             for ( int s = lane; s < P.S; s += 32 ) row[s] = lbl[s * TILE + j];
          }
       }
