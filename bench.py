@@ -230,6 +230,61 @@ def dense_leg(L, vp, check_pairs=1000000):
     return out
 
 
+def kmeans_leg(L, vp, cpu=True):
+    """K-means (k <= 3, BIC) + Pearson on the uneven 10,000 x 4,000 workload (kinc_gb300.synthetic workload 4:
+    per-gene NaN rate ~U(0,0.6), so usable-sample counts span ~600-4,000; 5% planted 2-cluster pairs):
+    two device blocks of 65,536 pairs timed with CUDA events, and the oracle on the host cores over a
+    bounded sample of the same workload."""
+    import ctypes
+
+    import torch
+
+    from kinc_gb300 import Similarity, _native, synthetic
+    from oracle import pyoracle
+    gem = synthetic.generate(4)
+    G, S = gem.shape
+    args = dict(clusmethod="kmeans", corrmethod="pearson", minclus=1, maxclus=3, crit="BIC", minsamp=30)
+    sim = Similarity(gem, **args)
+    sim.initialize()
+    ctx = sim._ctx
+    n = 65536
+    dK = torch.empty(n, dtype=torch.int8, device="cuda")
+    dL = torch.empty((n, S), dtype=torch.int8, device="cuda")
+    dC = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        def once(s0):
+            _native.check(L.kinc_sim_execute_block_device(ctx, s0, n, vp(dK.data_ptr()), vp(dL.data_ptr()),
+                                                          vp(dC.data_ptr()), vp(stream.cuda_stream)), ctx)
+        once(0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        once(n)
+        once(2 * n)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 2
+    _native.check(L.kinc_sim_synchronize(ctx), ctx)
+    sim.close()
+    out = {"workload": "K-means k<=3 (BIC) + Pearson, GEM 10000x4000 float32, per-gene NaN rate ~U(0,0.6), "
+                       "5% planted 2-cluster pairs, minsamp 30", "pairs_per_step": n, "ms_per_step": ms,
+           "pairs_per_s": n / (ms / 1e3)}
+    if cpu:
+        threads = os.cpu_count() or 1
+        total = G * (G - 1) // 2
+        rng = np.random.default_rng(11)
+        starts = rng.choice((total - 1) // 32768, size=threads, replace=False).astype(np.int64) * 32768
+        p = pyoracle.params(clus_method=2, corr_method=0, min_clusters=1, max_clusters=3, criterion=0, min_samples=30)
+        done, secs = pyoracle.run_segments_parallel(gem, p, starts, np.full(threads, 6, np.int64), threads)
+        out["cpu_baseline"] = {"value": done / secs, "unit": "pairs/s", "cores": threads, "kind": "port",
+                               "sample": f"{done} pairs: {threads} threads x 6 consecutive pairs from seeded "
+                                         f"random work blocks, {secs:.1f} s"}
+        out["gpu_over_cpu"] = out["pairs_per_s"] / out["cpu_baseline"]["value"]
+    return out
+
+
 def config_dict(args, gem):
     G, S = gem.shape
     return {"workload": "GMM k<=5 + Spearman, GEM 5000x1000 float32, 10% NaN, 10 planted modules; "
@@ -251,6 +306,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-dense", action="store_true")
+    ap.add_argument("--no-kmeans", action="store_true")
     ap.add_argument("--dense-check-pairs", type=int, default=1000000)
     args = ap.parse_args()
 
@@ -396,6 +452,7 @@ def main():
                 "kernel": "k_similarity", "units": units, "flops_per_unit": FLOPS_PER_UNIT, "fits": fits}
 
     tensor_core = None if args.no_dense else dense_leg(L, vp, args.dense_check_pairs)
+    kmeans = None if args.no_kmeans else kmeans_leg(L, vp, cpu=not args.no_cpu)
 
     cpu = None
     if not args.no_cpu:
@@ -409,7 +466,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded; no public dataset)",
             "config": config_dict(args, gem), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-            "cpu_baseline": cpu, "clocks": clk, "tensor_core": tensor_core}
+            "cpu_baseline": cpu, "clocks": clk, "tensor_core": tensor_core, "kmeans_uneven": kmeans}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

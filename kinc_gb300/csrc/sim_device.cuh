@@ -38,6 +38,9 @@ constexpr int TILE = 32;            /* pairs per warp tile */
 #define KINC_SAMPLE_UNROLL 1
 #endif
 constexpr int SAMPLE_UNROLL = KINC_SAMPLE_UNROLL;   /* unroll factor of the EM sample loops */
+#ifndef KINC_UNROLL_SMALL_K
+#define KINC_UNROLL_SMALL_K 0       /* fits with K <= this unroll their sample loops by 2 (more ILP) */
+#endif
 #ifndef KINC_STATIC_K
 #define KINC_STATIC_K 1             /* 1: one compiled fit per K (K known to the compiler); 0: one fit for all K <= KS */
 #endif
@@ -414,6 +417,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
    constexpr int KA = KT > 0 ? KT : 64;
    constexpr int UF = KT > 0 ? KT : 1;
    constexpr bool STORE_G = KT > 0 && KINC_STORE_GAMMA;
+   constexpr int SU = (KT > 0 && KT <= KINC_UNROLL_SMALL_K) ? 2 : SAMPLE_UNROLL;
    float m0[KA], m1[KA], ia[KA], ib[KA], ic[KA], nrm[KA], logpi[KA];
 
    if ( rng.mode == 1 ) rng.lcg = 1;
@@ -450,7 +454,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
          maxG[k] = -INFINITY;
       }
       float2 xn = X[0];
-      #pragma unroll SAMPLE_UNROLL
+      #pragma unroll SU
       for ( int i = 0; i < N; ++i )
       {
          const float2 xv = xn;
@@ -503,7 +507,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
          }
          xn = X[0];
          float ln = lpx[0];
-         #pragma unroll SAMPLE_UNROLL
+         #pragma unroll SU
          for ( int i = 0; i < N; ++i )
          {
             const float2 xv = xn;
@@ -565,7 +569,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
       }
       xn = X[0];
       float ln = lpx[0];
-      #pragma unroll SAMPLE_UNROLL
+      #pragma unroll SU
       for ( int i = 0; i < N; ++i )
       {
          const float2 xv = xn;
