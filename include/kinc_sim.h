@@ -47,7 +47,9 @@ typedef struct kinc_sim_ctx kinc_sim_ctx;
 typedef struct kinc_sim_params
 {
    int32_t clus_method;   /* --clusmethod: 0 none, 1 gmm, 2 kmeans            (default 0) */
-   int32_t corr_method;   /* --corrmethod: 0 pearson, 1 spearman              (default 0) */
+   int32_t corr_method;   /* --corrmethod: 0 pearson, 1 spearman              (default 0);
+                             2 both (Pearson and Spearman per cluster in one pass; not in the reference,
+                             which runs one method per analytic) */
    float   min_expr;      /* --minexpr                                        (default -inf) */
    int32_t min_samples;   /* --minsamp, >= 1                                  (default 30) */
    int32_t min_clusters;  /* --minclus, 1..64                                 (default 1) */
@@ -96,7 +98,8 @@ int32_t kinc_sim_num_work_blocks(const kinc_sim_ctx* ctx);
  *   out_labels[size * samples]   int8   per-sample labels: cluster id >= 0, or -9 missing,
  *                                        -6 below minexpr, -7 pre-outlier, -8 post-outlier
  *                                        (meaningful when K > 1)
- *   out_corr[size * max_clusters] float correlation per cluster k < K, NaN elsewhere
+ *   out_corr[size * max_clusters * nc] float correlation per cluster k < K, NaN elsewhere;
+ *                                  nc = 2 when corr_method is 2 (row [k][0] Pearson, [k][1] Spearman)
  * Any output pointer may be NULL.  Blocks may be executed in any order; the
  * position on the rand() stream is derived from `start`.
  */

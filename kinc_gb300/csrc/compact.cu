@@ -1,7 +1,8 @@
 /*
  * compact.cu -- Similarity::process on the GPU (src/core/similarity.cpp:66-127):
  * the clusters of a block whose correlation passes
- * !isnan(r) && mincorr <= |r| <= maxcorr, renumbered 0..c-1 per pair and
+ * !isnan(r) && mincorr <= |r| <= maxcorr (with two correlations per cluster:
+ * either of them), renumbered 0..c-1 per pair and
  * compacted, in pair order, into CMX items (x, y, c, r) and -- for pairs with
  * K > 1 -- CCM items (x, y, c, sample codes packed two per byte as the CCM
  * file stores them, sample 2i in the low nibble).  Only the kept items then
@@ -22,9 +23,11 @@ namespace {
 constexpr int CHUNK = 64;          /* pairs per thread */
 constexpr int THREADS = 256;
 
-__device__ __forceinline__ bool keep(float r, float lo, float hi)
+__device__ __forceinline__ bool keep(const float* r, int nc, float lo, float hi)
 {
-   return !isnan(r) && lo <= fabsf(r) && fabsf(r) <= hi;
+   for ( int c = 0; c < nc; ++c )
+      if ( !isnan(r[c]) && lo <= fabsf(r[c]) && fabsf(r[c]) <= hi ) return true;
+   return false;
 }
 
 __device__ __forceinline__ void pair_of(int64_t p, int32_t& x, int32_t& y)
@@ -36,7 +39,7 @@ __device__ __forceinline__ void pair_of(int64_t p, int32_t& x, int32_t& y)
    y = (int32_t)(p - xx * (xx - 1) / 2);
 }
 
-__global__ void k_compact_count(int64_t size, int max_k, const int8_t* __restrict__ K,
+__global__ void k_compact_count(int64_t size, int max_k, int nc, const int8_t* __restrict__ K,
                                 const float* __restrict__ corr, float lo, float hi,
                                 unsigned long long* __restrict__ cnt_cmx, unsigned long long* __restrict__ cnt_ccm)
 {
@@ -50,7 +53,7 @@ __global__ void k_compact_count(int64_t size, int max_k, const int8_t* __restric
       const int k_n = K[q];
       for ( int k = 0; k < k_n; ++k )
       {
-         if ( keep(corr[q * max_k + k], lo, hi) )
+         if ( keep(corr + (q * max_k + k) * nc, nc, lo, hi) )
          {
             ++a;
             if ( k_n > 1 ) ++b;
@@ -94,7 +97,8 @@ __global__ void k_compact_scan(unsigned long long* __restrict__ v, int64_t n)
    }
 }
 
-__global__ void k_compact_write(int64_t start, int64_t size, int max_k, int S, const int8_t* __restrict__ K,
+__global__ void k_compact_write(int64_t start, int64_t size, int max_k, int nc, int S,
+                                const int8_t* __restrict__ K,
                                 const int8_t* __restrict__ labels, const float* __restrict__ corr, float lo, float hi,
                                 const unsigned long long* __restrict__ off_cmx,
                                 const unsigned long long* __restrict__ off_ccm, int64_t cap_cmx, int64_t cap_ccm,
@@ -115,14 +119,14 @@ __global__ void k_compact_write(int64_t start, int64_t size, int max_k, int S, c
       int c1 = 0, c2 = 0;
       for ( int k = 0; k < k_n; ++k )
       {
-         const float r = corr[q * max_k + k];
-         if ( !keep(r, lo, hi) ) continue;
+         const float* r = corr + (q * max_k + k) * nc;
+         if ( !keep(r, nc, lo, hi) ) continue;
          if ( (int64_t)a < cap_cmx && cmx_x )
          {
             cmx_x[a] = x;
             cmx_y[a] = y;
             cmx_c[a] = (int8_t)c1;
-            cmx_r[a] = r;
+            for ( int c = 0; c < nc; ++c ) cmx_r[a * nc + c] = r[c];
          }
          ++a;
          ++c1;
@@ -169,7 +173,7 @@ size_t compact_scratch_words(int64_t size)
    return 2 * (size_t)((size + CHUNK - 1) / CHUNK + 1);
 }
 
-cudaError_t compact_enqueue(int64_t start, int64_t size, int max_k, int S, const int8_t* d_K,
+cudaError_t compact_enqueue(int64_t start, int64_t size, int max_k, int nc, int S, const int8_t* d_K,
                             const int8_t* d_labels, const float* d_corr, float lo, float hi,
                             unsigned long long* d_scratch, int64_t cap_cmx, int64_t cap_ccm, int32_t* cmx_x,
                             int32_t* cmx_y, int8_t* cmx_c, float* cmx_r, int32_t* ccm_x, int32_t* ccm_y,
@@ -179,10 +183,10 @@ cudaError_t compact_enqueue(int64_t start, int64_t size, int max_k, int S, const
    unsigned long long* c_cmx = d_scratch;
    unsigned long long* c_ccm = d_scratch + chunks + 1;
    const int blocks = (int)((chunks + THREADS - 1) / THREADS);
-   k_compact_count<<<blocks, THREADS, 0, st>>>(size, max_k, d_K, d_corr, lo, hi, c_cmx, c_ccm);
+   k_compact_count<<<blocks, THREADS, 0, st>>>(size, max_k, nc, d_K, d_corr, lo, hi, c_cmx, c_ccm);
    k_compact_scan<<<1, 1024, 0, st>>>(c_cmx, chunks);
    k_compact_scan<<<1, 1024, 0, st>>>(c_ccm, chunks);
-   k_compact_write<<<blocks, THREADS, 0, st>>>(start, size, max_k, S, d_K, d_labels, d_corr, lo, hi, c_cmx, c_ccm,
+   k_compact_write<<<blocks, THREADS, 0, st>>>(start, size, max_k, nc, S, d_K, d_labels, d_corr, lo, hi, c_cmx, c_ccm,
                                                cap_cmx, cap_ccm, cmx_x, cmx_y, cmx_c, cmx_r, ccm_x, ccm_y, ccm_c,
                                                ccm_nibbles);
    cudaError_t e = cudaMemcpyAsync(d_counts, c_cmx + chunks, sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st);

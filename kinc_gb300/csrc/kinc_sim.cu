@@ -36,7 +36,7 @@ using namespace kinc;
 
 /* compact.cu */
 size_t compact_scratch_words(int64_t size);
-cudaError_t compact_enqueue(int64_t start, int64_t size, int max_k, int S, const int8_t* d_K,
+cudaError_t compact_enqueue(int64_t start, int64_t size, int max_k, int ncorr, int S, const int8_t* d_K,
                             const int8_t* d_labels, const float* d_corr, float lo, float hi,
                             unsigned long long* d_scratch, int64_t cap_cmx, int64_t cap_ccm, int32_t* cmx_x,
                             int32_t* cmx_y, int8_t* cmx_c, float* cmx_r, int32_t* ccm_x, int32_t* ccm_y,
@@ -384,7 +384,11 @@ int validate(const kinc_sim_params* p, int32_t G, int32_t S, std::string& why)
    if ( G < 2 ) { snprintf(buf, sizeof buf, "genes must be >= 2 (got %d)", G); why = buf; return 0; }
    if ( S < 1 ) { snprintf(buf, sizeof buf, "samples must be >= 1 (got %d)", S); why = buf; return 0; }
    if ( p->clus_method < 0 || p->clus_method > 2 ) { why = "clus_method must be 0 (none), 1 (gmm) or 2 (kmeans)"; return 0; }
-   if ( p->corr_method < 0 || p->corr_method > 1 ) { why = "corr_method must be 0 (pearson) or 1 (spearman)"; return 0; }
+   if ( p->corr_method < 0 || p->corr_method > 2 )
+   {
+      why = "corr_method must be 0 (pearson), 1 (spearman) or 2 (both)";
+      return 0;
+   }
    if ( p->min_samples < 1 ) { why = "min_samples must be >= 1"; return 0; }
    if ( p->min_clusters < 1 || p->min_clusters > 64 ) { why = "min_clusters must be in 1..64"; return 0; }
    if ( p->max_clusters < 1 || p->max_clusters > 64 ) { why = "max_clusters must be in 1..64"; return 0; }
@@ -578,16 +582,20 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    dp.c2 = 2 * std::log(2.0f * M_PI);
    dp.P2 = next_pow2_host(std::max(S, 2));
    const bool need_sort = (params->clus_method != 0 && (params->pre_out || params->post_out))
-                          || params->corr_method == 1;
-   dp.sort_floats = params->corr_method == 1 ? 3 * dp.P2 : (need_sort ? dp.P2 : 0);
+                          || params->corr_method >= 1;
+   dp.sort_floats = params->corr_method >= 1 ? 3 * dp.P2 : (need_sort ? dp.P2 : 0);
+   dp.ncorr = params->corr_method == 2 ? 2 : 1;
 
    /* launch shape: sort buffers in shared memory when they fit */
    const size_t sort_bytes_warp = (size_t)dp.sort_floats * sizeof(float);
-   ctx->smem_sort = need_sort && sort_bytes_warp * WARPS_PER_BLOCK <= 160 * 1024;
-   ctx->smem_bytes = ctx->smem_sort ? (int)(sort_bytes_warp * WARPS_PER_BLOCK) : 0;
    ctx->kern = params->clus_method == 0 ? sim_kernel_none()
              : params->clus_method == 1 ? sim_kernel_gmm(params->max_clusters)
                                         : sim_kernel_kmeans(params->max_clusters);
+   /* GMM parameters in shared memory take the room the sort buffers would use */
+   const size_t param_bytes_warp = (KINC_GMM_PARAMS_SMEM && ctx->kern.clus == 1 && ctx->kern.ks > 0)
+                                      ? (size_t)7 * ctx->kern.ks * TILE * sizeof(float) : 0;
+   ctx->smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * WARPS_PER_BLOCK <= 160 * 1024;
+   ctx->smem_bytes = (int)((ctx->smem_sort ? sort_bytes_warp : 0) + param_bytes_warp) * WARPS_PER_BLOCK;
    if ( ctx->smem_bytes > 48 * 1024 )
       CKC(cudaFuncSetAttribute(ctx->kern.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_bytes));
    int per_sm = 0;
@@ -670,7 +678,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    CKC(cudaMalloc(&ctx->d_status, sizeof(int)));
    CKC(cudaMalloc(&ctx->d_K, ctx->max_block));
    if ( params->precision == 0 ) CKC(cudaMalloc(&ctx->d_labels, (size_t)ctx->max_block * S));
-   CKC(cudaMalloc(&ctx->d_corr, (size_t)ctx->max_block * params->max_clusters * sizeof(float)));
+   CKC(cudaMalloc(&ctx->d_corr, (size_t)ctx->max_block * params->max_clusters * dp.ncorr * sizeof(float)));
    CKC(cudaMemsetAsync(ctx->d_qbase, 0, sizeof(unsigned long long), ctx->stream));
    CKC(cudaMemsetAsync(ctx->d_status, 0, sizeof(int), ctx->stream));
    ctx->q_valid_end = 0;
@@ -742,8 +750,9 @@ static int enqueue_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t*
       launches += 3;
       ctx->q_valid_end = end;
    }
-   if ( dp.corr == 0 && dp.semantics == 0 )
+   if ( (dp.corr == 0 || dp.corr == 2) && dp.semantics == 0 )
    {
+      /* every Pearson run with the reference's packed-array reads needs the links */
       const int64_t nwb = (end - 1) / KINC_SIM_WORK_BLOCK_SIZE - lo / KINC_SIM_WORK_BLOCK_SIZE + 1;
       k_prev<<<(int)((nwb + 63) / 64), 64, 0, st>>>(ctx->d_N, lo, end, ctx->d_pg);
       ++launches;
@@ -834,7 +843,7 @@ extern "C" int kinc_sim_execute_block(kinc_sim_ctx* ctx, int64_t start, int64_t 
    if ( rc ) return rc;
    ctx->launches = 0;
    const int S = ctx->S;
-   const int maxK = ctx->params.max_clusters;
+   const int maxK = ctx->params.max_clusters * ctx->dp.ncorr;   /* floats per pair */
    for ( int64_t done = 0; done < size; )
    {
       const int64_t n = std::min<int64_t>(ctx->max_block, size - done);
@@ -873,7 +882,8 @@ extern "C" int kinc_sim_compact_block_device(kinc_sim_ctx* ctx, int64_t start, i
                                            stream ? (cudaStream_t)stream : ctx->stream) == cudaSuccess
                              ? KINC_SIM_OK : KINC_SIM_ECUDA;
    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
-   CK(compact_enqueue(start, size, ctx->params.max_clusters, ctx->S, d_K, d_labels, d_corr, ctx->params.min_corr,
+   CK(compact_enqueue(start, size, ctx->params.max_clusters, ctx->dp.ncorr, ctx->S, d_K, d_labels, d_corr,
+                      ctx->params.min_corr,
                       ctx->params.max_corr, ctx->d_compact, cap_cmx, cap_ccm, cmx_x, cmx_y, cmx_c, cmx_r, ccm_x,
                       ccm_y, ccm_c, ccm_packed, (unsigned long long*)d_counts, st));
    return KINC_SIM_OK;
@@ -907,8 +917,14 @@ extern "C" int kinc_sim_process_pairs(const kinc_sim_params* params, int32_t sam
       return fail(nullptr, KINC_SIM_EINVAL, "invalid arguments to kinc_sim_process_pairs");
    const int S = samples;
    const int maxK = params->max_clusters;
+   const int ncorr = params->corr_method == 2 ? 2 : 1;   /* correlations per cluster */
    const float lo = params->min_corr;
    const float hi = params->max_corr;
+   auto passes = [&](const float* r) {
+      for ( int c = 0; c < ncorr; ++c )
+         if ( !std::isnan(r[c]) && lo <= std::fabs(r[c]) && std::fabs(r[c]) <= hi ) return true;
+      return false;
+   };
    int64_t nc = 0, nm = 0;
    /* pair index -> (x, y) and then ++ (src/core/pairwise_index.cpp:32-57,85-94) */
    int64_t x = 1, pos = 0;
@@ -923,8 +939,7 @@ extern "C" int kinc_sim_process_pairs(const kinc_sim_params* params, int32_t sam
          int c = 0;
          for ( int k = 0; k < Kq; ++k )
          {
-            const float r = corr[q * maxK + k];
-            if ( !std::isnan(r) && lo <= std::fabs(r) && std::fabs(r) <= hi )
+            if ( passes(corr + (q * maxK + k) * ncorr) )
             {
                if ( nm >= cap_ccm )
                   return fail(nullptr, KINC_SIM_EINVAL, "CCM capacity %lld exceeded", (long long)cap_ccm);
@@ -945,15 +960,15 @@ extern "C" int kinc_sim_process_pairs(const kinc_sim_params* params, int32_t sam
          int c = 0;
          for ( int k = 0; k < Kq; ++k )
          {
-            const float r = corr[q * maxK + k];
-            if ( !std::isnan(r) && lo <= std::fabs(r) && std::fabs(r) <= hi )
+            const float* r = corr + (q * maxK + k) * ncorr;
+            if ( passes(r) )
             {
                if ( nc >= cap_cmx )
                   return fail(nullptr, KINC_SIM_EINVAL, "CMX capacity %lld exceeded", (long long)cap_cmx);
                cmx_x[nc] = (int32_t)x;
                cmx_y[nc] = (int32_t)y;
                cmx_c[nc] = (int8_t)c++;
-               cmx_r[nc] = r;
+               for ( int cc = 0; cc < ncorr; ++cc ) cmx_r[nc * ncorr + cc] = r[cc];
                ++nc;
             }
          }
@@ -1145,12 +1160,15 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
                           || params->corr_method == 1;
    dp.sort_floats = params->corr_method == 1 ? 3 * dp.P2 : (need_sort ? dp.P2 : 0);
    dp.gam_k = 0;
+   dp.ncorr = 1;
    const size_t sort_bytes_warp = (size_t)dp.sort_floats * sizeof(float);
-   const int smem_sort = need_sort && sort_bytes_warp * WARPS_PER_BLOCK <= 160 * 1024;
-   const int smem_bytes = smem_sort ? (int)(sort_bytes_warp * WARPS_PER_BLOCK) : 0;
    const SimKernel kern = params->clus_method == 0 ? sim_kernel_none()
                         : params->clus_method == 1 ? sim_kernel_gmm(params->max_clusters)
                                                    : sim_kernel_kmeans(params->max_clusters);
+   const size_t param_bytes_warp = (KINC_GMM_PARAMS_SMEM && kern.clus == 1 && kern.ks > 0)
+                                      ? (size_t)7 * kern.ks * TILE * sizeof(float) : 0;
+   const int smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * WARPS_PER_BLOCK <= 160 * 1024;
+   const int smem_bytes = (int)((smem_sort ? sort_bytes_warp : 0) + param_bytes_warp) * WARPS_PER_BLOCK;
    if ( smem_bytes > 48 * 1024 )
       CK(cudaFuncSetAttribute(kern.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
 

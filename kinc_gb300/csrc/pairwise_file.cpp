@@ -390,12 +390,13 @@ extern "C" int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, co
    const int64_t pair0 = first_block * KINC_SIM_WORK_BLOCK_SIZE;
    const int64_t pair1 = std::min<int64_t>(total, last_block * KINC_SIM_WORK_BLOCK_SIZE);
    const int maxK = p.max_clusters;
+   const int ncorr = p.corr_method == 2 ? 2 : 1;
    const bool want_ccm = ccm_path != nullptr && p.clus_method != 0;
    kinc_pm* ccm = nullptr;
    kinc_pm* cmx = nullptr;
    int rc = KINC_SIM_OK;
    if ( ccm_path && (rc = kinc_pm_create(ccm_path, KINC_PM_CCM, G, maxK, S, little_endian, &ccm)) ) return rc;
-   if ( cmx_path && (rc = kinc_pm_create(cmx_path, KINC_PM_CMX, G, maxK, 1, little_endian, &cmx)) )
+   if ( cmx_path && (rc = kinc_pm_create(cmx_path, KINC_PM_CMX, G, maxK, ncorr, little_endian, &cmx)) )
    {
       if ( ccm ) kinc_pm_close(ccm);
       return rc;
@@ -419,7 +420,7 @@ extern "C" int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, co
    uint64_t* hCount = nullptr;
    bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
    ok = ok && cudaMalloc(&dK, Bn) == cudaSuccess;
-   ok = ok && cudaMalloc(&dC, (size_t)Bn * maxK * sizeof(float)) == cudaSuccess;
+   ok = ok && cudaMalloc(&dC, (size_t)Bn * maxK * ncorr * sizeof(float)) == cudaSuccess;
    ok = ok && (!want_ccm || cudaMalloc(&dL, (size_t)Bn * S) == cudaSuccess);
    ok = ok && cudaMalloc(&dCount, 2 * sizeof(uint64_t)) == cudaSuccess;
    ok = ok && cudaMallocHost(&hCount, 2 * sizeof(uint64_t)) == cudaSuccess;
@@ -430,10 +431,10 @@ extern "C" int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, co
       dCx = dCy = dMx = dMy = nullptr; dCc = dMc = nullptr; dCr = nullptr; dMp = nullptr;
       hx = hy = nullptr; hc = nullptr; hp = nullptr;
       bool good = cudaMalloc(&dCx, n * 4) == cudaSuccess && cudaMalloc(&dCy, n * 4) == cudaSuccess
-                  && cudaMalloc(&dCc, n) == cudaSuccess && cudaMalloc(&dCr, n * 4) == cudaSuccess
+                  && cudaMalloc(&dCc, n) == cudaSuccess && cudaMalloc(&dCr, n * 4 * ncorr) == cudaSuccess
                   && cudaMallocHost(&hx, n * 4) == cudaSuccess && cudaMallocHost(&hy, n * 4) == cudaSuccess
                   && cudaMallocHost(&hc, n) == cudaSuccess
-                  && cudaMallocHost(&hp, (size_t)n * std::max<int>(nbytes, 4)) == cudaSuccess;
+                  && cudaMallocHost(&hp, (size_t)n * std::max<int>(nbytes, 4 * ncorr)) == cudaSuccess;
       if ( good && want_ccm )
          good = cudaMalloc(&dMx, n * 4) == cudaSuccess && cudaMalloc(&dMy, n * 4) == cudaSuccess
                 && cudaMalloc(&dMc, n) == cudaSuccess && cudaMalloc(&dMp, (size_t)n * nbytes) == cudaSuccess;
@@ -482,7 +483,7 @@ extern "C" int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, co
          bool good = cudaMemcpyAsync(hx, dCx, n_cmx * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
                      && cudaMemcpyAsync(hy, dCy, n_cmx * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
                      && cudaMemcpyAsync(hc, dCc, n_cmx, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                     && cudaMemcpyAsync(hp, dCr, n_cmx * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                     && cudaMemcpyAsync(hp, dCr, n_cmx * 4 * ncorr, cudaMemcpyDeviceToHost, st) == cudaSuccess
                      && cudaStreamSynchronize(st) == cudaSuccess;
          if ( !good ) { rc = pm_fail(KINC_SIM_ECUDA, "copy of CMX items failed"); break; }
          if ( (rc = kinc_pm_write_items(cmx, n_cmx, hx, hy, hc, hp)) ) break;

@@ -44,6 +44,17 @@ constexpr int SAMPLE_UNROLL = KINC_SAMPLE_UNROLL;   /* unroll factor of the EM s
 #ifndef KINC_STATIC_K
 #define KINC_STATIC_K 1             /* 1: one compiled fit per K (K known to the compiler); 0: one fit for all K <= KS */
 #endif
+#ifndef KINC_GMM_PARAMS_SMEM
+#define KINC_GMM_PARAMS_SMEM 0      /* 1: GMM component parameters live in shared memory, read per use */
+#endif
+#ifndef KINC_PARAMS_VOLATILE
+#define KINC_PARAMS_VOLATILE 0
+#endif
+#if KINC_PARAMS_VOLATILE
+#define PARAM_QUAL volatile
+#else
+#define PARAM_QUAL
+#endif
 #ifndef KINC_STORE_GAMMA
 #define KINC_STORE_GAMMA 0          /* 1: keep the M1 responsibilities for M2 instead of recomputing them */
 #endif
@@ -66,6 +77,7 @@ struct DevParams
    int32_t P2;                      /* next power of two >= max(S, 2) */
    int32_t sort_floats;             /* floats of sort buffer per warp */
    int32_t gam_k;                   /* components per sample in DevScratch::gam (0: none) */
+   int32_t ncorr;                   /* correlations per cluster: 1, or 2 for Pearson and Spearman */
 };
 
 struct DevData
@@ -366,6 +378,23 @@ __device__ inline float warp_spearman(const DevParams& P, const DevData& D, cons
 
 /* ------------------------------------------------------ lane-local fits */
 
+/* A lane's per-component parameter array: registers, or (SMEM) a lane-strided
+ * shared-memory column read at every use, which frees the registers for more
+ * resident warps. */
+template <int KA, bool SMEM> struct ParamArr;
+template <int KA> struct ParamArr<KA, false>
+{
+   float v[KA];
+   __device__ __forceinline__ ParamArr(float*, int) {}
+   __device__ __forceinline__ float& operator[](int k) { return v[k]; }
+};
+template <int KA> struct ParamArr<KA, true>
+{
+   PARAM_QUAL float* p;
+   __device__ __forceinline__ ParamArr(float* base, int which) : p(base + which * KA * TILE) {}
+   __device__ __forceinline__ PARAM_QUAL float& operator[](int k) { return p[k * TILE]; }
+};
+
 __device__ __forceinline__ float log_mvn(float x0, float x1, float m0, float m1, float a, float b, float c,
                                          float nrm)
 {
@@ -407,7 +436,7 @@ __device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, dou
  */
 template <int KT>
 __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int N, int Kr, LaneRng& rng,
-                        double c2, float& out_logL, float& out_E, unsigned long long& units)
+                        double c2, float& out_logL, float& out_E, unsigned long long& units, float* pbuf)
 {
    const int K = (KINC_STATIC_K && KT > 0) ? KT : Kr;
    /* KT > 0: up to KT components in registers (K <= KT at run time);
@@ -418,7 +447,8 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
    constexpr int UF = KT > 0 ? KT : 1;
    constexpr bool STORE_G = KT > 0 && KINC_STORE_GAMMA;
    constexpr int SU = (KT > 0 && KT <= KINC_UNROLL_SMALL_K) ? 2 : SAMPLE_UNROLL;
-   float m0[KA], m1[KA], ia[KA], ib[KA], ic[KA], nrm[KA], logpi[KA];
+   constexpr bool PS = KINC_GMM_PARAMS_SMEM && KT > 0;
+   ParamArr<KA, PS> m0(pbuf, 0), m1(pbuf, 1), ia(pbuf, 2), ib(pbuf, 3), ic(pbuf, 4), nrm(pbuf, 5), logpi(pbuf, 6);
 
    if ( rng.mode == 1 ) rng.lcg = 1;
    {

@@ -79,12 +79,20 @@ __device__ inline float lane_pearson(const DevParams& P, const DevData& D, const
             ++n;
          }
       }
-      int32_t c = B.pg[p - B.lo];
+      /* links point strictly backwards inside the block's span [0, p - lo); anything else ends
+       * the walk (defensive: the links are always written before this kernel runs) */
+      const int32_t self = (int32_t)(p - B.lo);
+      int32_t c = B.pg[self];
+      if ( c >= self ) c = -1;
       PackedCursor cur;
       for ( int i = N; i < P.S; ++i )
       {
          if ( lbl[i * TILE] != k ) continue;
-         while ( c >= 0 && B.N[c] <= i ) c = B.pg[c];
+         while ( c >= 0 && B.N[c] <= i )
+         {
+            const int32_t nxt = B.pg[c];
+            c = nxt < c ? nxt : -1;
+         }
          const float2 v = c >= 0 ? cur.at(P, D, B.lo + c, i) : make_float2(0.f, 0.f);
          sumx += v.x; sumy += v.y; sumx2 += v.x * v.x; sumy2 += v.y * v.y; sumxy += v.x * v.y;
          ++n;
@@ -126,11 +134,12 @@ __device__ __forceinline__ float criterion_value(const DevParams& P, const DevDa
 template <int CLUS, int KT>
 __device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, float* lpx, float* gam,
                                          int8_t*& wl, int8_t*& ya, int8_t*& yb, int8_t*& yc, int N, int K,
-                                         LaneRng& rng, float& logL, float& E, unsigned long long& units)
+                                         LaneRng& rng, float& logL, float& E, unsigned long long& units,
+                                         float* pbuf)
 {
    if ( CLUS == 1 )
    {
-      return gmm_fit<KT>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units);
+      return gmm_fit<KT>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units, pbuf);
    }
    logL = kmeans_fit<KT>(X, ya, yb, yc, N, K, rng, units);
    E = 0.f;
@@ -144,7 +153,7 @@ __device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, fl
  * passes, for this lane's pair; labels merged into lbl. */
 template <int CLUS, int KS>
 __device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* X, float* lpx, float* gam,
-                            int8_t* wl,
+                            float* pbuf, int8_t* wl,
                             int8_t* ya, int8_t* yb, int8_t* yc, int8_t* lbl, int N, LaneRng& rng,
                             unsigned long long& units, unsigned long long& fits)
 {
@@ -156,12 +165,12 @@ __device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* 
       float logL = 0.f, E = 0.f;
       bool ok;
       if ( !KINC_STATIC_K || KS == 0 )
-         ok = lane_fit<CLUS, KS>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
-      else if ( K == 1 ) ok = lane_fit<CLUS, 1>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
-      else if ( K == 2 ) ok = lane_fit<CLUS, 2>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
-      else if ( K == 3 || KS < 4 ) ok = lane_fit<CLUS, 3>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
-      else if ( K == 4 ) ok = lane_fit<CLUS, 4>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
-      else ok = lane_fit<CLUS, 5>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units);
+         ok = lane_fit<CLUS, KS>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+      else if ( K == 1 ) ok = lane_fit<CLUS, 1>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+      else if ( K == 2 ) ok = lane_fit<CLUS, 2>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+      else if ( K == 3 || KS < 4 ) ok = lane_fit<CLUS, 3>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+      else if ( K == 4 ) ok = lane_fit<CLUS, 4>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+      else ok = lane_fit<CLUS, 5>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
       ++fits;
       if ( !ok ) continue;
       const float value = criterion_value(P, D, K, logL, N, E);
@@ -202,6 +211,10 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
    int8_t* yc = W.yc + slot * col;
    uint32_t* ring = W.rng + slot * (size_t)(RNG_WORDS * TILE);
    float* sbuf = smem_sort ? smem + (size_t)warp * P.sort_floats : W.sortbuf + slot * (size_t)P.sort_floats;
+   /* GMM parameters in shared memory (KINC_GMM_PARAMS_SMEM): 7 arrays of KS x 32 floats per warp */
+   float* pbuf = (CLUS == 1 && KINC_GMM_PARAMS_SMEM && KS > 0)
+                    ? smem + (smem_sort ? (size_t)WARPS_PER_BLOCK * P.sort_floats : 0) + (size_t)warp * 7 * KS * TILE
+                    : nullptr;
 
    const int64_t ntiles = (B.size + TILE - 1) / TILE;
    for ( ;; )
@@ -258,7 +271,8 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
             rng.head = 0;
             rng.mode = P.rand_mode;
             rng.lcg = 1;
-            K = lane_cluster<CLUS, KS>(P, D, X + lane, lpx + lane, gam ? gam + lane : nullptr, wl + lane,
+            K = lane_cluster<CLUS, KS>(P, D, X + lane, lpx + lane, gam ? gam + lane : nullptr,
+                                       pbuf ? pbuf + lane : nullptr, wl + lane,
                                        ya + lane, yb + lane, yc + lane, lbl + lane, myN, rng, units, fits);
          }
          for ( int o = 16; o > 0; o >>= 1 )
@@ -292,33 +306,36 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
          }
       }
 
-      /* ---- correlations */
-      if ( P.corr == 0 )
+      /* ---- correlations: row [k][c], c = 0 the method asked for (or Pearson when both),
+       * c = 1 Spearman when both are asked for */
+      const int nc = P.ncorr;
+      if ( P.corr == 0 || P.corr == 2 )
       {
          if ( lane < npairs && B.outCorr )
          {
-            float* corr_row = B.outCorr + (myp - B.start) * P.max_k;
+            float* corr_row = B.outCorr + (myp - B.start) * P.max_k * nc;
             for ( int k = 0; k < P.max_k; ++k )
             {
-               corr_row[k] = k < K ? lane_pearson(P, D, B, X + lane, lbl + lane, myp, mx, my, myN, (int8_t)k)
-                                   : __int_as_float(0x7fc00000);
+               corr_row[k * nc] = k < K ? lane_pearson(P, D, B, X + lane, lbl + lane, myp, mx, my, myN, (int8_t)k)
+                                        : __int_as_float(0x7fc00000);
             }
          }
       }
-      else
+      if ( P.corr == 1 || P.corr == 2 )
       {
+         const int c = P.corr == 2 ? 1 : 0;
          for ( int j = 0; j < npairs; ++j )
          {
             const int Kj = __shfl_sync(0xffffffffu, K, j);
             const int xj = __shfl_sync(0xffffffffu, mx, j);
             const int yj = __shfl_sync(0xffffffffu, my, j);
             const int64_t pj = __shfl_sync(0xffffffffu, myp, j);
-            float* row = B.outCorr ? B.outCorr + (pj - B.start) * P.max_k : nullptr;
+            float* row = B.outCorr ? B.outCorr + (pj - B.start) * P.max_k * nc : nullptr;
             for ( int k = 0; k < P.max_k; ++k )
             {
                float r = __int_as_float(0x7fc00000);
                if ( k < Kj ) r = warp_spearman(P, D, X, lbl, xj, yj, (int8_t)k, sbuf, j, lane);
-               if ( lane == 0 && row ) row[k] = r;
+               if ( lane == 0 && row ) row[k * nc + c] = r;
             }
          }
       }

@@ -17,7 +17,7 @@ import numpy as np
 from . import _native
 
 CLUSTERING_NAMES = ["none", "gmm", "kmeans"]
-CORRELATION_NAMES = ["pearson", "spearman"]
+CORRELATION_NAMES = ["pearson", "spearman", "both"]
 CRITERION_NAMES = ["BIC", "ICL"]
 SEMANTICS_NAMES = ["reference", "fixed"]
 RAND_NAMES = ["glibc", "lcg"]
@@ -41,7 +41,7 @@ class ResultBlock:
     start: int
     K: np.ndarray          # int8 [size]
     labels: np.ndarray     # int8 [size, samples]
-    corr: np.ndarray       # float32 [size, maxclus]
+    corr: np.ndarray       # float32 [size, maxclus] ([size, maxclus, 2] with corrmethod both)
 
 
 def _choice(value, names, what):
@@ -192,7 +192,7 @@ class Similarity:
         S, maxk = self.samples, self.params.max_clusters
         K = np.empty(size, np.int8)
         labels = np.empty((size, S), np.int8)
-        corr = np.empty((size, maxk), np.float32)
+        corr = np.empty((size, maxk, 2) if self.params.corr_method == 2 else (size, maxk), np.float32)
         rc = _native.load().kinc_sim_execute_block(self._ctx, start, size, K.ctypes.data_as(ctypes.c_void_p),
                                                    labels.ctypes.data_as(ctypes.c_void_p),
                                                    corr.ctypes.data_as(ctypes.c_void_p))
@@ -204,9 +204,10 @@ class Similarity:
         L = _native.load()
         size = len(result.K)
         S, maxk = self.samples, self.params.max_clusters
+        nc = 2 if self.params.corr_method == 2 else 1
         cap = max(1, size * maxk)
         cx, cy, cc, cr = (np.empty(cap, np.int32), np.empty(cap, np.int32), np.empty(cap, np.int8),
-                          np.empty(cap, np.float32))
+                          np.empty((cap, nc), np.float32))
         mx, my, mc = np.empty(cap, np.int32), np.empty(cap, np.int32), np.empty(cap, np.int8)
         codes = np.empty((cap, S), np.int8)
         n_cmx, n_ccm = ctypes.c_int64(0), ctypes.c_int64(0)
@@ -215,7 +216,8 @@ class Similarity:
                                       vp(result.corr), vp(cx), vp(cy), vp(cc), vp(cr), cap, ctypes.byref(n_cmx),
                                       vp(mx), vp(my), vp(mc), vp(codes), cap, ctypes.byref(n_ccm))
         _native.check(rc, self._ctx)
-        self._append(self.cmx, cx[:n_cmx.value], cy[:n_cmx.value], cc[:n_cmx.value], list(cr[:n_cmx.value]))
+        self._append(self.cmx, cx[:n_cmx.value], cy[:n_cmx.value], cc[:n_cmx.value],
+                     list(cr[:n_cmx.value, 0]) if nc == 1 else [tuple(r) for r in cr[:n_cmx.value]])
         self._append(self.ccm, mx[:n_ccm.value], my[:n_ccm.value], mc[:n_ccm.value],
                      [codes[i] for i in range(n_ccm.value)])
 

@@ -48,3 +48,21 @@ def test_gpu_matches_oracle(case):
     assert np.array_equal(res.labels[multi], labels[multi])
     diff = np.abs(np.nan_to_num(res.corr, nan=9.0) - np.nan_to_num(corr, nan=9.0))
     assert _corr_equal(res.corr, corr), f"max |dr| {diff.max()} on {(diff > 0).sum()} entries"
+
+
+@pytest.mark.parametrize("clus", ["gmm", "kmeans", "none"])
+def test_both_correlations_equal_single_method_runs(clus):
+    """corrmethod both: column 0 equals the Pearson run, column 1 the Spearman run, bit for bit."""
+    gem = synthetic.generate(5, genes=50, samples=90)
+    args = dict(clusmethod=clus, crit="ICL", preout=True, postout=True, maxclus=4)
+    runs = {}
+    for method in ("pearson", "spearman", "both"):
+        sim = Similarity(gem, corrmethod=method, **args)
+        sim.initialize()
+        runs[method] = sim.execute(None, start=0, size=sim.total_pairs())
+        sim.close()
+    both = runs["both"]
+    assert both.corr.shape[-1] == 2
+    assert np.array_equal(both.K, runs["pearson"].K)
+    assert _corr_equal(both.corr[..., 0], runs["pearson"].corr)
+    assert _corr_equal(both.corr[..., 1], runs["spearman"].corr)
