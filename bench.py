@@ -4,10 +4,11 @@ Workload (the headline configuration): expression matrix 5,000 genes x 1,000
 samples float32, 10% NaN, 10 planted mixture modules (kinc_gb300.synthetic
 workload 2); clusmethod gmm, minclus 1, maxclus 5, crit BIC, preout + postout,
 minsamp 30, corrmethod spearman.  A "step" is one device block of pairs
-(--block, default 131,072 = 4 of KINC's 32,768-pair work blocks) taken in
+(--block, default 1,048,576 = 32 of KINC's 32,768-pair work blocks) taken in
 pair order; warm-up and timed steps walk consecutive blocks, so every timed
 pair is distinct.  Under torchrun every rank takes its own disjoint range of
-blocks (weak scaling, no collective on the data path).
+blocks (weak scaling, no collective on the data path); the ranges wrap around
+the 12,497,500 pairs only when ranks x steps x block exceed them.
 
 Lines printed by rank 0 (one JSON object):
   value    pairs/s with the matrix already resident in HBM, timed with CUDA
@@ -101,9 +102,10 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_sample(gem, threads, pairs_per_thread, seed):
+def cpu_sample(gem, threads, pairs_per_thread, seed, outputs=False):
     """Time the oracle on `threads` segments of consecutive pairs, each starting
-    at a seeded random work-block boundary; returns (pairs/s, pairs, seconds)."""
+    at a seeded random work-block boundary; returns (pairs/s, pairs, seconds),
+    plus (starts, sizes, (K, labels, corr)) when `outputs` is set."""
     from oracle import pyoracle
     G = gem.shape[0]
     total = G * (G - 1) // 2
@@ -113,8 +115,33 @@ def cpu_sample(gem, threads, pairs_per_thread, seed):
     starts = blocks.astype(np.int64) * 32768
     sizes = np.full(threads, pairs_per_thread, np.int64)
     p = pyoracle.params(**ORACLE_ARGS)
-    done, secs = pyoracle.run_segments_parallel(gem, p, starts, sizes, threads)
-    return done / secs, int(done), secs
+    if not outputs:
+        done, secs = pyoracle.run_segments_parallel(gem, p, starts, sizes, threads)
+        return done / secs, int(done), secs
+    done, secs, res = pyoracle.run_segments_parallel(gem, p, starts, sizes, threads, outputs=True)
+    return done / secs, int(done), secs, starts, sizes, res
+
+
+def parity_block(gpu, cpu):
+    """Agreement of the GPU results with the oracle's on the same pairs: K, the
+    sample label strings of pairs with K > 1, and the correlations of k < K."""
+    Kg, Lg, Cg = gpu
+    Kc, Lc, Cc = cpu
+    same_k = Kg == Kc
+    rows = same_k & (Kc > 1)
+    labels_eq = np.all(Lg[rows] == Lc[rows], axis=1) if rows.any() else np.ones(0, bool)
+    mask = (np.arange(Cc.shape[1])[None, :] < Kc[:, None]) & same_k[:, None]
+    a, b = Cg[mask], Cc[mask]
+    nan_a, nan_b = np.isnan(a), np.isnan(b)
+    both = ~nan_a & ~nan_b
+    dr = float(np.max(np.abs(a[both] - b[both]))) if both.any() else 0.0
+    return {"pairs": int(len(Kc)), "k_agreement": float(same_k.mean()),
+            "label_agreement": float(labels_eq.mean()) if len(labels_eq) else 1.0,
+            "label_rows": int(rows.sum()), "correlations": int(mask.sum()),
+            "nan_mismatches": int((nan_a != nan_b).sum()), "max_abs_dr": dr,
+            "bit_exact": bool(np.array_equal(Kg, Kc) and (not rows.any() or labels_eq.all())
+                              and np.array_equal(a.view(np.uint32), b.view(np.uint32))),
+            "vs": "oracle: C restatement of KINC's serial path, pinned bit-exact to KINC's compiled Pairwise code"}
 
 
 def run_reference(args, gem):
@@ -277,12 +304,59 @@ def kmeans_leg(L, vp, cpu=True):
         rng = np.random.default_rng(11)
         starts = rng.choice((total - 1) // 32768, size=threads, replace=False).astype(np.int64) * 32768
         p = pyoracle.params(clus_method=2, corr_method=0, min_clusters=1, max_clusters=3, criterion=0, min_samples=30)
-        done, secs = pyoracle.run_segments_parallel(gem, p, starts, np.full(threads, 6, np.int64), threads)
+        sizes = np.full(threads, 6, np.int64)
+        done, secs, ref = pyoracle.run_segments_parallel(gem, p, starts, sizes, threads, outputs=True)
         out["cpu_baseline"] = {"value": done / secs, "unit": "pairs/s", "cores": threads, "kind": "port",
                                "sample": f"{done} pairs: {threads} threads x 6 consecutive pairs from seeded "
                                          f"random work blocks, {secs:.1f} s"}
         out["gpu_over_cpu"] = out["pairs_per_s"] / out["cpu_baseline"]["value"]
+        chk = Similarity(gem, **args)
+        parts = [chk.execute(None, int(a), int(b)) for a, b in zip(starts, sizes)]
+        chk.close()
+        out["parity"] = parity_block((np.concatenate([r.K for r in parts]), np.concatenate([r.labels for r in parts]),
+                                      np.concatenate([r.corr for r in parts])), ref)
     return out
+
+
+def stream_leg(device_block, nblk):
+    """The large streamed run (kinc_gb300.synthetic workload 5: GEM 30,000 x 500, 8% NaN, 5% planted
+    2-4 component mixture pairs; GMM k <= 5, ICL, pre+post outliers, Pearson and Spearman per cluster)
+    end to end through kinc_sim_run_to_files_ex: `nblk` device blocks of `device_block` pairs from the
+    middle of the 449,985,000 pairs, computed, filtered and compacted on the GPU, kept items streamed
+    back through pinned buffers and written as CCM/CMX files.  Wall clock of the whole call."""
+    import shutil
+    import tempfile
+
+    from kinc_gb300 import Similarity, synthetic
+    gem = synthetic.generate(5)
+    G, S = gem.shape
+    sim = Similarity(gem, clusmethod="gmm", corrmethod="both", minclus=1, maxclus=5, crit="ICL", preout=True,
+                     postout=True, minsamp=30, mincorr=0.5, maxcorr=1.0)
+    sim.initialize()
+    wb_per_dev = device_block // 32768
+    first = (sim.size() // 2) // wb_per_dev * wb_per_dev
+    pairs = min(sim.total_pairs(), (first + nblk * wb_per_dev) * 32768) - first * 32768
+    tmp = tempfile.mkdtemp(prefix="kinc_stream_")
+    try:
+        ccm, cmx = os.path.join(tmp, "out.ccm"), os.path.join(tmp, "out.cmx")
+        t0 = time.perf_counter()
+        sim.run(ccm_path=ccm, cmx_path=cmx, first_block=first, nblocks=nblk * wb_per_dev, device_block=device_block)
+        secs = time.perf_counter() - t0
+        ccm_bytes, cmx_bytes = os.path.getsize(ccm), os.path.getsize(cmx)
+        items_cmx = (cmx_bytes - 31) // (9 + 8)
+        items_ccm = (ccm_bytes - 34) // (9 + (S + 1) // 2)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+        sim.close()
+    rate = pairs / secs
+    return {"workload": "GMM k<=5 (ICL) + pre/post outliers + Pearson and Spearman per cluster, GEM 30000x500 "
+                        "float32, 8% NaN, 5% planted 2-4 component mixture pairs, minsamp 30, mincorr 0.5",
+            "pairs": int(pairs), "first_pair": int(first * 32768), "device_block": device_block,
+            "device_blocks": nblk, "seconds": secs, "pairs_per_s": rate,
+            "cmx_items": int(items_cmx), "ccm_items": int(items_ccm), "bytes_written": int(ccm_bytes + cmx_bytes),
+            "projected_full_run_s": sim.total_pairs() / rate,
+            "includes": "kinc_sim_run_to_files_ex: compute, device-side process(), pinned D2H of kept items "
+                        "overlapped with the next block, CCM/CMX file writes"}
 
 
 def config_dict(args, gem):
@@ -300,14 +374,16 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--block", type=int, default=131072)
+    ap.add_argument("--block", type=int, default=1048576)
     ap.add_argument("--ref-pairs-per-thread", type=int, default=24)
-    ap.add_argument("--cpu-pairs-per-thread", type=int, default=64)
+    ap.add_argument("--cpu-pairs-per-thread", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-dense", action="store_true")
     ap.add_argument("--no-kmeans", action="store_true")
     ap.add_argument("--dense-check-pairs", type=int, default=1000000)
+    ap.add_argument("--stream-blocks", type=int, default=2,
+                    help="device blocks of 2^22 pairs in the streamed 30000x500 leg (0 = skip)")
     args = ap.parse_args()
 
     from kinc_gb300 import synthetic
@@ -336,10 +412,14 @@ def main():
     total = G * (G - 1) // 2
     B = args.block
     nsteps = args.warmup + args.steps
-    per_rank = nsteps * B
-    if per_rank * world > total:
-        raise SystemExit(f"{world} ranks x {nsteps} steps x {B} pairs exceeds the {total} pairs of the workload")
-    base = rank * per_rank
+    nfull = total // B
+    if nfull < 1:
+        raise SystemExit(f"--block {B} exceeds the {total} pairs of the workload")
+
+    def block_start(i):
+        """Rank-disjoint consecutive device blocks; ranges wrap around the workload
+        only when ranks x steps x block exceed its pairs."""
+        return ((rank * nsteps + i) % nfull) * B
 
     sim = Similarity(gem, **sim_args)
     sim.initialize()
@@ -354,7 +434,7 @@ def main():
 
     def step(i):
         flush.zero_()
-        rc = L.kinc_sim_execute_block_device(ctx, base + i * B, B, vp(dK.data_ptr()), vp(dL.data_ptr()),
+        rc = L.kinc_sim_execute_block_device(ctx, block_start(i), B, vp(dK.data_ptr()), vp(dL.data_ptr()),
                                              vp(dC.data_ptr()), vp(stream.cuda_stream))
         _native.check(rc, ctx)
         return L.kinc_sim_last_launch_count(ctx)
@@ -399,7 +479,6 @@ def main():
         hC = torch.empty((B, maxk), dtype=torch.float32, pin_memory=True)
         gem_pinned = torch.from_numpy(gem).pin_memory()
         e2e_steps = max(1, min(args.steps, 3))
-        e2e_base = base + args.warmup * B
         params = _native.SimParams()
         params_src = Similarity(gem, **sim_args).params
         ctypes.memmove(ctypes.byref(params), ctypes.byref(params_src), ctypes.sizeof(params))
@@ -410,7 +489,7 @@ def main():
         c2 = ctypes.c_void_p()
         _native.check(L.kinc_sim_create(vp(gem_pinned.data_ptr()), G, S, ctypes.byref(params), ctypes.byref(c2)))
         for i in range(e2e_steps):
-            rc = L.kinc_sim_execute_block(c2, e2e_base + i * B, B, vp(hK.data_ptr()), vp(hL.data_ptr()),
+            rc = L.kinc_sim_execute_block(c2, block_start(args.warmup + i), B, vp(hK.data_ptr()), vp(hL.data_ptr()),
                                           vp(hC.data_ptr()))
             _native.check(rc, c2)
         L.kinc_sim_destroy(c2)
@@ -453,20 +532,30 @@ def main():
 
     tensor_core = None if args.no_dense else dense_leg(L, vp, args.dense_check_pairs)
     kmeans = None if args.no_kmeans else kmeans_leg(L, vp, cpu=not args.no_cpu)
+    streamed = None if args.stream_blocks <= 0 else stream_leg(1 << 22, args.stream_blocks)
 
     cpu = None
+    parity = None
     if not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, n, s = cpu_sample(gem, threads, args.cpu_pairs_per_thread, seed=7)
+        v, n, s, starts, sizes, ref = cpu_sample(gem, threads, args.cpu_pairs_per_thread, seed=7, outputs=True)
         cpu = {"value": v, "unit": "pairs/s", "cores": threads, "kind": "port",
                "sample": f"{n} pairs: {threads} threads x {args.cpu_pairs_per_thread} consecutive pairs from "
                          f"seeded random work blocks, {s:.1f} s"}
+        # the same pairs on the GPU, through the host-buffer entry point
+        chk = Similarity(gem, **sim_args)
+        parts = [chk.execute(None, int(a), int(b)) for a, b in zip(starts, sizes)]
+        chk.close()
+        gpu = (np.concatenate([r.K for r in parts]), np.concatenate([r.labels for r in parts]),
+               np.concatenate([r.corr for r in parts]))
+        parity = parity_block(gpu, ref)
 
     line = {"metric": "gene pairs/sec", "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded; no public dataset)",
             "config": config_dict(args, gem), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
-            "cpu_baseline": cpu, "clocks": clk, "tensor_core": tensor_core, "kmeans_uneven": kmeans}
+            "cpu_baseline": cpu, "parity": parity, "clocks": clk, "tensor_core": tensor_core, "kmeans_uneven": kmeans,
+            "streamed_30000x500": streamed}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

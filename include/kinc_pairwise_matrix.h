@@ -84,6 +84,16 @@ const char* kinc_pm_last_error(void);
 int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, const char* cmx_path, int32_t little_endian,
                           int64_t first_block, int64_t nblocks);
 
+/*
+ * The same with the device block size chosen by the caller: device_block pairs
+ * (rounded down to whole work blocks; 0 = kinc_sim_max_device_block).  Both
+ * forms run two result slots, so the GPU computes device block b while block
+ * b-1's kept items come back through pinned buffers on a second stream and
+ * are written.
+ */
+int kinc_sim_run_to_files_ex(kinc_sim_ctx* ctx, const char* ccm_path, const char* cmx_path, int32_t little_endian,
+                             int64_t first_block, int64_t nblocks, int64_t device_block);
+
 #ifdef __cplusplus
 }
 #endif

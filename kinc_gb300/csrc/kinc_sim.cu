@@ -16,6 +16,7 @@
  * (src/core/similarity_opencl.cpp:34-70, src/core/similarity_opencl_worker.cpp:50-271).
  */
 #include "../../include/kinc_sim.h"
+#include "sim_internal.h"
 #include "sim_kernel.cuh"
 #include "pearson_tc.h"
 
@@ -594,9 +595,10 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    /* GMM parameters in shared memory take the room the sort buffers would use */
    const size_t param_bytes_warp = (KINC_GMM_PARAMS_SMEM && ctx->kern.clus == 1 && ctx->kern.ks > 0)
                                       ? (size_t)7 * ctx->kern.ks * TILE * sizeof(float) : 0;
-   ctx->smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * WARPS_PER_BLOCK <= 160 * 1024;
+   ctx->smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * WARPS_PER_BLOCK <= 200 * 1024;
    ctx->smem_bytes = (int)((ctx->smem_sort ? sort_bytes_warp : 0) + param_bytes_warp) * WARPS_PER_BLOCK;
-   if ( ctx->smem_bytes > 48 * 1024 )
+   /* opt in whenever dynamic shared memory is used: the kernel's own static words count against 48 KB too */
+   if ( ctx->smem_bytes > 0 )
       CKC(cudaFuncSetAttribute(ctx->kern.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_bytes));
    int per_sm = 0;
    CKC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ctx->kern.fn, WARPS_PER_BLOCK * 32,
@@ -651,7 +653,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
 
    /* one device block of pairs (the tensor-core form writes no labels, so its blocks can be far larger) */
    const int64_t total = (int64_t)genes * (genes - 1) / 2;
-   int64_t mb = 1 << 20;
+   int64_t mb = (int64_t)1 << 22;
    while ( mb > 4096 && (size_t)mb * S > ((size_t)1 << 31) ) mb >>= 1;
    if ( params->precision != 0 ) mb = (int64_t)1 << 27;
    ctx->max_block = std::min<int64_t>(mb, std::max<int64_t>(total, 1));
@@ -803,6 +805,14 @@ static int check_range(kinc_sim_ctx* ctx, int64_t start, int64_t size)
    if ( start < 0 || size < 0 || start + size > total )
       return fail(ctx, KINC_SIM_EINVAL, "pair range [%lld, %lld) outside [0, %lld)", (long long)start,
                   (long long)(start + size), (long long)total);
+   return KINC_SIM_OK;
+}
+
+int kinc_sim_status_copy_async(kinc_sim_ctx* ctx, uint64_t* dst, cudaStream_t stream)
+{
+   if ( !ctx || !dst ) return KINC_SIM_EINVAL;
+   CK(cudaMemsetAsync(dst, 0, sizeof(uint64_t), stream));
+   CK(cudaMemcpyAsync(dst, ctx->d_status, sizeof(int), cudaMemcpyDeviceToDevice, stream));
    return KINC_SIM_OK;
 }
 
@@ -1169,7 +1179,7 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
                                       ? (size_t)7 * kern.ks * TILE * sizeof(float) : 0;
    const int smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * WARPS_PER_BLOCK <= 160 * 1024;
    const int smem_bytes = (int)((smem_sort ? sort_bytes_warp : 0) + param_bytes_warp) * WARPS_PER_BLOCK;
-   if ( smem_bytes > 48 * 1024 )
+   if ( smem_bytes > 0 )
       CK(cudaFuncSetAttribute(kern.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
 
    /* carve the static array: fixed parts first, then as many warp slots as fit */

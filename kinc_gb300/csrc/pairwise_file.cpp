@@ -8,6 +8,7 @@
  * ExpressionMatrix's data section (src/core/expressionmatrix.cpp:21-37).
  */
 #include "../../include/kinc_pairwise_matrix.h"
+#include "sim_internal.h"
 
 #include <cuda_runtime.h>
 
@@ -377,8 +378,80 @@ extern "C" int kinc_emx_read(const char* path, int32_t little_endian, float* gem
    return KINC_SIM_OK;
 }
 
+namespace {
+
+/* One of the runner's two result slots: a device block's results, its compacted
+ * items on the device and their pinned host copies. */
+struct RunSlot
+{
+   int8_t* dK = nullptr;
+   int8_t* dL = nullptr;
+   float* dC = nullptr;
+   int32_t *dCx = nullptr, *dCy = nullptr, *dMx = nullptr, *dMy = nullptr;
+   int8_t *dCc = nullptr, *dMc = nullptr;
+   float* dCr = nullptr;
+   uint8_t* dMp = nullptr;
+   int32_t *hCx = nullptr, *hCy = nullptr, *hMx = nullptr, *hMy = nullptr;
+   int8_t *hCc = nullptr, *hMc = nullptr;
+   float* hCr = nullptr;
+   uint8_t* hMp = nullptr;
+   uint64_t* dCount = nullptr;
+   uint64_t* hCount = nullptr;   /* [0] CMX items, [1] CCM items, [2] kernel status */
+   cudaEvent_t counted = nullptr;
+   int64_t cap = 0, start = 0, size = 0;
+
+   void free_items()
+   {
+      cudaFree(dCx); cudaFree(dCy); cudaFree(dCc); cudaFree(dCr);
+      cudaFree(dMx); cudaFree(dMy); cudaFree(dMc); cudaFree(dMp);
+      cudaFreeHost(hCx); cudaFreeHost(hCy); cudaFreeHost(hCc); cudaFreeHost(hCr);
+      cudaFreeHost(hMx); cudaFreeHost(hMy); cudaFreeHost(hMc); cudaFreeHost(hMp);
+      dCx = dCy = dMx = dMy = hCx = hCy = hMx = hMy = nullptr;
+      dCc = dMc = hCc = hMc = nullptr;
+      dCr = hCr = nullptr;
+      dMp = hMp = nullptr;
+      cap = 0;
+   }
+
+   bool alloc_items(int64_t n, int ncorr, bool ccm, int nbytes)
+   {
+      free_items();
+      bool ok = cudaMalloc(&dCx, n * 4) == cudaSuccess && cudaMalloc(&dCy, n * 4) == cudaSuccess
+                && cudaMalloc(&dCc, n) == cudaSuccess && cudaMalloc(&dCr, n * 4 * ncorr) == cudaSuccess
+                && cudaMallocHost(&hCx, n * 4) == cudaSuccess && cudaMallocHost(&hCy, n * 4) == cudaSuccess
+                && cudaMallocHost(&hCc, n) == cudaSuccess && cudaMallocHost(&hCr, n * 4 * ncorr) == cudaSuccess;
+      if ( ok && ccm )
+         ok = cudaMalloc(&dMx, n * 4) == cudaSuccess && cudaMalloc(&dMy, n * 4) == cudaSuccess
+              && cudaMalloc(&dMc, n) == cudaSuccess && cudaMalloc(&dMp, (size_t)n * nbytes) == cudaSuccess
+              && cudaMallocHost(&hMx, n * 4) == cudaSuccess && cudaMallocHost(&hMy, n * 4) == cudaSuccess
+              && cudaMallocHost(&hMc, n) == cudaSuccess && cudaMallocHost(&hMp, (size_t)n * nbytes) == cudaSuccess;
+      cap = ok ? n : 0;
+      return ok;
+   }
+
+   void release()
+   {
+      free_items();
+      cudaFree(dK); cudaFree(dL); cudaFree(dC); cudaFree(dCount); cudaFreeHost(hCount);
+      if ( counted ) cudaEventDestroy(counted);
+      dK = dL = nullptr;
+      dC = nullptr;
+      dCount = hCount = nullptr;
+      counted = nullptr;
+   }
+};
+
+}  // namespace
+
 extern "C" int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, const char* cmx_path,
                                      int32_t little_endian, int64_t first_block, int64_t nblocks)
+{
+   return kinc_sim_run_to_files_ex(ctx, ccm_path, cmx_path, little_endian, first_block, nblocks, 0);
+}
+
+extern "C" int kinc_sim_run_to_files_ex(kinc_sim_ctx* ctx, const char* ccm_path, const char* cmx_path,
+                                        int32_t little_endian, int64_t first_block, int64_t nblocks,
+                                        int64_t device_block)
 {
    kinc_sim_params p;
    int32_t G = 0, S = 0;
@@ -386,6 +459,10 @@ extern "C" int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, co
    const int64_t total = kinc_sim_total_pairs(ctx);
    const int64_t nb = kinc_sim_num_work_blocks(ctx);
    if ( first_block < 0 || first_block > nb ) return pm_fail(KINC_SIM_EINVAL, "first_block out of range");
+   const int64_t max_dev = kinc_sim_max_device_block(ctx);
+   if ( device_block < 0 || device_block > std::max<int64_t>(max_dev, KINC_SIM_WORK_BLOCK_SIZE) )
+      return pm_fail(KINC_SIM_EINVAL, "device_block %lld outside [0, %lld]", (long long)device_block,
+                     (long long)max_dev);
    const int64_t last_block = nblocks < 0 ? nb : std::min<int64_t>(nb, first_block + nblocks);
    const int64_t pair0 = first_block * KINC_SIM_WORK_BLOCK_SIZE;
    const int64_t pair1 = std::min<int64_t>(total, last_block * KINC_SIM_WORK_BLOCK_SIZE);
@@ -401,97 +478,109 @@ extern "C" int kinc_sim_run_to_files(kinc_sim_ctx* ctx, const char* ccm_path, co
       if ( ccm ) kinc_pm_close(ccm);
       return rc;
    }
-   /* device blocks of whole work blocks; items are filtered and compacted on the GPU and only
-    * the kept ones are copied back (Similarity::process, src/core/similarity.cpp:66-127) */
+   /*
+    * Device blocks of whole work blocks, in two slots: while the GPU computes
+    * block b into one slot, block b-1's kept items (filtered and compacted on
+    * the GPU, Similarity::process, src/core/similarity.cpp:66-127) come back
+    * from the other slot on a copy stream into pinned buffers and are appended
+    * to the files in pair order.
+    */
    const int64_t B = std::max<int64_t>(KINC_SIM_WORK_BLOCK_SIZE,
-                                       kinc_sim_max_device_block(ctx) / KINC_SIM_WORK_BLOCK_SIZE * KINC_SIM_WORK_BLOCK_SIZE);
+                                       (device_block > 0 ? device_block : max_dev) / KINC_SIM_WORK_BLOCK_SIZE
+                                          * KINC_SIM_WORK_BLOCK_SIZE);
    const int64_t Bn = std::min<int64_t>(B, std::max<int64_t>(pair1 - pair0, 1));
    const int nbytes = (S + 1) / 2;
-   int64_t cap = Bn * maxK;
-   cudaStream_t st = nullptr;
-   int8_t *dK = nullptr, *dL = nullptr, *dCc = nullptr, *dMc = nullptr;
-   float *dC = nullptr, *dCr = nullptr;
-   int32_t *dCx = nullptr, *dCy = nullptr, *dMx = nullptr, *dMy = nullptr;
-   uint8_t* dMp = nullptr;
-   uint64_t* dCount = nullptr;
-   int32_t *hx = nullptr, *hy = nullptr;
-   int8_t* hc = nullptr;
-   void* hp = nullptr;
-   uint64_t* hCount = nullptr;
-   bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess;
-   ok = ok && cudaMalloc(&dK, Bn) == cudaSuccess;
-   ok = ok && cudaMalloc(&dC, (size_t)Bn * maxK * ncorr * sizeof(float)) == cudaSuccess;
-   ok = ok && (!want_ccm || cudaMalloc(&dL, (size_t)Bn * S) == cudaSuccess);
-   ok = ok && cudaMalloc(&dCount, 2 * sizeof(uint64_t)) == cudaSuccess;
-   ok = ok && cudaMallocHost(&hCount, 2 * sizeof(uint64_t)) == cudaSuccess;
-   /* item buffers grow on demand (cap starts at every cluster of the block passing) */
-   auto alloc_items = [&](int64_t n) {
-      cudaFree(dCx); cudaFree(dCy); cudaFree(dCc); cudaFree(dCr); cudaFree(dMx); cudaFree(dMy); cudaFree(dMc);
-      cudaFree(dMp); cudaFreeHost(hx); cudaFreeHost(hy); cudaFreeHost(hc); cudaFreeHost(hp);
-      dCx = dCy = dMx = dMy = nullptr; dCc = dMc = nullptr; dCr = nullptr; dMp = nullptr;
-      hx = hy = nullptr; hc = nullptr; hp = nullptr;
-      bool good = cudaMalloc(&dCx, n * 4) == cudaSuccess && cudaMalloc(&dCy, n * 4) == cudaSuccess
-                  && cudaMalloc(&dCc, n) == cudaSuccess && cudaMalloc(&dCr, n * 4 * ncorr) == cudaSuccess
-                  && cudaMallocHost(&hx, n * 4) == cudaSuccess && cudaMallocHost(&hy, n * 4) == cudaSuccess
-                  && cudaMallocHost(&hc, n) == cudaSuccess
-                  && cudaMallocHost(&hp, (size_t)n * std::max<int>(nbytes, 4 * ncorr)) == cudaSuccess;
-      if ( good && want_ccm )
-         good = cudaMalloc(&dMx, n * 4) == cudaSuccess && cudaMalloc(&dMy, n * 4) == cudaSuccess
-                && cudaMalloc(&dMc, n) == cudaSuccess && cudaMalloc(&dMp, (size_t)n * nbytes) == cudaSuccess;
-      return good;
-   };
-   cap = std::min<int64_t>(cap, (int64_t)1 << 24);
-   ok = ok && alloc_items(cap);
-   if ( !ok ) rc = pm_fail(KINC_SIM_ENOMEM, "cannot allocate the runner's buffers");
-   for ( int64_t start = pair0; rc == KINC_SIM_OK && start < pair1; start += Bn )
+   cudaStream_t st = nullptr, cs = nullptr;
+   RunSlot slot[2];
+   bool ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess
+             && cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess;
+   for ( int i = 0; i < 2 && ok; ++i )
    {
-      const int64_t size = std::min<int64_t>(Bn, pair1 - start);
-      rc = kinc_sim_execute_block_device(ctx, start, size, dK, dL, dC, st);
-      if ( rc ) { t_err = kinc_sim_last_error(ctx); break; }
-      for ( int attempt = 0; attempt < 2 && rc == KINC_SIM_OK; ++attempt )
-      {
-         rc = kinc_sim_compact_block_device(ctx, start, size, dK, dL, dC, dCx, dCy, dCc, dCr, cap, dMx, dMy, dMc,
-                                            dMp, want_ccm ? cap : 0, dCount, st);
-         if ( rc ) { t_err = kinc_sim_last_error(ctx); break; }
-         if ( cudaMemcpyAsync(hCount, dCount, 2 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess
-              || cudaStreamSynchronize(st) != cudaSuccess )
-         {
-            rc = pm_fail(KINC_SIM_ECUDA, "device process failed: %s", kinc_sim_last_error(ctx));
-            break;
-         }
-         rc = kinc_sim_synchronize(ctx);
-         if ( rc ) { t_err = kinc_sim_last_error(ctx); break; }
-         const int64_t need = (int64_t)std::max(hCount[0], hCount[1]);
-         if ( need <= cap ) break;
-         cap = need;
-         if ( !alloc_items(cap) ) rc = pm_fail(KINC_SIM_ENOMEM, "cannot grow the item buffers to %lld", (long long)cap);
-      }
-      if ( rc ) break;
-      const int64_t n_cmx = (int64_t)hCount[0], n_ccm = want_ccm ? (int64_t)hCount[1] : 0;
-      if ( ccm && n_ccm > 0 )
-      {
-         bool good = cudaMemcpyAsync(hx, dMx, n_ccm * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                     && cudaMemcpyAsync(hy, dMy, n_ccm * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                     && cudaMemcpyAsync(hc, dMc, n_ccm, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                     && cudaMemcpyAsync(hp, dMp, (size_t)n_ccm * nbytes, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                     && cudaStreamSynchronize(st) == cudaSuccess;
-         if ( !good ) { rc = pm_fail(KINC_SIM_ECUDA, "copy of CCM items failed"); break; }
-         if ( (rc = kinc_pm_write_items_packed(ccm, n_ccm, hx, hy, hc, hp)) ) break;
-      }
-      if ( cmx && n_cmx > 0 )
-      {
-         bool good = cudaMemcpyAsync(hx, dCx, n_cmx * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                     && cudaMemcpyAsync(hy, dCy, n_cmx * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                     && cudaMemcpyAsync(hc, dCc, n_cmx, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                     && cudaMemcpyAsync(hp, dCr, n_cmx * 4 * ncorr, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                     && cudaStreamSynchronize(st) == cudaSuccess;
-         if ( !good ) { rc = pm_fail(KINC_SIM_ECUDA, "copy of CMX items failed"); break; }
-         if ( (rc = kinc_pm_write_items(cmx, n_cmx, hx, hy, hc, hp)) ) break;
-      }
+      RunSlot& s = slot[i];
+      ok = cudaMalloc(&s.dK, Bn) == cudaSuccess
+           && cudaMalloc(&s.dC, (size_t)Bn * maxK * ncorr * sizeof(float)) == cudaSuccess
+           && (!want_ccm || cudaMalloc(&s.dL, (size_t)Bn * S) == cudaSuccess)
+           && cudaMalloc(&s.dCount, 3 * sizeof(uint64_t)) == cudaSuccess
+           && cudaMallocHost(&s.hCount, 3 * sizeof(uint64_t)) == cudaSuccess
+           && cudaEventCreateWithFlags(&s.counted, cudaEventDisableTiming) == cudaSuccess
+           /* item buffers start at 2^21 (or every cluster of the block) and grow on demand */
+           && s.alloc_items(std::min<int64_t>(Bn * maxK, (int64_t)1 << 21), ncorr, want_ccm, nbytes);
    }
-   alloc_items(0);
-   cudaFree(dK); cudaFree(dC); cudaFree(dL); cudaFree(dCount); cudaFreeHost(hCount);
+   if ( !ok ) rc = pm_fail(KINC_SIM_ENOMEM, "cannot allocate the runner's buffers");
+
+   /* enqueue block [start, start+size) into slot s: compute, compact, counts and status to the host */
+   auto launch = [&](RunSlot& s, bool compute) -> int {
+      int r = KINC_SIM_OK;
+      if ( compute && (r = kinc_sim_execute_block_device(ctx, s.start, s.size, s.dK, s.dL, s.dC, st)) )
+         return pm_fail(r, "%s", kinc_sim_last_error(ctx));
+      r = kinc_sim_compact_block_device(ctx, s.start, s.size, s.dK, s.dL, s.dC, s.dCx, s.dCy, s.dCc, s.dCr, s.cap,
+                                        s.dMx, s.dMy, s.dMc, s.dMp, want_ccm ? s.cap : 0, s.dCount, st);
+      if ( r ) return pm_fail(r, "%s", kinc_sim_last_error(ctx));
+      if ( kinc_sim_status_copy_async(ctx, s.dCount + 2, st) != KINC_SIM_OK
+           || cudaMemcpyAsync(s.hCount, s.dCount, 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess
+           || cudaEventRecord(s.counted, st) != cudaSuccess )
+         return pm_fail(KINC_SIM_ECUDA, "cannot enqueue the block's counts");
+      return KINC_SIM_OK;
+   };
+
+   /* wait for slot s's counts, copy its items back on the copy stream and append them to the files */
+   auto drain = [&](RunSlot& s) -> int {
+      if ( cudaEventSynchronize(s.counted) != cudaSuccess )
+         return pm_fail(KINC_SIM_ECUDA, "device block failed: %s", cudaGetErrorString(cudaGetLastError()));
+      if ( s.hCount[2] != 0 )
+      {
+         const int r = kinc_sim_synchronize(ctx);
+         return pm_fail(r ? r : KINC_SIM_EKERNEL, "%s", kinc_sim_last_error(ctx));
+      }
+      int64_t need = (int64_t)std::max(s.hCount[0], want_ccm ? s.hCount[1] : 0);
+      if ( need > s.cap )
+      {
+         /* more kept items than the slot holds: grow it and compact this block again */
+         if ( cudaStreamSynchronize(st) != cudaSuccess ) return pm_fail(KINC_SIM_ECUDA, "device block failed");
+         if ( !s.alloc_items(need, ncorr, want_ccm, nbytes) )
+            return pm_fail(KINC_SIM_ENOMEM, "cannot grow the item buffers to %lld", (long long)need);
+         int r = launch(s, false);
+         if ( r ) return r;
+         if ( cudaEventSynchronize(s.counted) != cudaSuccess ) return pm_fail(KINC_SIM_ECUDA, "compaction failed");
+      }
+      const int64_t n_cmx = (int64_t)s.hCount[0], n_ccm = want_ccm ? (int64_t)s.hCount[1] : 0;
+      bool good = cudaStreamWaitEvent(cs, s.counted, 0) == cudaSuccess;
+      if ( good && ccm && n_ccm > 0 )
+         good = cudaMemcpyAsync(s.hMx, s.dMx, n_ccm * 4, cudaMemcpyDeviceToHost, cs) == cudaSuccess
+                && cudaMemcpyAsync(s.hMy, s.dMy, n_ccm * 4, cudaMemcpyDeviceToHost, cs) == cudaSuccess
+                && cudaMemcpyAsync(s.hMc, s.dMc, n_ccm, cudaMemcpyDeviceToHost, cs) == cudaSuccess
+                && cudaMemcpyAsync(s.hMp, s.dMp, (size_t)n_ccm * nbytes, cudaMemcpyDeviceToHost, cs) == cudaSuccess;
+      if ( good && cmx && n_cmx > 0 )
+         good = cudaMemcpyAsync(s.hCx, s.dCx, n_cmx * 4, cudaMemcpyDeviceToHost, cs) == cudaSuccess
+                && cudaMemcpyAsync(s.hCy, s.dCy, n_cmx * 4, cudaMemcpyDeviceToHost, cs) == cudaSuccess
+                && cudaMemcpyAsync(s.hCc, s.dCc, n_cmx, cudaMemcpyDeviceToHost, cs) == cudaSuccess
+                && cudaMemcpyAsync(s.hCr, s.dCr, n_cmx * 4 * ncorr, cudaMemcpyDeviceToHost, cs) == cudaSuccess;
+      if ( !good || cudaStreamSynchronize(cs) != cudaSuccess )
+         return pm_fail(KINC_SIM_ECUDA, "copy of the kept items failed");
+      int r = KINC_SIM_OK;
+      if ( ccm && n_ccm > 0 && (r = kinc_pm_write_items_packed(ccm, n_ccm, s.hMx, s.hMy, s.hMc, s.hMp)) ) return r;
+      if ( cmx && n_cmx > 0 && (r = kinc_pm_write_items(cmx, n_cmx, s.hCx, s.hCy, s.hCc, s.hCr)) ) return r;
+      return KINC_SIM_OK;
+   };
+
+   const int64_t nblk = pair1 > pair0 ? (pair1 - pair0 + Bn - 1) / Bn : 0;
+   for ( int64_t b = 0; rc == KINC_SIM_OK && b <= nblk; ++b )
+   {
+      if ( b < nblk )
+      {
+         RunSlot& s = slot[b & 1];
+         s.start = pair0 + b * Bn;
+         s.size = std::min<int64_t>(Bn, pair1 - s.start);
+         rc = launch(s, true);
+      }
+      if ( rc == KINC_SIM_OK && b > 0 ) rc = drain(slot[(b - 1) & 1]);
+   }
+   if ( st ) cudaStreamSynchronize(st);
+   if ( cs ) cudaStreamSynchronize(cs);
+   slot[0].release();
+   slot[1].release();
    if ( st ) cudaStreamDestroy(st);
+   if ( cs ) cudaStreamDestroy(cs);
    const int rc1 = ccm ? kinc_pm_close(ccm) : KINC_SIM_OK;
    const int rc2 = cmx ? kinc_pm_close(cmx) : KINC_SIM_OK;
    return rc ? rc : (rc1 ? rc1 : rc2);

@@ -232,18 +232,21 @@ class Similarity:
             matrix.write_pair(int(x[i]), int(y[i]), payloads[i:j])
             i = j
 
-    def run(self, ccm_path=None, cmx_path=None, little_endian=False):
-        """Run every work block in order.  With file paths, the native runner writes the CCM/CMX
-        files (include/kinc_pairwise_matrix.h); otherwise the items are kept in memory and
-        (ccm, cmx) PairwiseMatrix objects are returned."""
+    def run(self, ccm_path=None, cmx_path=None, little_endian=False, first_block=0, nblocks=-1, device_block=0):
+        """Run work blocks [first_block, first_block + nblocks) in order (all of them by default).
+        With file paths, the native runner writes the CCM/CMX files (include/kinc_pairwise_matrix.h)
+        in device blocks of `device_block` pairs (0 = the largest the worker holds); otherwise the
+        items are kept in memory and (ccm, cmx) PairwiseMatrix objects are returned."""
         self.initialize()
         if ccm_path is not None or cmx_path is not None:
             L = _native.load()
-            rc = L.kinc_sim_run_to_files(self._ctx, str(ccm_path).encode() if ccm_path else None,
-                                         str(cmx_path).encode() if cmx_path else None, int(little_endian), 0, -1)
+            rc = L.kinc_sim_run_to_files_ex(self._ctx, str(ccm_path).encode() if ccm_path else None,
+                                            str(cmx_path).encode() if cmx_path else None, int(little_endian),
+                                            int(first_block), int(nblocks), int(device_block))
             if rc != _native.OK:
                 raise _native.SimError(rc, L.kinc_pm_last_error().decode())
             return ccm_path, cmx_path
-        for b in range(self.size()):
+        last = self.size() if nblocks < 0 else min(self.size(), first_block + nblocks)
+        for b in range(first_block, last):
             self.process(self.execute(self.make_work(b)))
         return self.ccm, self.cmx

@@ -956,6 +956,10 @@ typedef struct
    const int64_t* starts;
    const int64_t* sizes;
    const uint64_t* rand_pos;
+   int8_t* out_K;
+   int8_t* out_labels;
+   float* out_corr;
+   const int64_t* out_off;
    int32_t nseg;
    int32_t next;
    pthread_mutex_t lock;
@@ -987,8 +991,11 @@ static void* par_worker(void* argp)
    pthread_barrier_wait(&st->barrier);
    for ( s = a->tid; s < st->nseg; s += a->nthreads )
    {
-      ko_run_block(st->gem, st->G, st->S, st->p, &rngs[s], st->starts[s], st->sizes[s], NULL, NULL,
-                   NULL, NULL);
+      const int64_t o = st->out_off ? st->out_off[s] : 0;
+      ko_run_block(st->gem, st->G, st->S, st->p, &rngs[s], st->starts[s], st->sizes[s],
+                   st->out_K ? st->out_K + o : NULL,
+                   st->out_labels ? st->out_labels + o * st->S : NULL,
+                   st->out_corr ? st->out_corr + o * st->p->max_clusters : NULL, NULL);
       pthread_mutex_lock(&st->lock);
       st->done += st->sizes[s];
       pthread_mutex_unlock(&st->lock);
@@ -998,25 +1005,33 @@ static void* par_worker(void* argp)
    return NULL;
 }
 
-int64_t ko_run_segments_parallel(const float* gem, int32_t G, int32_t S, const ko_params* p,
-                                 const int64_t* starts, const int64_t* sizes, const uint64_t* rand_pos,
-                                 int32_t nseg, int32_t threads, double* seconds);
-
-int64_t ko_run_segments_parallel(const float* gem, int32_t G, int32_t S, const ko_params* p,
-                                 const int64_t* starts, const int64_t* sizes, const uint64_t* rand_pos,
-                                 int32_t nseg, int32_t threads, double* seconds)
+int64_t ko_run_segments_parallel_out(const float* gem, int32_t G, int32_t S, const ko_params* p,
+                                     const int64_t* starts, const int64_t* sizes, const uint64_t* rand_pos,
+                                     int32_t nseg, int32_t threads, double* seconds,
+                                     int8_t* out_K, int8_t* out_labels, float* out_corr)
 {
    par_state st;
    pthread_t* th;
    par_arg* args;
    int32_t t;
    struct timespec t0, t1;
+   int64_t* offs = NULL;
    if ( threads < 1 )
    {
       threads = 1;
    }
+   if ( out_K || out_labels || out_corr )
+   {
+      int32_t s;
+      offs = (int64_t*)calloc((size_t)nseg + 1, sizeof(int64_t));
+      for ( s = 0; s < nseg; ++s )
+      {
+         offs[s + 1] = offs[s] + sizes[s];
+      }
+   }
    st.gem = gem; st.G = G; st.S = S; st.p = p; st.starts = starts; st.sizes = sizes;
    st.rand_pos = rand_pos; st.nseg = nseg; st.next = 0; st.done = 0;
+   st.out_K = out_K; st.out_labels = out_labels; st.out_corr = out_corr; st.out_off = offs;
    pthread_mutex_init(&st.lock, NULL);
    pthread_barrier_init(&st.barrier, NULL, (unsigned)threads + 1);
    th = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
@@ -1043,7 +1058,16 @@ int64_t ko_run_segments_parallel(const float* gem, int32_t G, int32_t S, const k
    pthread_mutex_destroy(&st.lock);
    free(th);
    free(args);
+   free(offs);
    return st.done;
+}
+
+int64_t ko_run_segments_parallel(const float* gem, int32_t G, int32_t S, const ko_params* p,
+                                 const int64_t* starts, const int64_t* sizes, const uint64_t* rand_pos,
+                                 int32_t nseg, int32_t threads, double* seconds)
+{
+   return ko_run_segments_parallel_out(gem, G, S, p, starts, sizes, rand_pos, nseg, threads, seconds, NULL, NULL,
+                                       NULL);
 }
 
 int64_t ko_run_blocks_parallel(const float* gem, int32_t G, int32_t S, const ko_params* p,

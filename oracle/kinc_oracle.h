@@ -78,6 +78,18 @@ int ko_run_block(const float* gem, int32_t G, int32_t S, const ko_params* p, ko_
 /* Same, over `nblocks` work blocks of 32768 pairs (block indices in `blocks`)
  * with `threads` POSIX threads, each block positioned on the rand() stream
  * independently.  Used by the CPU baseline.  Returns pairs processed. */
+/* Segments [starts[s], starts[s]+sizes[s]) with `threads` POSIX threads, each
+ * positioned at rand_pos[s] on the rand() stream; wall time of the compute in
+ * *seconds.  The _out form also stores each segment's results back to back
+ * (K [Σsizes], labels [Σsizes][S], corr [Σsizes][max_clusters]); any may be NULL. */
+int64_t ko_run_segments_parallel(const float* gem, int32_t G, int32_t S, const ko_params* p,
+                                 const int64_t* starts, const int64_t* sizes, const uint64_t* rand_pos,
+                                 int32_t nseg, int32_t threads, double* seconds);
+int64_t ko_run_segments_parallel_out(const float* gem, int32_t G, int32_t S, const ko_params* p,
+                                     const int64_t* starts, const int64_t* sizes, const uint64_t* rand_pos,
+                                     int32_t nseg, int32_t threads, double* seconds,
+                                     int8_t* out_K, int8_t* out_labels, float* out_corr);
+
 int64_t ko_run_blocks_parallel(const float* gem, int32_t G, int32_t S, const ko_params* p,
                                const int64_t* blocks, int32_t nblocks, int32_t threads);
 

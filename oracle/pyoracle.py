@@ -60,6 +60,8 @@ def lib():
                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.c_int32, ctypes.c_int32, P(ctypes.c_double)]
         L.ko_run_segments_parallel.restype = ctypes.c_int64
+        L.ko_run_segments_parallel_out.argtypes = L.ko_run_segments_parallel.argtypes + [ctypes.c_void_p] * 3
+        L.ko_run_segments_parallel_out.restype = ctypes.c_int64
         L.ko_process_block.argtypes = [ctypes.c_int32, P(KoParams), ctypes.c_int64, ctypes.c_int64,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p] + \
             [ctypes.c_void_p] * 8 + [P(ctypes.c_int64)]
@@ -175,8 +177,9 @@ def process_block(S, p, start, K, labels, corr):
             dict(x=mx[:m], y=my[:m], c=mc[:m], codes=codes[:m]))
 
 
-def run_segments_parallel(gem, p, starts, sizes, threads):
-    """Time the restatement over segments with POSIX threads; returns (pairs, seconds)."""
+def run_segments_parallel(gem, p, starts, sizes, threads, outputs=False):
+    """Time the restatement over segments with POSIX threads; returns (pairs, seconds), plus
+    (K, labels, corr) of the segments back to back when `outputs` is set."""
     L = lib()
     gem = np.ascontiguousarray(gem, dtype=np.float32)
     G, S = gem.shape
@@ -184,9 +187,18 @@ def run_segments_parallel(gem, p, starts, sizes, threads):
     sizes = np.ascontiguousarray(sizes, dtype=np.int64)
     pos = np.array([rand_position(gem, p, int(s)) for s in starts], dtype=np.uint64)
     secs = ctypes.c_double(0)
-    done = L.ko_run_segments_parallel(_ptr(gem), G, S, ctypes.byref(p), _ptr(starts), _ptr(sizes), _ptr(pos),
-                                      len(starts), threads, ctypes.byref(secs))
-    return done, secs.value
+    if not outputs:
+        done = L.ko_run_segments_parallel(_ptr(gem), G, S, ctypes.byref(p), _ptr(starts), _ptr(sizes), _ptr(pos),
+                                          len(starts), threads, ctypes.byref(secs))
+        return done, secs.value
+    n = int(sizes.sum())
+    K = np.zeros(n, np.int8)
+    labels = np.zeros((n, S), np.int8)
+    corr = np.zeros((n, p.max_clusters), np.float32)
+    done = L.ko_run_segments_parallel_out(_ptr(gem), G, S, ctypes.byref(p), _ptr(starts), _ptr(sizes), _ptr(pos),
+                                          len(starts), threads, ctypes.byref(secs), _ptr(K), _ptr(labels),
+                                          _ptr(corr))
+    return done, secs.value, (K, labels, corr)
 
 
 def pearson_fp64(gem, x, y, min_expr=float("-inf"), min_samples=30):

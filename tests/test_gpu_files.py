@@ -16,15 +16,9 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
-def test_run_to_files_matches_process(tmp_path, case):
-    name, wl, G, S, gargs, oargs = case
-    gem = synthetic.generate(wl, genes=G, samples=S)
-    sim = Similarity(gem, **gargs)
-    ccm_path, cmx_path = tmp_path / "out.ccm", tmp_path / "out.cmx"
-    sim.run(ccm_path=ccm_path, cmx_path=cmx_path)
-    sim.close()
-    p = pyoracle.params(**oargs)
+def _oracle_items(gem, p, S):
+    """The oracle's process() items over every work block, in order."""
+    G = gem.shape[0]
     total = G * (G - 1) // 2
     cmx_want, ccm_want = {"x": [], "y": [], "c": [], "r": []}, {"x": [], "y": [], "c": [], "codes": []}
     for start in range(0, total, 32768):
@@ -35,15 +29,80 @@ def test_run_to_files_matches_process(tmp_path, case):
             cmx_want[k].append(cmx[k])
         for k in ccm_want:
             ccm_want[k].append(ccm[k])
+    return ({k: np.concatenate(v) for k, v in cmx_want.items()},
+            {k: (np.concatenate(v) if v else np.zeros((0, S), np.int8)) for k, v in ccm_want.items()})
+
+
+def _check_files(cmx_path, ccm_path, cmx_want, ccm_want, S):
     cmx = pm.read(cmx_path, pm.CMX)
-    ccm = pm.read(ccm_path, pm.CCM)
-    assert np.array_equal(cmx["x"], np.concatenate(cmx_want["x"]))
-    assert np.array_equal(cmx["c"], np.concatenate(cmx_want["c"]))
-    assert np.array_equal(cmx["payload"][:, 0], np.concatenate(cmx_want["r"]))
-    assert np.array_equal(ccm["x"], np.concatenate(ccm_want["x"]))
-    codes = np.concatenate(ccm_want["codes"]) if ccm_want["codes"] else np.zeros((0, S), np.int8)
-    assert np.array_equal(ccm["payload"], codes.reshape(-1, S))
+    assert np.array_equal(cmx["x"], cmx_want["x"])
+    assert np.array_equal(cmx["y"], cmx_want["y"])
+    assert np.array_equal(cmx["c"], cmx_want["c"])
+    assert np.array_equal(cmx["payload"][:, 0], cmx_want["r"])
+    if ccm_path is not None:
+        ccm = pm.read(ccm_path, pm.CCM)
+        assert np.array_equal(ccm["x"], ccm_want["x"])
+        assert np.array_equal(ccm["payload"], ccm_want["codes"].reshape(-1, S))
     assert len(cmx["x"]) > 0
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_run_to_files_matches_process(tmp_path, case):
+    name, wl, G, S, gargs, oargs = case
+    gem = synthetic.generate(wl, genes=G, samples=S)
+    sim = Similarity(gem, **gargs)
+    ccm_path, cmx_path = tmp_path / "out.ccm", tmp_path / "out.cmx"
+    sim.run(ccm_path=ccm_path, cmx_path=cmx_path)
+    sim.close()
+    cmx_want, ccm_want = _oracle_items(gem, pyoracle.params(**oargs), S)
+    _check_files(cmx_path, ccm_path, cmx_want, ccm_want, S)
+
+
+def test_run_to_files_two_slots_many_device_blocks(tmp_path):
+    """Device blocks of one work block each: the two result slots alternate over
+    three blocks and the files equal the single-device-block run byte for byte."""
+    G, S = 400, 64
+    gem = synthetic.generate(2, genes=G, samples=S)
+    args = dict(clusmethod="gmm", crit="ICL", preout=True, postout=True, mincorr=0.3)
+    one = Similarity(gem, **args)
+    one.run(ccm_path=tmp_path / "a.ccm", cmx_path=tmp_path / "a.cmx")
+    one.close()
+    many = Similarity(gem, **args)
+    many.run(ccm_path=tmp_path / "b.ccm", cmx_path=tmp_path / "b.cmx", device_block=32768)
+    many.close()
+    for ext in ("ccm", "cmx"):
+        assert (tmp_path / f"a.{ext}").read_bytes() == (tmp_path / f"b.{ext}").read_bytes()
+    p = pyoracle.params(clus_method=1, criterion=1, pre_out=1, post_out=1, min_corr=0.3)
+    cmx_want, ccm_want = _oracle_items(gem, p, S)
+    _check_files(tmp_path / "b.cmx", tmp_path / "b.ccm", cmx_want, ccm_want, S)
+
+
+def test_run_to_files_partial_range(tmp_path):
+    """first_block / nblocks select work blocks; the files hold exactly their items."""
+    G, S = 400, 48
+    gem = synthetic.generate(1, genes=G, samples=S)
+    sim = Similarity(gem, mincorr=0.2)
+    sim.run(cmx_path=tmp_path / "p.cmx", first_block=1, nblocks=1, device_block=32768)
+    sim.close()
+    p = pyoracle.params(min_corr=0.2)
+    K, labels, corr, _ = pyoracle.run_block(gem, p, 32768, 32768)
+    cmx, _ = pyoracle.process_block(S, p, 32768, K, labels, corr)
+    got = pm.read(tmp_path / "p.cmx", pm.CMX)
+    assert np.array_equal(got["x"], cmx["x"]) and np.array_equal(got["y"], cmx["y"])
+    assert np.array_equal(got["payload"][:, 0], cmx["r"])
+
+
+def test_run_to_files_grows_item_buffers(tmp_path):
+    """A device block keeping more than 2^21 items (every pair of a 2^22-pair block
+    with mincorr 0) makes the runner grow its item buffers and compact again."""
+    G, S = 3000, 40
+    gem = synthetic.generate(1, genes=G, samples=S)
+    sim = Similarity(gem, mincorr=0.0, minsamp=30)
+    sim.run(cmx_path=tmp_path / "g.cmx")
+    sim.close()
+    cmx_want, _ = _oracle_items(gem, pyoracle.params(min_corr=0.0, min_samples=30), S)
+    assert len(cmx_want["x"]) > (1 << 21)
+    _check_files(tmp_path / "g.cmx", None, cmx_want, None, S)
 
 
 def test_device_process_matches_host_process():
