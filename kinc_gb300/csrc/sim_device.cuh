@@ -33,11 +33,21 @@
 
 namespace kinc {
 
+/* L2 prefetch of one lane's scratch word; the callers keep the address inside
+ * the lane's own [0, N) samples */
+__device__ __forceinline__ void prefetch_l2(const void* p)
+{
+   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 constexpr int TILE = 32;            /* pairs per warp tile */
 #ifndef KINC_SAMPLE_UNROLL
 #define KINC_SAMPLE_UNROLL 1
 #endif
 constexpr int SAMPLE_UNROLL = KINC_SAMPLE_UNROLL;   /* unroll factor of the EM sample loops */
+#ifndef KINC_PREFETCH
+#define KINC_PREFETCH 8             /* samples ahead the EM / Lloyd sweeps prefetch into L2 (0: none) */
+#endif
 #ifndef KINC_UNROLL_SMALL_K
 #define KINC_UNROLL_SMALL_K 0       /* fits with K <= this unroll their sample loops by 2 (more ILP) */
 #endif
@@ -489,6 +499,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
       {
          const float2 xv = xn;
          if ( i + 1 < N ) xn = X[(i + 1) * TILE];
+         if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N ) prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
          float lg[KA];
          float m = -INFINITY;
 #pragma unroll UF
@@ -546,6 +557,11 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
             {
                xn = X[(i + 1) * TILE];
                ln = lpx[(i + 1) * TILE];
+            }
+            if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N )
+            {
+               prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
+               prefetch_l2(&lpx[(i + KINC_PREFETCH) * TILE]);
             }
 #pragma unroll UF
             for ( int k = 0; k < KA; ++k )
@@ -608,6 +624,11 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
          {
             xn = X[(i + 1) * TILE];
             ln = lpx[(i + 1) * TILE];
+         }
+         if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N )
+         {
+            prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
+            prefetch_l2(&lpx[(i + KINC_PREFETCH) * TILE]);
          }
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
@@ -738,6 +759,11 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
          {
             const float2 xv = xn;
             if ( i + 1 < N ) xn = X[(i + 1) * TILE];
+            if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N )
+            {
+               prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
+               if ( !first ) prefetch_l2(&ya[(i + KINC_PREFETCH) * TILE]);
+            }
             int min_k = -1;
             float min_d = 0.f;
 #pragma unroll UF
