@@ -716,7 +716,7 @@ __device__ __forceinline__ float diff_norm(float x0, float x1, float m0, float m
  * the assignment (and dropped when the labels did not change).  The first
  * iteration compares against the all-zero initial labels without reading them. */
 template <int KT>
-__device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*& best, int N, int Kr,
+__device__ float kmeans_fit_inits_in_step(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*& best, int N, int Kr,
                             LaneRng& rng, unsigned long long& units)
 {
    /* KT > 0: up to KT centroids in registers (K <= KT at run time);
@@ -742,6 +742,9 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
       int8_t* yb = nxt;     /* labels being assigned */
       bool first = true;    /* ya is the all-zero initial vector, not yet written */
       bool converged = false;
+      int nprev[KA];        /* cluster sizes behind the current means */
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k ) nprev[k] = -1;
       for ( int t = 0; t < 300; ++t )
       {
          units += (unsigned long long)N * K;
@@ -759,11 +762,7 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
          {
             const float2 xv = xn;
             if ( i + 1 < N ) xn = X[(i + 1) * TILE];
-            if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N )
-            {
-               prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
-               if ( !first ) prefetch_l2(&ya[(i + KINC_PREFETCH) * TILE]);
-            }
+            if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N ) prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
             int min_k = -1;
             float min_d = 0.f;
 #pragma unroll UF
@@ -778,8 +777,6 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
                }
             }
             yb[i * TILE] = (int8_t)min_k;
-            const int8_t prev = first ? (int8_t)0 : ya[i * TILE];
-            same = same && (prev == (int8_t)min_k);
 #pragma unroll UF
             for ( int k = 0; k < KA; ++k )
             {
@@ -791,6 +788,37 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
                   nk[k]++;
                }
             }
+         }
+         /*
+          * "no label changed", decided without reading the previous labels in the sweep:
+          * first iteration: the previous labels are all zero, so unchanged <=> every sample in
+          * cluster 0.  Later: the means are formed from the labels by the same ordered sums, so
+          * unchanged labels give bit-identical means and counts; when those match, the label
+          * arrays are compared to decide exactly.
+          */
+         float n0[KA], n1[KA];
+         bool means_same = true;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            const float sc = 1.0f / nk[k];
+            n0[k] = s0[k] * sc;
+            n1[k] = s1[k] * sc;
+            means_same = means_same && __float_as_uint(n0[k]) == __float_as_uint(mu0[k])
+                         && __float_as_uint(n1[k]) == __float_as_uint(mu1[k]) && nk[k] == nprev[k];
+         }
+         if ( first )
+         {
+            same = nk[0] == N;
+         }
+         else if ( means_same )
+         {
+            for ( int i = 0; i < N && same; ++i ) same = ya[i * TILE] == yb[i * TILE];
+         }
+         else
+         {
+            same = false;
          }
          if ( same )
          {
@@ -805,9 +833,9 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
          for ( int k = 0; k < KA; ++k )
          {
             if ( k >= K ) continue;
-            const float sc = 1.0f / nk[k];
-            mu0[k] = s0[k] * sc;
-            mu1[k] = s1[k] * sc;
+            mu0[k] = n0[k];
+            mu1[k] = n1[k];
+            nprev[k] = nk[k];
          }
       }
       /* the labels: the unchanged assignment (in yb) if converged, else the last one (ya) */
@@ -843,6 +871,168 @@ __device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*
       }
    }
    return bestLogL;
+}
+
+/* 1: lane-independent initialisations (below); measured slower on the uneven 10,000 x 4,000 workload
+ * (12.8k vs 15.0k pairs/s): the cluster-major log-likelihood pass of a lane that finishes an
+ * initialisation then runs divergently beside the other lanes' Lloyd sweeps */
+#ifndef KINC_KMEANS_LANE_INDEPENDENT
+#define KINC_KMEANS_LANE_INDEPENDENT 0
+#endif
+
+/*
+ * KMeans::fit (src/core/pairwise_kmeans.cpp:12-99) for one lane's pair with K
+ * clusters: 10 initialisations (means drawn from rand()), each up to 300
+ * Lloyd iterations until no label changes, the one with the largest
+ * log-likelihood kept.  Each lane walks its own (init, iteration) sequence:
+ * a lane whose initialisation has converged starts its next one while the
+ * other lanes of the warp are still iterating, so a warp costs the largest
+ * total of iterations over its lanes rather than the sum over inits of the
+ * largest count.  The arithmetic of every lane is unchanged.
+ */
+template <int KT>
+__device__ float kmeans_fit(const float2* X, int8_t*& cur, int8_t*& nxt, int8_t*& best, int N, int Kr,
+                            LaneRng& rng, unsigned long long& units)
+{
+#if !KINC_KMEANS_LANE_INDEPENDENT
+   return kmeans_fit_inits_in_step<KT>(X, cur, nxt, best, N, Kr, rng, units);
+#else
+   const int K = (KINC_STATIC_K && KT > 0) ? KT : Kr;
+   constexpr int KA = KT > 0 ? KT : 64;
+   constexpr int UF = KT > 0 ? KT : 1;
+   float bestLogL = -INFINITY;
+   if ( rng.mode == 1 ) rng.lcg = 1;
+   float mu0[KA], mu1[KA];
+   int8_t* ya = cur;     /* labels of the previous iteration */
+   int8_t* yb = nxt;     /* labels being assigned */
+   bool first = true;    /* ya is the all-zero initial vector, not yet written */
+   bool fresh = true;    /* an initialisation is to be drawn */
+   int t = 0;
+   int init = 0;
+   while ( init < 10 )
+   {
+      if ( fresh )
+      {
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            const int ii = rng.next() % N;
+            const float2 xv = X[ii * TILE];
+            mu0[k] = xv.x;
+            mu1[k] = xv.y;
+         }
+         ya = cur;
+         yb = nxt;
+         first = true;
+         fresh = false;
+         t = 0;
+      }
+
+      /* one Lloyd iteration: assign, compare with the previous labels, sum the new means */
+      units += (unsigned long long)N * K;
+      bool same = true;
+      float s0[KA], s1[KA];
+      int nk[KA];
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k )
+      {
+         if ( k >= K ) continue;
+         s0[k] = 0.f; s1[k] = 0.f; nk[k] = 0;
+      }
+      float2 xn = X[0];
+      for ( int i = 0; i < N; ++i )
+      {
+         const float2 xv = xn;
+         if ( i + 1 < N ) xn = X[(i + 1) * TILE];
+         if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N )
+         {
+            prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
+            if ( !first ) prefetch_l2(&ya[(i + KINC_PREFETCH) * TILE]);
+         }
+         int min_k = -1;
+         float min_d = 0.f;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            const float d = diff_norm(xv.x, xv.y, mu0[k], mu1[k]);
+            if ( min_k == -1 || d < min_d )
+            {
+               min_k = k;
+               min_d = d;
+            }
+         }
+         yb[i * TILE] = (int8_t)min_k;
+         const int8_t prev = first ? (int8_t)0 : ya[i * TILE];
+         same = same && (prev == (int8_t)min_k);
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            if ( k == min_k )
+            {
+               s0[k] += xv.x;
+               s1[k] += xv.y;
+               nk[k]++;
+            }
+         }
+      }
+      bool done = same;
+      if ( !same )
+      {
+         int8_t* tmp = ya;
+         ya = yb;
+         yb = tmp;
+         first = false;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            const float sc = 1.0f / nk[k];
+            mu0[k] = s0[k] * sc;
+            mu1[k] = s1[k] * sc;
+         }
+         done = ++t == 300;
+      }
+      if ( !done ) continue;
+
+      /* the labels: the unchanged assignment (in yb) if converged, else the last one (ya);
+       * computeLogLikelihood: one accumulator, cluster-major order */
+      int8_t* lab = same ? yb : ya;
+      float S = 0.f;
+      for ( int k = 0; k < K; ++k )
+      {
+         float c0 = 0.f, c1 = 0.f;
+#pragma unroll UF
+         for ( int kk = 0; kk < KA; ++kk )
+         {
+            if ( kk >= K ) continue;
+            if ( kk == k ) { c0 = mu0[kk]; c1 = mu1[kk]; }
+         }
+         for ( int i = 0; i < N; ++i )
+         {
+            if ( lab[i * TILE] != k ) continue;
+            const float2 xv = X[i * TILE];
+            const float d = diff_norm(xv.x, xv.y, c0, c1);
+            S += d * d;
+         }
+      }
+      const float logL = -S;
+      /* keep the buffers distinct: cur/nxt are this run's, best the kept one */
+      if ( bestLogL < logL )
+      {
+         bestLogL = logL;
+         int8_t* old = best;
+         best = lab;
+         cur = (lab == cur) ? old : cur;
+         nxt = (lab == nxt) ? old : nxt;
+      }
+      ++init;
+      fresh = true;
+   }
+   return bestLogL;
+#endif
 }
 
 } /* namespace kinc */
