@@ -260,8 +260,8 @@ def dense_leg(L, vp, check_pairs=1000000):
 def kmeans_leg(L, vp, cpu=True):
     """K-means (k <= 3, BIC) + Pearson on the uneven 10,000 x 4,000 workload (kinc_gb300.synthetic workload 4:
     per-gene NaN rate ~U(0,0.6), so usable-sample counts span ~600-4,000; 5% planted 2-cluster pairs):
-    two device blocks of 65,536 pairs timed with CUDA events, and the oracle on the host cores over a
-    bounded sample of the same workload."""
+    two device blocks of 262,144 pairs timed with CUDA events (after a 32,768-pair warm-up block), and the
+    oracle on the host cores over a bounded sample of the same workload."""
     import ctypes
 
     import torch
@@ -274,22 +274,22 @@ def kmeans_leg(L, vp, cpu=True):
     sim = Similarity(gem, **args)
     sim.initialize()
     ctx = sim._ctx
-    n = 65536
+    n = 262144
     dK = torch.empty(n, dtype=torch.int8, device="cuda")
     dL = torch.empty((n, S), dtype=torch.int8, device="cuda")
     dC = torch.empty((n, 3), dtype=torch.float32, device="cuda")
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
-        def once(s0):
-            _native.check(L.kinc_sim_execute_block_device(ctx, s0, n, vp(dK.data_ptr()), vp(dL.data_ptr()),
+        def once(s0, size=n):
+            _native.check(L.kinc_sim_execute_block_device(ctx, s0, size, vp(dK.data_ptr()), vp(dL.data_ptr()),
                                                           vp(dC.data_ptr()), vp(stream.cuda_stream)), ctx)
-        once(0)
+        once(0, 32768)
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        once(n)
-        once(2 * n)
+        once(32768)
+        once(32768 + n)
         e1.record(stream)
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / 2

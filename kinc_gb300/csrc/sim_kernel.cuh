@@ -25,7 +25,7 @@ constexpr int WARPS_PER_BLOCK = KINC_WARPS_PER_BLOCK;
  * same time (a warp that drifts into another fit or phase evicts the others'
  * instructions) */
 #ifndef KINC_CTA_ROUNDS
-#define KINC_CTA_ROUNDS 1
+#define KINC_CTA_ROUNDS 3           /* bit c set: rounds for clusmethod c (0 none, 1 gmm, 2 kmeans) */
 #endif
 #ifndef KINC_MIN_BLOCKS
 #define KINC_MIN_BLOCKS (16 / KINC_WARPS_PER_BLOCK)
@@ -227,25 +227,27 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
                     : nullptr;
 
    const int64_t ntiles = (B.size + TILE - 1) / TILE;
-#if KINC_CTA_ROUNDS
+   constexpr bool ROUNDS = ((KINC_CTA_ROUNDS) >> CLUS) & 1;
    __shared__ unsigned long long round_base;
-#endif
    for ( ;; )
    {
       unsigned long long t = 0;
-#if KINC_CTA_ROUNDS
-      __syncthreads();                       /* every warp is done with the previous round */
-      if ( threadIdx.x == 0 ) round_base = atomicAdd(B.tiles, (unsigned long long)WARPS_PER_BLOCK);
-      __syncthreads();
-      const unsigned long long base = round_base;
-      if ( (int64_t)base >= ntiles ) break;  /* uniform over the CTA */
-      t = base + warp;
-      if ( (int64_t)t >= ntiles ) continue;  /* idle this round, back to the barrier */
-#else
-      if ( lane == 0 ) t = atomicAdd(B.tiles, 1ull);
-      t = __shfl_sync(0xffffffffu, t, 0);
-      if ( (int64_t)t >= ntiles ) break;
-#endif
+      if constexpr ( ROUNDS )
+      {
+         __syncthreads();                       /* every warp is done with the previous round */
+         if ( threadIdx.x == 0 ) round_base = atomicAdd(B.tiles, (unsigned long long)WARPS_PER_BLOCK);
+         __syncthreads();
+         const unsigned long long base = round_base;
+         if ( (int64_t)base >= ntiles ) break;  /* uniform over the CTA */
+         t = base + warp;
+         if ( (int64_t)t >= ntiles ) continue;  /* idle this round, back to the barrier */
+      }
+      else
+      {
+         if ( lane == 0 ) t = atomicAdd(B.tiles, 1ull);
+         t = __shfl_sync(0xffffffffu, t, 0);
+         if ( (int64_t)t >= ntiles ) break;
+      }
       const int64_t slot0 = (int64_t)t * TILE;
       const int64_t left = B.size - slot0;
       const int npairs = left < TILE ? (int)left : TILE;
