@@ -1,0 +1,78 @@
+"""Run and time device blocks of one synthetic workload through the worker.
+
+    python -m kinc_gb300.blockrun --workload 2 --clusmethod gmm --corrmethod spearman \\
+        --crit BIC --preout --postout --blocks 32768,262144
+
+Each entry of --blocks is one kinc_sim_execute_block_device call of that many
+pairs, taken consecutively from --start (default: pair 0; "mid" = the work
+block in the middle of the workload), timed with CUDA events on a stream of
+its own.  Prints one line per block with the time, pairs/s and the clustering
+work counters (model units = iterations x N x K summed over fits), so a single
+kernel launch can be captured by a profiler with -s/-c on k_similarity.
+"""
+import argparse
+import ctypes
+import json
+
+from . import Similarity, _native, synthetic
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--workload", type=int, default=2, help="kinc_gb300.synthetic workload (1-5)")
+    ap.add_argument("--clusmethod", default="gmm")
+    ap.add_argument("--corrmethod", default="spearman")
+    ap.add_argument("--crit", default="BIC")
+    ap.add_argument("--minclus", type=int, default=1)
+    ap.add_argument("--maxclus", type=int, default=5)
+    ap.add_argument("--minsamp", type=int, default=30)
+    ap.add_argument("--preout", action="store_true")
+    ap.add_argument("--postout", action="store_true")
+    ap.add_argument("--semantics", default="reference")
+    ap.add_argument("--precision", default="fp32")
+    ap.add_argument("--start", default="0", help="first pair, or 'mid'")
+    ap.add_argument("--blocks", default="32768,262144", help="comma-separated device block sizes")
+    args = ap.parse_args(argv)
+
+    import torch
+
+    gem = synthetic.generate(args.workload)
+    G, S = gem.shape
+    sim = Similarity(gem, clusmethod=args.clusmethod, corrmethod=args.corrmethod, crit=args.crit,
+                     minclus=args.minclus, maxclus=args.maxclus, minsamp=args.minsamp, preout=args.preout,
+                     postout=args.postout, semantics=args.semantics, precision=args.precision)
+    sim.initialize()
+    L = _native.load()
+    ctx = sim._ctx
+    vp = ctypes.c_void_p
+    sizes = [int(b) for b in args.blocks.split(",") if b]
+    pos = (sim.total_pairs() // 2) // 32768 * 32768 if args.start == "mid" else int(args.start)
+    n = max(sizes)
+    nc = 2 if sim.params.corr_method == 2 else 1
+    dK = torch.empty(n, dtype=torch.int8, device="cuda")
+    dL = torch.empty((n, S), dtype=torch.int8, device="cuda")
+    dC = torch.empty((n, sim.params.max_clusters * nc), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()   # the worker's stream argument 0 would mean its own stream
+    counters = (ctypes.c_uint64 * 4)()
+    for size in sizes:
+        _native.check(L.kinc_sim_work_counters(ctx, counters, 1), ctx)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rc = L.kinc_sim_execute_block_device(ctx, pos, size, vp(dK.data_ptr()), vp(dL.data_ptr()),
+                                             vp(dC.data_ptr()), vp(stream.cuda_stream))
+        _native.check(rc, ctx)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        _native.check(L.kinc_sim_synchronize(ctx), ctx)
+        _native.check(L.kinc_sim_work_counters(ctx, counters, 1), ctx)
+        ms = e0.elapsed_time(e1)
+        print(json.dumps({"workload": args.workload, "start": pos, "pairs": size, "ms": ms,
+                          "pairs_per_s": size / (ms / 1e3), "units": int(counters[0]), "fits": int(counters[1]),
+                          "launches": int(L.kinc_sim_last_launch_count(ctx))}), flush=True)
+        pos += size
+    sim.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1169,7 +1169,9 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    const bool need_sort = (params->clus_method != 0 && (params->pre_out || params->post_out))
                           || params->corr_method == 1;
    dp.sort_floats = params->corr_method == 1 ? 3 * dp.P2 : (need_sort ? dp.P2 : 0);
-   dp.gam_k = 0;
+   /* room for the GMM responsibilities the fit keeps between its two M passes (as in kinc_sim_create) */
+   dp.gam_k = (KINC_STORE_GAMMA && params->clus_method == 1)
+                 ? (params->max_clusters <= 3 ? 3 : params->max_clusters <= 5 ? 5 : 0) : 0;
    dp.ncorr = 1;
    const size_t sort_bytes_warp = (size_t)dp.sort_floats * sizeof(float);
    const SimKernel kern = params->clus_method == 0 ? sim_kernel_none()
@@ -1202,6 +1204,7 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    const size_t oSmall = take(8 * sizeof(unsigned long long));
    const size_t col = (size_t)S * TILE;
    const size_t slot_bytes = ((col * sizeof(float2) + 255) & ~(size_t)255) + ((col * sizeof(float) + 255) & ~(size_t)255)
+                             + ((col * sizeof(float) * dp.gam_k + 255) & ~(size_t)255)
                              + 5 * ((col + 255) & ~(size_t)255)
                              + (((size_t)RNG_WORDS * TILE * sizeof(uint32_t) + 255) & ~(size_t)255)
                              + (smem_sort ? 0 : ((sort_bytes_warp + 255) & ~(size_t)255));
@@ -1221,7 +1224,7 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
       };
       ds.X = (float2*)carve(nslots * col * sizeof(float2));
       ds.lpx = (float*)carve(nslots * col * sizeof(float));
-      ds.gam = nullptr;
+      ds.gam = dp.gam_k ? (float*)carve(nslots * col * sizeof(float) * dp.gam_k) : nullptr;
       ds.lbl = (int8_t*)carve(nslots * col);
       ds.wl = (int8_t*)carve(nslots * col);
       ds.ya = (int8_t*)carve(nslots * col);

@@ -66,7 +66,7 @@ constexpr int SAMPLE_UNROLL = KINC_SAMPLE_UNROLL;   /* unroll factor of the EM s
 #define PARAM_QUAL
 #endif
 #ifndef KINC_STORE_GAMMA
-#define KINC_STORE_GAMMA 0          /* 1: keep the M1 responsibilities for M2 instead of recomputing them */
+#define KINC_STORE_GAMMA 1          /* 1: keep the M1 responsibilities for M2 instead of recomputing them */
 #endif
 constexpr int RNG_WORDS = 31;       /* glibc TYPE_3 state words */
 constexpr int RNG_BITS = 48;        /* jump table covers positions < 2^48 */
@@ -628,7 +628,19 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
          if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N )
          {
             prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
-            prefetch_l2(&lpx[(i + KINC_PREFETCH) * TILE]);
+            if ( STORE_G )
+            {
+#pragma unroll UF
+               for ( int k = 0; k < KA; ++k )
+               {
+                  if ( k >= K ) continue;
+                  prefetch_l2(&gam[((i + KINC_PREFETCH) * KA + k) * TILE]);
+               }
+            }
+            else
+            {
+               prefetch_l2(&lpx[(i + KINC_PREFETCH) * TILE]);
+            }
          }
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
