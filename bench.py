@@ -519,16 +519,26 @@ def main():
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
     achieved = units * FLOPS_PER_UNIT / (ms / 1e3) / 1e12
     traffic = None
+    issue = None
     tpath = os.path.join(REPO, "profiles", "k_similarity_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as fh:
             tj = json.load(fh)
         traffic = tj.get("bytes_per_pair", 0) * B   # DRAM bytes of one launch (one step), scaled from the capture
+        tpu = tj.get("thread_inst_per_unit")
+        if tpu:
+            # the bound that binds: instruction issue (exp/log are polynomials, sums are ordered float adds)
+            lane_peak = props.multi_processor_count * 4 * 32 * sm_max * 1e6
+            rate = units * tpu / (ms / 1e3)
+            issue = {"thread_inst_per_unit": tpu, "achieved_thread_inst_per_s": rate,
+                     "peak_thread_inst_per_s": lane_peak, "frac": rate / lane_peak,
+                     "source": "thread instructions per unit from the ncu capture in profiles/"}
     roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak, "traffic": traffic,
                 "peak_source": f"nominal FP32 FMA rate: {props.multi_processor_count} SMs x 128 lanes x 2 flops x "
                                f"{sm_max:.0f} MHz (MEASURED_PEAKS.json holds no FP32 figure)",
-                "kernel": "k_similarity", "units": units, "flops_per_unit": FLOPS_PER_UNIT, "fits": fits}
+                "kernel": "k_similarity", "units": units, "flops_per_unit": FLOPS_PER_UNIT, "fits": fits,
+                "issue": issue}
 
     tensor_core = None if args.no_dense else dense_leg(L, vp, args.dense_check_pairs)
     kmeans = None if args.no_kmeans else kmeans_leg(L, vp, cpu=not args.no_cpu)

@@ -50,7 +50,7 @@ def main(argv=None):
     n = max(sizes)
     nc = 2 if sim.params.corr_method == 2 else 1
     dK = torch.empty(n, dtype=torch.int8, device="cuda")
-    dL = torch.empty((n, S), dtype=torch.int8, device="cuda")
+    dL = torch.empty((n, S), dtype=torch.int8, device="cuda") if args.precision == "fp32" else None
     dC = torch.empty((n, sim.params.max_clusters * nc), dtype=torch.float32, device="cuda")
     stream = torch.cuda.Stream()   # the worker's stream argument 0 would mean its own stream
     counters = (ctypes.c_uint64 * 4)()
@@ -59,8 +59,9 @@ def main(argv=None):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        rc = L.kinc_sim_execute_block_device(ctx, pos, size, vp(dK.data_ptr()), vp(dL.data_ptr()),
-                                             vp(dC.data_ptr()), vp(stream.cuda_stream))
+        labels = vp(dL.data_ptr()) if dL is not None else None   # the tensor-core form writes no labels
+        rc = L.kinc_sim_execute_block_device(ctx, pos, size, vp(dK.data_ptr()), labels, vp(dC.data_ptr()),
+                                             vp(stream.cuda_stream))
         _native.check(rc, ctx)
         e1.record(stream)
         torch.cuda.synchronize()
