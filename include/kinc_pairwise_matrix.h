@@ -71,6 +71,16 @@ int kinc_emx_write(const char* path, const float* gem, int32_t genes, int32_t sa
 int kinc_emx_read_header(const char* path, int32_t little_endian, int32_t* genes, int32_t* samples);
 int kinc_emx_read(const char* path, int32_t little_endian, float* gem, int64_t capacity);
 
+/*
+ * ExportCorrelationMatrix (src/core/exportcorrelationmatrix.cpp:17-117): the CMX and CCM files as
+ * tab-separated text, one line per CMX cluster: x, y, cluster, clusters of the pair, then the
+ * counts of sample codes 1 (in the cluster), 9 (missing), 8 (post-outlier), 7 (pre-outlier) and
+ * 6 (below minexpr) from the CCM cluster, the cluster's first correlation (%.6g) and the sample
+ * mask ('0' + code per sample).  Pairs with a single CMX cluster take no CCM data: zero counts
+ * and a mask of '0's, as the reference writes them.
+ */
+int kinc_pm_export_text(const char* ccm_path, const char* cmx_path, int32_t little_endian, const char* out_path);
+
 /* Message of the last failed kinc_pm_* / kinc_emx_* / kinc_sim_run_to_files call on this thread. */
 const char* kinc_pm_last_error(void);
 

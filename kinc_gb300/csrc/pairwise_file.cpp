@@ -378,6 +378,157 @@ extern "C" int kinc_emx_read(const char* path, int32_t little_endian, float* gem
    return KINC_SIM_OK;
 }
 
+/*
+ * ExportCorrelationMatrix::process (src/core/exportcorrelationmatrix.cpp:17-117): one text line
+ * per CMX cluster, "x y k clusterSize samples missing postOutliers preOutliers threshold r mask"
+ * separated by tabs.  The counts and the sample mask come from the CCM cluster only when the
+ * CMX pair has more than one cluster (else zeros and a mask of '0's); r is the cluster's first
+ * correlation, printed as the reference's text stream prints a float at precision 6 (%.6g of its
+ * double value).  CMX and CCM are both in pair order, so the CCM pair is found by walking a
+ * second cursor forward.
+ */
+extern "C" int kinc_pm_export_text(const char* ccm_path, const char* cmx_path, int32_t little_endian,
+                                   const char* out_path)
+{
+   if ( !ccm_path || !cmx_path || !out_path )
+      return pm_fail(KINC_SIM_EINVAL, "Did not get valid input and/or output arguments.");
+   kinc_pm *cmx = nullptr, *ccm = nullptr;
+   int32_t g1 = 0, k1 = 0, nc = 0, g2 = 0, k2 = 0, S = 0;
+   int64_t p1 = 0, n_cmx = 0, p2 = 0, n_ccm = 0;
+   int rc = kinc_pm_open(cmx_path, KINC_PM_CMX, little_endian, &cmx, &g1, &k1, &nc, &p1, &n_cmx);
+   if ( rc ) return rc;
+   if ( (rc = kinc_pm_open(ccm_path, KINC_PM_CCM, little_endian, &ccm, &g2, &k2, &S, &p2, &n_ccm)) )
+   {
+      kinc_pm_close(cmx);
+      return rc;
+   }
+   FILE* out = fopen(out_path, "wb");
+   if ( !out )
+   {
+      kinc_pm_close(cmx);
+      kinc_pm_close(ccm);
+      return pm_fail(KINC_SIM_EINVAL, "cannot open %s for writing", out_path);
+   }
+   std::vector<char> obuf(1 << 22);
+   setvbuf(out, obuf.data(), _IOFBF, obuf.size());
+
+   constexpr int64_t CHUNK = 1 << 16;
+   /* CMX items, read a chunk at a time */
+   std::vector<int32_t> ax(CHUNK), ay(CHUNK);
+   std::vector<int8_t> ac(CHUNK);
+   std::vector<float> ar((size_t)CHUNK * nc);
+   int64_t a_base = 0, a_len = 0;
+   /* CCM items: a window that always starts at the cursor */
+   std::vector<int32_t> bx(CHUNK), by(CHUNK);
+   std::vector<int8_t> bc(CHUNK);
+   std::vector<int8_t> bcodes((size_t)CHUNK * S);
+   int64_t b_base = 0, b_len = 0, b_cur = 0;
+   std::string mask((size_t)S, '0');
+   std::vector<int8_t> codes;   /* the CCM clusters of the current pair, [cluster][S] */
+   char line[256];
+
+   auto fill_ccm = [&](int64_t first) -> int {
+      b_base = first;
+      b_len = std::min<int64_t>(CHUNK, n_ccm - first);
+      if ( b_len <= 0 ) return KINC_SIM_OK;
+      return kinc_pm_read_items(ccm, first, b_len, bx.data(), by.data(), bc.data(), bcodes.data());
+   };
+   auto pair_of = [](int32_t x, int32_t y) { return (int64_t)x * (x - 1) / 2 + y; };
+
+   int64_t i = 0;
+   while ( rc == KINC_SIM_OK && i < n_cmx )
+   {
+      /* the CMX pair starting at item i: its clusters are items [i, j) */
+      auto at = [&](int64_t q) -> int64_t {
+         if ( q < a_base || q >= a_base + a_len )
+         {
+            a_base = q;
+            a_len = std::min<int64_t>(CHUNK, n_cmx - q);
+            if ( kinc_pm_read_items(cmx, q, a_len, ax.data(), ay.data(), ac.data(), ar.data()) ) return -1;
+         }
+         return q - a_base;
+      };
+      int64_t o = at(i);
+      if ( o < 0 ) { rc = KINC_SIM_EINVAL; break; }
+      const int32_t x = ax[o], y = ay[o];
+      std::vector<float> r;
+      int64_t j = i;
+      while ( j < n_cmx )
+      {
+         const int64_t q = at(j);
+         if ( q < 0 ) { rc = KINC_SIM_EINVAL; break; }
+         if ( ax[q] != x || ay[q] != y ) break;
+         r.push_back(ar[(size_t)q * nc]);
+         ++j;
+      }
+      if ( rc ) break;
+      const int clusters = (int)(j - i);
+      codes.clear();
+      if ( clusters > 1 )
+      {
+         /* advance the CCM cursor to this pair and collect its clusters */
+         const int64_t want = pair_of(x, y);
+         for ( ;; )
+         {
+            if ( b_cur >= n_ccm ) break;
+            if ( b_cur < b_base || b_cur >= b_base + b_len )
+               if ( (rc = fill_ccm(b_cur)) ) break;
+            const int64_t q = b_cur - b_base;
+            const int64_t have = pair_of(bx[q], by[q]);
+            if ( have < want ) { ++b_cur; continue; }
+            if ( have > want ) break;
+            codes.insert(codes.end(), bcodes.begin() + q * S, bcodes.begin() + (q + 1) * S);
+            ++b_cur;
+         }
+         if ( rc ) break;
+         if ( (int)(codes.size() / (size_t)std::max(S, 1)) < clusters )
+         {
+            rc = pm_fail(KINC_SIM_EINVAL, "CCM holds %zu clusters for pair (%d, %d), CMX %d",
+                         codes.size() / (size_t)std::max(S, 1), x, y, clusters);
+            break;
+         }
+      }
+      for ( int k = 0; k < clusters; ++k )
+      {
+         int ns = 0, nmiss = 0, npost = 0, npre = 0, nthr = 0;
+         if ( clusters > 1 )
+         {
+            const int8_t* c = codes.data() + (size_t)k * S;
+            for ( int s2 = 0; s2 < S; ++s2 )
+            {
+               switch ( c[s2] )
+               {
+               case 1: ++ns; break;
+               case 6: ++nthr; break;
+               case 7: ++npre; break;
+               case 8: ++npost; break;
+               case 9: ++nmiss; break;
+               default: break;
+               }
+               mask[(size_t)s2] = (char)('0' + c[s2]);
+            }
+         }
+         else
+         {
+            std::fill(mask.begin(), mask.end(), '0');
+         }
+         const int n = snprintf(line, sizeof line, "%d\t%d\t%d\t%d\t%d\t%d\t%d\t%d\t%d\t%.6g\t", x, y, k, clusters, ns,
+                                nmiss, npost, npre, nthr, (double)r[(size_t)k]);
+         if ( fwrite(line, 1, (size_t)n, out) != (size_t)n || fwrite(mask.data(), 1, mask.size(), out) != mask.size()
+              || fputc('\n', out) == EOF )
+         {
+            rc = pm_fail(KINC_SIM_EINVAL, "write to %s failed", out_path);
+            break;
+         }
+      }
+      i = j;
+   }
+   if ( fclose(out) != 0 && rc == KINC_SIM_OK ) rc = pm_fail(KINC_SIM_EINVAL, "write to %s failed", out_path);
+   kinc_pm_close(cmx);
+   kinc_pm_close(ccm);
+   return rc;
+}
+
 namespace {
 
 /* One of the runner's two result slots: a device block's results, its compacted

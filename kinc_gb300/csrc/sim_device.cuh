@@ -48,6 +48,10 @@ constexpr int SAMPLE_UNROLL = KINC_SAMPLE_UNROLL;   /* unroll factor of the EM s
 #ifndef KINC_PREFETCH
 #define KINC_PREFETCH 8             /* samples ahead the EM / Lloyd sweeps prefetch into L2 (0: none) */
 #endif
+#ifndef KINC_KM_RING
+#define KINC_KM_RING 2              /* samples the Lloyd sweep keeps in flight in registers */
+#endif
+constexpr int KM_RING = KINC_KM_RING;
 #ifndef KINC_UNROLL_SMALL_K
 #define KINC_UNROLL_SMALL_K 0       /* fits with K <= this unroll their sample loops by 2 (more ILP) */
 #endif
@@ -769,11 +773,16 @@ __device__ float kmeans_fit_inits_in_step(const float2* X, int8_t*& cur, int8_t*
             if ( k >= K ) continue;
             s0[k] = 0.f; s1[k] = 0.f; nk[k] = 0;
          }
-         float2 xn = X[0];
+         /* the next KM_RING samples are in flight in registers (N >= min_samples >= 1) */
+         float2 ring[KM_RING];
+#pragma unroll
+         for ( int d = 0; d < KM_RING; ++d ) ring[d] = d < N ? X[d * TILE] : make_float2(0.f, 0.f);
          for ( int i = 0; i < N; ++i )
          {
-            const float2 xv = xn;
-            if ( i + 1 < N ) xn = X[(i + 1) * TILE];
+            const float2 xv = ring[0];
+#pragma unroll
+            for ( int d = 0; d + 1 < KM_RING; ++d ) ring[d] = ring[d + 1];
+            if ( i + KM_RING < N ) ring[KM_RING - 1] = X[(i + KM_RING) * TILE];
             if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N ) prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
             int min_k = -1;
             float min_d = 0.f;

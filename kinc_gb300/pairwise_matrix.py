@@ -67,3 +67,9 @@ def read_emx(path, little_endian=False):
     gem = np.empty((g.value, s.value), np.float32)
     _check(L.kinc_emx_read(str(path).encode(), int(little_endian), gem.ctypes.data_as(ctypes.c_void_p), gem.size))
     return gem
+
+
+def export_text(ccm_path, cmx_path, out_path, little_endian=False):
+    """ExportCorrelationMatrix: the CMX/CCM pair as tab-separated text (one line per CMX cluster)."""
+    _check(_native.load().kinc_pm_export_text(str(ccm_path).encode(), str(cmx_path).encode(), int(little_endian),
+                                              str(out_path).encode()))

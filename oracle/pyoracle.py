@@ -238,3 +238,35 @@ def rand_stream(n, seed=1, skip=0):
     L.ko_rand_seed(ctypes.byref(g), seed)
     L.ko_rand_skip(ctypes.byref(g), skip)
     return np.array([L.ko_rand_next(ctypes.byref(g)) for _ in range(n)], dtype=np.int32)
+
+
+def export_text(cmx, ccm, S):
+    """ExportCorrelationMatrix::process restated (src/core/exportcorrelationmatrix.cpp:17-117) over
+    item dicts as pairwise_matrix.read returns them; returns the text."""
+    lines = []
+    n = len(cmx["x"])
+    ccm_at = {}
+    for q in range(len(ccm["x"])):
+        ccm_at.setdefault((int(ccm["x"][q]), int(ccm["y"][q])), []).append(ccm["payload"][q])
+    i = 0
+    while i < n:
+        x, y = int(cmx["x"][i]), int(cmx["y"][i])
+        j = i
+        while j < n and int(cmx["x"][j]) == x and int(cmx["y"][j]) == y:
+            j += 1
+        size = j - i
+        for k in range(size):
+            r = float(cmx["payload"][i + k][0])
+            counts = {1: 0, 6: 0, 7: 0, 8: 0, 9: 0}
+            if size > 1:
+                codes = ccm_at[(x, y)][k]
+                for c in codes:
+                    if int(c) in counts:
+                        counts[int(c)] += 1
+                mask = "".join(chr(ord("0") + int(c)) for c in codes)
+            else:
+                mask = "0" * S
+            lines.append(f"{x}\t{y}\t{k}\t{size}\t{counts[1]}\t{counts[9]}\t{counts[8]}\t{counts[7]}\t"
+                         f"{counts[6]}\t{'%.6g' % r}\t{mask}\n")
+        i = j
+    return "".join(lines)

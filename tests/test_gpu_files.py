@@ -75,6 +75,11 @@ def test_run_to_files_two_slots_many_device_blocks(tmp_path):
     p = pyoracle.params(clus_method=1, criterion=1, pre_out=1, post_out=1, min_corr=0.3)
     cmx_want, ccm_want = _oracle_items(gem, p, S)
     _check_files(tmp_path / "b.cmx", tmp_path / "b.ccm", cmx_want, ccm_want, S)
+    # the text export of the files equals the export restated over the oracle's items
+    pm.export_text(tmp_path / "b.ccm", tmp_path / "b.cmx", tmp_path / "b.txt")
+    want = pyoracle.export_text(dict(x=cmx_want["x"], y=cmx_want["y"], payload=cmx_want["r"].reshape(-1, 1)),
+                                dict(x=ccm_want["x"], y=ccm_want["y"], payload=ccm_want["codes"].reshape(-1, S)), S)
+    assert (tmp_path / "b.txt").read_text() == want
 
 
 def test_run_to_files_partial_range(tmp_path):

@@ -113,3 +113,50 @@ def test_truncated_expression_matrix(tmp_path, native):
         fh.write(b"\0\0")
     with pytest.raises(_native.SimError, match="truncated EMX header"):
         pm.read_emx(path)
+
+
+@pytest.mark.parametrize("little", [False, True])
+def test_export_text_matches_restatement(tmp_path, native, little):
+    """kinc_pm_export_text equals ExportCorrelationMatrix::process restated over the same files:
+    CCM data only for pairs with more than one CMX cluster, first correlation at %.6g."""
+    from oracle import pyoracle
+    rng = np.random.default_rng(7)
+    genes, maxk, samples = 12, 4, 9
+    xs, ys, cs, codes, corr = [], [], [], [], []
+    mx, my, mc, mcodes = [], [], [], []
+    specials = [1e-5, -0.0, 0.5, 1.0, -0.999999, 123456.7, 3.0e-7]
+    for x in range(1, genes):
+        for y in range(x):
+            k = int(rng.integers(0, maxk + 1))
+            in_ccm = k > 1 or (k == 1 and rng.random() < 0.5)   # a K > 1 pair with one kept cluster
+            for c in range(k):
+                xs.append(x)
+                ys.append(y)
+                cs.append(c)
+                r0 = specials[len(corr) % len(specials)] if rng.random() < 0.2 else rng.uniform(-1, 1)
+                corr.append([r0, rng.uniform(-1, 1)])
+                if in_ccm:
+                    mx.append(x)
+                    my.append(y)
+                    mc.append(c)
+                    mcodes.append(rng.choice([0, 1, 6, 7, 8, 9], size=samples))
+    corr = np.array(corr, np.float32)
+    ccm_path, cmx_path, out = tmp_path / "e.ccm", tmp_path / "e.cmx", tmp_path / "e.txt"
+    pm.write(cmx_path, pm.CMX, genes, maxk, 2, xs, ys, cs, corr, little_endian=little)
+    pm.write(ccm_path, pm.CCM, genes, maxk, samples, mx, my, mc, np.array(mcodes, np.int8).reshape(-1, samples),
+             little_endian=little)
+    pm.export_text(ccm_path, cmx_path, out, little_endian=little)
+    want = pyoracle.export_text(pm.read(cmx_path, pm.CMX, little_endian=little),
+                                pm.read(ccm_path, pm.CCM, little_endian=little), samples)
+    got = out.read_text()
+    assert got == want
+    assert len(got.splitlines()) == len(xs)
+    assert "\t1e-05\t" in got or "\t-0\t" in got or "\t0.5\t" in got
+
+
+def test_export_text_rejects_missing_ccm_pair(tmp_path, native):
+    """A CMX pair with several clusters needs its CCM clusters (the reference would read past them)."""
+    pm.write(tmp_path / "m.cmx", pm.CMX, 5, 3, 1, [2, 2], [1, 1], [0, 1], np.array([[0.9], [0.8]], np.float32))
+    pm.write(tmp_path / "m.ccm", pm.CCM, 5, 3, 4, [3], [0], [0], np.zeros((1, 4), np.int8))
+    with pytest.raises(_native.SimError):
+        pm.export_text(tmp_path / "m.ccm", tmp_path / "m.cmx", tmp_path / "m.txt")
