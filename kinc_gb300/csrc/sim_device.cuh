@@ -69,6 +69,12 @@ constexpr int KM_RING = KINC_KM_RING;
 #else
 #define PARAM_QUAL
 #endif
+/* 1: the E step keeps log(gamma/pi) per sample and component for M1 and the label pass; measured
+ * slower (96k vs 130k pairs/s on GMM k <= 5, 5,000 x 1,000): M1's exps then wait on a load per
+ * component instead of recomputing the log-density from the sample already in a register */
+#ifndef KINC_STORE_LOGGAMMA
+#define KINC_STORE_LOGGAMMA 0
+#endif
 #ifndef KINC_STORE_GAMMA
 #define KINC_STORE_GAMMA 1          /* 1: keep the M1 responsibilities for M2 instead of recomputing them */
 #endif
@@ -460,6 +466,10 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
    constexpr int KA = KT > 0 ? KT : 64;
    constexpr int UF = KT > 0 ? KT : 1;
    constexpr bool STORE_G = KT > 0 && KINC_STORE_GAMMA;
+   /* the E step's log(gamma/pi) in the same buffer: M1 reads it (no second log-density, no log p(x)),
+    * overwrites it with gamma for M2; the label pass reads what is left, exactly the values the
+    * reference's loggamma array holds when EM stops */
+   constexpr bool STORE_V = STORE_G && KINC_STORE_LOGGAMMA;
    constexpr int SU = (KT > 0 && KT <= KINC_UNROLL_SMALL_K) ? 2 : SAMPLE_UNROLL;
    constexpr bool PS = KINC_GMM_PARAMS_SMEM && KT > 0;
    ParamArr<KA, PS> m0(pbuf, 0), m1(pbuf, 1), ia(pbuf, 2), ib(pbuf, 3), ic(pbuf, 4), nrm(pbuf, 5), logpi(pbuf, 6);
@@ -523,13 +533,14 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
          }
          const float logpx = m + kinc_logf(sum);
          logL += logpx;
-         lpx[i * TILE] = logpx;
+         if ( !STORE_V ) lpx[i * TILE] = logpx;
 #pragma unroll UF
          for ( int k = 0; k < KA; ++k )
          {
             if ( k >= K ) continue;
             const float v = lg[k] + (-logpx);
             if ( v > maxG[k] ) maxG[k] = v;
+            if ( STORE_V ) gam[(i * KA + k) * TILE] = v;
          }
       }
       prevL = curL;
@@ -551,7 +562,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
             sG[k] = 0.f; nm0[k] = 0.f; nm1[k] = 0.f;
          }
          xn = X[0];
-         float ln = lpx[0];
+         float ln = STORE_V ? 0.f : lpx[0];
          #pragma unroll SU
          for ( int i = 0; i < N; ++i )
          {
@@ -560,18 +571,31 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
             if ( i + 1 < N )
             {
                xn = X[(i + 1) * TILE];
-               ln = lpx[(i + 1) * TILE];
+               if ( !STORE_V ) ln = lpx[(i + 1) * TILE];
             }
             if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N )
             {
                prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
-               prefetch_l2(&lpx[(i + KINC_PREFETCH) * TILE]);
+               if ( STORE_V )
+               {
+#pragma unroll UF
+                  for ( int k = 0; k < KA; ++k )
+                  {
+                     if ( k >= K ) continue;
+                     prefetch_l2(&gam[((i + KINC_PREFETCH) * KA + k) * TILE]);
+                  }
+               }
+               else
+               {
+                  prefetch_l2(&lpx[(i + KINC_PREFETCH) * TILE]);
+               }
             }
 #pragma unroll UF
             for ( int k = 0; k < KA; ++k )
             {
                if ( k >= K ) continue;
-               const float lgk = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
+               const float lgk = STORE_V ? gam[(i * KA + k) * TILE]
+                                         : log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
                sG[k] += kinc_expf(lgk - maxG[k]);
                const float g = kinc_expf(lgk);
                if ( STORE_G ) gam[(i * KA + k) * TILE] = g;
@@ -692,16 +716,24 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
    float E = 0.f;
    for ( int i = 0; i < N; ++i )
    {
-      const float2 xv = X[i * TILE];
-      const float logpx = lpx[i * TILE];
+      const float2 xv = STORE_V ? make_float2(0.f, 0.f) : X[i * TILE];
+      const float logpx = STORE_V ? 0.f : lpx[i * TILE];
       int max_k = -1;
       float max_g = -INFINITY;
 #pragma unroll UF
       for ( int k = 0; k < KA; ++k )
       {
          if ( k >= K ) continue;
-         float v = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
-         if ( !converged ) v = kinc_expf(v);
+         float v;
+         if ( STORE_V )
+         {
+            v = gam[(i * KA + k) * TILE];   /* log(gamma/pi) if converged, else the last M1's exp of it */
+         }
+         else
+         {
+            v = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
+            if ( !converged ) v = kinc_expf(v);
+         }
          if ( max_g < v )
          {
             max_k = k;
