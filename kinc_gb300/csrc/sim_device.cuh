@@ -929,6 +929,250 @@ __device__ float kmeans_fit_inits_in_step(const float2* X, int8_t*& cur, int8_t*
 /* 1: lane-independent initialisations (below); measured slower on the uneven 10,000 x 4,000 workload
  * (12.8k vs 15.0k pairs/s): the cluster-major log-likelihood pass of a lane that finishes an
  * initialisation then runs divergently beside the other lanes' Lloyd sweeps */
+/* K-means initialisations pipelined across the lanes of a warp (below); 0: in lockstep */
+#ifndef KINC_KMEANS_PIPELINE
+#define KINC_KMEANS_PIPELINE 1
+#endif
+
+/* computeLogLikelihood (pairwise_kmeans.cpp:105-127): one accumulator, cluster-major order */
+template <int KT>
+__device__ __forceinline__ float kmeans_loglik(const float2* X, const int8_t* lab, int N, int K, const float* mu0,
+                                               const float* mu1)
+{
+   constexpr int KA = KT > 0 ? KT : 64;
+   constexpr int UF = KT > 0 ? KT : 1;
+   float S = 0.f;
+   for ( int k = 0; k < K; ++k )
+   {
+      float c0 = 0.f, c1 = 0.f;
+#pragma unroll UF
+      for ( int kk = 0; kk < KA; ++kk )
+      {
+         if ( kk >= K ) continue;
+         if ( kk == k ) { c0 = mu0[kk]; c1 = mu1[kk]; }
+      }
+      for ( int i = 0; i < N; ++i )
+      {
+         if ( lab[i * TILE] != k ) continue;
+         const float2 xv = X[i * TILE];
+         const float d = diff_norm(xv.x, xv.y, c0, c1);
+         S += d * d;
+      }
+   }
+   return -S;
+}
+
+/*
+ * KMeans::fit (pairwise_kmeans.cpp:12-99) with the 10 initialisations of the
+ * warp's lanes pipelined one deep.  A lane whose initialisation has converged
+ * parks its result (labels and means) as "pending" and starts its next
+ * initialisation at once, while slower lanes still iterate; the pending
+ * results' log-likelihoods are computed together, by every lane at the same
+ * time, when each lane holds one (or has nothing left to run).  A lane that
+ * finishes a second initialisation before that waits.  Every lane draws its
+ * means, iterates and compares log-likelihoods in exactly the reference's
+ * order, so its results are those of the lockstep form; only the schedule
+ * changes.  Four label buffers per lane: the running initialisation's two,
+ * the pending one and the best so far (returned in `best`).
+ *
+ * Warp votes use the lanes that entered together (__activemask at entry);
+ * every one of them runs the loop until the same voted exit.
+ */
+template <int KT>
+__device__ float kmeans_fit_pipelined(const float2* X, int8_t*& ya, int8_t*& yb, int8_t*& pl, int8_t*& best,
+                                      int N, int Kr, LaneRng& rng, unsigned long long& units)
+{
+   const int K = (KINC_STATIC_K && KT > 0) ? KT : Kr;
+   constexpr int KA = KT > 0 ? KT : 64;
+   constexpr int UF = KT > 0 ? KT : 1;
+   const unsigned mask = __activemask();
+   float bestLogL = -INFINITY;
+   if ( rng.mode == 1 ) rng.lcg = 1;
+   float mu0[KA], mu1[KA];      /* the running (or held) initialisation's means */
+   float pm0[KA], pm1[KA];      /* the pending initialisation's means */
+   int nprev[KA];
+   int started = 0;             /* initialisations begun */
+   bool running = false;        /* an initialisation is iterating */
+   bool held = false;           /* a finished initialisation waits for the pending one */
+   bool pending = false;
+   bool first = true;
+   int t = 0;
+   int8_t* hl = nullptr;        /* labels of the held initialisation (ya or yb) */
+
+   for ( ;; )
+   {
+      /* start the next initialisation where possible */
+      if ( !running && !held && started < 10 )
+      {
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            const int ii = rng.next() % N;
+            const float2 xv = X[ii * TILE];
+            mu0[k] = xv.x;
+            mu1[k] = xv.y;
+            nprev[k] = -1;
+         }
+         ++started;
+         running = true;
+         first = true;
+         t = 0;
+      }
+      const bool any_running = __any_sync(mask, running);
+      const bool all_ready = __all_sync(mask, pending || (!running && !held && started >= 10));
+      if ( !any_running || all_ready )
+      {
+         /* the pending results, all lanes together, in each lane's initialisation order */
+         if ( __all_sync(mask, !pending && !held && !running && started >= 10) ) break;
+         if ( pending )
+         {
+            const float logL = kmeans_loglik<KT>(X, pl, N, K, pm0, pm1);
+            if ( bestLogL < logL )
+            {
+               bestLogL = logL;
+               int8_t* tmp = best;
+               best = pl;
+               pl = tmp;
+            }
+            pending = false;
+         }
+         if ( held )
+         {
+            /* the held result becomes the pending one; its buffer trades places with the free pending one */
+            int8_t* tmp = pl;
+            pl = hl;
+            if ( hl == ya ) ya = tmp; else yb = tmp;
+#pragma unroll UF
+            for ( int k = 0; k < KA; ++k )
+            {
+               if ( k >= K ) continue;
+               pm0[k] = mu0[k];
+               pm1[k] = mu1[k];
+            }
+            pending = true;
+            held = false;
+         }
+         continue;
+      }
+      if ( !running ) continue;
+
+      /* one Lloyd iteration of the running initialisation (as in kmeans_fit_inits_in_step) */
+      units += (unsigned long long)N * K;
+      float s0[KA], s1[KA];
+      int nk[KA];
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k )
+      {
+         if ( k >= K ) continue;
+         s0[k] = 0.f; s1[k] = 0.f; nk[k] = 0;
+      }
+      float2 ring[KM_RING];
+#pragma unroll
+      for ( int d = 0; d < KM_RING; ++d ) ring[d] = d < N ? X[d * TILE] : make_float2(0.f, 0.f);
+      for ( int i = 0; i < N; ++i )
+      {
+         const float2 xv = ring[0];
+#pragma unroll
+         for ( int d = 0; d + 1 < KM_RING; ++d ) ring[d] = ring[d + 1];
+         if ( i + KM_RING < N ) ring[KM_RING - 1] = X[(i + KM_RING) * TILE];
+         if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N ) prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
+         int min_k = -1;
+         float min_d = 0.f;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            const float d = diff_norm(xv.x, xv.y, mu0[k], mu1[k]);
+            if ( min_k == -1 || d < min_d )
+            {
+               min_k = k;
+               min_d = d;
+            }
+         }
+         yb[i * TILE] = (int8_t)min_k;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            if ( k == min_k )
+            {
+               s0[k] += xv.x;
+               s1[k] += xv.y;
+               nk[k]++;
+            }
+         }
+      }
+      float n0[KA], n1[KA];
+      bool means_same = true;
+#pragma unroll UF
+      for ( int k = 0; k < KA; ++k )
+      {
+         if ( k >= K ) continue;
+         const float sc = 1.0f / nk[k];
+         n0[k] = s0[k] * sc;
+         n1[k] = s1[k] * sc;
+         means_same = means_same && __float_as_uint(n0[k]) == __float_as_uint(mu0[k])
+                      && __float_as_uint(n1[k]) == __float_as_uint(mu1[k]) && nk[k] == nprev[k];
+      }
+      bool same;
+      if ( first )
+      {
+         same = nk[0] == N;
+      }
+      else if ( means_same )
+      {
+         same = true;
+         for ( int i = 0; i < N && same; ++i ) same = ya[i * TILE] == yb[i * TILE];
+      }
+      else
+      {
+         same = false;
+      }
+      bool done = same;
+      int8_t* lab = yb;            /* converged: the unchanged assignment, means unchanged */
+      if ( !same )
+      {
+         int8_t* tmp = ya;
+         ya = yb;
+         yb = tmp;
+         first = false;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            mu0[k] = n0[k];
+            mu1[k] = n1[k];
+            nprev[k] = nk[k];
+         }
+         done = ++t == 300;
+         lab = ya;                 /* ran out: the last assignment, means updated from it */
+      }
+      if ( !done ) continue;
+      running = false;
+      if ( !pending )
+      {
+         int8_t* tmp = pl;
+         pl = lab;
+         if ( lab == ya ) ya = tmp; else yb = tmp;
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            pm0[k] = mu0[k];
+            pm1[k] = mu1[k];
+         }
+         pending = true;
+      }
+      else
+      {
+         held = true;
+         hl = lab;
+      }
+   }
+   return bestLogL;
+}
+
 #ifndef KINC_KMEANS_LANE_INDEPENDENT
 #define KINC_KMEANS_LANE_INDEPENDENT 0
 #endif

@@ -151,7 +151,11 @@ __device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, fl
    {
       return gmm_fit<KT>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units, pbuf);
    }
+#if KINC_KMEANS_PIPELINE
+   logL = kmeans_fit_pipelined<KT>(X, ya, yb, wl, yc, N, K, rng, units);
+#else
    logL = kmeans_fit<KT>(X, ya, yb, yc, N, K, rng, units);
+#endif
    E = 0.f;
    int8_t* t = wl;   /* the best labels become the work labels */
    wl = yc;
