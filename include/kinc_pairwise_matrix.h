@@ -81,6 +81,18 @@ int kinc_emx_read(const char* path, int32_t little_endian, float* gem, int64_t c
  */
 int kinc_pm_export_text(const char* ccm_path, const char* cmx_path, int32_t little_endian, const char* out_path);
 
+/*
+ * Extract (src/core/extract.cpp:24-274): the co-expression network of the CMX clusters whose first
+ * correlation r has min_corr <= |r| <= max_corr (the reference's defaults: 0.85, 1.0), written as
+ * a tab-separated edge list (tsv_path) and as GraphML (graphml_path); either may be NULL.
+ * Multi-cluster pairs take their code counts and sample mask from the CCM; single-cluster pairs
+ * take the mask from the EMX ('9' where either gene is NaN, else '1').  names_path: one gene name
+ * per line (NULL: the gene indices).
+ */
+int kinc_pm_extract(const char* emx_path, const char* ccm_path, const char* cmx_path, const char* names_path,
+                    int32_t little_endian, float min_corr, float max_corr, const char* tsv_path,
+                    const char* graphml_path);
+
 /* Message of the last failed kinc_pm_* / kinc_emx_* / kinc_sim_run_to_files call on this thread. */
 const char* kinc_pm_last_error(void);
 

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -526,6 +527,224 @@ extern "C" int kinc_pm_export_text(const char* ccm_path, const char* cmx_path, i
    if ( fclose(out) != 0 && rc == KINC_SIM_OK ) rc = pm_fail(KINC_SIM_EINVAL, "write to %s failed", out_path);
    kinc_pm_close(cmx);
    kinc_pm_close(ccm);
+   return rc;
+}
+
+/*
+ * Extract::process (src/core/extract.cpp:24-274): the network of the clusters whose first
+ * correlation r has mincorr <= |r| <= maxcorr, as a tab-separated edge list (header line, then
+ * "source target r co cluster clusters samples missing postOutliers preOutliers threshold mask")
+ * and as GraphML (every gene a node, every kept cluster an undirected edge with its sample
+ * mask).  Multi-cluster pairs take counts and mask from the CCM; single-cluster pairs take the
+ * mask from the expression matrix ('9' where either gene is NaN, else '1') and zero counts, as
+ * the reference does.  Gene names are read from names_path (one per line) when given, else the
+ * gene indices are the names.  Both outputs come from one walk over the CMX.
+ */
+extern "C" int kinc_pm_extract(const char* emx_path, const char* ccm_path, const char* cmx_path,
+                               const char* names_path, int32_t little_endian, float min_corr, float max_corr,
+                               const char* tsv_path, const char* graphml_path)
+{
+   if ( !emx_path || !ccm_path || !cmx_path || (!tsv_path && !graphml_path) )
+      return pm_fail(KINC_SIM_EINVAL, "Did not get valid input and/or output arguments.");
+   int32_t G = 0, S = 0;
+   int rc = kinc_emx_read_header(emx_path, little_endian, &G, &S);
+   if ( rc ) return rc;
+   std::vector<float> gem((size_t)G * S);
+   if ( (rc = kinc_emx_read(emx_path, little_endian, gem.data(), (int64_t)gem.size())) ) return rc;
+   std::vector<std::string> names((size_t)G);
+   if ( names_path )
+   {
+      FILE* nf = fopen(names_path, "rb");
+      if ( !nf ) return pm_fail(KINC_SIM_EINVAL, "cannot open %s", names_path);
+      std::string cur;
+      int32_t n = 0;
+      for ( int ch; (ch = fgetc(nf)) != EOF; )
+      {
+         if ( ch == '\n' )
+         {
+            if ( !cur.empty() && cur.back() == '\r' ) cur.pop_back();
+            if ( n < G ) names[(size_t)n] = cur;
+            ++n;
+            cur.clear();
+         }
+         else
+         {
+            cur.push_back((char)ch);
+         }
+      }
+      if ( !cur.empty() )
+      {
+         if ( n < G ) names[(size_t)n] = cur;
+         ++n;
+      }
+      fclose(nf);
+      if ( n != G ) return pm_fail(KINC_SIM_EINVAL, "%s holds %d names for %d genes", names_path, n, G);
+   }
+   else
+   {
+      for ( int32_t g = 0; g < G; ++g ) names[(size_t)g] = std::to_string(g);
+   }
+
+   kinc_pm *cmx = nullptr, *ccm = nullptr;
+   int32_t g1 = 0, k1 = 0, nc = 0, g2 = 0, k2 = 0, S2 = 0;
+   int64_t p1 = 0, n_cmx = 0, p2 = 0, n_ccm = 0;
+   if ( (rc = kinc_pm_open(cmx_path, KINC_PM_CMX, little_endian, &cmx, &g1, &k1, &nc, &p1, &n_cmx)) ) return rc;
+   if ( (rc = kinc_pm_open(ccm_path, KINC_PM_CCM, little_endian, &ccm, &g2, &k2, &S2, &p2, &n_ccm)) )
+   {
+      kinc_pm_close(cmx);
+      return rc;
+   }
+   if ( g1 != G || g2 != G || S2 != S )
+   {
+      kinc_pm_close(cmx);
+      kinc_pm_close(ccm);
+      return pm_fail(KINC_SIM_EINVAL, "EMX %d x %d, CMX %d genes, CCM %d genes x %d samples do not match", G, S, g1, g2,
+                     S2);
+   }
+   FILE* tsv = tsv_path ? fopen(tsv_path, "wb") : nullptr;
+   FILE* gml = graphml_path ? fopen(graphml_path, "wb") : nullptr;
+   if ( (tsv_path && !tsv) || (graphml_path && !gml) )
+   {
+      if ( tsv ) fclose(tsv);
+      if ( gml ) fclose(gml);
+      kinc_pm_close(cmx);
+      kinc_pm_close(ccm);
+      return pm_fail(KINC_SIM_EINVAL, "cannot open the output files");
+   }
+   std::vector<char> tb(1 << 22), gb(1 << 22);
+   if ( tsv ) setvbuf(tsv, tb.data(), _IOFBF, tb.size());
+   if ( gml ) setvbuf(gml, gb.data(), _IOFBF, gb.size());
+   bool io_ok = true;
+   auto put = [&](FILE* f, const std::string& str) {
+      if ( f && fwrite(str.data(), 1, str.size(), f) != str.size() ) io_ok = false;
+   };
+   put(tsv, "Source\tTarget\tsc\tInteraction\tCluster\tNum_Clusters\tCluster_Samples\tMissing_Samples\t"
+            "Cluster_Outliers\tPair_Outliers\tToo_Low\tSamples\n");
+   put(gml, "<?xml version=\"1.0\" encoding=\"UTF-8\"?>\n"
+            "<graphml xmlns=\"http://graphml.graphdrawing.org/xmlns\"\n"
+            "    xmlns:xsi=\"http://www.w3.org/2001/XMLSchema-instance\"\n"
+            "    xsi:schemaLocation=\"http://graphml.graphdrawing.org/xmlns/1.0/graphml.xsd\">\n"
+            "  <graph id=\"G\" edgedefault=\"undirected\">\n");
+   for ( int32_t g = 0; g < G && gml; ++g ) put(gml, "    <node id=\"" + names[(size_t)g] + "\"/>\n");
+
+   constexpr int64_t CHUNK = 1 << 16;
+   std::vector<int32_t> ax(CHUNK), ay(CHUNK), bx(CHUNK), by(CHUNK);
+   std::vector<int8_t> ac(CHUNK), bc(CHUNK), bcodes((size_t)CHUNK * S);
+   std::vector<float> ar((size_t)CHUNK * nc);
+   int64_t a_base = 0, a_len = 0, b_base = 0, b_len = 0, b_cur = 0;
+   std::vector<int8_t> codes;
+   std::string mask((size_t)S, '0');
+   char num[64];
+   auto pair_of = [](int32_t x, int32_t y) { return (int64_t)x * (x - 1) / 2 + y; };
+   auto at = [&](int64_t q) -> int64_t {
+      if ( q < a_base || q >= a_base + a_len )
+      {
+         a_base = q;
+         a_len = std::min<int64_t>(CHUNK, n_cmx - q);
+         if ( kinc_pm_read_items(cmx, q, a_len, ax.data(), ay.data(), ac.data(), ar.data()) ) return -1;
+      }
+      return q - a_base;
+   };
+
+   int64_t i = 0;
+   while ( rc == KINC_SIM_OK && io_ok && i < n_cmx )
+   {
+      int64_t o = at(i);
+      if ( o < 0 ) { rc = KINC_SIM_EINVAL; break; }
+      const int32_t x = ax[o], y = ay[o];
+      if ( x >= G || y >= G ) { rc = pm_fail(KINC_SIM_EINVAL, "pair (%d, %d) outside %d genes", x, y, G); break; }
+      std::vector<float> r;
+      int64_t j = i;
+      while ( j < n_cmx )
+      {
+         const int64_t q = at(j);
+         if ( q < 0 ) { rc = KINC_SIM_EINVAL; break; }
+         if ( ax[q] != x || ay[q] != y ) break;
+         r.push_back(ar[(size_t)q * nc]);
+         ++j;
+      }
+      if ( rc ) break;
+      const int clusters = (int)(j - i);
+      codes.clear();
+      if ( clusters > 1 )
+      {
+         const int64_t want = pair_of(x, y);
+         for ( ;; )
+         {
+            if ( b_cur >= n_ccm ) break;
+            if ( b_cur < b_base || b_cur >= b_base + b_len )
+            {
+               b_base = b_cur;
+               b_len = std::min<int64_t>(CHUNK, n_ccm - b_cur);
+               if ( (rc = kinc_pm_read_items(ccm, b_base, b_len, bx.data(), by.data(), bc.data(), bcodes.data())) ) break;
+            }
+            const int64_t q = b_cur - b_base;
+            const int64_t have = pair_of(bx[q], by[q]);
+            if ( have < want ) { ++b_cur; continue; }
+            if ( have > want ) break;
+            codes.insert(codes.end(), bcodes.begin() + q * S, bcodes.begin() + (q + 1) * S);
+            ++b_cur;
+         }
+         if ( rc ) break;
+         if ( (int)(codes.size() / (size_t)std::max(S, 1)) < clusters )
+         {
+            rc = pm_fail(KINC_SIM_EINVAL, "CCM holds %zu clusters for pair (%d, %d), CMX %d",
+                         codes.size() / (size_t)std::max(S, 1), x, y, clusters);
+            break;
+         }
+      }
+      for ( int k = 0; k < clusters; ++k )
+      {
+         const float corr = r[(size_t)k];
+         if ( fabsf(corr) < min_corr || max_corr < fabsf(corr) ) continue;
+         int ns = 0, nmiss = 0, npost = 0, npre = 0, nthr = 0;
+         if ( clusters > 1 )
+         {
+            const int8_t* c = codes.data() + (size_t)k * S;
+            for ( int s2 = 0; s2 < S; ++s2 )
+            {
+               switch ( c[s2] )
+               {
+               case 1: ++ns; break;
+               case 6: ++nthr; break;
+               case 7: ++npre; break;
+               case 8: ++npost; break;
+               case 9: ++nmiss; break;
+               default: break;
+               }
+               mask[(size_t)s2] = (char)('0' + c[s2]);
+            }
+         }
+         else
+         {
+            const float* gx = gem.data() + (size_t)x * S;
+            const float* gy = gem.data() + (size_t)y * S;
+            for ( int s2 = 0; s2 < S; ++s2 ) mask[(size_t)s2] = (std::isnan(gx[s2]) || std::isnan(gy[s2])) ? '9' : '1';
+         }
+         const std::string& src = names[(size_t)x];
+         const std::string& dst = names[(size_t)y];
+         if ( tsv )
+         {
+            snprintf(num, sizeof num, "%.6g", (double)corr);
+            std::string line;
+            line.reserve(96 + src.size() + dst.size() + (size_t)S);
+            line += src; line += '\t'; line += dst; line += '\t'; line += num; line += "\tco\t";
+            line += std::to_string(k); line += '\t'; line += std::to_string(clusters); line += '\t';
+            line += std::to_string(ns); line += '\t'; line += std::to_string(nmiss); line += '\t';
+            line += std::to_string(npost); line += '\t'; line += std::to_string(npre); line += '\t';
+            line += std::to_string(nthr); line += '\t'; line += mask; line += '\n';
+            put(tsv, line);
+         }
+         if ( gml ) put(gml, "    <edge source=\"" + src + "\" target=\"" + dst + "\" samples=\"" + mask + "\"/>\n");
+      }
+      i = j;
+   }
+   put(gml, "  </graph>\n</graphml>\n");
+   if ( tsv && fclose(tsv) != 0 ) io_ok = false;
+   if ( gml && fclose(gml) != 0 ) io_ok = false;
+   kinc_pm_close(cmx);
+   kinc_pm_close(ccm);
+   if ( rc == KINC_SIM_OK && !io_ok ) rc = pm_fail(KINC_SIM_EINVAL, "writing the network files failed");
    return rc;
 }
 

@@ -73,3 +73,12 @@ def export_text(ccm_path, cmx_path, out_path, little_endian=False):
     """ExportCorrelationMatrix: the CMX/CCM pair as tab-separated text (one line per CMX cluster)."""
     _check(_native.load().kinc_pm_export_text(str(ccm_path).encode(), str(cmx_path).encode(), int(little_endian),
                                               str(out_path).encode()))
+
+
+def extract(emx_path, ccm_path, cmx_path, tsv_path=None, graphml_path=None, names_path=None, min_corr=0.85,
+            max_corr=1.0, little_endian=False):
+    """Extract: the network of clusters with min_corr <= |r| <= max_corr as TSV and/or GraphML."""
+    enc = lambda p: str(p).encode() if p is not None else None  # noqa: E731
+    _check(_native.load().kinc_pm_extract(enc(emx_path), enc(ccm_path), enc(cmx_path), enc(names_path),
+                                          int(little_endian), float(min_corr), float(max_corr), enc(tsv_path),
+                                          enc(graphml_path)))

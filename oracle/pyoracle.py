@@ -270,3 +270,49 @@ def export_text(cmx, ccm, S):
                          f"{counts[6]}\t{'%.6g' % r}\t{mask}\n")
         i = j
     return "".join(lines)
+
+
+def extract_network(gem, cmx, ccm, S, names=None, min_corr=0.85, max_corr=1.0):
+    """Extract::process restated (src/core/extract.cpp:24-274) over item dicts as
+    pairwise_matrix.read returns them; returns (tsv text, graphml text)."""
+    G = gem.shape[0]
+    names = [str(g) for g in range(G)] if names is None else list(names)
+    lo, hi = np.float32(min_corr), np.float32(max_corr)
+    tsv = ["Source\tTarget\tsc\tInteraction\tCluster\tNum_Clusters\tCluster_Samples\tMissing_Samples\t"
+           "Cluster_Outliers\tPair_Outliers\tToo_Low\tSamples\n"]
+    gml = ['<?xml version="1.0" encoding="UTF-8"?>\n',
+           '<graphml xmlns="http://graphml.graphdrawing.org/xmlns"\n',
+           '    xmlns:xsi="http://www.w3.org/2001/XMLSchema-instance"\n',
+           '    xsi:schemaLocation="http://graphml.graphdrawing.org/xmlns/1.0/graphml.xsd">\n',
+           '  <graph id="G" edgedefault="undirected">\n']
+    gml += [f'    <node id="{names[g]}"/>\n' for g in range(G)]
+    ccm_at = {}
+    for q in range(len(ccm["x"])):
+        ccm_at.setdefault((int(ccm["x"][q]), int(ccm["y"][q])), []).append(ccm["payload"][q])
+    n = len(cmx["x"])
+    i = 0
+    while i < n:
+        x, y = int(cmx["x"][i]), int(cmx["y"][i])
+        j = i
+        while j < n and int(cmx["x"][j]) == x and int(cmx["y"][j]) == y:
+            j += 1
+        size = j - i
+        for k in range(size):
+            r = np.float32(cmx["payload"][i + k][0])
+            if abs(r) < lo or hi < abs(r):
+                continue
+            counts = {1: 0, 6: 0, 7: 0, 8: 0, 9: 0}
+            if size > 1:
+                codes = ccm_at[(x, y)][k]
+                for c in codes:
+                    if int(c) in counts:
+                        counts[int(c)] += 1
+                mask = "".join(chr(ord("0") + int(c)) for c in codes)
+            else:
+                mask = "".join("9" if (np.isnan(gem[x, s]) or np.isnan(gem[y, s])) else "1" for s in range(S))
+            tsv.append(f"{names[x]}\t{names[y]}\t{'%.6g' % float(r)}\tco\t{k}\t{size}\t{counts[1]}\t{counts[9]}\t"
+                       f"{counts[8]}\t{counts[7]}\t{counts[6]}\t{mask}\n")
+            gml.append(f'    <edge source="{names[x]}" target="{names[y]}" samples="{mask}"/>\n')
+        i = j
+    gml.append("  </graph>\n</graphml>\n")
+    return "".join(tsv), "".join(gml)

@@ -80,6 +80,15 @@ def test_run_to_files_two_slots_many_device_blocks(tmp_path):
     want = pyoracle.export_text(dict(x=cmx_want["x"], y=cmx_want["y"], payload=cmx_want["r"].reshape(-1, 1)),
                                 dict(x=ccm_want["x"], y=ccm_want["y"], payload=ccm_want["codes"].reshape(-1, S)), S)
     assert (tmp_path / "b.txt").read_text() == want
+    # the extracted network (clusters with |r| >= 0.5) equals Extract restated over the oracle's items
+    pm.write_emx(tmp_path / "b.emx", gem)
+    pm.extract(tmp_path / "b.emx", tmp_path / "b.ccm", tmp_path / "b.cmx", tsv_path=tmp_path / "b.tsv",
+               graphml_path=tmp_path / "b.graphml", min_corr=0.5)
+    want_tsv, want_gml = pyoracle.extract_network(
+        gem, dict(x=cmx_want["x"], y=cmx_want["y"], payload=cmx_want["r"].reshape(-1, 1)),
+        dict(x=ccm_want["x"], y=ccm_want["y"], payload=ccm_want["codes"].reshape(-1, S)), S, min_corr=0.5)
+    assert (tmp_path / "b.tsv").read_text() == want_tsv
+    assert (tmp_path / "b.graphml").read_text() == want_gml
 
 
 def test_run_to_files_partial_range(tmp_path):

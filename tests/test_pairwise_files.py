@@ -160,3 +160,42 @@ def test_export_text_rejects_missing_ccm_pair(tmp_path, native):
     pm.write(tmp_path / "m.ccm", pm.CCM, 5, 3, 4, [3], [0], [0], np.zeros((1, 4), np.int8))
     with pytest.raises(_native.SimError):
         pm.export_text(tmp_path / "m.ccm", tmp_path / "m.cmx", tmp_path / "m.txt")
+
+
+@pytest.mark.parametrize("named", [False, True])
+def test_extract_matches_restatement(tmp_path, native, named):
+    """kinc_pm_extract writes the TSV edge list and the GraphML that Extract::process restated
+    writes from the same EMX/CCM/CMX: threshold on the first correlation, CCM counts and mask for
+    multi-cluster pairs, EMX missing-value mask for single-cluster pairs."""
+    from oracle import pyoracle
+    rng = np.random.default_rng(11)
+    genes, maxk, samples = 14, 4, 10
+    gem = (8 + 2 * rng.standard_normal((genes, samples))).astype(np.float32)
+    gem[rng.random(gem.shape) < 0.2] = np.nan
+    xs, ys, cs, corr, mx, my, mc, mcodes = [], [], [], [], [], [], [], []
+    for x in range(1, genes):
+        for y in range(x):
+            k = int(rng.integers(0, maxk + 1))
+            for c in range(k):
+                xs.append(x); ys.append(y); cs.append(c)
+                corr.append([rng.choice([0.85, -0.85, 0.9, -0.99, 1.0, 0.5, 0.84999996]), rng.uniform(-1, 1)])
+                if k > 1:
+                    mx.append(x); my.append(y); mc.append(c)
+                    mcodes.append(rng.choice([0, 1, 6, 7, 8, 9], size=samples))
+    corr = np.array(corr, np.float32)
+    emx, ccm_path, cmx_path = tmp_path / "g.emx", tmp_path / "g.ccm", tmp_path / "g.cmx"
+    pm.write_emx(emx, gem)
+    pm.write(cmx_path, pm.CMX, genes, maxk, 2, xs, ys, cs, corr)
+    pm.write(ccm_path, pm.CCM, genes, maxk, samples, mx, my, mc, np.array(mcodes, np.int8).reshape(-1, samples))
+    names = [f"gene_{g:03d}" for g in range(genes)] if named else None
+    names_path = None
+    if named:
+        names_path = tmp_path / "names.txt"
+        names_path.write_text("\n".join(names) + "\n")
+    pm.extract(emx, ccm_path, cmx_path, tsv_path=tmp_path / "n.tsv", graphml_path=tmp_path / "n.graphml",
+               names_path=names_path)
+    want_tsv, want_gml = pyoracle.extract_network(gem, pm.read(cmx_path, pm.CMX), pm.read(ccm_path, pm.CCM), samples,
+                                                  names=names)
+    assert (tmp_path / "n.tsv").read_text() == want_tsv
+    assert (tmp_path / "n.graphml").read_text() == want_gml
+    assert want_tsv.count("\n") > 5
