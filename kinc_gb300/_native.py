@@ -26,6 +26,17 @@ class SimParams(ctypes.Structure):
                 ("semantics", ctypes.c_int32), ("rand_mode", ctypes.c_int32), ("precision", ctypes.c_int32)]
 
 
+class RmtParams(ctypes.Structure):
+    """kinc_rmt_params (include/kinc_rmt.h)."""
+    _fields_ = [("threshold_start", ctypes.c_float), ("threshold_step", ctypes.c_float),
+                ("threshold_stop", ctypes.c_float), ("chi_square_threshold1", ctypes.c_float),
+                ("chi_square_threshold2", ctypes.c_float), ("min_eigenvalue_size", ctypes.c_int32),
+                ("min_unfolding_pace", ctypes.c_int32), ("max_unfolding_pace", ctypes.c_int32),
+                ("histogram_bin_size", ctypes.c_int32)]
+
+
+RMT_ENOTHRESHOLD, RMT_ESPLINE = 6, 7
+
 # name -> (restype, argtypes); every symbol include/kinc_sim.h declares
 _VP = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -68,6 +79,16 @@ SIGNATURES = {
     "kinc_emx_read": (ctypes.c_int, [ctypes.c_char_p, _I32, _VP, _I64]),
     "kinc_pm_last_error": (ctypes.c_char_p, []),
     "kinc_sim_run_to_files": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_char_p, _I32, _I64, _I64]),
+    "kinc_rmt_params_default": (None, [ctypes.POINTER(RmtParams)]),
+    "kinc_rmt_run_items": (ctypes.c_int, [_I32, _I32, _I64, _VP, _VP, _VP, _VP, ctypes.POINTER(RmtParams),
+                                           ctypes.c_char_p, ctypes.POINTER(ctypes.c_float), _VP, _I32,
+                                           ctypes.POINTER(_I32)]),
+    "kinc_rmt_run": (ctypes.c_int, [ctypes.c_char_p, _I32, ctypes.POINTER(RmtParams), ctypes.c_char_p,
+                                     ctypes.POINTER(ctypes.c_float)]),
+    "kinc_rmt_chi_square": (ctypes.c_int, [_VP, _I32, ctypes.POINTER(RmtParams), ctypes.POINTER(ctypes.c_float)]),
+    "kinc_rmt_prune_eigenvalues": (ctypes.c_int, [_I32, _I32, _I64, _VP, _VP, _VP, _VP, ctypes.c_float, _VP,
+                                                   ctypes.POINTER(_I32)]),
+    "kinc_rmt_last_error": (ctypes.c_char_p, []),
     "kinc_pm_extract": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _I32,
                                         ctypes.c_float, ctypes.c_float, ctypes.c_char_p, ctypes.c_char_p]),
     "kinc_pm_export_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _I32, ctypes.c_char_p]),

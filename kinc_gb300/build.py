@@ -29,6 +29,7 @@ UNITS = [
     ("pearson_gemm.cu", []),
     ("compact.cu", []),
     ("pairwise_file.cpp", []),
+    ("rmt.cu", []),
 ]
 
 
@@ -76,7 +77,7 @@ def build(force=False, verbose=False):
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         objs = list(ex.map(run, jobs))
     tmp = LIB + ".tmp"
-    subprocess.check_call([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"])
+    subprocess.check_call([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lcusolver"])
     os.replace(tmp, LIB)
     return LIB
 

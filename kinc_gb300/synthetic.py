@@ -89,3 +89,25 @@ def generate(workload, scale=1.0, genes=None, samples=None, seed=None):
     else:
         raise ValueError(f"unknown workload {workload}")
     return np.ascontiguousarray(gem, dtype=np.float32)
+
+
+def clique_network(blocks, size, seed=20260106, eps=0.002, mid_grid=0.01):
+    """A correlation network of `blocks` cliques of `size` genes for the RMT analytic: every pair of a
+    clique correlates at the clique's level (a value half-way between two points of a 0.01 threshold
+    grid, 0.985 down to 0.695) plus uniform noise of +-eps, so a threshold of that grid keeps or drops
+    whole cliques and the pruned matrices stay positive definite.  Returns (genes, x, y, c, r) CMX
+    items in pair order (x > y), one cluster per pair."""
+    rng = np.random.default_rng(seed)
+    levels = 0.985 - mid_grid * rng.integers(0, 30, blocks)
+    xs, ys, rs = [], [], []
+    for b in range(blocks):
+        base = b * size
+        for a in range(1, size):
+            for c in range(a):
+                xs.append(base + a)
+                ys.append(base + c)
+                rs.append(levels[b] + rng.uniform(-eps, eps))
+    xs, ys = np.array(xs, np.int32), np.array(ys, np.int32)
+    order = np.lexsort((ys, xs))
+    return (blocks * size, xs[order], ys[order], np.zeros(len(xs), np.int8),
+            np.array(rs, np.float32)[order])

@@ -316,3 +316,126 @@ def extract_network(gem, cmx, ccm, S, names=None, min_corr=0.85, max_corr=1.0):
         i = j
     gml.append("  </graph>\n</graphml>\n")
     return "".join(tsv), "".join(gml)
+
+
+# ----------------------------------------------------------------------------- RMT
+# RMT::process and its helpers restated (src/core/rmt.cpp:33-122,164-439) with numpy:
+# the dense pruned matrix, LAPACK's symmetric eigensolver (numpy.linalg.eigvalsh on
+# the lower triangle, double), scipy's Akima spline for the unfolding, float32 where
+# the reference keeps floats.
+
+RMT_DEFAULTS = dict(threshold_start=0.99, threshold_step=0.001, threshold_stop=0.5, chi_square_threshold1=99.607,
+                    chi_square_threshold2=200.0, min_eigenvalue_size=50, min_unfolding_pace=10,
+                    max_unfolding_pace=40, histogram_bin_size=60)
+
+
+class RMTSplineError(ValueError):
+    """The unfolding spline got knots that do not increase (the reference's spline library rejects them)."""
+
+
+def rmt_dense(G, K, x, y, c, r):
+    """CorrelationMatrix::dumpRawData (src/core/correlationmatrix.cpp:144-177): [G][G][K], zeros elsewhere."""
+    m = np.zeros((G, G, K), np.float32)
+    m[x, y, c] = r
+    m[y, x, c] = r
+    return m
+
+
+def rmt_maximums(mat):
+    """computeMaximums: per (gene, cluster) the largest |r| over the other genes (0 when none)."""
+    a = np.abs(mat)
+    a = np.where(np.isnan(a), 0, a)
+    return a.max(axis=1).reshape(-1)
+
+
+def rmt_prune_eigenvalues(mat, maximums, threshold):
+    """computePruneMatrix + computeEigenvalues: eigenvalues sorted by ascending |lambda|, as float32."""
+    G, _, K = mat.shape
+    t = np.float32(threshold)
+    idx = np.nonzero(maximums >= t)[0]
+    m = len(idx)
+    if m == 0:
+        return np.zeros(0, np.float32)
+    P = np.zeros((m, m), np.float64)
+    gi, ki = idx // K, idx % K
+    for i in range(m):
+        js = np.arange(i)
+        same = ki[js] == ki[i]
+        js = js[same]
+        v = mat[gi[i], gi[js], ki[i]]
+        keep = np.abs(v) >= t
+        P[i, js[keep]] = v[keep]
+        P[i, i] = 1.0
+    w = np.linalg.eigvalsh(P, UPLO="L")
+    order = np.argsort(np.abs(w), kind="stable")
+    return w[order].astype(np.float32)
+
+
+def rmt_chi_square(eigens, p):
+    """computeChiSquare / computePaceChiSquare / degenerate / unfold; -1 with too few unique values."""
+    from scipy.interpolate import Akima1DInterpolator
+    e = [np.float32(v) for v in eigens]
+    uniq = []
+    for i in range(1, len(e)):
+        if not uniq or abs(np.float32(e[i] - uniq[-1])) > np.float32(1e-6):
+            uniq.append(e[i])
+    n = len(uniq)
+    if n < p["min_eigenvalue_size"]:
+        return np.float32(-1)
+    chi, count = np.float32(0), 0
+    bins = p["histogram_bin_size"]
+    w = np.float32(np.float32(3.0) / np.float32(bins))
+    for pace in range(p["min_unfolding_pace"], p["max_unfolding_pace"] + 1):
+        if n // pace < 5:
+            break
+        ns = n // pace
+        xs = np.array([float(uniq[i * pace]) for i in range(ns)])
+        ys = np.array([(i * pace + 1) / n for i in range(ns)])
+        xs[-1] = float(uniq[-1])
+        ys[-1] = 1.0
+        if np.any(np.diff(xs) <= 0):
+            raise RMTSplineError(f"unfolding at pace {pace}: eigenvalues not increasing in |lambda| order")
+        spline = Akima1DInterpolator(xs, ys)
+        se = np.zeros(n, np.float32)
+        se[-1] = 1.0
+        se[1:-1] = spline(np.array([float(v) for v in uniq[1:-1]])).astype(np.float32)
+        spacings = (se[1:] - se[:-1]) * np.float32(n)
+        hist = np.zeros(bins, np.float32)
+        for s in spacings:
+            if np.float32(0) <= s < np.float32(3):
+                b = int(np.float32(s / w))
+                if b < bins:
+                    hist[b] += 1
+        c = np.float32(0)
+        for i in range(bins):
+            E = np.float32((np.exp(np.float32(-i * w)) - np.exp(np.float32(-(i + 1) * w))) * np.float32(n))
+            c = np.float32(c + np.float32((hist[i] - E) * (hist[i] - E)) / E)
+        chi = np.float32(chi + c)
+        count += 1
+    return np.float32(chi / np.float32(count))
+
+
+def rmt_run(G, K, x, y, c, r, **kw):
+    """RMT::process: returns (threshold or None when no threshold above tstop passes, steps)."""
+    p = dict(RMT_DEFAULTS)
+    p.update(kw)
+    mat = rmt_dense(G, K, np.asarray(x), np.asarray(y), np.asarray(c), np.asarray(r, np.float32))
+    maxs = rmt_maximums(mat)
+    final_t, final_chi, max_chi = np.float32(0), np.float32(np.inf), np.float32(-np.inf)
+    t = np.float32(p["threshold_start"])
+    steps = []
+    while max_chi < np.float32(p["chi_square_threshold2"]):
+        e = rmt_prune_eigenvalues(mat, maxs, t)
+        chi = np.float32(-1)
+        if len(e) > 0:
+            chi = rmt_chi_square(e, p)
+        if chi != np.float32(-1):
+            if chi < np.float32(p["chi_square_threshold1"]):
+                final_chi, final_t = chi, t
+            if final_chi < np.float32(p["chi_square_threshold1"]) and chi > final_chi:
+                max_chi = chi
+        steps.append((float(t), len(e), float(chi)))
+        t = np.float32(t - np.float32(p["threshold_step"]))
+        if t < np.float32(p["threshold_stop"]):
+            return None, steps
+    return float(final_t), steps
