@@ -359,6 +359,40 @@ def stream_leg(device_block, nblk):
                         "overlapped with the next block, CCM/CMX file writes"}
 
 
+def rmt_leg(blocks=1000, size=5, cpu=True):
+    """RMT thresholding (include/kinc_rmt.h) with the reference's defaults except a 0.01 threshold step,
+    on a clique network of blocks x size genes (kinc_gb300.synthetic.clique_network): pruned matrices
+    grow to a few thousand rows before the spacing test finds the threshold.  GPU wall clock of the
+    whole analytic (pruned matrices in HBM, cuSOLVER eigenvalues, host unfolding) beside the oracle
+    (numpy eigensolver, scipy spline) on the host cores, with the step sequences compared."""
+    from kinc_gb300 import synthetic
+    from kinc_gb300.rmt import RMT
+    G, x, y, c, r = synthetic.clique_network(blocks, size)
+    rmt = RMT(tstep=0.01)
+    rmt.run(items=(x, y, c, r), genes=G, max_clusters=1, strict=False)      # warm-up (solver, allocations)
+    t0 = time.perf_counter()
+    thr, steps = rmt.run(items=(x, y, c, r), genes=G, max_clusters=1, strict=False)
+    secs = time.perf_counter() - t0
+    out = {"workload": f"RMT, clique network of {G} genes ({blocks} cliques of {size}), {len(r)} CMX items, "
+                       "tstep 0.01, other arguments at the reference's defaults",
+           "seconds": secs, "steps": int(len(steps)), "largest_pruned_matrix": int(steps[:, 1].max()),
+           "threshold": thr}
+    if cpu:
+        from oracle import pyoracle
+        t0 = time.perf_counter()
+        want_t, want_steps = pyoracle.rmt_run(G, 1, x, y, c, r, threshold_step=0.01)
+        csecs = time.perf_counter() - t0
+        dchi = max((abs(float(a[2]) - b[2]) for a, b in zip(steps, want_steps)), default=0.0)
+        out["cpu_baseline"] = {"seconds": csecs, "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": "the whole analytic: numpy (LAPACK) eigensolver, scipy Akima unfolding"}
+        out["gpu_over_cpu"] = csecs / secs
+        out["parity"] = {"same_threshold": (want_t is None and thr is None)
+                         or (want_t is not None and thr is not None and np.float32(want_t) == np.float32(thr)),
+                         "same_sizes": [int(a[1]) for a in steps] == [b[1] for b in want_steps],
+                         "max_abs_dchi": dchi}
+    return out
+
+
 def config_dict(args, gem):
     G, S = gem.shape
     return {"workload": "GMM k<=5 + Spearman, GEM 5000x1000 float32, 10% NaN, 10 planted modules; "
@@ -381,6 +415,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-dense", action="store_true")
     ap.add_argument("--no-kmeans", action="store_true")
+    ap.add_argument("--no-rmt", action="store_true")
     ap.add_argument("--dense-check-pairs", type=int, default=1000000)
     ap.add_argument("--stream-blocks", type=int, default=2,
                     help="device blocks of 2^22 pairs in the streamed 30000x500 leg (0 = skip)")
@@ -543,6 +578,7 @@ def main():
     tensor_core = None if args.no_dense else dense_leg(L, vp, args.dense_check_pairs)
     kmeans = None if args.no_kmeans else kmeans_leg(L, vp, cpu=not args.no_cpu)
     streamed = None if args.stream_blocks <= 0 else stream_leg(1 << 22, args.stream_blocks)
+    rmt = None if args.no_rmt else rmt_leg(cpu=not args.no_cpu)
 
     cpu = None
     parity = None
@@ -565,7 +601,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded; no public dataset)",
             "config": config_dict(args, gem), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "cpu_baseline": cpu, "parity": parity, "clocks": clk, "tensor_core": tensor_core, "kmeans_uneven": kmeans,
-            "streamed_30000x500": streamed}
+            "streamed_30000x500": streamed, "rmt": rmt}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

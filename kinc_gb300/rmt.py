@@ -32,9 +32,11 @@ class RMT:
             raise _native.SimError(rc, _native.load().kinc_rmt_last_error().decode())
 
     def run(self, input=None, log=None, items=None, genes=None, max_clusters=None, little_endian=False,
-            max_steps=4096):
+            max_steps=4096, strict=True):
         """The threshold for a CMX file (`input`) or for items (x, y, c, r) of a `genes` x `max_clusters`
-        matrix; returns (threshold, steps) with steps an array of (threshold, size, chi) rows."""
+        matrix; returns (threshold, steps) with steps an array of (threshold, size, chi) rows.  When no
+        threshold above tstop passes, raises (the reference's error) unless `strict` is false, which
+        returns (None, steps) for items."""
         L = _native.load()
         out = ctypes.c_float(0)
         log_b = str(log).encode() if log is not None else None
@@ -46,9 +48,12 @@ class RMT:
         steps = np.zeros((max_steps, 3), np.float32)
         nsteps = ctypes.c_int32(0)
         vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
-        self._check(L.kinc_rmt_run_items(int(genes), int(max_clusters), len(x), vp(x), vp(y), vp(c), vp(r),
-                                         ctypes.byref(self.params), log_b, ctypes.byref(out), vp(steps), max_steps,
-                                         ctypes.byref(nsteps)))
+        rc = L.kinc_rmt_run_items(int(genes), int(max_clusters), len(x), vp(x), vp(y), vp(c), vp(r),
+                                  ctypes.byref(self.params), log_b, ctypes.byref(out), vp(steps), max_steps,
+                                  ctypes.byref(nsteps))
+        if rc == _native.RMT_ENOTHRESHOLD and not strict:
+            return None, steps[:min(nsteps.value, max_steps)]
+        self._check(rc)
         return float(out.value), steps[:min(nsteps.value, max_steps)]
 
     def prune_eigenvalues(self, items, genes, max_clusters, threshold):
