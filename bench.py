@@ -386,8 +386,9 @@ def rmt_leg(blocks=1000, size=5, cpu=True):
         out["cpu_baseline"] = {"seconds": csecs, "cores": os.cpu_count() or 1, "kind": "port",
                                "sample": "the whole analytic: numpy (LAPACK) eigensolver, scipy Akima unfolding"}
         out["gpu_over_cpu"] = csecs / secs
-        out["parity"] = {"same_threshold": (want_t is None and thr is None)
-                         or (want_t is not None and thr is not None and np.float32(want_t) == np.float32(thr)),
+        out["parity"] = {"same_threshold": bool((want_t is None and thr is None)
+                                                or (want_t is not None and thr is not None
+                                                    and np.float32(want_t) == np.float32(thr))),
                          "same_sizes": [int(a[1]) for a in steps] == [b[1] for b in want_steps],
                          "max_abs_dchi": dchi}
     return out
