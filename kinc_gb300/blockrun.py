@@ -32,6 +32,7 @@ def main(argv=None):
     ap.add_argument("--precision", default="fp32")
     ap.add_argument("--start", default="0", help="first pair, or 'mid'")
     ap.add_argument("--blocks", default="32768,262144", help="comma-separated device block sizes")
+    ap.add_argument("--repeat", type=int, default=1, help="run each block this many times from the same pair")
     args = ap.parse_args(argv)
 
     import torch
@@ -54,7 +55,7 @@ def main(argv=None):
     dC = torch.empty((n, sim.params.max_clusters * nc), dtype=torch.float32, device="cuda")
     stream = torch.cuda.Stream()   # the worker's stream argument 0 would mean its own stream
     counters = (ctypes.c_uint64 * 4)()
-    for size in sizes:
+    for size in [b for b in sizes for _ in range(max(1, args.repeat))]:
         _native.check(L.kinc_sim_work_counters(ctx, counters, 1), ctx)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -71,7 +72,8 @@ def main(argv=None):
         print(json.dumps({"workload": args.workload, "start": pos, "pairs": size, "ms": ms,
                           "pairs_per_s": size / (ms / 1e3), "units": int(counters[0]), "fits": int(counters[1]),
                           "launches": int(L.kinc_sim_last_launch_count(ctx))}), flush=True)
-        pos += size
+        if args.repeat <= 1:
+            pos += size
     sim.close()
 
 

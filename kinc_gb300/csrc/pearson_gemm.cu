@@ -138,19 +138,51 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
    return d;
 }
 
-/* instruction descriptor: D f32, A/B format, both K-major, N = BN, M = BM */
-template <int MODE>
+/* instruction descriptor: D f32, A/B format, both K-major, N columns, M = BM */
+template <int MODE, int N = BN>
 __host__ __device__ constexpr uint32_t instr_desc()
 {
+   static_assert(N % 16 == 0 && N >= 16 && N <= 256, "M = 128 takes N in 16..256, a multiple of 16");
    return (1u << 4)                                /* D format f32 */
           | (Cfg<MODE>::A_FMT << 7) | (Cfg<MODE>::B_FMT << 10)
-          | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+          | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 }
 
+/*
+ * TF32: the six contractions share three x-side operands, so they are issued as three MMAs
+ * with the y-side operands stacked along N -- A_x.[A_y; M_y], A2_x.M_y, M_x.[A2_y; A_y; M_y]
+ * (N = 128, 64, 192) -- which reads each x-side operand from shared memory once per K step
+ * instead of two or three times (with N = 64 the operand reads, not the tensor pipe, bound the
+ * MMAs).  The y-side planes sit in shared memory as [A2_y][A_y][M_y] so both stacks are
+ * contiguous; the accumulators land in TMEM columns Sxy 0, Sx 64, Sxx 128, Syy 192, Sy 256, n 320.
+ */
+#ifndef KINC_TC_MERGE
+#define KINC_TC_MERGE 1
+#endif
 template <int MODE>
+__host__ __device__ constexpr bool merged()
+{
+   return MODE == 1 && KINC_TC_MERGE;
+}
+
+/* shared-memory slot of y-side operand m (0 A, 1 A2, 2 M for TF32) */
+template <int MODE>
+__host__ __device__ constexpr int yslot(int m)
+{
+   return merged<MODE>() ? (m == 0 ? 1 : m == 1 ? 0 : 2) : m;
+}
+
+/* TMEM column of accumulator a (0 Sxy, 1 Sx, 2 Sy, 3 Sxx, 4 Syy, 5 n) */
+template <int MODE>
+__host__ __device__ constexpr int acc_col(int a)
+{
+   return merged<MODE>() ? (a == 0 ? 0 : a == 1 ? 64 : a == 2 ? 256 : a == 3 ? 128 : a == 4 ? 192 : 320) : a * BN;
+}
+
+template <int MODE, int N = BN>
 __device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate)
 {
-   constexpr uint32_t idesc = instr_desc<MODE>();
+   constexpr uint32_t idesc = instr_desc<MODE, N>();
    if ( MODE == 1 )
    {
       asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
@@ -348,7 +380,8 @@ __global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant
          for ( int m = 0; m < C::NMAT; ++m )
          {
             tma_load_2d(stage + m * L::XMAT, &maps.x[m], kc * C::BK, I * BM, full0 + 8 * s);
-            tma_load_2d(stage + C::NMAT * L::XMAT + m * L::YMAT, &maps.y[m], kc * C::BK, J * BN, full0 + 8 * s);
+            tma_load_2d(stage + C::NMAT * L::XMAT + yslot<MODE>(m) * L::YMAT, &maps.y[m], kc * C::BK, J * BN,
+                        full0 + 8 * s);
          }
          ++issued;
       }
@@ -371,7 +404,19 @@ __global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant
          {
             const uint32_t koff = ks * C::UMMA_K * C::ELEM;   /* byte step along K inside the row */
             const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-            if ( MODE == 1 )
+            if ( merged<MODE>() )
+            {
+               const uint64_t xa = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
+               const uint64_t xq = smem_desc<MODE>(stage + 1 * L::XMAT + koff);
+               const uint64_t xm = smem_desc<MODE>(stage + 2 * L::XMAT + koff);
+               const uint64_t y_q_a_m = smem_desc<MODE>(ysb + 0 * L::YMAT + koff);   /* [A2_y; A_y; M_y] */
+               const uint64_t y_a_m = smem_desc<MODE>(ysb + 1 * L::YMAT + koff);     /* [A_y; M_y] */
+               const uint64_t y_m = smem_desc<MODE>(ysb + 2 * L::YMAT + koff);       /* M_y */
+               mma<MODE, 2 * BN>(tmem + acc_col<MODE>(0), xa, y_a_m, acc);     /* Sxy | Sx */
+               mma<MODE, BN>(tmem + acc_col<MODE>(3), xq, y_m, acc);           /* Sxx */
+               mma<MODE, 3 * BN>(tmem + acc_col<MODE>(4), xm, y_q_a_m, acc);   /* Syy | Sy | n */
+            }
+            else if ( MODE == 1 )
             {
                /* x side: 0 A, 1 A2, 2 M; y side likewise */
                const uint64_t xa = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
@@ -431,7 +476,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant
       {
          float v[NACC][16];
 #pragma unroll
-         for ( int a = 0; a < NACC; ++a ) tmem_ld16(lane_base + a * BN + c * 16, v[a]);
+         for ( int a = 0; a < NACC; ++a ) tmem_ld16(lane_base + acc_col<MODE>(a) + c * 16, v[a]);
          if ( x < args.G )
          {
 #pragma unroll
