@@ -43,6 +43,57 @@ def shard_pairs(genes, world, rank, block=WORK_BLOCK_SIZE):
     return Shard(rank, start, end - start)
 
 
+def block_costs(gem, min_expr=float("-inf"), block=WORK_BLOCK_SIZE):
+    """Estimated cost of every work block: the sum over its pairs of n_x * n_y / S, with n_g the
+    gene's usable samples -- the expected pairwise usable count when missing values are
+    independent, to which every per-pair pass (fetch, EM and Lloyd sweeps, correlations) is
+    proportional.  O(genes + blocks): each row of pairs spans at most two blocks while
+    genes < block, and is summed from a prefix over n_y."""
+    import numpy as np
+    gem = np.asarray(gem)
+    G, S = gem.shape
+    usable = ~np.isnan(gem) & ~(gem < min_expr)
+    n = usable.sum(axis=1).astype(np.float64)
+    prefix = np.concatenate([[0.0], np.cumsum(n)])
+    total = total_pairs(G)
+    nblocks = (total + block - 1) // block
+    costs = np.zeros(nblocks, np.float64)
+    for x in range(1, G):
+        p0 = x * (x - 1) // 2          # pairs (x, 0) .. (x, x-1)
+        y = 0
+        while y < x:
+            b = (p0 + y) // block
+            y_end = min(x, (b + 1) * block - p0)
+            costs[b] += n[x] * (prefix[y_end] - prefix[y]) / max(S, 1)
+            y = y_end
+    return costs
+
+
+def shard_pairs_by_cost(costs, genes, world, rank, block=WORK_BLOCK_SIZE):
+    """Contiguous range of whole work blocks for `rank` of `world`, cut where the running sum of
+    the blocks' estimated costs crosses rank/world and (rank+1)/world of the total."""
+    import numpy as np
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError(f"rank {rank} outside world of {world}")
+    total = total_pairs(genes)
+    c = np.concatenate([[0.0], np.cumsum(np.asarray(costs, np.float64))])
+    whole = c[-1]
+    if whole <= 0:
+        return shard_pairs(genes, world, rank, block)
+
+    def cut(r):
+        if r <= 0:
+            return 0
+        if r >= world:
+            return len(costs)
+        return int(np.searchsorted(c, whole * r / world, side="left"))
+
+    b0, b1 = cut(rank), cut(rank + 1)
+    start = min(b0 * block, total)
+    end = min(b1 * block, total)
+    return Shard(rank, start, max(end - start, 0))
+
+
 def merge_items(per_rank):
     """Concatenate per-rank item lists (each a dict of equal-length sequences) in rank order,
     checking that the pair order is strictly increasing across the seams."""

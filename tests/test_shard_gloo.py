@@ -38,7 +38,11 @@ def _worker(rank, world, port, genes, samples, kw, q):
     os.environ["MASTER_PORT"] = str(port)
     dist.init_process_group("gloo", rank=rank, world_size=world)
     gem = synthetic.generate(2, genes=genes, samples=samples)
-    sh = shard.shard_pairs(genes, world, rank, block=128)
+    kw = dict(kw)
+    if kw.pop("by_cost", False):
+        sh = shard.shard_pairs_by_cost(shard.block_costs(gem, block=128), genes, world, rank, block=128)
+    else:
+        sh = shard.shard_pairs(genes, world, rank, block=128)
     mine = _items(gem, sh.start, sh.size, kw)
     gathered = [None] * world
     dist.all_gather_object(gathered, (sh.start, sh.size, mine))
@@ -49,7 +53,8 @@ def _worker(rank, world, port, genes, samples, kw, q):
 
 
 @pytest.mark.parametrize("kw", [dict(clus_method=1, corr_method=0, criterion=0, post_out=1),
-                                dict(clus_method=0, corr_method=1)])
+                                dict(clus_method=0, corr_method=1),
+                                dict(clus_method=1, corr_method=1, criterion=1, by_cost=True)])
 def test_two_ranks_equal_one(kw):
     import torch.multiprocessing as mp
     genes, samples, world = 28, 60, 2
@@ -70,7 +75,7 @@ def test_two_ranks_equal_one(kw):
     cmx = shard.merge_items([g[2][0] for g in gathered])
     ccm = shard.merge_items([g[2][1] for g in gathered])
     gem = synthetic.generate(2, genes=genes, samples=samples)
-    one_cmx, one_ccm = _items(gem, 0, shard.total_pairs(genes), kw)
+    one_cmx, one_ccm = _items(gem, 0, shard.total_pairs(genes), {k: v for k, v in kw.items() if k != "by_cost"})
     for k in one_cmx:
         assert list(cmx[k]) == list(one_cmx[k]), k
     for k in one_ccm:
@@ -85,3 +90,33 @@ def test_shards_cover_all_pairs():
             assert all(a.end == b.start for a, b in zip(shards, shards[1:]))
             assert shards[-1].end == shard.total_pairs(genes)
             assert all(s.start % shard.WORK_BLOCK_SIZE == 0 for s in shards if s.size)
+
+
+def test_block_costs_estimate_pairwise_counts():
+    """The per-block cost proxy (n_x n_y / S summed over the block's pairs) tracks the true
+    pairwise usable counts on a matrix with per-gene missing rates (uneven workload)."""
+    gem = synthetic.generate(4, genes=300, samples=200)
+    costs = shard.block_costs(gem, block=256)
+    u = ~np.isnan(gem)
+    x, y = np.tril_indices(gem.shape[0], -1)
+    order = np.lexsort((y, x))
+    true = (u[x[order]] & u[y[order]]).sum(axis=1)
+    per_block = np.add.reduceat(true, np.arange(0, len(true), 256))
+    assert np.allclose(costs, per_block, rtol=0.05)
+    assert abs(costs.sum() / true.sum() - 1) < 1e-3
+
+
+@pytest.mark.parametrize("world", [2, 3, 5])
+def test_cost_shards_cover_and_balance(world):
+    gem = synthetic.generate(4, genes=500, samples=150)
+    G = gem.shape[0]
+    costs = shard.block_costs(gem, block=512)
+    shs = [shard.shard_pairs_by_cost(costs, G, world, r, block=512) for r in range(world)]
+    assert shs[0].start == 0 and shs[-1].end == G * (G - 1) // 2
+    assert all(a.end == b.start for a, b in zip(shs, shs[1:]))
+    assert all(s.start % 512 == 0 for s in shs)
+    share = [costs[s.start // 512:(s.end + 511) // 512].sum() / costs.sum() for s in shs]
+    by_count = [shard.shard_pairs(G, world, r, block=512) for r in range(world)]
+    share_count = [costs[s.start // 512:(s.end + 511) // 512].sum() / costs.sum() for s in by_count]
+    assert max(share) - min(share) <= max(share_count) - min(share_count) + 1e-12
+    assert max(share) - 1 / world < 2 * costs.max() / costs.sum()
