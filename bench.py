@@ -410,7 +410,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--block", type=int, default=1048576)
-    ap.add_argument("--ref-pairs-per-thread", type=int, default=24)
+    ap.add_argument("--ref-pairs-per-thread", type=int, default=64)
     ap.add_argument("--cpu-pairs-per-thread", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
