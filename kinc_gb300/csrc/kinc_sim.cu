@@ -609,8 +609,10 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    const size_t col = (size_t)S * TILE;
    dp.gam_k = (KINC_STORE_GAMMA && params->clus_method == 1)
                  ? (params->max_clusters <= 3 ? 3 : params->max_clusters <= 5 ? 5 : 0) : 0;
-   const size_t slot_bytes = col * sizeof(float2) + col * sizeof(float) * (1 + dp.gam_k) + 5 * col
-                             + (size_t)RNG_WORDS * TILE * sizeof(uint32_t)
+   /* K-means sweeps read each lane's samples from its own contiguous copy */
+   const bool lane_major = params->clus_method == 2 && KINC_KMEANS_LANE_MAJOR;
+   const size_t slot_bytes = col * sizeof(float2) * (lane_major ? 2 : 1) + col * sizeof(float) * (1 + dp.gam_k)
+                             + 5 * col + (size_t)RNG_WORDS * TILE * sizeof(uint32_t)
                              + (ctx->smem_sort ? 0 : sort_bytes_warp) + 256 * 8;
    size_t free_b = 0, total_b = 0;
    CKC(cudaMemGetInfo(&free_b, &total_b));
@@ -637,6 +639,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
       const size_t oC = take(slots * col);
       const size_t oR = take(slots * RNG_WORDS * TILE * sizeof(uint32_t));
       const size_t oS = take(ctx->smem_sort ? 0 : slots * sort_bytes_warp);
+      const size_t oXl = take(lane_major ? slots * col * sizeof(float2) : 0);
       CKC(cudaMalloc(&ctx->d_scratch, off));
       char* base = (char*)ctx->d_scratch;
       ctx->ds.X = (float2*)(base + oX);
@@ -649,6 +652,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
       ctx->ds.yc = (int8_t*)(base + oC);
       ctx->ds.rng = (uint32_t*)(base + oR);
       ctx->ds.sortbuf = ctx->smem_sort ? nullptr : (float*)(base + oS);
+      ctx->ds.Xl = lane_major ? (float2*)(base + oXl) : nullptr;
    }
 
    /* one device block of pairs (the tensor-core form writes no labels, so its blocks can be far larger) */
@@ -1207,7 +1211,9 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
                              + ((col * sizeof(float) * dp.gam_k + 255) & ~(size_t)255)
                              + 5 * ((col + 255) & ~(size_t)255)
                              + (((size_t)RNG_WORDS * TILE * sizeof(uint32_t) + 255) & ~(size_t)255)
-                             + (smem_sort ? 0 : ((sort_bytes_warp + 255) & ~(size_t)255));
+                             + (smem_sort ? 0 : ((sort_bytes_warp + 255) & ~(size_t)255))
+                             + ((params->clus_method == 2 && KINC_KMEANS_LANE_MAJOR)
+                                   ? ((col * sizeof(float2) + 255) & ~(size_t)255) : 0);
    if ( off >= NOALLOC_SCRATCH_BYTES || (NOALLOC_SCRATCH_BYTES - off) / slot_bytes < (size_t)WARPS_PER_BLOCK )
       return fail(nullptr, KINC_SIM_EINVAL,
                   "%d genes x %d samples and %lld pairs do not fit the %zu-byte allocation-free scratch",
@@ -1232,6 +1238,8 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
       ds.yc = (int8_t*)carve(nslots * col);
       ds.rng = (uint32_t*)carve(nslots * RNG_WORDS * TILE * sizeof(uint32_t));
       ds.sortbuf = smem_sort ? nullptr : (float*)carve(nslots * sort_bytes_warp);
+      ds.Xl = (params->clus_method == 2 && KINC_KMEANS_LANE_MAJOR) ? (float2*)carve(nslots * col * sizeof(float2))
+                                                                  : nullptr;
       if ( o > NOALLOC_SCRATCH_BYTES )
          return fail(nullptr, KINC_SIM_EINVAL, "allocation-free scratch layout overflow");
    }

@@ -121,6 +121,7 @@ struct DevScratch
    int8_t* yc;
    uint32_t* rng;                   /* per warp slot: [31][32] */
    float* sortbuf;                  /* per warp slot: sort_floats, used when not in shared memory */
+   float2* Xl;                      /* K-means: per lane [S], the lane's samples contiguous */
 };
 
 struct DevBlock
@@ -929,13 +930,18 @@ __device__ float kmeans_fit_inits_in_step(const float2* X, int8_t*& cur, int8_t*
 /* 1: lane-independent initialisations (below); measured slower on the uneven 10,000 x 4,000 workload
  * (12.8k vs 15.0k pairs/s): the cluster-major log-likelihood pass of a lane that finishes an
  * initialisation then runs divergently beside the other lanes' Lloyd sweeps */
+/* K-means sweeps over a per-lane contiguous copy of the samples (1) or the interleaved X (0) */
+#ifndef KINC_KMEANS_LANE_MAJOR
+#define KINC_KMEANS_LANE_MAJOR 1
+#endif
+
 /* K-means initialisations pipelined across the lanes of a warp (below); 0: in lockstep */
 #ifndef KINC_KMEANS_PIPELINE
 #define KINC_KMEANS_PIPELINE 1
 #endif
 
 /* computeLogLikelihood (pairwise_kmeans.cpp:105-127): one accumulator, cluster-major order */
-template <int KT>
+template <int KT, int XS = TILE>
 __device__ __forceinline__ float kmeans_loglik(const float2* X, const int8_t* lab, int N, int K, const float* mu0,
                                                const float* mu1)
 {
@@ -954,7 +960,7 @@ __device__ __forceinline__ float kmeans_loglik(const float2* X, const int8_t* la
       for ( int i = 0; i < N; ++i )
       {
          if ( lab[i * TILE] != k ) continue;
-         const float2 xv = X[i * TILE];
+         const float2 xv = X[i * XS];
          const float d = diff_norm(xv.x, xv.y, c0, c1);
          S += d * d;
       }
@@ -978,7 +984,7 @@ __device__ __forceinline__ float kmeans_loglik(const float2* X, const int8_t* la
  * Warp votes use the lanes that entered together (__activemask at entry);
  * every one of them runs the loop until the same voted exit.
  */
-template <int KT>
+template <int KT, int XS = TILE>
 __device__ float kmeans_fit_pipelined(const float2* X, int8_t*& ya, int8_t*& yb, int8_t*& pl, int8_t*& best,
                                       int N, int Kr, LaneRng& rng, unsigned long long& units)
 {
@@ -1009,7 +1015,7 @@ __device__ float kmeans_fit_pipelined(const float2* X, int8_t*& ya, int8_t*& yb,
          {
             if ( k >= K ) continue;
             const int ii = rng.next() % N;
-            const float2 xv = X[ii * TILE];
+            const float2 xv = X[ii * XS];
             mu0[k] = xv.x;
             mu1[k] = xv.y;
             nprev[k] = -1;
@@ -1027,7 +1033,7 @@ __device__ float kmeans_fit_pipelined(const float2* X, int8_t*& ya, int8_t*& yb,
          if ( __all_sync(mask, !pending && !held && !running && started >= 10) ) break;
          if ( pending )
          {
-            const float logL = kmeans_loglik<KT>(X, pl, N, K, pm0, pm1);
+            const float logL = kmeans_loglik<KT, XS>(X, pl, N, K, pm0, pm1);
             if ( bestLogL < logL )
             {
                bestLogL = logL;
@@ -1069,14 +1075,14 @@ __device__ float kmeans_fit_pipelined(const float2* X, int8_t*& ya, int8_t*& yb,
       }
       float2 ring[KM_RING];
 #pragma unroll
-      for ( int d = 0; d < KM_RING; ++d ) ring[d] = d < N ? X[d * TILE] : make_float2(0.f, 0.f);
+      for ( int d = 0; d < KM_RING; ++d ) ring[d] = d < N ? X[d * XS] : make_float2(0.f, 0.f);
       for ( int i = 0; i < N; ++i )
       {
          const float2 xv = ring[0];
 #pragma unroll
          for ( int d = 0; d + 1 < KM_RING; ++d ) ring[d] = ring[d + 1];
-         if ( i + KM_RING < N ) ring[KM_RING - 1] = X[(i + KM_RING) * TILE];
-         if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N ) prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
+         if ( i + KM_RING < N ) ring[KM_RING - 1] = X[(i + KM_RING) * XS];
+         if ( XS != 1 && KINC_PREFETCH > 0 && i + KINC_PREFETCH < N ) prefetch_l2(&X[(i + KINC_PREFETCH) * XS]);
          int min_k = -1;
          float min_d = 0.f;
 #pragma unroll UF

@@ -142,9 +142,9 @@ __device__ __forceinline__ float criterion_value(const DevParams& P, const DevDa
 }
 
 template <int CLUS, int KT>
-__device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, float* lpx, float* gam,
-                                         int8_t*& wl, int8_t*& ya, int8_t*& yb, int8_t*& yc, int N, int K,
-                                         LaneRng& rng, float& logL, float& E, unsigned long long& units,
+__device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, const float2* Xl, float* lpx,
+                                         float* gam, int8_t*& wl, int8_t*& ya, int8_t*& yb, int8_t*& yc, int N,
+                                         int K, LaneRng& rng, float& logL, float& E, unsigned long long& units,
                                          float* pbuf)
 {
    if ( CLUS == 1 )
@@ -152,7 +152,12 @@ __device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, fl
       return gmm_fit<KT>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units, pbuf);
    }
 #if KINC_KMEANS_PIPELINE
-   logL = kmeans_fit_pipelined<KT>(X, ya, yb, wl, yc, N, K, rng, units);
+#if KINC_KMEANS_LANE_MAJOR
+   /* the lane's own contiguous copy of its samples (both allocation paths provide it) */
+   logL = kmeans_fit_pipelined<KT, 1>(Xl, ya, yb, wl, yc, N, K, rng, units);
+#else
+   logL = kmeans_fit_pipelined<KT, TILE>(X, ya, yb, wl, yc, N, K, rng, units);
+#endif
 #else
    logL = kmeans_fit<KT>(X, ya, yb, yc, N, K, rng, units);
 #endif
@@ -166,25 +171,27 @@ __device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, fl
 /* Clustering::compute (pairwise_clustering.cpp:23-103) minus the outlier
  * passes, for this lane's pair; labels merged into lbl. */
 template <int CLUS, int KS>
-__device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* X, float* lpx, float* gam,
-                            float* pbuf, int8_t* wl,
+__device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* X, float2* Xl, float* lpx,
+                            float* gam, float* pbuf, int8_t* wl,
                             int8_t* ya, int8_t* yb, int8_t* yc, int8_t* lbl, int N, LaneRng& rng,
                             unsigned long long& units, unsigned long long& fits)
 {
    int bestK = 0;
    if ( N < P.min_samples ) return 0;
+   if ( CLUS == 2 && KINC_KMEANS_LANE_MAJOR )
+      for ( int i = 0; i < N; ++i ) Xl[i] = X[i * TILE];
    float bestValue = INFINITY;
    for ( int K = P.min_k; K <= P.max_k; ++K )
    {
       float logL = 0.f, E = 0.f;
       bool ok;
       if ( !KINC_STATIC_K || KS == 0 )
-         ok = lane_fit<CLUS, KS>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
-      else if ( K == 1 ) ok = lane_fit<CLUS, 1>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
-      else if ( K == 2 ) ok = lane_fit<CLUS, 2>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
-      else if ( K == 3 || KS < 4 ) ok = lane_fit<CLUS, 3>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
-      else if ( K == 4 ) ok = lane_fit<CLUS, 4>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
-      else ok = lane_fit<CLUS, 5>(P, X, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+         ok = lane_fit<CLUS, KS>(P, X, Xl, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+      else if ( K == 1 ) ok = lane_fit<CLUS, 1>(P, X, Xl, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+      else if ( K == 2 ) ok = lane_fit<CLUS, 2>(P, X, Xl, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+      else if ( K == 3 || KS < 4 ) ok = lane_fit<CLUS, 3>(P, X, Xl, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+      else if ( K == 4 ) ok = lane_fit<CLUS, 4>(P, X, Xl, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
+      else ok = lane_fit<CLUS, 5>(P, X, Xl, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
       ++fits;
       if ( !ok ) continue;
       const float value = criterion_value(P, D, K, logL, N, E);
@@ -300,7 +307,9 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
             rng.head = 0;
             rng.mode = P.rand_mode;
             rng.lcg = 1;
-            K = lane_cluster<CLUS, KS>(P, D, X + lane, lpx + lane, gam ? gam + lane : nullptr,
+            K = lane_cluster<CLUS, KS>(P, D, X + lane,
+                                       W.Xl ? W.Xl + ((size_t)slot * TILE + lane) * (size_t)P.S : nullptr,
+                                       lpx + lane, gam ? gam + lane : nullptr,
                                        pbuf ? pbuf + lane : nullptr, wl + lane,
                                        ya + lane, yb + lane, yc + lane, lbl + lane, myN, rng, units, fits);
          }
