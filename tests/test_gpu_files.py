@@ -162,3 +162,33 @@ def test_device_process_matches_host_process():
     unpacked[:, 1::2] = (pk >> 4)[:, :S // 2]
     assert np.array_equal(unpacked, codes)
     sim.close()
+
+
+def test_command_line_similarity_and_rmt(tmp_path, capsys):
+    """python -m kinc_gb300 run similarity writes the files the Python API writes; run rmt reports the
+    threshold the API finds."""
+    from kinc_gb300 import __main__ as cli
+    from kinc_gb300.rmt import RMT
+    G, S = 120, 70
+    gem = synthetic.generate(2, genes=G, samples=S)
+    pm.write_emx(tmp_path / "g.emx", gem)
+    assert cli.main(["run", "similarity", "--input", str(tmp_path / "g.emx"), "--ccm", str(tmp_path / "a.ccm"),
+                     "--cmx", str(tmp_path / "a.cmx"), "--clusmethod", "gmm", "--corrmethod", "spearman",
+                     "--crit", "BIC", "--preout", "--postout", "true", "--mincorr", "0.3"]) == 0
+    sim = Similarity(gem, clusmethod="gmm", corrmethod="spearman", crit="BIC", preout=True, postout=True,
+                     mincorr=0.3)
+    sim.run(ccm_path=tmp_path / "b.ccm", cmx_path=tmp_path / "b.cmx")
+    sim.close()
+    for ext in ("ccm", "cmx"):
+        assert (tmp_path / f"a.{ext}").read_bytes() == (tmp_path / f"b.{ext}").read_bytes()
+    Gn, x, y, c, r = synthetic.clique_network(80, 5)
+    pm.write(tmp_path / "n.cmx", pm.CMX, Gn, 1, 1, x, y, c, r.reshape(-1, 1))
+    capsys.readouterr()
+    assert cli.main(["run", "rmt", "--input", str(tmp_path / "n.cmx"), "--log", str(tmp_path / "rmt.log"),
+                     "--tstep", "0.01"]) in (0, 1)
+    out = capsys.readouterr()
+    try:
+        t, _ = RMT(tstep=0.01).run(input=tmp_path / "n.cmx")
+        assert out.out.strip() == f"threshold: {t:g}"
+    except Exception:
+        assert "rmt:" in out.err
