@@ -14,13 +14,15 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libkinc_gb300.so")
+CLI = os.path.join(OUT_DIR, "kinc-gb300")
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-I", os.path.join(REPO, "include"), "-I", CSRC]
 
-# (source, extra flags)
+# (source, extra flags); kinc_cli.cpp is the command-line program, linked against the library
+CLI_SRC = "kinc_cli.cpp"
 UNITS = [
     ("kinc_sim.cu", ["--fmad=false"]),
     ("sim_none.cu", ["--fmad=false"]),
@@ -47,9 +49,9 @@ def _deps():
 
 
 def up_to_date():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
     return all(os.path.getmtime(d) <= t for d in _deps())
 
 
@@ -79,6 +81,11 @@ def build(force=False, verbose=False):
     tmp = LIB + ".tmp"
     subprocess.check_call([NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lcusolver"])
     os.replace(tmp, LIB)
+    # the command-line program finds the library next to itself
+    tmp = CLI + ".tmp"
+    subprocess.check_call([NVCC, *COMMON, os.path.join(CSRC, CLI_SRC), "-o", tmp, "-L", OUT_DIR, "-lkinc_gb300",
+                           "-Xlinker", "-rpath=$ORIGIN"])
+    os.replace(tmp, CLI)
     return LIB
 
 

@@ -59,3 +59,48 @@ def test_errors_are_reported_not_raised(tmp_path, native, capsys):
     assert cli.main(["run", "export-cmx", "--ccm", str(tmp_path / "none.ccm"), "--cmx", str(tmp_path / "none.cmx"),
                      "--output", str(tmp_path / "o.txt")]) == 1
     assert "export-cmx" in capsys.readouterr().err
+
+
+def _native_cli():
+    import os
+
+    from kinc_gb300 import build
+    if not os.path.exists(build.CLI):
+        pytest.skip("command-line program not built")
+    return build.CLI
+
+
+def test_native_program_export_and_extract(tmp_path, native):
+    """kinc-gb300 (the C++ host driver) writes what the library calls write."""
+    import subprocess
+    exe = _native_cli()
+    rng = np.random.default_rng(8)
+    genes, samples = 7, 5
+    gem = (8 + rng.standard_normal((genes, samples))).astype(np.float32)
+    pm.write_emx(tmp_path / "g.emx", gem)
+    pm.write(tmp_path / "g.cmx", pm.CMX, genes, 2, 1, [2, 4, 4], [1, 3, 3], [0, 0, 1],
+             np.array([[0.9], [0.95], [-0.88]], np.float32))
+    pm.write(tmp_path / "g.ccm", pm.CCM, genes, 2, samples, [4, 4], [3, 3], [0, 1],
+             np.array([[1, 1, 0, 9, 7], [0, 0, 1, 6, 1]], np.int8))
+    r = subprocess.run([exe, "run", "export-cmx", "--ccm", str(tmp_path / "g.ccm"), "--cmx", str(tmp_path / "g.cmx"),
+                        "--output", str(tmp_path / "a.txt")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    pm.export_text(tmp_path / "g.ccm", tmp_path / "g.cmx", tmp_path / "b.txt")
+    assert (tmp_path / "a.txt").read_text() == (tmp_path / "b.txt").read_text()
+    r = subprocess.run([exe, "run", "extract", "--emx", str(tmp_path / "g.emx"), "--ccm", str(tmp_path / "g.ccm"),
+                        "--cmx", str(tmp_path / "g.cmx"), "--output", str(tmp_path / "n1.txt"),
+                        "--mincorr", "0.85"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    pm.extract(tmp_path / "g.emx", tmp_path / "g.ccm", tmp_path / "g.cmx", tsv_path=tmp_path / "n2.txt")
+    assert (tmp_path / "n1.txt").read_text() == (tmp_path / "n2.txt").read_text()
+
+
+@pytest.mark.parametrize("argv,code", [([], 2), (["run"], 2), (["run", "nope"], 2),
+                                       (["run", "similarity", "--input"], 2),
+                                       (["run", "similarity", "--input", "x.emx"], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--preout", "maybe"], 2),
+                                       (["run", "export-cmx", "--ccm", "a", "--cmx", "b", "--output", "c"], 1)])
+def test_native_program_argument_errors(tmp_path, native, argv, code):
+    import subprocess
+    r = subprocess.run([_native_cli(), *argv], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == code, r.stderr

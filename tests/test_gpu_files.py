@@ -181,6 +181,17 @@ def test_command_line_similarity_and_rmt(tmp_path, capsys):
     sim.close()
     for ext in ("ccm", "cmx"):
         assert (tmp_path / f"a.{ext}").read_bytes() == (tmp_path / f"b.{ext}").read_bytes()
+    # the native host driver, same arguments
+    import subprocess
+
+    from kinc_gb300 import build
+    r = subprocess.run([build.CLI, "run", "similarity", "--input", str(tmp_path / "g.emx"),
+                        "--ccm", str(tmp_path / "c.ccm"), "--cmx", str(tmp_path / "c.cmx"), "--clusmethod", "gmm",
+                        "--corrmethod", "spearman", "--crit", "BIC", "--preout", "--postout", "true",
+                        "--mincorr", "0.3"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for ext in ("ccm", "cmx"):
+        assert (tmp_path / f"c.{ext}").read_bytes() == (tmp_path / f"b.{ext}").read_bytes()
     Gn, x, y, c, r = synthetic.clique_network(80, 5)
     pm.write(tmp_path / "n.cmx", pm.CMX, Gn, 1, 1, x, y, c, r.reshape(-1, 1))
     capsys.readouterr()
