@@ -12,6 +12,9 @@ pytestmark = pytest.mark.gpu
 CASES = [
     ("gmm_pearson_bic_post", 2, 44, 90, dict(clusmethod="gmm", crit="BIC", postout=True, mincorr=0.3),
      dict(clus_method=1, criterion=0, post_out=1, min_corr=0.3)),
+    ("kmeans_spearman_icl", 4, 40, 120, dict(clusmethod="kmeans", corrmethod="spearman", crit="ICL", maxclus=3,
+                                             mincorr=0.3),
+     dict(clus_method=2, corr_method=1, criterion=1, max_clusters=3, min_corr=0.3)),
     ("none_pearson_two_blocks", 1, 260, 36, dict(mincorr=0.2), dict(min_corr=0.2)),
 ]
 
@@ -203,3 +206,22 @@ def test_command_line_similarity_and_rmt(tmp_path, capsys):
         assert out.out.strip() == f"threshold: {t:g}"
     except Exception:
         assert "rmt:" in out.err
+
+
+@pytest.mark.parametrize("precision", ["tf32", "3xbf16"])
+def test_run_to_files_tensor_core_matches_execute(tmp_path, precision):
+    """The tensor-core form through the file runner keeps exactly the correlations execute() returns
+    (filtered at mincorr) -- the runner and the host process() see the same device results."""
+    G, S = 300, 64
+    gem = synthetic.generate(3, genes=G, samples=S, seed=4)
+    sim = Similarity(gem, semantics="fixed", precision=precision, mincorr=0.5)
+    sim.run(cmx_path=tmp_path / "t.cmx", device_block=32768)
+    res = sim.execute(None, start=0, size=sim.total_pairs())
+    sim.close()
+    r = res.corr[:, 0]
+    keep = ~np.isnan(r) & (np.abs(r) >= np.float32(0.5)) & (np.abs(r) <= np.float32(1.0))
+    x, y = pyoracle.pair_xy(np.nonzero(keep)[0])
+    got = pm.read(tmp_path / "t.cmx", pm.CMX)
+    assert np.array_equal(got["x"], x) and np.array_equal(got["y"], y)
+    assert np.array_equal(got["payload"][:, 0], r[keep])
+    assert len(x) > 0
