@@ -159,24 +159,47 @@ __host__ __device__ constexpr uint32_t instr_desc()
 #ifndef KINC_TC_MERGE
 #define KINC_TC_MERGE 1
 #endif
+/*
+ * 3xBF16: twelve products (Sxy = Ah.Ah + Ah.Al + Al.Ah, Sx = Ah.M + Al.M, Sy = M.Ah + M.Al,
+ * Sxx = Qh.M + Ql.M, Syy = M.Qh + M.Ql, n = M.M; Q = A2) as seven MMAs: Ah_x.[Ah; M; Al]_y
+ * (N = 192), Al_x.[Ah; M]_y accumulated onto its first 128 columns, Qh_x.M_y and Ql_x.M_y,
+ * M_x.[Qh; Ah; M]_y (N = 192), M_x.Ql_y and M_x.Al_y accumulated onto the Syy and Sy columns.
+ * The y-side planes sit as [Ql][Qh][Ah][M][Al] so every stack is contiguous.  Sxy is kept in two
+ * FP32 accumulators (Ah.Ah + Al.Ah in columns 0-63, Ah.Al in 128-191) added in the epilogue;
+ * Sx 64, Sxx 192, Syy 256, Sy 320, n 384 (448 of 512 columns).
+ */
+#ifndef KINC_TC_MERGE_BF16
+#define KINC_TC_MERGE_BF16 1
+#endif
 template <int MODE>
 __host__ __device__ constexpr bool merged()
 {
-   return MODE == 1 && KINC_TC_MERGE;
+   return (MODE == 1 && KINC_TC_MERGE) || (MODE == 2 && KINC_TC_MERGE_BF16);
 }
 
-/* shared-memory slot of y-side operand m (0 A, 1 A2, 2 M for TF32) */
+/* shared-memory slot of y-side operand m (TF32: 0 A, 1 A2, 2 M; 3xBF16: 0 Ah, 1 Al, 2 Qh, 3 Ql, 4 M) */
 template <int MODE>
 __host__ __device__ constexpr int yslot(int m)
 {
-   return merged<MODE>() ? (m == 0 ? 1 : m == 1 ? 0 : 2) : m;
+   return !merged<MODE>() ? m
+          : MODE == 1     ? (m == 0 ? 1 : m == 1 ? 0 : 2)
+                          : (m == 0 ? 2 : m == 1 ? 4 : m == 2 ? 1 : m == 3 ? 0 : 3);
 }
 
 /* TMEM column of accumulator a (0 Sxy, 1 Sx, 2 Sy, 3 Sxx, 4 Syy, 5 n) */
 template <int MODE>
 __host__ __device__ constexpr int acc_col(int a)
 {
-   return merged<MODE>() ? (a == 0 ? 0 : a == 1 ? 64 : a == 2 ? 256 : a == 3 ? 128 : a == 4 ? 192 : 320) : a * BN;
+   return !merged<MODE>() ? a * BN
+          : MODE == 1     ? (a == 0 ? 0 : a == 1 ? 64 : a == 2 ? 256 : a == 3 ? 128 : a == 4 ? 192 : 320)
+                          : (a == 0 ? 0 : a == 1 ? 64 : a == 2 ? 320 : a == 3 ? 192 : a == 4 ? 256 : 384);
+}
+
+/* the second Sxy accumulator of merged 3xBF16 (Ah.Al), -1 when there is none */
+template <int MODE>
+__host__ __device__ constexpr int sxy2_col()
+{
+   return (merged<MODE>() && MODE == 2) ? 128 : -1;
 }
 
 template <int MODE, int N = BN>
@@ -404,7 +427,28 @@ __global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant
          {
             const uint32_t koff = ks * C::UMMA_K * C::ELEM;   /* byte step along K inside the row */
             const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-            if ( merged<MODE>() )
+            if ( merged<MODE>() && MODE == 2 )
+            {
+               /* x side: 0 Ah, 1 Al, 2 Qh, 3 Ql, 4 M; y side in slots [Ql][Qh][Ah][M][Al] */
+               const uint64_t xah = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
+               const uint64_t xal = smem_desc<MODE>(stage + 1 * L::XMAT + koff);
+               const uint64_t xqh = smem_desc<MODE>(stage + 2 * L::XMAT + koff);
+               const uint64_t xql = smem_desc<MODE>(stage + 3 * L::XMAT + koff);
+               const uint64_t xm = smem_desc<MODE>(stage + 4 * L::XMAT + koff);
+               const uint64_t y_ql = smem_desc<MODE>(ysb + 0 * L::YMAT + koff);
+               const uint64_t y_qh_ah_m = smem_desc<MODE>(ysb + 1 * L::YMAT + koff);
+               const uint64_t y_ah_m_al = smem_desc<MODE>(ysb + 2 * L::YMAT + koff);
+               const uint64_t y_m = smem_desc<MODE>(ysb + 3 * L::YMAT + koff);
+               const uint64_t y_al = smem_desc<MODE>(ysb + 4 * L::YMAT + koff);
+               mma<MODE, 3 * BN>(tmem + 0, xah, y_ah_m_al, acc);      /* Sxy(hh) | Sx(h) | Sxy(hl) */
+               mma<MODE, 2 * BN>(tmem + 0, xal, y_ah_m_al, 1u);       /* += Sxy(lh) | Sx(l) */
+               mma<MODE, BN>(tmem + acc_col<MODE>(3), xqh, y_m, acc); /* Sxx */
+               mma<MODE, BN>(tmem + acc_col<MODE>(3), xql, y_m, 1u);
+               mma<MODE, 3 * BN>(tmem + acc_col<MODE>(4), xm, y_qh_ah_m, acc);   /* Syy(h) | Sy(h) | n */
+               mma<MODE, BN>(tmem + acc_col<MODE>(4), xm, y_ql, 1u);             /* Syy += l */
+               mma<MODE, BN>(tmem + acc_col<MODE>(2), xm, y_al, 1u);             /* Sy += l */
+            }
+            else if ( merged<MODE>() )
             {
                const uint64_t xa = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
                const uint64_t xq = smem_desc<MODE>(stage + 1 * L::XMAT + koff);
@@ -477,6 +521,13 @@ __global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant
          float v[NACC][16];
 #pragma unroll
          for ( int a = 0; a < NACC; ++a ) tmem_ld16(lane_base + acc_col<MODE>(a) + c * 16, v[a]);
+         if constexpr ( sxy2_col<MODE>() >= 0 )
+         {
+            float w[16];
+            tmem_ld16(lane_base + (uint32_t)sxy2_col<MODE>() + c * 16, w);
+#pragma unroll
+            for ( int jj = 0; jj < 16; ++jj ) v[0][jj] += w[jj];
+         }
          if ( x < args.G )
          {
 #pragma unroll
