@@ -199,3 +199,45 @@ def test_extract_matches_restatement(tmp_path, native, named):
     assert (tmp_path / "n.tsv").read_text() == want_tsv
     assert (tmp_path / "n.graphml").read_text() == want_gml
     assert want_tsv.count("\n") > 5
+
+
+def test_export_text_literal_lines(tmp_path, native):
+    """Exact text for a small case written out by hand from ExportCorrelationMatrix::process
+    (src/core/exportcorrelationmatrix.cpp:44-100): counts of codes 1, 9, 8, 7, 6 in that column
+    order, the first correlation at precision 6, the mask '0' + code; a single-cluster pair gets
+    zero counts and an all-'0' mask even when the CCM holds its cluster."""
+    pm.write(tmp_path / "l.cmx", pm.CMX, 5, 3, 2, [2, 2, 4], [0, 0, 3], [0, 1, 0],
+             np.array([[0.123456789, 9.0], [-1.0, 9.0], [0.5, 9.0]], np.float32))
+    pm.write(tmp_path / "l.ccm", pm.CCM, 5, 3, 6, [2, 2, 4], [0, 0, 3], [0, 1, 0],
+             np.array([[1, 1, 9, 8, 7, 6], [0, 0, 1, 1, 1, 9], [1, 1, 1, 1, 1, 1]], np.int8))
+    pm.export_text(tmp_path / "l.ccm", tmp_path / "l.cmx", tmp_path / "l.txt")
+    assert (tmp_path / "l.txt").read_text().splitlines() == [
+        "2\t0\t0\t2\t2\t1\t1\t1\t1\t0.123457\t119876",
+        "2\t0\t1\t2\t3\t1\t0\t0\t0\t-1\t001119",
+        "4\t3\t0\t1\t0\t0\t0\t0\t0\t0.5\t000000",
+    ]
+
+
+def test_extract_literal_lines(tmp_path, native):
+    """Exact TSV and GraphML for a small case written out by hand from Extract::process
+    (src/core/extract.cpp:24-274): the header line, |r| >= mincorr only, single-cluster masks from
+    the expression matrix ('9' where either gene is NaN)."""
+    gem = np.array([[1, 2, np.nan, 4], [1, 2, 3, 4], [1, np.nan, 3, 4]], np.float32)
+    pm.write_emx(tmp_path / "e.emx", gem)
+    pm.write(tmp_path / "e.cmx", pm.CMX, 3, 2, 1, [1, 2, 2], [0, 1, 1], [0, 0, 1],
+             np.array([[0.9], [0.95], [0.2]], np.float32))
+    pm.write(tmp_path / "e.ccm", pm.CCM, 3, 2, 4, [2, 2], [1, 1], [0, 1],
+             np.array([[1, 9, 1, 7], [0, 9, 0, 1]], np.int8))
+    pm.extract(tmp_path / "e.emx", tmp_path / "e.ccm", tmp_path / "e.cmx", tsv_path=tmp_path / "e.tsv",
+               graphml_path=tmp_path / "e.graphml", min_corr=0.85)
+    assert (tmp_path / "e.tsv").read_text().splitlines() == [
+        "Source\tTarget\tsc\tInteraction\tCluster\tNum_Clusters\tCluster_Samples\tMissing_Samples\t"
+        "Cluster_Outliers\tPair_Outliers\tToo_Low\tSamples",
+        "1\t0\t0.9\tco\t0\t1\t0\t0\t0\t0\t0\t1191",
+        "2\t1\t0.95\tco\t0\t2\t2\t1\t0\t1\t0\t1917",
+    ]
+    g = (tmp_path / "e.graphml").read_text()
+    assert g.count('<node id="') == 3
+    assert '<edge source="1" target="0" samples="1191"/>' in g
+    assert '<edge source="2" target="1" samples="1917"/>' in g
+    assert g.endswith("  </graph>\n</graphml>\n")
