@@ -7,8 +7,10 @@
  * local-memory form for any maxclus <= 64).
  * Each specialisation is instantiated in its own translation unit
  * (sim_none.cu, sim_gmm.cu, sim_kmeans.cu) so the register budget of one
- * does not constrain the others.  Blocks of 4 warps are limited to 128
- * registers per thread so 16 warps stay resident per SM.
+ * does not constrain the others.  One CTA of 16 warps per SM (a persistent
+ * grid), 128 registers per thread; warps take 32-pair tiles from a counter in
+ * global memory, together per CTA round for GMM and no clustering (so the
+ * SM's warps run the same code region at a time), one at a time for K-means.
  */
 #pragma once
 
