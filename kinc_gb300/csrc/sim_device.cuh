@@ -2,7 +2,8 @@
  * sim_device.cuh -- device code of the GB300 Similarity worker.
  *
  * Execution model.  One warp owns a tile of 32 gene pairs at a time (a
- * persistent grid pulls tiles from an atomic queue).  Work whose result does
+ * persistent grid takes tiles from a counter in global memory; the pairs of
+ * a launch are ordered by usable-sample count, largest first).  Work whose result does
  * not depend on evaluation order -- fetching and compacting the pair,
  * Tukey quartiles (order statistics), the Spearman bitonic network -- runs
  * warp-cooperatively, one pair after another, with the pair's data staged in
@@ -446,10 +447,11 @@ __device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, dou
  * Per EM iteration it makes three passes over the samples: E (log-densities,
  * per-sample log-sum-exp, logL, and the per-component maxima calcLogGammaK
  * needs), M1 (per-component log-sum-exp of the responsibilities, and the mean
- * sums) and M2 (covariance sums around the new means).  loggamma is never
- * stored: M1/M2 recompute it bit-identically from the parameters of the E
- * step (the inverse covariances and normalisers only change after M2, the new
- * means are held apart until then) and the stored per-sample log p(x).  Each
+ * sums) and M2 (covariance sums around the new means).  loggamma is not
+ * stored: M1 recomputes it bit-identically from the parameters of the E step
+ * (the inverse covariances and normalisers only change after M2, the new
+ * means are held apart until then) and the stored per-sample log p(x); M1
+ * keeps the responsibilities it forms for M2 (KINC_STORE_GAMMA).  Each
  * accumulator is still summed in sample order, so every value equals the
  * reference's.  The update of the last iteration is only checked (a
  * non-positive determinant still fails the fit), since the reference labels
