@@ -17,6 +17,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -82,6 +83,8 @@ struct kinc_pm
    int64_t last_indent = -1;
    int64_t last_pair = -1;
    std::vector<unsigned char> buf;
+   std::unique_ptr<unsigned char[]> items;   /* item bytes of one write, not zero-filled */
+   size_t items_cap = 0;
 };
 
 namespace {
@@ -197,18 +200,30 @@ static int write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y
          last = indent;
       }
    }
-   m->buf.reserve((size_t)n * item);
-   for ( int64_t i = 0; i < n; ++i )
+   /* items are laid out straight into the buffer: 4-byte fields byte-swapped when the file's
+    * order differs from the host's (both hosts this builds for are little-endian) */
+   if ( (size_t)n * item > m->items_cap )
+   {
+      m->items.reset(new unsigned char[(size_t)n * item]);
+      m->items_cap = (size_t)n * item;
+   }
+   const bool swap = !m->e.little;
+   auto put32 = [swap](unsigned char* o, uint32_t v) {
+      if ( swap ) v = __builtin_bswap32(v);
+      memcpy(o, &v, 4);
+   };
+   unsigned char* o = m->items.get();
+   for ( int64_t i = 0; i < n; ++i, o += item )
    {
       const int64_t pair = (int64_t)x[i] * (x[i] - 1) / 2 + y[i];
       const int64_t indent = pair * MAX_CLUSTER_SIZE + c[i];
-      m->e.put<int32_t>(m->buf, x[i]);
-      m->e.put<int32_t>(m->buf, y[i]);
-      m->e.put<int8_t>(m->buf, c[i]);
+      put32(o, (uint32_t)x[i]);
+      put32(o + 4, (uint32_t)y[i]);
+      o[8] = (unsigned char)c[i];
+      unsigned char* d = o + ITEM_HEADER;
       if ( m->type == KINC_PM_CCM && packed )
       {
-         const unsigned char* b = (const unsigned char*)payload + (size_t)i * m->data_size;
-         m->buf.insert(m->buf.end(), b, b + m->data_size);
+         memcpy(d, (const unsigned char*)payload + (size_t)i * m->data_size, (size_t)m->data_size);
       }
       else if ( m->type == KINC_PM_CCM )
       {
@@ -217,13 +232,18 @@ static int write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y
          {
             int8_t v = (int8_t)(codes[s] & 0x0F);
             if ( s + 1 < m->subsize ) v = (int8_t)(v | (int8_t)(codes[s + 1] << 4));
-            m->buf.push_back((unsigned char)v);
+            d[s / 2] = (unsigned char)v;
          }
       }
       else
       {
          const float* r = (const float*)payload + (size_t)i * m->subsize;
-         for ( int k = 0; k < m->subsize; ++k ) m->e.put<float>(m->buf, r[k]);
+         for ( int k = 0; k < m->subsize; ++k )
+         {
+            uint32_t bits;
+            memcpy(&bits, &r[k], 4);
+            put32(d + 4 * k, bits);
+         }
       }
       if ( pair != m->last_pair )
       {
@@ -234,7 +254,8 @@ static int write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y
       m->last_indent = indent;
    }
    const long pos = (long)(HEADER + m->offset) + (long)((m->clusters - n) * (int64_t)item);
-   if ( fseek(m->f, pos, SEEK_SET) != 0 || fwrite(m->buf.data(), 1, m->buf.size(), m->f) != m->buf.size() )
+   const size_t bytes = (size_t)n * item;
+   if ( fseek(m->f, pos, SEEK_SET) != 0 || (bytes > 0 && fwrite(m->items.get(), 1, bytes, m->f) != bytes) )
       return pm_fail(KINC_SIM_ECUDA, "write failed");
    return KINC_SIM_OK;
 }
