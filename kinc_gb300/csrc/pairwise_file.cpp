@@ -82,7 +82,6 @@ struct kinc_pm
    int64_t pairs = 0, clusters = 0;
    int64_t last_indent = -1;
    int64_t last_pair = -1;
-   std::vector<unsigned char> buf;
    std::unique_ptr<unsigned char[]> items;   /* item bytes of one write, not zero-filled */
    size_t items_cap = 0;
 };
@@ -181,7 +180,6 @@ static int write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y
 {
    if ( !m || !m->writing ) return pm_fail(KINC_SIM_EINVAL, "Attempting to write data to uninitialized object.");
    if ( n < 0 || (n > 0 && (!x || !y || !c || !payload)) ) return pm_fail(KINC_SIM_EINVAL, "invalid item arrays");
-   m->buf.clear();
    const size_t item = ITEM_HEADER + (size_t)m->data_size;
    /* validate the whole batch first so a rejected batch leaves the file as it was */
    {
