@@ -16,9 +16,16 @@ Lines printed by rank 0 (one JSON object):
   e2e      the same through the C ABI with host buffers: kinc_sim_create
            (host->device upload of the matrix) + kinc_sim_execute_block into
            pinned host arrays (device->host K, labels, correlations);
-  roofline the similarity kernel's algorithmic FP32 rate;
+  roofline the similarity kernel's algorithmic FP32 rate, and its thread-
+           instruction issue rate (roofline.issue);
   cpu_baseline  the oracle (C restatement of KINC's serial path) on the host
-           cores over a bounded sample.
+           cores over a bounded sample;
+  parity   the same sampled pairs through the GPU, compared with the oracle;
+  and one object per further leg: tensor_core (dense 20,000 x 2,000 masked
+  Pearson, TF32 / 3xBF16 / per-pair FP32, errors against FP64), kmeans_uneven
+  (10,000 x 4,000), streamed_30000x500 (GMM ICL, both correlations, to CCM/CMX
+  files) and rmt (RMT thresholding); each can be skipped (--no-dense,
+  --no-kmeans, --stream-blocks 0, --no-rmt).
 --impl reference runs that CPU path as the timed arm instead.
 """
 import argparse
