@@ -33,6 +33,7 @@ extern "C" {
 #define KINC_SIM_ENOMEM 3      /* device or host allocation failed */
 #define KINC_SIM_EKERNEL 4     /* a kernel reported an error status */
 #define KINC_SIM_EORDER 5      /* out-of-order write to a pairwise matrix */
+#define KINC_SIM_EIO 8         /* a file could not be written (codes 6 and 7: include/kinc_rmt.h) */
 
 /* Work-block size the reference splits all pairs into (src/core/similarity.cpp:20). */
 #define KINC_SIM_WORK_BLOCK_SIZE 32768

@@ -12,7 +12,7 @@ from . import build as _build
 
 _lib = None
 
-OK, EINVAL, ECUDA, ENOMEM, EKERNEL, EORDER = 0, 1, 2, 3, 4, 5
+OK, EINVAL, ECUDA, ENOMEM, EKERNEL, EORDER, EIO = 0, 1, 2, 3, 4, 5, 8
 WORK_BLOCK_SIZE = 32768
 
 

@@ -110,7 +110,7 @@ int write_header(kinc_pm* m)
    if ( m->type == KINC_PM_CCM ) m->e.put<int32_t>(h, m->subsize);
    else m->e.put<int8_t>(h, (int8_t)m->subsize);
    if ( fseek(m->f, 0, SEEK_SET) != 0 || fwrite(h.data(), 1, h.size(), m->f) != h.size() )
-      return pm_fail(KINC_SIM_ECUDA, "cannot write the pairwise matrix header");
+      return pm_fail(KINC_SIM_EIO, "cannot write the pairwise matrix header");
    return KINC_SIM_OK;
 }
 
@@ -254,7 +254,7 @@ static int write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y
    const long pos = (long)(HEADER + m->offset) + (long)((m->clusters - n) * (int64_t)item);
    const size_t bytes = (size_t)n * item;
    if ( fseek(m->f, pos, SEEK_SET) != 0 || (bytes > 0 && fwrite(m->items.get(), 1, bytes, m->f) != bytes) )
-      return pm_fail(KINC_SIM_ECUDA, "write failed");
+      return pm_fail(KINC_SIM_EIO, "write failed");
    return KINC_SIM_OK;
 }
 
@@ -362,7 +362,7 @@ extern "C" int kinc_emx_write(const char* path, const float* gem, int32_t genes,
    for ( int64_t i = 0; i < (int64_t)genes * samples; ++i ) e.put<float>(b, gem[i]);
    const bool ok = fwrite(b.data(), 1, b.size(), f) == b.size();
    fclose(f);
-   return ok ? KINC_SIM_OK : pm_fail(KINC_SIM_EINVAL, "write failed");
+   return ok ? KINC_SIM_OK : pm_fail(KINC_SIM_EIO, "write failed");
 }
 
 extern "C" int kinc_emx_read_header(const char* path, int32_t little_endian, int32_t* genes, int32_t* samples)
@@ -537,13 +537,13 @@ extern "C" int kinc_pm_export_text(const char* ccm_path, const char* cmx_path, i
          if ( fwrite(line, 1, (size_t)n, out) != (size_t)n || fwrite(mask.data(), 1, mask.size(), out) != mask.size()
               || fputc('\n', out) == EOF )
          {
-            rc = pm_fail(KINC_SIM_EINVAL, "write to %s failed", out_path);
+            rc = pm_fail(KINC_SIM_EIO, "write to %s failed", out_path);
             break;
          }
       }
       i = j;
    }
-   if ( fclose(out) != 0 && rc == KINC_SIM_OK ) rc = pm_fail(KINC_SIM_EINVAL, "write to %s failed", out_path);
+   if ( fclose(out) != 0 && rc == KINC_SIM_OK ) rc = pm_fail(KINC_SIM_EIO, "write to %s failed", out_path);
    kinc_pm_close(cmx);
    kinc_pm_close(ccm);
    return rc;
@@ -763,7 +763,7 @@ extern "C" int kinc_pm_extract(const char* emx_path, const char* ccm_path, const
    if ( gml && fclose(gml) != 0 ) io_ok = false;
    kinc_pm_close(cmx);
    kinc_pm_close(ccm);
-   if ( rc == KINC_SIM_OK && !io_ok ) rc = pm_fail(KINC_SIM_EINVAL, "writing the network files failed");
+   if ( rc == KINC_SIM_OK && !io_ok ) rc = pm_fail(KINC_SIM_EIO, "writing the network files failed");
    return rc;
 }
 

@@ -241,3 +241,18 @@ def test_extract_literal_lines(tmp_path, native):
     assert '<edge source="1" target="0" samples="1191"/>' in g
     assert '<edge source="2" target="1" samples="1917"/>' in g
     assert g.endswith("  </graph>\n</graphml>\n")
+
+
+def test_unwritable_output_is_an_io_error(tmp_path, native):
+    """A file that cannot be written reports KINC_SIM_EIO (or EINVAL when it cannot even be opened)."""
+    import os
+    if os.geteuid() == 0:
+        target = "/proc/self/does-not-exist/x.cmx"     # root can write anywhere else
+    else:
+        d = tmp_path / "ro"
+        d.mkdir()
+        os.chmod(d, 0o500)
+        target = str(d / "x.cmx")
+    with pytest.raises(_native.SimError) as err:
+        pm.write(target, pm.CMX, 4, 2, 1, [1], [0], [0], np.array([[0.5]], np.float32))
+    assert err.value.code in (_native.EINVAL, _native.EIO)
