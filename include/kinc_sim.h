@@ -116,6 +116,17 @@ int kinc_sim_execute_block_device(kinc_sim_ctx* ctx, int64_t start, int64_t size
                                   int8_t* d_labels, float* d_corr, void* stream);
 int64_t kinc_sim_max_device_block(const kinc_sim_ctx* ctx);
 
+/*
+ * Same with HOST output arrays, stream-ordered on the context's stream: the
+ * block is computed and its K, labels and correlations copied back (to pinned
+ * arrays for the copies to run asynchronously) without waiting; the arrays
+ * are complete after kinc_sim_synchronize.  size must be <=
+ * kinc_sim_max_device_block(ctx), and one block may be in flight per context
+ * (the context's device buffers hold it).
+ */
+int kinc_sim_execute_block_async(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t* out_K,
+                                 int8_t* out_labels, float* out_corr);
+
 /* Synchronise the context's stream and report any kernel error status. */
 int kinc_sim_synchronize(kinc_sim_ctx* ctx);
 

@@ -49,6 +49,7 @@ SIGNATURES = {
     "kinc_sim_total_pairs": (_I64, [_VP]),
     "kinc_sim_num_work_blocks": (_I32, [_VP]),
     "kinc_sim_execute_block": (ctypes.c_int, [_VP, _I64, _I64, _VP, _VP, _VP]),
+    "kinc_sim_execute_block_async": (ctypes.c_int, [_VP, _I64, _I64, _VP, _VP, _VP]),
     "kinc_sim_execute_block_device": (ctypes.c_int, [_VP, _I64, _I64, _VP, _VP, _VP, _VP]),
     "kinc_sim_max_device_block": (_I64, [_VP]),
     "kinc_sim_synchronize": (ctypes.c_int, [_VP]),

@@ -880,6 +880,31 @@ extern "C" int kinc_sim_execute_block(kinc_sim_ctx* ctx, int64_t start, int64_t 
    return KINC_SIM_OK;
 }
 
+extern "C" int kinc_sim_execute_block_async(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t* out_K,
+                                            int8_t* out_labels, float* out_corr)
+{
+   if ( !ctx ) return KINC_SIM_EINVAL;
+   int rc = check_range(ctx, start, size);
+   if ( rc ) return rc;
+   if ( size > ctx->max_block )
+      return fail(ctx, KINC_SIM_EINVAL, "size %lld exceeds the device block limit %lld", (long long)size,
+                  (long long)ctx->max_block);
+   ctx->launches = 0;
+   if ( size == 0 ) return KINC_SIM_OK;
+   const int S = ctx->S;
+   const int floats = ctx->params.max_clusters * ctx->dp.ncorr;   /* per pair */
+   rc = enqueue_block(ctx, start, size, ctx->d_K, (out_labels && ctx->d_labels) ? ctx->d_labels : nullptr,
+                      ctx->d_corr, ctx->stream);
+   if ( rc ) return rc;
+   if ( out_K ) CK(cudaMemcpyAsync(out_K, ctx->d_K, size, cudaMemcpyDeviceToHost, ctx->stream));
+   if ( out_labels && ctx->d_labels )
+      CK(cudaMemcpyAsync(out_labels, ctx->d_labels, (size_t)size * S, cudaMemcpyDeviceToHost, ctx->stream));
+   if ( out_corr )
+      CK(cudaMemcpyAsync(out_corr, ctx->d_corr, (size_t)size * floats * sizeof(float), cudaMemcpyDeviceToHost,
+                         ctx->stream));
+   return KINC_SIM_OK;
+}
+
 extern "C" int kinc_sim_compact_block_device(kinc_sim_ctx* ctx, int64_t start, int64_t size, const int8_t* d_K,
                                              const int8_t* d_labels, const float* d_corr, int32_t* cmx_x,
                                              int32_t* cmx_y, int8_t* cmx_c, float* cmx_r, int64_t cap_cmx,

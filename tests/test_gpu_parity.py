@@ -66,3 +66,30 @@ def test_both_correlations_equal_single_method_runs(clus):
     assert np.array_equal(both.K, runs["pearson"].K)
     assert _corr_equal(both.corr[..., 0], runs["pearson"].corr)
     assert _corr_equal(both.corr[..., 1], runs["spearman"].corr)
+
+
+def test_execute_block_async_equals_execute_block():
+    """kinc_sim_execute_block_async into pinned host arrays, completed by kinc_sim_synchronize, returns
+    what the synchronous entry point returns."""
+    import ctypes
+
+    import torch
+
+    from kinc_gb300 import _native
+    gem = synthetic.generate(2, genes=70, samples=90)
+    sim = Similarity(gem, clusmethod="gmm", corrmethod="spearman", crit="BIC", postout=True)
+    sim.initialize()
+    L = _native.load()
+    start, size = 100, 1500
+    want = sim.execute(None, start=start, size=size)
+    K = torch.empty(size, dtype=torch.int8, pin_memory=True)
+    lab = torch.empty((size, 90), dtype=torch.int8, pin_memory=True)
+    corr = torch.empty((size, 5), dtype=torch.float32, pin_memory=True)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    _native.check(L.kinc_sim_execute_block_async(sim._ctx, start, size, vp(K), vp(lab), vp(corr)), sim._ctx)
+    _native.check(L.kinc_sim_synchronize(sim._ctx), sim._ctx)
+    sim.close()
+    assert np.array_equal(K.numpy(), want.K)
+    multi = want.K > 1
+    assert np.array_equal(lab.numpy()[multi], want.labels[multi])
+    assert _corr_equal(corr.numpy(), want.corr)
