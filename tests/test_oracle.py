@@ -150,3 +150,32 @@ def test_work_block_boundary_renews_packed_array():
     first = pyoracle.run_block(gem, p, 32000, 768)
     second = pyoracle.run_block(gem, p, 32768, 832)
     assert same_corr(both[2][:768], first[2]) and same_corr(both[2][768:], second[2])
+
+
+def _edge_cases():
+    import importlib.util
+    import os
+    path = os.path.join(os.path.dirname(__file__), "test_gpu_edge_cases.py")
+    spec = importlib.util.spec_from_file_location("edge_cases_for_oracle", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.CASES
+
+
+@pytest.mark.parametrize("case", _edge_cases(), ids=[c[0] for c in _edge_cases()])
+def test_oracle_equals_compiled_reference_on_edge_inputs(case):
+    """The restatement against KINC's own compiled Pairwise code on the GPU edge-case inputs
+    (fits beyond five clusters, long sorts, degenerate genes, tiny matrices): the oracle the GPU
+    edge tests compare with is itself pinned there."""
+    if pyoracle.ref_lib(0) is None:
+        pytest.skip("KINC source tree not present: compiled reference unavailable")
+    name, make, _, oargs = case
+    gem = make()
+    G = gem.shape[0]
+    total = G * (G - 1) // 2
+    p = pyoracle.params(**oargs)
+    a = pyoracle.run_block(gem, p, 0, total)
+    b = pyoracle.run_ref(gem, p, 0, total)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[3], b[3])
+    assert np.array_equal(a[1][a[0] > 1], b[1][b[0] > 1])
+    assert same_corr(a[2], b[2])
