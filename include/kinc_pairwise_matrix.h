@@ -93,6 +93,59 @@ int kinc_pm_extract(const char* emx_path, const char* ccm_path, const char* cmx_
                     int32_t little_endian, float min_corr, float max_corr, const char* tsv_path,
                     const char* graphml_path);
 
+/*
+ * ImportCorrelationMatrix (src/core/importcorrelationmatrix.cpp:22-141): the 11-column text that
+ * kinc_pm_export_text writes (and any file of that shape), read back into a CCM and a CMX file.
+ * Lines are split on white space.  A line of 11 fields is one cluster: fields 0 and 1 are the
+ * pair (x, y), field 9 the correlation and field 10 the sample mask (one digit per sample); the
+ * cluster number, cluster count and code counts are not read, the clusters of a pair being
+ * numbered in line order.  Consecutive lines of one pair form one pair; the CMX
+ * (one correlation per cluster) receives every pair, the CCM the pairs with
+ * more than one cluster (codes = the mask's digits, any other character code 15).  Lines of 0
+ * or 1 fields are skipped; any other field count, a mask whose length is not `samples`, a pair
+ * out of increasing order or outside `genes`, or more than max_clusters clusters is an error
+ * (KINC_SIM_EINVAL or KINC_SIM_EORDER) naming the line.  A field that is not a number reads as
+ * 0, as Qt's toInt/toFloat return it.
+ */
+int kinc_pm_import_text(const char* in_path, const char* ccm_path, const char* cmx_path, int32_t genes,
+                        int32_t max_clusters, int32_t samples, int32_t little_endian);
+
+/* ExpressionMatrix::Transform (src/core/expressionmatrix.h), the element-wise transform an
+ * expression matrix is imported with: "none", "natural logarithm", "logarithm base 2",
+ * "logarithm base 10". */
+#define KINC_EMX_TRANSFORM_NONE 0
+#define KINC_EMX_TRANSFORM_NLOG 1
+#define KINC_EMX_TRANSFORM_LOG2 2
+#define KINC_EMX_TRANSFORM_LOG10 3
+
+/*
+ * ImportExpressionMatrix (src/core/importexpressionmatrix.cpp:20-180): white-space separated
+ * text, one gene per line (name, then one value per sample), into an EMX file.  samples == 0:
+ * the first line holds the sample names and sets the sample count; else the samples are named
+ * 0..samples-1 and every line is a gene.  A value equal to nan_token (NULL or "": none) is NaN;
+ * any other is read as a double, rounded to float, then transformed (the float functions
+ * logf / log2f / log10f).  Blank lines are skipped.  A line whose field count is not
+ * samples + 1, or a value that is not a number, is KINC_SIM_EINVAL.  Gene and sample names,
+ * which KINC keeps as metadata, are written one per line to gene_names_path and
+ * sample_names_path when those are not NULL.
+ */
+int kinc_emx_import_text(const char* in_path, const char* nan_token, int32_t samples, int32_t transform,
+                         int32_t little_endian, const char* emx_path, const char* gene_names_path,
+                         const char* sample_names_path);
+
+/*
+ * ExportExpressionMatrix (src/core/exportexpressionmatrix.cpp:20-100): the EMX as text.  First
+ * line: each sample name followed by a tab; then per gene its name and, per sample, a tab and
+ * either nan_token (NaN; NULL = "") or the value with the import's transform undone (expf(v);
+ * 2^v, 10^v by pow in double, rounded to float) at 12 significant digits (%.12g).  Names are read one per
+ * line from gene_names_path / sample_names_path, or are the indices when NULL.  transform is the
+ * one the matrix was imported with (KINC stores it as metadata, which the EMX data section does
+ * not hold).
+ */
+int kinc_emx_export_text(const char* emx_path, int32_t little_endian, const char* gene_names_path,
+                         const char* sample_names_path, int32_t transform, const char* nan_token,
+                         const char* out_path);
+
 /* Message of the last failed kinc_pm_* / kinc_emx_* / kinc_sim_run_to_files call on this thread. */
 const char* kinc_pm_last_error(void);
 

@@ -4,9 +4,10 @@ The per-pair work (fetch/mask, Tukey outliers, GMM / K-means with BIC/ICL
 model selection, per-cluster Pearson / Spearman) runs in hand-written sm_103a
 CUDA kernels behind the C ABI in include/kinc_sim.h; this package is the
 host-side mirror of KINC's Similarity analytic over that ABI (Similarity),
-of the CCM/CMX/EMX files and the analytics that read them (pairwise_matrix:
-export-CMX text, network extraction; rmt.RMT: RMT thresholding), plus
-sharding (shard) and seeded synthetic workloads (synthetic).
+of the CCM/CMX/EMX files and the analytics on either side of them
+(pairwise_matrix: import/export of EMX and CMX text, network extraction;
+rmt.RMT: RMT thresholding), plus sharding (shard) and seeded synthetic
+workloads (synthetic).
 """
 from .similarity import (CLUSTERING_NAMES, CORRELATION_NAMES, CRITERION_NAMES, InvalidArgument,  # noqa: F401
                          PairwiseMatrix, ResultBlock, Similarity, WorkBlock)

@@ -5,14 +5,20 @@
     python -m kinc_gb300 run export-cmx --ccm a.ccm --cmx a.cmx --output a.txt
     python -m kinc_gb300 run extract --emx a.emx --ccm a.ccm --cmx a.cmx --output net.txt --graphml net.graphml
     python -m kinc_gb300 run rmt --input a.cmx --log rmt.log
+    python -m kinc_gb300 run import-emx --input a.txt --output a.emx --nan NA --names a.genes
+    python -m kinc_gb300 run export-emx --input a.emx --output b.txt --nan NA --names a.genes
+    python -m kinc_gb300 run import-cmx --input a.txt --ccm a.ccm --cmx a.cmx --genes 100 --maxclusters 5 \\
+        --samples 40 --corrname pearson
 
-Analytic names follow src/core/analyticfactory.cpp:53-59; arguments follow each
+Analytic names follow src/core/analyticfactory.cpp:49-55; arguments follow each
 analytic's input class (src/core/similarity_input.cpp, exportcorrelationmatrix_input.cpp,
-extract_input.cpp, rmt_input.cpp), with the reference's defaults.  Boolean
-arguments take no value or an explicit true/false.  Expression matrices are
-the EMX data section (include/kinc_pairwise_matrix.h); --names gives gene names
-for extract (one per line).  Files use the big-endian byte order unless
---little-endian is given.
+extract_input.cpp, rmt_input.cpp, importexpressionmatrix_input.cpp,
+exportexpressionmatrix_input.cpp, importcorrelationmatrix_input.cpp), with the
+reference's defaults.  Boolean arguments take no value or an explicit true/false.
+Expression matrices are the EMX data section (include/kinc_pairwise_matrix.h);
+gene and sample names, metadata in KINC, are text files with one name per line
+(--names, --sample-names): written by import-emx, read by export-emx and
+extract.  Files use the big-endian byte order unless --little-endian is given.
 """
 import argparse
 import math
@@ -87,6 +93,37 @@ def _parser():
     rmt.add_argument("--maxpace", type=int, default=40)
     rmt.add_argument("--bins", type=int, default=60)
     common(rmt)
+
+    from .pairwise_matrix import TRANSFORMS
+    iem = an.add_parser("import-emx", help="text -> expression matrix (EMX)")
+    iem.add_argument("--input", required=True, help="text: one gene per line, name then one value per sample")
+    iem.add_argument("--output", required=True, help="expression matrix (EMX data section)")
+    iem.add_argument("--nan", help="token of a missing value")
+    iem.add_argument("--samples", type=int, default=0, help="sample count; 0: the first line names the samples")
+    iem.add_argument("--transform", default=TRANSFORMS[0], choices=TRANSFORMS)
+    iem.add_argument("--names", help="gene names written here, one per line")
+    iem.add_argument("--sample-names", help="sample names written here, one per line")
+    common(iem)
+
+    eem = an.add_parser("export-emx", help="expression matrix (EMX) -> text")
+    eem.add_argument("--input", required=True)
+    eem.add_argument("--output", required=True)
+    eem.add_argument("--nan", help="token written for a missing value")
+    eem.add_argument("--transform", default=TRANSFORMS[0], choices=TRANSFORMS,
+                     help="the transform the matrix was imported with (undone on export)")
+    eem.add_argument("--names", help="gene names, one per line")
+    eem.add_argument("--sample-names", help="sample names, one per line")
+    common(eem)
+
+    icm = an.add_parser("import-cmx", help="text (as export-cmx writes it) -> CCM + CMX")
+    icm.add_argument("--input", required=True)
+    icm.add_argument("--ccm", required=True)
+    icm.add_argument("--cmx", required=True)
+    icm.add_argument("--genes", type=int, required=True)
+    icm.add_argument("--maxclusters", type=int, required=True)
+    icm.add_argument("--samples", type=int, required=True)
+    icm.add_argument("--corrname", required=True, help="correlation name (KINC metadata; not stored in the files)")
+    common(icm)
     return ap
 
 
@@ -124,6 +161,17 @@ def main(argv=None):
                        maxpace=args.maxpace, bins=args.bins).run(input=args.input, log=args.log,
                                                                  little_endian=args.little_endian)
             print(f"threshold: {t:g}")
+        elif args.analytic == "import-emx":
+            pm.import_emx_text(args.input, args.output, nan=args.nan, samples=args.samples, transform=args.transform,
+                               gene_names_path=args.names, sample_names_path=args.sample_names,
+                               little_endian=args.little_endian)
+        elif args.analytic == "export-emx":
+            pm.export_emx_text(args.input, args.output, nan=args.nan, transform=args.transform,
+                               gene_names_path=args.names, sample_names_path=args.sample_names,
+                               little_endian=args.little_endian)
+        elif args.analytic == "import-cmx":
+            pm.import_text(args.input, args.ccm, args.cmx, args.genes, args.maxclusters, args.samples,
+                           little_endian=args.little_endian)
     except (_native.SimError, ValueError) as e:
         print(f"{args.analytic}: {e}", file=sys.stderr)
         return 1

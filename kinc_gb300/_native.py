@@ -93,6 +93,11 @@ SIGNATURES = {
     "kinc_pm_extract": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _I32,
                                         ctypes.c_float, ctypes.c_float, ctypes.c_char_p, ctypes.c_char_p]),
     "kinc_pm_export_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _I32, ctypes.c_char_p]),
+    "kinc_pm_import_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _I32, _I32, _I32, _I32]),
+    "kinc_emx_import_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _I32, _I32, _I32, ctypes.c_char_p,
+                                            ctypes.c_char_p, ctypes.c_char_p]),
+    "kinc_emx_export_text": (ctypes.c_int, [ctypes.c_char_p, _I32, ctypes.c_char_p, ctypes.c_char_p, _I32,
+                                            ctypes.c_char_p, ctypes.c_char_p]),
     "kinc_sim_run_to_files_ex": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_char_p, _I32, _I64, _I64, _I64]),
     "kinc_sim_execute_block_noalloc": (ctypes.c_int, [_VP, _I32, _I32, ctypes.POINTER(SimParams), _I64, _I64,
                                                       _VP, _VP, _VP, _VP]),

@@ -31,6 +31,7 @@ UNITS = [
     ("pearson_gemm.cu", []),
     ("compact.cu", []),
     ("pairwise_file.cpp", []),
+    ("text_io.cpp", []),
     ("rmt.cu", []),
 ]
 

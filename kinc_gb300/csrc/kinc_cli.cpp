@@ -1,10 +1,12 @@
 /*
  * kinc_cli.cpp -- the native host driver: `kinc-gb300 run <analytic> --arg value ...` with
- * KINC's analytic names (src/core/analyticfactory.cpp:53-59) and argument names and defaults
+ * KINC's analytic names (src/core/analyticfactory.cpp:49-55) and argument names and defaults
  * (src/core/similarity_input.cpp, exportcorrelationmatrix_input.cpp, extract_input.cpp,
- * rmt_input.cpp).  It does what ACE's serial runner does for these analytics, through the C ABI
- * only: read the expression matrix, create the worker, run the ordered block loop into the
- * CCM/CMX files (include/kinc_pairwise_matrix.h), or run the analytics downstream of them.
+ * rmt_input.cpp, importexpressionmatrix_input.cpp, exportexpressionmatrix_input.cpp,
+ * importcorrelationmatrix_input.cpp).  It does what ACE's serial runner does for these
+ * analytics, through the C ABI only: read the expression matrix, create the worker, run the
+ * ordered block loop into the CCM/CMX files (include/kinc_pairwise_matrix.h), run the analytics
+ * downstream of them, or convert text to and from the matrix files.
  */
 #include "../../include/kinc_pairwise_matrix.h"
 #include "../../include/kinc_rmt.h"
@@ -54,7 +56,15 @@ int usage()
            "       kinc-gb300 run extract --emx EMX --ccm CCM --cmx CMX [--output TXT] [--graphml XML] [--mincorr F]\n"
            "           [--maxcorr F] [--names TXT]\n"
            "       kinc-gb300 run rmt --input CMX --log TXT [--tstart F] [--tstep F] [--tstop F] [--minpace N]\n"
-           "           [--maxpace N] [--bins N]\n");
+           "           [--maxpace N] [--bins N]\n"
+           "       kinc-gb300 run import-emx --input TXT --output EMX [--nan TOKEN] [--samples N] [--transform NAME]\n"
+           "           [--names TXT] [--sample-names TXT]\n"
+           "       kinc-gb300 run export-emx --input EMX --output TXT [--nan TOKEN] [--transform NAME] [--names TXT]\n"
+           "           [--sample-names TXT]\n"
+           "       kinc-gb300 run import-cmx --input TXT --ccm CCM --cmx CMX --genes N --maxclusters N --samples N\n"
+           "           --corrname NAME\n"
+           "  (every analytic takes --little-endian; --transform: none, \"natural logarithm\", \"logarithm base 2\",\n"
+           "   \"logarithm base 10\")\n");
    return 2;
 }
 
@@ -226,6 +236,69 @@ int run_rmt(const Args& a)
    return 0;
 }
 
+const std::vector<std::string> TRANSFORMS = { "none", "natural logarithm", "logarithm base 2", "logarithm base 10" };
+
+const char* opt(const Args& a, const char* k)
+{
+   auto it = a.kv.find(k);
+   return it == a.kv.end() ? nullptr : it->second.c_str();
+}
+
+int run_import_emx(const Args& a)
+{
+   if ( !a.has("input") || !a.has("output") )
+   {
+      fprintf(stderr, "import-emx: --input and --output are required\n");
+      return 2;
+   }
+   bool ok = true;
+   const int t = choice(a.str("transform", "none"), TRANSFORMS, "transform", ok);
+   if ( !ok ) return 2;
+   const int rc = kinc_emx_import_text(opt(a, "input"), opt(a, "nan"), std::atoi(a.str("samples", "0").c_str()), t,
+                                       a.str("little-endian", "0") == "1", opt(a, "output"), opt(a, "names"),
+                                       opt(a, "sample-names"));
+   if ( rc != KINC_SIM_OK ) fprintf(stderr, "import-emx: %s\n", kinc_pm_last_error());
+   return rc == KINC_SIM_OK ? 0 : 1;
+}
+
+int run_export_emx(const Args& a)
+{
+   if ( !a.has("input") || !a.has("output") )
+   {
+      fprintf(stderr, "export-emx: --input and --output are required\n");
+      return 2;
+   }
+   bool ok = true;
+   const int t = choice(a.str("transform", "none"), TRANSFORMS, "transform", ok);
+   if ( !ok ) return 2;
+   const int rc = kinc_emx_export_text(opt(a, "input"), a.str("little-endian", "0") == "1", opt(a, "names"),
+                                       opt(a, "sample-names"), t, opt(a, "nan"), opt(a, "output"));
+   if ( rc != KINC_SIM_OK ) fprintf(stderr, "export-emx: %s\n", kinc_pm_last_error());
+   return rc == KINC_SIM_OK ? 0 : 1;
+}
+
+int run_import_cmx(const Args& a)
+{
+   for ( const char* k : { "input", "ccm", "cmx", "genes", "maxclusters", "samples" } )
+      if ( !a.has(k) )
+      {
+         fprintf(stderr, "import-cmx: --input, --ccm, --cmx, --genes, --maxclusters, --samples and --corrname are "
+                         "required\n");
+         return 2;
+      }
+   /* the correlation's name is metadata in KINC; it is required there, and not stored in the files */
+   if ( a.str("corrname").empty() )
+   {
+      fprintf(stderr, "import-cmx: Correlation name is required.\n");
+      return 2;
+   }
+   const int rc = kinc_pm_import_text(opt(a, "input"), opt(a, "ccm"), opt(a, "cmx"), std::atoi(a.str("genes").c_str()),
+                                      std::atoi(a.str("maxclusters").c_str()), std::atoi(a.str("samples").c_str()),
+                                      a.str("little-endian", "0") == "1");
+   if ( rc != KINC_SIM_OK ) fprintf(stderr, "import-cmx: %s\n", kinc_pm_last_error());
+   return rc == KINC_SIM_OK ? 0 : 1;
+}
+
 }  // namespace
 
 int main(int argc, char** argv)
@@ -243,6 +316,9 @@ int main(int argc, char** argv)
    if ( an == "export-cmx" ) return run_export(a);
    if ( an == "extract" ) return run_extract(a);
    if ( an == "rmt" ) return run_rmt(a);
+   if ( an == "import-emx" ) return run_import_emx(a);
+   if ( an == "export-emx" ) return run_export_emx(a);
+   if ( an == "import-cmx" ) return run_import_cmx(a);
    fprintf(stderr, "unknown analytic %s\n", an.c_str());
    return usage();
 }

@@ -25,14 +25,20 @@ namespace {
 
 thread_local std::string t_err;
 
-int pm_fail(int code, const char* fmt, ...)
+int pm_vfail(int code, const char* fmt, va_list ap)
 {
    char buf[512];
+   vsnprintf(buf, sizeof buf, fmt, ap);
+   t_err = buf;
+   return code;
+}
+
+__attribute__((format(printf, 2, 3))) int pm_fail(int code, const char* fmt, ...)
+{
    va_list ap;
    va_start(ap, fmt);
-   vsnprintf(buf, sizeof buf, fmt, ap);
+   pm_vfail(code, fmt, ap);
    va_end(ap);
-   t_err = buf;
    return code;
 }
 
@@ -115,6 +121,15 @@ int write_header(kinc_pm* m)
 }
 
 }  // namespace
+
+int kinc_pm_fail(int code, const char* fmt, ...)
+{
+   va_list ap;
+   va_start(ap, fmt);
+   pm_vfail(code, fmt, ap);
+   va_end(ap);
+   return code;
+}
 
 extern "C" const char* kinc_pm_last_error(void)
 {
@@ -570,39 +585,8 @@ extern "C" int kinc_pm_extract(const char* emx_path, const char* ccm_path, const
    if ( rc ) return rc;
    std::vector<float> gem((size_t)G * S);
    if ( (rc = kinc_emx_read(emx_path, little_endian, gem.data(), (int64_t)gem.size())) ) return rc;
-   std::vector<std::string> names((size_t)G);
-   if ( names_path )
-   {
-      FILE* nf = fopen(names_path, "rb");
-      if ( !nf ) return pm_fail(KINC_SIM_EINVAL, "cannot open %s", names_path);
-      std::string cur;
-      int32_t n = 0;
-      for ( int ch; (ch = fgetc(nf)) != EOF; )
-      {
-         if ( ch == '\n' )
-         {
-            if ( !cur.empty() && cur.back() == '\r' ) cur.pop_back();
-            if ( n < G ) names[(size_t)n] = cur;
-            ++n;
-            cur.clear();
-         }
-         else
-         {
-            cur.push_back((char)ch);
-         }
-      }
-      if ( !cur.empty() )
-      {
-         if ( n < G ) names[(size_t)n] = cur;
-         ++n;
-      }
-      fclose(nf);
-      if ( n != G ) return pm_fail(KINC_SIM_EINVAL, "%s holds %d names for %d genes", names_path, n, G);
-   }
-   else
-   {
-      for ( int32_t g = 0; g < G; ++g ) names[(size_t)g] = std::to_string(g);
-   }
+   std::vector<std::string> names;
+   if ( (rc = kinc_pm_read_names(names_path, G, "genes", names)) ) return rc;
 
    kinc_pm *cmx = nullptr, *ccm = nullptr;
    int32_t g1 = 0, k1 = 0, nc = 0, g2 = 0, k2 = 0, S2 = 0;

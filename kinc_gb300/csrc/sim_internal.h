@@ -16,4 +16,16 @@
  * without synchronising the context. */
 int kinc_sim_status_copy_async(kinc_sim_ctx* ctx, uint64_t* dst, cudaStream_t stream);
 
+/* Record the message kinc_pm_last_error returns on this thread; returns code. */
+int kinc_pm_fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+
+#ifdef __cplusplus
+#include <string>
+#include <vector>
+
+/* Names one per line (a trailing '\r' dropped); exactly `expected` of them, else
+ * KINC_SIM_EINVAL naming `what`.  path NULL: the indices 0..expected-1. */
+int kinc_pm_read_names(const char* path, int64_t expected, const char* what, std::vector<std::string>& names);
+#endif
+
 #endif

@@ -82,3 +82,43 @@ def extract(emx_path, ccm_path, cmx_path, tsv_path=None, graphml_path=None, name
     _check(_native.load().kinc_pm_extract(enc(emx_path), enc(ccm_path), enc(cmx_path), enc(names_path),
                                           int(little_endian), float(min_corr), float(max_corr), enc(tsv_path),
                                           enc(graphml_path)))
+
+
+def import_text(in_path, ccm_path, cmx_path, genes, max_clusters, samples, little_endian=False):
+    """ImportCorrelationMatrix: 11-column text (as export_text writes it) -> CCM + CMX files."""
+    _check(_native.load().kinc_pm_import_text(str(in_path).encode(), str(ccm_path).encode(), str(cmx_path).encode(),
+                                              int(genes), int(max_clusters), int(samples), int(little_endian)))
+
+
+# ExpressionMatrix::TRANSFORM_NAMES (src/core/expressionmatrix.cpp:8-14), in their enum order
+TRANSFORMS = ("none", "natural logarithm", "logarithm base 2", "logarithm base 10")
+
+
+def _transform(t):
+    if isinstance(t, int):
+        if not 0 <= t < len(TRANSFORMS):
+            raise ValueError(f"transform {t} is not one of 0..{len(TRANSFORMS) - 1}")
+        return t
+    names = [n.lower() for n in TRANSFORMS]
+    if str(t).lower() not in names:
+        raise ValueError(f"transform must be one of {', '.join(TRANSFORMS)}")
+    return names.index(str(t).lower())
+
+
+def import_emx_text(in_path, emx_path, nan=None, samples=0, transform="none", gene_names_path=None,
+                    sample_names_path=None, little_endian=False):
+    """ImportExpressionMatrix: text (gene name + one value per sample per line; with samples=0 the
+    first line names the samples) -> EMX; the names go one per line to the *_names_path files."""
+    enc = lambda p: str(p).encode() if p is not None else None  # noqa: E731
+    _check(_native.load().kinc_emx_import_text(enc(in_path), enc(nan), int(samples), _transform(transform),
+                                               int(little_endian), enc(emx_path), enc(gene_names_path),
+                                               enc(sample_names_path)))
+
+
+def export_emx_text(emx_path, out_path, nan=None, transform="none", gene_names_path=None, sample_names_path=None,
+                    little_endian=False):
+    """ExportExpressionMatrix: EMX -> text, undoing the transform the matrix was imported with."""
+    enc = lambda p: str(p).encode() if p is not None else None  # noqa: E731
+    _check(_native.load().kinc_emx_export_text(enc(emx_path), int(little_endian), enc(gene_names_path),
+                                               enc(sample_names_path), _transform(transform), enc(nan),
+                                               enc(out_path)))

@@ -9,7 +9,10 @@ arm may import this module.  It wraps:
   to build them.
 """
 import ctypes
+import ctypes.util
+import math
 import os
+import re
 
 import numpy as np
 
@@ -316,6 +319,185 @@ def extract_network(gem, cmx, ccm, S, names=None, min_corr=0.85, max_corr=1.0):
         i = j
     gml.append("  </graph>\n</graphml>\n")
     return "".join(tsv), "".join(gml)
+
+
+# ----------------------------------------------------------------------------- text import / export
+# The text analytics restated over Python strings: QTextStream's readLine + split on white
+# space, QString::toInt / toDouble / toFloat in the C locale, and the number formats of the
+# writers.  Parse failures raise TextError.
+
+class TextError(ValueError):
+    """A line the reference's import rejects; .order is True for a pair out of increasing order."""
+
+    def __init__(self, msg, order=False):
+        super().__init__(msg)
+        self.order = order
+
+
+_NUMBER = re.compile(r"(\d+\.?\d*|\.\d+)([eE][+-]?\d+)?")
+_INT = re.compile(r"[+-]?\d+")
+_SPACE = re.compile(r"[ \t\n\r\v\f]+")
+
+
+def _fields(line):
+    """The line split on ASCII white space, empty parts dropped."""
+    return [w for w in _SPACE.split(line) if w]
+
+
+def qt_to_double(w):
+    """QString::toDouble: a float, or None when the field is not a number (overflow and
+    underflow to zero included)."""
+    sign, body = (w[0], w[1:]) if w[:1] in ("+", "-") else ("", w)
+    if body.lower() == "inf":
+        return -math.inf if sign == "-" else math.inf
+    if not sign and body.lower() == "nan":
+        return math.nan
+    m = _NUMBER.fullmatch(body)
+    if not m:
+        return None
+    v = float(body)
+    if math.isinf(v) or (v == 0.0 and any(ch in "123456789" for ch in m.group(1))):
+        return None
+    return -v if sign == "-" else v
+
+
+def qt_to_int(w):
+    """QString::toInt: 0 unless the field is an int."""
+    if not _INT.fullmatch(w):
+        return 0
+    v = int(w)
+    return v if -2**31 <= v < 2**31 else 0
+
+
+_libm = None
+
+
+def _libm_float(name):
+    """The C library's float function `name` (logf, expf, ...), which the reference's calls on a
+    float value resolve to."""
+    global _libm
+    if _libm is None:
+        _libm = ctypes.CDLL(ctypes.util.find_library("m") or "libm.so.6")
+    f = getattr(_libm, name)
+    f.restype, f.argtypes = ctypes.c_float, [ctypes.c_float]
+    return f
+
+
+def _transform_value(v, transform):
+    """ImportExpressionMatrix's transform of the float value (src/core/importexpressionmatrix.cpp:
+    108-123): log, log2, log10 of a float."""
+    v = np.float32(v)
+    if transform in (1, 2, 3):
+        return np.float32(_libm_float(("logf", "log2f", "log10f")[transform - 1])(float(v)))
+    return v
+
+
+def import_emx_text(text, nan=None, samples=0, transform=0):
+    """ImportExpressionMatrix::process restated (src/core/importexpressionmatrix.cpp:20-180);
+    returns (gem float32 [genes][samples], gene names, sample names).  Lines without fields are
+    skipped."""
+    S = samples
+    sample_names = [str(i) for i in range(S)]
+    gene_names, rows = [], []
+    for line in text.split("\n"):
+        w = _fields(line)
+        if not w:
+            continue
+        if S == 0:
+            S = len(w)
+            sample_names = list(w)
+            continue
+        if len(w) != S + 1:
+            raise TextError(f"Encountered gene expression line with incorrect amount of fields. Read in {len(w) - 1} "
+                            f"fields when it should have been {S}. Gene name is {w[0]}.")
+        row = []
+        for tok in w[1:]:
+            if nan and tok == nan:
+                row.append(np.float32(math.nan))
+                continue
+            d = qt_to_double(tok)
+            if d is None:
+                raise TextError(f'Failed to read expression value "{tok}" for gene {w[0]}.')
+            row.append(_transform_value(d, transform))
+        gene_names.append(w[0])
+        rows.append(row)
+    return np.array(rows, np.float32).reshape(len(rows), S), gene_names, sample_names
+
+
+def export_emx_text(gem, gene_names=None, sample_names=None, transform=0, nan=None):
+    """ExportExpressionMatrix::process restated (src/core/exportexpressionmatrix.cpp:20-100): the
+    transform undone on the float (exp of a float; pow(2 or 10, v) in double, rounded to float),
+    printed at 12 significant digits."""
+    G, S = gem.shape
+    gene_names = [str(g) for g in range(G)] if gene_names is None else gene_names
+    sample_names = [str(s) for s in range(S)] if sample_names is None else sample_names
+    out = ["".join(f"{n}\t" for n in sample_names), "\n"]
+    for g in range(G):
+        out.append(gene_names[g])
+        for s in range(S):
+            v = np.float32(gem[g, s])
+            if np.isnan(v):
+                out.append("\t" + (nan or ""))
+                continue
+            if transform == 1:
+                v = np.float32(_libm_float("expf")(float(v)))
+            elif transform == 2:
+                v = np.float32(math.pow(2.0, float(v)))
+            elif transform == 3:
+                v = np.float32(math.pow(10.0, float(v)))
+            out.append("\t%.12g" % float(v))
+        out.append("\n")
+    return "".join(out)
+
+
+def import_cmx_text(text, genes, max_clusters, samples):
+    """ImportCorrelationMatrix::process restated (src/core/importcorrelationmatrix.cpp:22-141) as
+    its loop intends: consecutive lines of one pair are its clusters, numbered in line order; the
+    pair is written once (CMX always, CCM when it has more than one cluster); lines of 0 or 1
+    fields are skipped.  Returns (ccm, cmx) item dicts like pairwise_matrix.read's."""
+    ccm = dict(x=[], y=[], c=[], payload=[])
+    cmx = dict(x=[], y=[], c=[], payload=[])
+    pending, cur, last = [], None, -1
+
+    def close():
+        for k, (r, codes) in enumerate(pending):
+            cmx["x"].append(cur[0]), cmx["y"].append(cur[1]), cmx["c"].append(k), cmx["payload"].append([r])
+            if len(pending) > 1:
+                ccm["x"].append(cur[0]), ccm["y"].append(cur[1]), ccm["c"].append(k), ccm["payload"].append(codes)
+        pending.clear()
+
+    for line in text.split("\n"):
+        w = _fields(line)
+        if len(w) <= 1:
+            continue
+        if len(w) != 11:
+            raise TextError(f"Encountered line with incorrect amount of fields. Read {len(w)} fields when there "
+                            f"should have been 11.")
+        x, y = qt_to_int(w[0]), qt_to_int(w[1])
+        d = qt_to_double(w[9])
+        r = np.float32(0.0 if d is None else d)
+        mask = w[10]
+        if len(mask) != samples:
+            raise TextError(f"Encountered sample mask with invalid length {len(mask)}. Sample size is {samples}.")
+        if x < 1 or y < 0 or x <= y or x >= genes:
+            raise TextError(f"Cannot initialize pairwise index ({x}, {y}).")
+        if not pending or (x, y) != cur:
+            p = x * (x - 1) // 2 + y
+            if p <= last:
+                raise TextError(f"pair ({x}, {y}) out of order", order=True)
+            close()
+            cur, last = (x, y), p
+        if len(pending) + 1 > max_clusters:
+            raise TextError(f"Cannot write pair with cluster size {len(pending) + 1} exceeding the max of "
+                            f"{max_clusters}.")
+        pending.append((r, [int(ch) if "0" <= ch <= "9" else -1 for ch in mask]))
+    close()
+    for d, dt in ((ccm, np.int8), (cmx, np.float32)):
+        for key in ("x", "y"):
+            d[key] = np.array(d[key], np.int32)
+        d["c"] = np.array(d["c"], np.int8)
+        d["payload"] = np.array(d["payload"], dt).reshape(len(d["c"]), samples if dt is np.int8 else 1)
+    return ccm, cmx
 
 
 # ----------------------------------------------------------------------------- RMT
