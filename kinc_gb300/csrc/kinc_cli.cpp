@@ -13,6 +13,8 @@
 #include "../../include/kinc_sim.h"
 
 #include <cctype>
+#include <cerrno>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -27,6 +29,8 @@ namespace {
 struct Args
 {
    std::map<std::string, std::string> kv;
+   /* cleared when a numeric argument does not parse (the message is printed) */
+   mutable bool ok {true};
 
    bool has(const std::string& k) const { return kv.count(k) > 0; }
    std::string str(const std::string& k, const std::string& d = "") const
@@ -34,6 +38,53 @@ struct Args
       auto it = kv.find(k);
       return it == kv.end() ? d : it->second;
    }
+   /* a decimal number (inf and nan included) */
+   double real(const std::string& k, double d) const
+   {
+      if ( !has(k) ) return d;
+      const std::string v = str(k);
+      char* end = nullptr;
+      const double x = std::strtod(v.c_str(), &end);
+      if ( v.empty() || *end != '\0' ) return bad(k, "a number"), d;
+      return x;
+   }
+   long long integer(const std::string& k, long long d) const
+   {
+      if ( !has(k) ) return d;
+      const std::string v = str(k);
+      char* end = nullptr;
+      errno = 0;
+      const long long x = std::strtoll(v.c_str(), &end, 10);
+      if ( v.empty() || *end != '\0' || errno == ERANGE ) return bad(k, "an integer"), d;
+      return x;
+   }
+   int int32(const std::string& k, int d) const
+   {
+      const long long x = integer(k, d);
+      if ( x < INT32_MIN || x > INT32_MAX ) return bad(k, "a 32-bit integer"), d;
+      return (int)x;
+   }
+
+private:
+   void bad(const std::string& k, const char* what) const
+   {
+      fprintf(stderr, "--%s takes %s, got %s\n", k.c_str(), what, str(k).c_str());
+      ok = false;
+   }
+};
+
+/* The arguments each analytic takes (its input class's command-line names, plus the shard
+ * and file options of this program). */
+const std::map<std::string, std::vector<std::string>> KEYS = {
+   { "similarity", { "input", "ccm", "cmx", "clusmethod", "corrmethod", "minexpr", "minsamp", "minclus", "maxclus",
+                     "crit", "preout", "postout", "mincorr", "maxcorr", "ksize", "semantics", "precision",
+                     "first-block", "blocks", "little-endian" } },
+   { "export-cmx", { "ccm", "cmx", "output", "little-endian" } },
+   { "extract", { "emx", "ccm", "cmx", "output", "graphml", "mincorr", "maxcorr", "names", "little-endian" } },
+   { "rmt", { "input", "log", "tstart", "tstep", "tstop", "minpace", "maxpace", "bins", "little-endian" } },
+   { "import-emx", { "input", "output", "nan", "samples", "transform", "names", "sample-names", "little-endian" } },
+   { "export-emx", { "input", "output", "nan", "transform", "names", "sample-names", "little-endian" } },
+   { "import-cmx", { "input", "ccm", "cmx", "genes", "maxclusters", "samples", "corrname", "little-endian" } },
 };
 
 const std::vector<std::string> BOOLEANS = { "preout", "postout", "little-endian" };
@@ -132,6 +183,26 @@ int run_similarity(const Args& a)
       fprintf(stderr, "similarity: --input and --ccm and/or --cmx are required\n");
       return 2;
    }
+   kinc_sim_params p;
+   kinc_sim_params_default(&p);
+   bool ok = true;
+   p.clus_method = choice(a.str("clusmethod", "none"), { "none", "gmm", "kmeans" }, "clusmethod", ok);
+   p.corr_method = choice(a.str("corrmethod", "pearson"), { "pearson", "spearman", "both" }, "corrmethod", ok);
+   p.criterion = choice(a.str("crit", "ICL"), { "BIC", "ICL" }, "crit", ok);
+   p.semantics = choice(a.str("semantics", "reference"), { "reference", "fixed" }, "semantics", ok);
+   p.precision = choice(a.str("precision", "fp32"), { "fp32", "tf32", "3xbf16" }, "precision", ok);
+   if ( !ok ) return 2;
+   p.min_expr = (float)a.real("minexpr", p.min_expr);
+   p.min_samples = a.int32("minsamp", 30);
+   p.min_clusters = a.int32("minclus", 1);
+   p.max_clusters = a.int32("maxclus", 5);
+   p.pre_out = a.str("preout", "0") == "1";
+   p.post_out = a.str("postout", "0") == "1";
+   p.min_corr = (float)a.real("mincorr", 0.5);
+   p.max_corr = (float)a.real("maxcorr", 1.0);
+   p.ksize = a.int32("ksize", 4096);
+   const long long first_block = a.integer("first-block", 0), blocks = a.integer("blocks", -1);
+   if ( !a.ok ) return 2;
    const int le = a.str("little-endian", "0") == "1";
    int32_t G = 0, S = 0;
    if ( kinc_emx_read_header(a.str("input").c_str(), le, &G, &S) != KINC_SIM_OK )
@@ -145,24 +216,6 @@ int run_similarity(const Args& a)
       fprintf(stderr, "similarity: %s\n", kinc_pm_last_error());
       return 1;
    }
-   kinc_sim_params p;
-   kinc_sim_params_default(&p);
-   bool ok = true;
-   p.clus_method = choice(a.str("clusmethod", "none"), { "none", "gmm", "kmeans" }, "clusmethod", ok);
-   p.corr_method = choice(a.str("corrmethod", "pearson"), { "pearson", "spearman", "both" }, "corrmethod", ok);
-   p.criterion = choice(a.str("crit", "ICL"), { "BIC", "ICL" }, "crit", ok);
-   p.semantics = choice(a.str("semantics", "reference"), { "reference", "fixed" }, "semantics", ok);
-   p.precision = choice(a.str("precision", "fp32"), { "fp32", "tf32", "3xbf16" }, "precision", ok);
-   if ( !ok ) return 2;
-   if ( a.has("minexpr") ) p.min_expr = (float)std::strtod(a.str("minexpr").c_str(), nullptr);
-   p.min_samples = std::atoi(a.str("minsamp", "30").c_str());
-   p.min_clusters = std::atoi(a.str("minclus", "1").c_str());
-   p.max_clusters = std::atoi(a.str("maxclus", "5").c_str());
-   p.pre_out = a.str("preout", "0") == "1";
-   p.post_out = a.str("postout", "0") == "1";
-   p.min_corr = (float)std::strtod(a.str("mincorr", "0.5").c_str(), nullptr);
-   p.max_corr = (float)std::strtod(a.str("maxcorr", "1").c_str(), nullptr);
-   p.ksize = std::atoi(a.str("ksize", "4096").c_str());
    kinc_sim_ctx* ctx = nullptr;
    int rc = kinc_sim_create(gem.data(), G, S, &p, &ctx);
    if ( rc != KINC_SIM_OK )
@@ -172,8 +225,7 @@ int run_similarity(const Args& a)
    }
    rc = kinc_sim_run_to_files_ex(ctx, a.has("ccm") ? a.str("ccm").c_str() : nullptr,
                                  a.has("cmx") ? a.str("cmx").c_str() : nullptr, le,
-                                 std::atoll(a.str("first-block", "0").c_str()),
-                                 std::atoll(a.str("blocks", "-1").c_str()), 0);
+                                 first_block, blocks, 0);
    if ( rc != KINC_SIM_OK ) fprintf(stderr, "similarity: %s\n", kinc_pm_last_error());
    kinc_sim_destroy(ctx);
    return rc == KINC_SIM_OK ? 0 : 1;
@@ -199,11 +251,12 @@ int run_extract(const Args& a)
       fprintf(stderr, "extract: --emx, --ccm, --cmx and --output and/or --graphml are required\n");
       return 2;
    }
+   const float min_corr = (float)a.real("mincorr", 0.85), max_corr = (float)a.real("maxcorr", 1.0);
+   if ( !a.ok ) return 2;
    const int rc = kinc_pm_extract(a.str("emx").c_str(), a.str("ccm").c_str(), a.str("cmx").c_str(),
                                   a.has("names") ? a.str("names").c_str() : nullptr,
                                   a.str("little-endian", "0") == "1",
-                                  (float)std::strtod(a.str("mincorr", "0.85").c_str(), nullptr),
-                                  (float)std::strtod(a.str("maxcorr", "1").c_str(), nullptr),
+                                  min_corr, max_corr,
                                   a.has("output") ? a.str("output").c_str() : nullptr,
                                   a.has("graphml") ? a.str("graphml").c_str() : nullptr);
    if ( rc != KINC_SIM_OK ) fprintf(stderr, "extract: %s\n", kinc_pm_last_error());
@@ -219,12 +272,13 @@ int run_rmt(const Args& a)
    }
    kinc_rmt_params p;
    kinc_rmt_params_default(&p);
-   if ( a.has("tstart") ) p.threshold_start = (float)std::strtod(a.str("tstart").c_str(), nullptr);
-   if ( a.has("tstep") ) p.threshold_step = (float)std::strtod(a.str("tstep").c_str(), nullptr);
-   if ( a.has("tstop") ) p.threshold_stop = (float)std::strtod(a.str("tstop").c_str(), nullptr);
-   if ( a.has("minpace") ) p.min_unfolding_pace = std::atoi(a.str("minpace").c_str());
-   if ( a.has("maxpace") ) p.max_unfolding_pace = std::atoi(a.str("maxpace").c_str());
-   if ( a.has("bins") ) p.histogram_bin_size = std::atoi(a.str("bins").c_str());
+   p.threshold_start = (float)a.real("tstart", p.threshold_start);
+   p.threshold_step = (float)a.real("tstep", p.threshold_step);
+   p.threshold_stop = (float)a.real("tstop", p.threshold_stop);
+   p.min_unfolding_pace = a.int32("minpace", p.min_unfolding_pace);
+   p.max_unfolding_pace = a.int32("maxpace", p.max_unfolding_pace);
+   p.histogram_bin_size = a.int32("bins", p.histogram_bin_size);
+   if ( !a.ok ) return 2;
    float t = 0.0f;
    const int rc = kinc_rmt_run(a.str("input").c_str(), a.str("little-endian", "0") == "1", &p, a.str("log").c_str(), &t);
    if ( rc != KINC_SIM_OK )
@@ -254,7 +308,9 @@ int run_import_emx(const Args& a)
    bool ok = true;
    const int t = choice(a.str("transform", "none"), TRANSFORMS, "transform", ok);
    if ( !ok ) return 2;
-   const int rc = kinc_emx_import_text(opt(a, "input"), opt(a, "nan"), std::atoi(a.str("samples", "0").c_str()), t,
+   const int samples = a.int32("samples", 0);
+   if ( !a.ok ) return 2;
+   const int rc = kinc_emx_import_text(opt(a, "input"), opt(a, "nan"), samples, t,
                                        a.str("little-endian", "0") == "1", opt(a, "output"), opt(a, "names"),
                                        opt(a, "sample-names"));
    if ( rc != KINC_SIM_OK ) fprintf(stderr, "import-emx: %s\n", kinc_pm_last_error());
@@ -292,8 +348,9 @@ int run_import_cmx(const Args& a)
       fprintf(stderr, "import-cmx: Correlation name is required.\n");
       return 2;
    }
-   const int rc = kinc_pm_import_text(opt(a, "input"), opt(a, "ccm"), opt(a, "cmx"), std::atoi(a.str("genes").c_str()),
-                                      std::atoi(a.str("maxclusters").c_str()), std::atoi(a.str("samples").c_str()),
+   const int genes = a.int32("genes", 0), maxk = a.int32("maxclusters", 0), samples = a.int32("samples", 0);
+   if ( !a.ok ) return 2;
+   const int rc = kinc_pm_import_text(opt(a, "input"), opt(a, "ccm"), opt(a, "cmx"), genes, maxk, samples,
                                       a.str("little-endian", "0") == "1");
    if ( rc != KINC_SIM_OK ) fprintf(stderr, "import-cmx: %s\n", kinc_pm_last_error());
    return rc == KINC_SIM_OK ? 0 : 1;
@@ -312,6 +369,22 @@ int main(int argc, char** argv)
       return usage();
    }
    const std::string an = argv[2];
+   const auto keys = KEYS.find(an);
+   if ( keys == KEYS.end() )
+   {
+      fprintf(stderr, "unknown analytic %s\n", an.c_str());
+      return usage();
+   }
+   for ( const auto& kv : a.kv )
+   {
+      bool known = false;
+      for ( const auto& k : keys->second ) known = known || k == kv.first;
+      if ( !known )
+      {
+         fprintf(stderr, "%s: unknown argument --%s\n", an.c_str(), kv.first.c_str());
+         return 2;
+      }
+   }
    if ( an == "similarity" ) return run_similarity(a);
    if ( an == "export-cmx" ) return run_export(a);
    if ( an == "extract" ) return run_extract(a);

@@ -99,8 +99,31 @@ def test_native_program_export_and_extract(tmp_path, native):
                                        (["run", "similarity", "--input"], 2),
                                        (["run", "similarity", "--input", "x.emx"], 2),
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--preout", "maybe"], 2),
-                                       (["run", "export-cmx", "--ccm", "a", "--cmx", "b", "--output", "c"], 1)])
+                                       (["run", "export-cmx", "--ccm", "a", "--cmx", "b", "--output", "c"], 1),
+                                       # unknown and malformed arguments are usage errors, as in argparse
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--minsmap", "3"], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--minsamp", "3x"], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--blocks", ""], 2),
+                                       (["run", "extract", "--emx", "a", "--ccm", "b", "--cmx", "c", "--output", "d",
+                                         "--mincorr", "high"], 2),
+                                       (["run", "rmt", "--input", "a", "--log", "b", "--bins", "1e9"], 2),
+                                       (["run", "rmt", "--input", "a", "--log", "b", "--bins", "99999999999"], 2),
+                                       (["run", "export-cmx", "--ccm", "a", "--cmx", "b", "--output", "c",
+                                         "--preout"], 2),
+                                       (["run", "import-cmx", "--input", "a", "--ccm", "b", "--cmx", "c", "--genes",
+                                         "5", "--maxclusters", "2", "--samples", "4"], 2),
+                                       (["run", "import-emx", "--input", "a", "--output", "b", "--transform", "log"],
+                                        2)])
 def test_native_program_argument_errors(tmp_path, native, argv, code):
     import subprocess
     r = subprocess.run([_native_cli(), *argv], capture_output=True, text=True, cwd=tmp_path)
     assert r.returncode == code, r.stderr
+
+
+@pytest.mark.parametrize("argv", [["run", "similarity", "--input", "x", "--cmx", "y", "--minsmap", "3"],
+                                  ["run", "similarity", "--input", "x", "--cmx", "y", "--minsamp", "3x"],
+                                  ["run", "import-emx", "--input", "a", "--output", "b", "--transform", "log"]])
+def test_python_command_line_rejects_what_the_native_one_rejects(argv):
+    with pytest.raises(SystemExit) as e:
+        cli._parser().parse_args(argv)
+    assert e.value.code == 2
