@@ -430,8 +430,10 @@ extern "C" int kinc_emx_export_text(const char* emx_path, int32_t little_endian,
          case KINC_EMX_TRANSFORM_LOG10: w = (float)std::pow(10.0, (double)v); break;
          default: break;
          }
-         const int n = snprintf(num, sizeof num, "\t%.12g", (double)w);
-         ok = fwrite(num, 1, (size_t)n, out) == (size_t)n;
+         /* to_chars with a precision prints as printf's %.12g does in the C locale */
+         num[0] = '\t';
+         const auto r = std::to_chars(num + 1, num + sizeof num, (double)w, std::chars_format::general, 12);
+         ok = r.ec == std::errc() && fwrite(num, 1, (size_t)(r.ptr - num), out) == (size_t)(r.ptr - num);
       }
       ok = ok && fputc('\n', out) != EOF;
    }

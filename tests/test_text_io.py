@@ -177,7 +177,7 @@ def test_export_emx_matches_restatement(tmp_path, native, transform):
     rng = np.random.default_rng(20 + transform)
     gem = rng.normal(2, 1.5, (30, 11)).astype(np.float32)
     gem[rng.random(gem.shape) < 0.1] = np.nan
-    gem[0, 0], gem[0, 1] = np.float32(1e-30), np.float32(-3.4e38)
+    gem[0, 0], gem[0, 1], gem[0, 2], gem[0, 3] = np.float32(1e-30), np.float32(-3.4e38), np.inf, -np.inf
     pm.write_emx(tmp_path / "g.emx", gem)
     (tmp_path / "genes").write_text("".join(f"G{g}\n" for g in range(30)))
     pm.export_emx_text(tmp_path / "g.emx", tmp_path / "g.txt", nan="NA", transform=transform,
