@@ -64,7 +64,9 @@ typedef struct kinc_sim_params
    int32_t semantics;     /* 0: the reference CPU path, including its packed-array indexing in
                                 Pearson/Spearman (default); 1: each sample's own values */
    int32_t rand_mode;     /* 0: the process-global glibc rand() stream of a serial KINC run (default);
-                             1: the POSIX LCG reset per fit used by the OpenCL worker */
+                             1: the OpenCL worker's GMM (src/opencl/gmm.cl): the POSIX LCG reset per
+                                fit, BIC/ICL evaluated in float, a fit failing only on a zero
+                                covariance determinant (K-means: the LCG with the CPU path's fit) */
    int32_t precision;     /* clusmethod none + pearson + semantics 1 only: 0 per-pair FP32 (default),
                              1 TF32 tensor cores, 2 3xBF16 tensor cores (pairwise-complete Pearson as a
                              masked contraction; labels are not written) */

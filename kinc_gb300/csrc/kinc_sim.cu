@@ -590,7 +590,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    /* launch shape: sort buffers in shared memory when they fit */
    const size_t sort_bytes_warp = (size_t)dp.sort_floats * sizeof(float);
    ctx->kern = params->clus_method == 0 ? sim_kernel_none()
-             : params->clus_method == 1 ? sim_kernel_gmm(params->max_clusters)
+             : params->clus_method == 1 ? sim_kernel_gmm(params->max_clusters, params->rand_mode == 1)
                                         : sim_kernel_kmeans(params->max_clusters);
    /* GMM parameters in shared memory take the room the sort buffers would use */
    const size_t param_bytes_warp = (KINC_GMM_PARAMS_SMEM && ctx->kern.clus == 1 && ctx->kern.ks > 0)
@@ -1204,7 +1204,7 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    dp.ncorr = 1;
    const size_t sort_bytes_warp = (size_t)dp.sort_floats * sizeof(float);
    const SimKernel kern = params->clus_method == 0 ? sim_kernel_none()
-                        : params->clus_method == 1 ? sim_kernel_gmm(params->max_clusters)
+                        : params->clus_method == 1 ? sim_kernel_gmm(params->max_clusters, params->rand_mode == 1)
                                                    : sim_kernel_kmeans(params->max_clusters);
    const size_t param_bytes_warp = (KINC_GMM_PARAMS_SMEM && kern.clus == 1 && kern.ks > 0)
                                       ? (size_t)7 * kern.ks * TILE * sizeof(float) : 0;

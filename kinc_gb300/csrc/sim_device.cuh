@@ -429,7 +429,11 @@ __device__ __forceinline__ float log_mvn(float x0, float x1, float m0, float m1,
    return nrm - 0.5f * dot;
 }
 
-/* matrixInverse + prepareCovariance (pairwise_linalg.cpp:163-173, pairwise_gmm.cpp:31-47) */
+/* matrixInverse + prepareCovariance (pairwise_linalg.cpp:163-173, pairwise_gmm.cpp:31-47).  The
+ * CPU code fails on det <= 0; the OpenCL kernel (OCL: GMM_Component_prepareCovariance,
+ * src/opencl/gmm.cl:46-64) only on fabs(det) <= 0, and goes on with the NaN normaliser of a
+ * negative determinant. */
+template <bool OCL>
 __device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, double c2, float& a, float& b,
                                             float& c, float& nrm)
 {
@@ -437,13 +441,14 @@ __device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, dou
    a = s11 / det;
    b = -s01 / det;
    c = s00 / det;
-   if ( det <= 0 ) return false;
+   if ( OCL ? (fabsf(det) <= 0.f) : (det <= 0) ) return false;
    nrm = (float)(-0.5 * (c2 + (double)kinc_logf(det)));
    return true;
 }
 
 /*
- * GMM::fit for one pair on this lane (pairwise_gmm.cpp:367-445).
+ * GMM::fit for one pair on this lane (pairwise_gmm.cpp:367-445); with OCL, the OpenCL kernel's
+ * GMM_fit (src/opencl/gmm.cl:424-495), which differs only in prepare_cov's failure rule.
  * Per EM iteration it makes three passes over the samples: E (log-densities,
  * per-sample log-sum-exp, logL, and the per-component maxima calcLogGammaK
  * needs), M1 (per-component log-sum-exp of the responsibilities, and the mean
@@ -457,7 +462,7 @@ __device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, dou
  * non-positive determinant still fails the fit), since the reference labels
  * samples with that iteration's E-step responsibilities.
  */
-template <int KT>
+template <int KT, bool OCL>
 __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int N, int Kr, LaneRng& rng,
                         double c2, float& out_logL, float& out_E, unsigned long long& units, float* pbuf)
 {
@@ -480,7 +485,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
    if ( rng.mode == 1 ) rng.lcg = 1;
    {
       float a0, b0, c0, n0;
-      prepare_cov(1.f, 0.f, 1.f, c2, a0, b0, c0, n0);
+      prepare_cov<OCL>(1.f, 0.f, 1.f, c2, a0, b0, c0, n0);
       const float lp0 = kinc_logf(1.0f / K);
 #pragma unroll UF
       for ( int k = 0; k < KA; ++k )
@@ -702,7 +707,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
          if ( k >= K ) continue;
          const float sc = 1.0f / Gam[k];
          float a, b, c, n;
-         ok = prepare_cov(s00[k] * sc, s01[k] * sc, s11[k] * sc, c2, a, b, c, n) && ok;
+         ok = prepare_cov<OCL>(s00[k] * sc, s01[k] * sc, s11[k] * sc, c2, a, b, c, n) && ok;
          if ( !last )
          {
             m0[k] = nm0[k]; m1[k] = nm1[k];

@@ -1,6 +1,7 @@
 /*
  * sim_kernel.cuh -- the per-pair Similarity kernel, specialised by
- * clustering method (CLUS: 0 none, 1 GMM, 2 K-means) and by the largest
+ * clustering method (CLUS: 0 none, 1 GMM, 2 K-means, 3 GMM as KINC's OpenCL
+ * kernels compute it, for rand_mode 1) and by the largest
  * cluster count compiled with static register arrays (KS = 3 or 5: every
  * fit, whatever its K <= KS, runs the same code with its per-component state
  * in registers, the host picks KS >= maxclus; KS = 0: the generic
@@ -133,11 +134,20 @@ __device__ inline float lane_pearson(const DevParams& P, const DevData& D, const
 }
 
 /* computeBIC / computeICL (pairwise_clustering.cpp:155-172): log of the int N
- * is double, 2*logL is float, the difference is double, the result float. */
+ * is double, 2*logL is float, the difference is double, the result float.  The
+ * OpenCL worker's GMM (OCL) evaluates them in float with log of (float)N
+ * (GMM_computeBIC / GMM_computeICL, src/opencl/gmm.cl:511-530). */
+template <bool OCL>
 __device__ __forceinline__ float criterion_value(const DevParams& P, const DevData& D, int K, float logL, int N,
                                                  float E)
 {
    const int pp = K * (1 + 2 + 2 * 2);
+   if ( OCL )
+   {
+      float f = kinc_logf((float)N) * (float)pp - 2.0f * logL;
+      if ( P.criterion == 1 ) f = f - 2.0f * E;
+      return f;
+   }
    double v = D.logn[N] * (double)pp - (double)(2.0f * logL);
    if ( P.criterion == 1 ) v = v - (double)(2.0f * E);
    return (float)v;
@@ -149,9 +159,9 @@ __device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, co
                                          int K, LaneRng& rng, float& logL, float& E, unsigned long long& units,
                                          float* pbuf)
 {
-   if ( CLUS == 1 )
+   if ( CLUS == 1 || CLUS == 3 )
    {
-      return gmm_fit<KT>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units, pbuf);
+      return gmm_fit<KT, CLUS == 3>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units, pbuf);
    }
 #if KINC_KMEANS_PIPELINE
 #if KINC_KMEANS_LANE_MAJOR
@@ -196,7 +206,7 @@ __device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* 
       else ok = lane_fit<CLUS, 5>(P, X, Xl, lpx, gam, wl, ya, yb, yc, N, K, rng, logL, E, units, pbuf);
       ++fits;
       if ( !ok ) continue;
-      const float value = criterion_value(P, D, K, logL, N, E);
+      const float value = criterion_value<CLUS == 3>(P, D, K, logL, N, E);
       if ( value < bestValue )
       {
          bestK = K;
@@ -218,6 +228,7 @@ template <int CLUS, int KS>
 __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32, KINC_MIN_BLOCKS)
 k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
 {
+   constexpr int CM = CLUS == 3 ? 1 : CLUS;    /* the clustering method (3: GMM, OpenCL worker's form) */
    extern __shared__ float smem[];
    const int lane = threadIdx.x & 31;
    const int warp = threadIdx.x >> 5;
@@ -235,12 +246,12 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
    uint32_t* ring = W.rng + slot * (size_t)(RNG_WORDS * TILE);
    float* sbuf = smem_sort ? smem + (size_t)warp * P.sort_floats : W.sortbuf + slot * (size_t)P.sort_floats;
    /* GMM parameters in shared memory (KINC_GMM_PARAMS_SMEM): 7 arrays of KS x 32 floats per warp */
-   float* pbuf = (CLUS == 1 && KINC_GMM_PARAMS_SMEM && KS > 0)
+   float* pbuf = (CM == 1 && KINC_GMM_PARAMS_SMEM && KS > 0)
                     ? smem + (smem_sort ? (size_t)WARPS_PER_BLOCK * P.sort_floats : 0) + (size_t)warp * 7 * KS * TILE
                     : nullptr;
 
    const int64_t ntiles = (B.size + TILE - 1) / TILE;
-   constexpr bool ROUNDS = ((KINC_CTA_ROUNDS) >> CLUS) & 1;
+   constexpr bool ROUNDS = ((KINC_CTA_ROUNDS) >> CM) & 1;
    __shared__ unsigned long long round_base;
    for ( ;; )
    {
@@ -395,18 +406,20 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
    }
 }
 
-/* host-side handle of one specialisation */
+/* host-side handle of one specialisation (clus: the clustering method; ocl: the OpenCL
+ * worker's GMM, CLUS 3) */
 struct SimKernel
 {
    const void* fn;
    int clus;
    int ks;
+   bool ocl;
 };
 
 template <int CLUS, int KS>
 inline SimKernel sim_kernel_handle()
 {
-   return SimKernel { (const void*)&k_similarity<CLUS, KS>, CLUS, KS };
+   return SimKernel { (const void*)&k_similarity<CLUS, KS>, CLUS == 3 ? 1 : CLUS, KS, CLUS == 3 };
 }
 
 template <int CLUS, int KS>
@@ -422,7 +435,7 @@ SimKernel sim_kernel_select(int clus, int max_k);
 cudaError_t sim_kernel_launch_any(const SimKernel& k, int grid, int smem, cudaStream_t st, const DevParams& P,
                                   const DevData& D, const DevScratch& W, const DevBlock& B, int smem_sort);
 SimKernel sim_kernel_none();
-SimKernel sim_kernel_gmm(int max_k);
+SimKernel sim_kernel_gmm(int max_k, bool opencl);
 SimKernel sim_kernel_kmeans(int max_k);
 cudaError_t sim_launch_none(const SimKernel& k, int grid, int smem, cudaStream_t st, const DevParams& P,
                             const DevData& D, const DevScratch& W, const DevBlock& B, int smem_sort);

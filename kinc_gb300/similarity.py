@@ -100,7 +100,13 @@ class PairwiseMatrix:
 
 
 class Similarity:
-    """KINC Similarity analytic on the GB300 worker."""
+    """KINC Similarity analytic on the GB300 worker.
+
+    Beyond KINC's arguments: semantics ("reference": KINC's serial path including its
+    packed-array reads in Pearson/Spearman; "fixed": each sample's own values), rand
+    ("glibc": the serial path's process-global rand() stream; "lcg": the OpenCL worker's GMM,
+    with its per-fit LCG, float BIC/ICL and zero-determinant failure rule) and precision
+    (tensor-core forms of pairwise-complete Pearson)."""
 
     WORK_BLOCK_SIZE = _native.WORK_BLOCK_SIZE
 

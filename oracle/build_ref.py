@@ -2,6 +2,9 @@
 
 * ``oracle/_build/libkinc_oracle.so`` -- the plain-C restatement
   (kinc_oracle.c).  Builds anywhere (x86 container or the Arm GPU host).
+* ``oracle/_ref/libkinc_ocl.so`` -- KINC's OpenCL kernels compiled as C++ for
+  the host (ref_shim/ocl_shim.h) and driven as the OpenCL worker drives them
+  (ocl_driver.cpp); also only with the KINC tree.
 * ``oracle/_ref/libkinc_ref{0,1,2}.so`` -- KINC's own CPU Pairwise:: sources,
   compiled unmodified from the KINC source tree with the stand-in ACE header
   in ref_shim/ and the restated serial driver ref_driver.cpp.  Only built when
@@ -75,10 +78,48 @@ def build_ref(math_mode=0):
     return out
 
 
+# KINC's OpenCL kernels in the order the OpenCL analytic concatenates them
+# (src/core/similarity_opencl.cpp:37-46)
+OCL_SOURCES = ["linalg.cl", "fetchpair.cl", "sort.cl", "outlier.cl", "gmm.cl", "kmeans.cl", "pearson.cl",
+               "spearman.cl"]
+
+
+def build_ocl():
+    """Compile KINC's OpenCL kernels as C++ for the host, with ref_shim/ocl_shim.h and the
+    worker restated in ocl_driver.cpp, into oracle/_ref/libkinc_ocl.so; None without the
+    KINC tree.  The kernels are read where they lie and piped to the compiler; the one
+    OpenCL-only construct in them, the vector literal "(float2) (a, b)"
+    (src/opencl/fetchpair.cl:62), is rewritten to a constructor call on the way."""
+    if not reference_available():
+        return None
+    cl_dir = os.path.join(REF_DIR, "src", "opencl")
+    out_dir = os.path.join(HERE, "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    out = os.path.join(out_dir, "libkinc_ocl.so")
+    srcs = [os.path.join(cl_dir, s) for s in OCL_SOURCES]
+    deps = srcs + [os.path.join(HERE, "ocl_driver.cpp"), os.path.join(HERE, "ref_shim", "ocl_shim.h"),
+                   os.path.join(REPO, "kinc_gb300", "csrc", "kinc_fmath.h")]
+    if _newer(out, deps):
+        return out
+    import re
+    text = ""
+    for path in srcs:
+        with open(path) as fh:
+            text += f'#line 1 "{path}"\n' + fh.read() + "\n"
+    text = re.sub(r"\(float2\)\s*\(", "float2(", text)
+    text += '#include "ocl_driver.cpp"\n'
+    cmd = ["g++", "-std=c++14", "-shared", *FP_FLAGS, "-w", "-fsigned-char", "-x", "c++",
+           "-include", os.path.join(HERE, "ref_shim", "ocl_shim.h"),
+           "-I", HERE, "-I", os.path.join(REPO, "kinc_gb300", "csrc"), "-o", out, "-"]
+    subprocess.run(cmd, input=text.encode(), check=True)
+    return out
+
+
 def build_all():
     paths = [build_oracle()]
     for m in (0, 1, 2):
         paths.append(build_ref(m))
+    paths.append(build_ocl())
     return paths
 
 

@@ -248,15 +248,18 @@ typedef struct
 } gcomp;
 
 
-static int comp_prepare(gcomp* c)
+static int comp_prepare(gcomp* c, int opencl)
 {
-   /* matrixInverse (pairwise_linalg.cpp:163-173) then prepareCovariance (pairwise_gmm.cpp:31-47) */
+   /* matrixInverse (pairwise_linalg.cpp:163-173) then prepareCovariance (pairwise_gmm.cpp:31-47).
+    * The CPU code fails on det <= 0; the OpenCL kernel's GMM_Component_prepareCovariance
+    * (src/opencl/gmm.cl:46-64) only on fabs(det) <= 0, and goes on with the NaN normaliser of
+    * a negative determinant. */
    const float det = c->sigma[0] * c->sigma[3] - c->sigma[1] * c->sigma[2];
    c->sinv[0] = +c->sigma[3] / det;
    c->sinv[1] = -c->sigma[1] / det;
    c->sinv[2] = -c->sigma[2] / det;
    c->sinv[3] = +c->sigma[0] / det;
-   if ( det <= 0 )
+   if ( opencl ? (fabsf(det) <= 0) : (det <= 0) )
    {
       return 0;
    }
@@ -298,7 +301,7 @@ static int gmm_fit(const v2* X, int N, int K, int8_t* labels, float* out_logL, f
       C[k].sigma[0] = 1; C[k].sigma[1] = 0; C[k].sigma[2] = 0; C[k].sigma[3] = 1;
       C[k].sinv[0] = 0; C[k].sinv[1] = 0; C[k].sinv[2] = 0; C[k].sinv[3] = 0;
       C[k].norm = 0;
-      comp_prepare(&C[k]);
+      comp_prepare(&C[k], rnd->mode == 1);
    }
    /* GMM::kmeans is a no-op: its loop condition `diff > TOLERANCE` starts with diff = 0
     * (pairwise_gmm.cpp:88-95) */
@@ -442,7 +445,7 @@ static int gmm_fit(const v2* X, int N, int K, int8_t* labels, float* out_logL, f
          }
          sc = 1.0f / logGamma[k];
          c->sigma[0] *= sc; c->sigma[1] *= sc; c->sigma[2] *= sc; c->sigma[3] *= sc;
-         if ( !comp_prepare(c) )
+         if ( !comp_prepare(c, rnd->mode == 1) )
          {
             return 0;   /* prepareCovariance throws; fit() reports failure */
          }
@@ -608,9 +611,17 @@ typedef struct
 static float criterion_value(const ko_params* p, int K, float logL, int N, float E)
 {
    /* computeBIC / computeICL (pairwise_clustering.cpp:155-172): log(N) of an int is
-    * double, 2*logL stays float, the difference is double, the return is float. */
+    * double, 2*logL stays float, the difference is double, the return is float.
+    * The OpenCL worker's GMM (rand_mode 1) evaluates them in float, with log of (float)N
+    * (GMM_computeBIC / GMM_computeICL, src/opencl/gmm.cl:511-530). */
    const int D = 2;
    const int pp = K * (1 + D + D * D);
+   if ( p->rand_mode == 1 && p->clus_method == 1 )
+   {
+      float v = kinc_logf((float)N) * (float)pp - 2.0f * logL;
+      if ( p->criterion == 1 ) v = v - 2.0f * E;
+      return v;
+   }
    if ( p->criterion == 0 )
    {
       return (float)(log((double)N) * pp - (double)(2 * logL));

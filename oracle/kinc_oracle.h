@@ -35,7 +35,8 @@ typedef struct ko_params
    float   min_corr;
    float   max_corr;
    int32_t semantics;     /* 0 reference CPU path, 1 fixed gathers */
-   int32_t rand_mode;     /* 0 glibc rand() stream, 1 per-fit POSIX LCG */
+   int32_t rand_mode;     /* 0 glibc rand() stream (serial path); 1 the OpenCL worker's GMM: per-fit
+                             POSIX LCG, float BIC/ICL, zero-determinant failure rule */
 } ko_params;
 
 /* glibc random_r TYPE_3 (the default rand()) restated from its published

@@ -95,6 +95,51 @@ def ref_lib(math_mode=0):
     return _ref[math_mode]
 
 
+class KoclParams(ctypes.Structure):
+    _fields_ = [("clus_method", ctypes.c_int32), ("corr_method", ctypes.c_int32), ("min_expr", ctypes.c_float),
+                ("min_samples", ctypes.c_int32), ("min_clusters", ctypes.c_int32), ("max_clusters", ctypes.c_int32),
+                ("criterion", ctypes.c_int32), ("pre_out", ctypes.c_int32), ("post_out", ctypes.c_int32),
+                ("ksize", ctypes.c_int32)]
+
+
+_ocl = []
+
+
+def ocl_lib():
+    """KINC's OpenCL kernels compiled for the host and driven like its OpenCL worker, or None
+    when the KINC tree is absent."""
+    if not _ocl:
+        path = build_ref.build_ocl()
+        L = None
+        if path is not None:
+            L = ctypes.CDLL(path)
+            L.kocl_run.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(KoclParams),
+                                   ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p]
+            L.kocl_run.restype = ctypes.c_int
+        _ocl.append(L)
+    return _ocl[0]
+
+
+def run_ocl(gem, p, start, size, ksize=4096):
+    """The OpenCL worker's results for pairs [start, start+size) (K, labels, corr), computed by
+    KINC's own OpenCL kernels on the CPU; None when they are not built.  `p` is a KoParams
+    (clustering none or GMM)."""
+    L = ocl_lib()
+    if L is None:
+        return None
+    gem = np.ascontiguousarray(gem, dtype=np.float32)
+    G, S = gem.shape
+    q = KoclParams(p.clus_method, p.corr_method, p.min_expr, p.min_samples, p.min_clusters, p.max_clusters,
+                   p.criterion, p.pre_out, p.post_out, ksize)
+    K = np.zeros(size, np.int8)
+    labels = np.zeros((size, S), np.int8)
+    corr = np.zeros((size, p.max_clusters), np.float32)
+    if L.kocl_run(_ptr(gem), G, S, ctypes.byref(q), start, size, _ptr(K), _ptr(labels), _ptr(corr)) != 0:
+        raise ValueError("the OpenCL worker would not run these arguments")
+    return K, labels, corr
+
+
 DEFAULTS = dict(clus_method=0, corr_method=0, min_expr=float("-inf"), min_samples=30, min_clusters=1,
                 max_clusters=5, criterion=1, pre_out=0, post_out=0, min_corr=0.5, max_corr=1.0,
                 semantics=0, rand_mode=0)

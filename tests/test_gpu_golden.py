@@ -1,6 +1,8 @@
 """GPU against the golden fixtures: outputs of KINC's own compiled Pairwise::
-code on seeded inputs (tests/golden/make_golden.py).  Bit-exact: K, labels of
-multi-cluster pairs, N-derived results and every correlation."""
+code, and of its OpenCL kernels compiled for the host (the ocl_* fixtures, run
+in the rand="lcg" mode), on seeded inputs (tests/golden/make_golden.py).
+Bit-exact: K, labels of multi-cluster pairs, N-derived results and every
+correlation the reference determines."""
 import glob
 import os
 
@@ -24,10 +26,12 @@ def test_gpu_reproduces_golden(path):
     sim = Similarity(g["gem"], clusmethod=NAMES[a["clus_method"]], corrmethod=a["corr_method"],
                      minexpr=a["min_expr"], minsamp=a["min_samples"], minclus=a["min_clusters"],
                      maxclus=a["max_clusters"], crit=a["criterion"], preout=a["pre_out"], postout=a["post_out"],
-                     mincorr=a["min_corr"], maxcorr=a["max_corr"])
+                     mincorr=a["min_corr"], maxcorr=a["max_corr"],
+                     rand="lcg" if a.get("rand_mode") == 1 else "glibc")
     sim.initialize()
     res = sim.execute(None, start=g["start"], size=g["size"])
     sim.close()
     assert np.array_equal(res.K, g["K"]), f"K differs on {(res.K != g['K']).sum()} pairs"
     assert np.array_equal(res.labels[g["multi"]], g["labels"])
-    assert same_corr(res.corr, g["corr"])
+    m = g["corr_mask"]
+    assert same_corr(res.corr[m], g["corr"][m])

@@ -3,7 +3,8 @@
 * glibc rand(): the restatement equals the C library's rand() stream.
 * kinc_expf / kinc_logf: within 1 ulp of the correctly rounded value.
 * the restatement reproduces the golden fixtures (generated by KINC's own
-  Pairwise:: sources, tests/golden/make_golden.py) bit for bit;
+  Pairwise:: sources, and by KINC's OpenCL kernels compiled for the host for
+  the rand="lcg" mode, tests/golden/make_golden.py) bit for bit;
 * when the KINC tree is present, it also equals KINC's compiled code on
   fresh cases, including blocks that start inside a work block.
 """
@@ -21,9 +22,18 @@ GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.n
 
 
 def load_golden(path):
+    """A fixture, plus corr_mask: the correlations the reference determines ([pair][cluster]; for the
+    OpenCL worker's fixtures the clusters below K of the pairs in corr_rows, for the others every
+    entry)."""
     z = np.load(path)
-    return dict(gem=z["gem"], K=z["K"], N=z["N"], corr=z["corr"], multi=z["multi"], labels=z["labels"],
-                start=int(z["start"]), size=int(z["size"]), params=json.loads(str(z["params"])))
+    g = dict(gem=z["gem"], K=z["K"], N=z["N"], corr=z["corr"], multi=z["multi"], labels=z["labels"],
+             start=int(z["start"]), size=int(z["size"]), params=json.loads(str(z["params"])))
+    if "corr_rows" in z.files:
+        cols = np.arange(g["corr"].shape[1])[None, :]
+        g["corr_mask"] = z["corr_rows"][:, None] & (cols < g["K"][:, None])
+    else:
+        g["corr_mask"] = np.ones(g["corr"].shape, bool)
+    return g
 
 
 def same_corr(a, b):
@@ -91,7 +101,7 @@ def test_oracle_reproduces_golden(path):
     assert np.array_equal(K, g["K"])
     assert np.array_equal(N, g["N"])
     assert np.array_equal(labels[g["multi"]], g["labels"])
-    assert same_corr(corr, g["corr"])
+    assert same_corr(corr[g["corr_mask"]], g["corr"][g["corr_mask"]])
 
 
 REF_CASES = [
