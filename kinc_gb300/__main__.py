@@ -62,6 +62,8 @@ def _parser():
     sim.add_argument("--ksize", type=int, default=4096)
     sim.add_argument("--semantics", default="reference", choices=["reference", "fixed"])
     sim.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "3xbf16"])
+    sim.add_argument("--rand", default="glibc", choices=["glibc", "lcg"],
+                     help="glibc: KINC's serial path; lcg: KINC's OpenCL worker (per-fit LCG GMM)")
     sim.add_argument("--first-block", type=int, default=0, help="first work block (for a shard)")
     sim.add_argument("--blocks", type=int, default=-1, help="work blocks to run (-1: to the end)")
     common(sim)
@@ -143,7 +145,7 @@ def main(argv=None):
                              minexpr=args.minexpr, minsamp=args.minsamp, minclus=args.minclus, maxclus=args.maxclus,
                              crit=args.crit, preout=args.preout, postout=args.postout, mincorr=args.mincorr,
                              maxcorr=args.maxcorr, ksize=args.ksize, semantics=args.semantics,
-                             precision=args.precision)
+                             precision=args.precision, rand=args.rand)
             sim.run(ccm_path=args.ccm, cmx_path=args.cmx, little_endian=args.little_endian,
                     first_block=args.first_block, nblocks=args.blocks)
             sim.close()

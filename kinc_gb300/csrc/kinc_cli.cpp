@@ -78,7 +78,7 @@ private:
 const std::map<std::string, std::vector<std::string>> KEYS = {
    { "similarity", { "input", "ccm", "cmx", "clusmethod", "corrmethod", "minexpr", "minsamp", "minclus", "maxclus",
                      "crit", "preout", "postout", "mincorr", "maxcorr", "ksize", "semantics", "precision",
-                     "first-block", "blocks", "little-endian" } },
+                     "rand", "first-block", "blocks", "little-endian" } },
    { "export-cmx", { "ccm", "cmx", "output", "little-endian" } },
    { "extract", { "emx", "ccm", "cmx", "output", "graphml", "mincorr", "maxcorr", "names", "little-endian" } },
    { "rmt", { "input", "log", "tstart", "tstep", "tstop", "minpace", "maxpace", "bins", "little-endian" } },
@@ -102,7 +102,8 @@ int usage()
            "usage: kinc-gb300 run similarity --input EMX [--ccm CCM] [--cmx CMX] [--clusmethod none|gmm|kmeans]\n"
            "           [--corrmethod pearson|spearman|both] [--minexpr F] [--minsamp N] [--minclus N] [--maxclus N]\n"
            "           [--crit BIC|ICL] [--preout [true|false]] [--postout [true|false]] [--mincorr F] [--maxcorr F]\n"
-           "           [--ksize N] [--first-block N] [--blocks N] [--little-endian]\n"
+           "           [--ksize N] [--semantics reference|fixed] [--precision fp32|tf32|3xbf16] [--rand glibc|lcg]\n"
+           "           [--first-block N] [--blocks N] [--little-endian]\n"
            "       kinc-gb300 run export-cmx --ccm CCM --cmx CMX --output TXT\n"
            "       kinc-gb300 run extract --emx EMX --ccm CCM --cmx CMX [--output TXT] [--graphml XML] [--mincorr F]\n"
            "           [--maxcorr F] [--names TXT]\n"
@@ -191,6 +192,7 @@ int run_similarity(const Args& a)
    p.criterion = choice(a.str("crit", "ICL"), { "BIC", "ICL" }, "crit", ok);
    p.semantics = choice(a.str("semantics", "reference"), { "reference", "fixed" }, "semantics", ok);
    p.precision = choice(a.str("precision", "fp32"), { "fp32", "tf32", "3xbf16" }, "precision", ok);
+   p.rand_mode = choice(a.str("rand", "glibc"), { "glibc", "lcg" }, "rand", ok);
    if ( !ok ) return 2;
    p.min_expr = (float)a.real("minexpr", p.min_expr);
    p.min_samples = a.int32("minsamp", 30);

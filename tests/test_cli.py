@@ -25,6 +25,13 @@ def test_boolean_arguments(argv, want):
     assert _args("run", "similarity", "--input", "x", "--cmx", "y", *argv).preout is want
 
 
+def test_rand_mode_argument():
+    assert _args("run", "similarity", "--input", "x", "--cmx", "y").rand == "glibc"
+    assert _args("run", "similarity", "--input", "x", "--cmx", "y", "--rand", "lcg").rand == "lcg"
+    with pytest.raises(SystemExit):
+        _args("run", "similarity", "--input", "x", "--cmx", "y", "--rand", "mt")
+
+
 def test_other_analytics_defaults():
     e = _args("run", "extract", "--emx", "a", "--ccm", "b", "--cmx", "c", "--output", "d")
     assert (e.mincorr, e.maxcorr) == (0.85, 1.0)
@@ -104,6 +111,8 @@ def test_native_program_export_and_extract(tmp_path, native):
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--minsmap", "3"], 2),
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--minsamp", "3x"], 2),
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--blocks", ""], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--rand", "mt"], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--rand", "lcg"], 1),
                                        (["run", "extract", "--emx", "a", "--ccm", "b", "--cmx", "c", "--output", "d",
                                          "--mincorr", "high"], 2),
                                        (["run", "rmt", "--input", "a", "--log", "b", "--bins", "1e9"], 2),
