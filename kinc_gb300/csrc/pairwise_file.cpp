@@ -458,8 +458,9 @@ extern "C" int kinc_pm_export_text(const char* ccm_path, const char* cmx_path, i
    std::vector<int8_t> bc(CHUNK);
    std::vector<int8_t> bcodes((size_t)CHUNK * S);
    int64_t b_base = 0, b_len = 0, b_cur = 0;
-   std::string mask((size_t)S, '0');
+   std::string mask((size_t)S, '0'), lbuf;
    std::vector<int8_t> codes;   /* the CCM clusters of the current pair, [cluster][S] */
+   std::vector<float> r;        /* the current pair's first correlations */
    char line[256];
 
    auto fill_ccm = [&](int64_t first) -> int {
@@ -486,7 +487,7 @@ extern "C" int kinc_pm_export_text(const char* ccm_path, const char* cmx_path, i
       int64_t o = at(i);
       if ( o < 0 ) { rc = KINC_SIM_EINVAL; break; }
       const int32_t x = ax[o], y = ay[o];
-      std::vector<float> r;
+      r.clear();
       int64_t j = i;
       while ( j < n_cmx )
       {
@@ -525,21 +526,14 @@ extern "C" int kinc_pm_export_text(const char* ccm_path, const char* cmx_path, i
       }
       for ( int k = 0; k < clusters; ++k )
       {
-         int ns = 0, nmiss = 0, npost = 0, npre = 0, nthr = 0;
+         /* per-code counts from a 16-bin histogram of the cluster's nibbles */
+         int hist[16] = { 0 };
          if ( clusters > 1 )
          {
             const int8_t* c = codes.data() + (size_t)k * S;
             for ( int s2 = 0; s2 < S; ++s2 )
             {
-               switch ( c[s2] )
-               {
-               case 1: ++ns; break;
-               case 6: ++nthr; break;
-               case 7: ++npre; break;
-               case 8: ++npost; break;
-               case 9: ++nmiss; break;
-               default: break;
-               }
+               ++hist[c[s2] & 15];
                mask[(size_t)s2] = (char)('0' + c[s2]);
             }
          }
@@ -547,10 +541,13 @@ extern "C" int kinc_pm_export_text(const char* ccm_path, const char* cmx_path, i
          {
             std::fill(mask.begin(), mask.end(), '0');
          }
-         const int n = snprintf(line, sizeof line, "%d\t%d\t%d\t%d\t%d\t%d\t%d\t%d\t%d\t%.6g\t", x, y, k, clusters, ns,
-                                nmiss, npost, npre, nthr, (double)r[(size_t)k]);
-         if ( fwrite(line, 1, (size_t)n, out) != (size_t)n || fwrite(mask.data(), 1, mask.size(), out) != mask.size()
-              || fputc('\n', out) == EOF )
+         const int n = snprintf(line, sizeof line, "%d\t%d\t%d\t%d\t%d\t%d\t%d\t%d\t%d\t%.6g\t", x, y, k, clusters, hist[1],
+                                hist[9], hist[8], hist[7], hist[6], (double)r[(size_t)k]);
+         /* the whole line in one write */
+         lbuf.assign(line, (size_t)n);
+         lbuf.append(mask);
+         lbuf.push_back('\n');
+         if ( fwrite(lbuf.data(), 1, lbuf.size(), out) != lbuf.size() )
          {
             rc = pm_fail(KINC_SIM_EIO, "write to %s failed", out_path);
             break;
@@ -636,6 +633,7 @@ extern "C" int kinc_pm_extract(const char* emx_path, const char* ccm_path, const
    std::vector<float> ar((size_t)CHUNK * nc);
    int64_t a_base = 0, a_len = 0, b_base = 0, b_len = 0, b_cur = 0;
    std::vector<int8_t> codes;
+   std::vector<float> r;        /* the current pair's first correlations */
    std::string mask((size_t)S, '0');
    char num[64];
    auto pair_of = [](int32_t x, int32_t y) { return (int64_t)x * (x - 1) / 2 + y; };
@@ -656,7 +654,7 @@ extern "C" int kinc_pm_extract(const char* emx_path, const char* ccm_path, const
       if ( o < 0 ) { rc = KINC_SIM_EINVAL; break; }
       const int32_t x = ax[o], y = ay[o];
       if ( x >= G || y >= G ) { rc = pm_fail(KINC_SIM_EINVAL, "pair (%d, %d) outside %d genes", x, y, G); break; }
-      std::vector<float> r;
+      r.clear();
       int64_t j = i;
       while ( j < n_cmx )
       {
@@ -700,21 +698,14 @@ extern "C" int kinc_pm_extract(const char* emx_path, const char* ccm_path, const
       {
          const float corr = r[(size_t)k];
          if ( fabsf(corr) < min_corr || max_corr < fabsf(corr) ) continue;
-         int ns = 0, nmiss = 0, npost = 0, npre = 0, nthr = 0;
+         /* per-code counts from a 16-bin histogram of the cluster's nibbles */
+         int hist[16] = { 0 };
          if ( clusters > 1 )
          {
             const int8_t* c = codes.data() + (size_t)k * S;
             for ( int s2 = 0; s2 < S; ++s2 )
             {
-               switch ( c[s2] )
-               {
-               case 1: ++ns; break;
-               case 6: ++nthr; break;
-               case 7: ++npre; break;
-               case 8: ++npost; break;
-               case 9: ++nmiss; break;
-               default: break;
-               }
+               ++hist[c[s2] & 15];
                mask[(size_t)s2] = (char)('0' + c[s2]);
             }
          }
@@ -733,9 +724,9 @@ extern "C" int kinc_pm_extract(const char* emx_path, const char* ccm_path, const
             line.reserve(96 + src.size() + dst.size() + (size_t)S);
             line += src; line += '\t'; line += dst; line += '\t'; line += num; line += "\tco\t";
             line += std::to_string(k); line += '\t'; line += std::to_string(clusters); line += '\t';
-            line += std::to_string(ns); line += '\t'; line += std::to_string(nmiss); line += '\t';
-            line += std::to_string(npost); line += '\t'; line += std::to_string(npre); line += '\t';
-            line += std::to_string(nthr); line += '\t'; line += mask; line += '\n';
+            line += std::to_string(hist[1]); line += '\t'; line += std::to_string(hist[9]); line += '\t';
+            line += std::to_string(hist[8]); line += '\t'; line += std::to_string(hist[7]); line += '\t';
+            line += std::to_string(hist[6]); line += '\t'; line += mask; line += '\n';
             put(tsv, line);
          }
          if ( gml ) put(gml, "    <edge source=\"" + src + "\" target=\"" + dst + "\" samples=\"" + mask + "\"/>\n");

@@ -81,7 +81,7 @@ def test_import_cmx_matches_restatement(tmp_path, native):
         for key in ("x", "y", "c"):
             assert np.array_equal(got[key], want[key]), key
     assert np.array_equal(got_cmx["payload"].view(np.uint32), cmx["payload"].view(np.uint32))
-    # CCM codes are stored as nibbles: -1 reads back as 15, sign-extended to -1 by the reader's int8
+    # CCM codes are stored as nibbles: the -1 of a non-digit mask character reads back as 15
     assert np.array_equal(got_ccm["payload"] & 0x0F, ccm["payload"] & 0x0F)
     assert (got_cmx["pairs"], got_ccm["pairs"]) == (4, 2)
     assert list(got_cmx["payload"][:, 0][[0, 3]]) == [np.float32(0.912345678), np.float32(0.0)]
