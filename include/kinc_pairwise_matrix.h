@@ -72,6 +72,14 @@ int kinc_emx_read_header(const char* path, int32_t little_endian, int32_t* genes
 int kinc_emx_read(const char* path, int32_t little_endian, float* gem, int64_t capacity);
 
 /*
+ * The CCM or CMX files of a sharded run (each rank's contiguous range of work blocks) joined into
+ * one, in the order given: the inputs must be of one type (detected from the first), agree on
+ * genes, maximum clusters and payload size, and keep strictly increasing indent order across the
+ * joins (else KINC_SIM_EINVAL / KINC_SIM_EORDER).  The output may not be one of the inputs.
+ */
+int kinc_pm_concat(const char* out_path, const char* const* in_paths, int32_t n, int32_t little_endian);
+
+/*
  * ExportCorrelationMatrix (src/core/exportcorrelationmatrix.cpp:17-117): the CMX and CCM files as
  * tab-separated text, one line per CMX cluster: x, y, cluster, clusters of the pair, then the
  * counts of sample codes 1 (in the cluster), 9 (missing), 8 (post-outlier), 7 (pre-outlier) and

@@ -9,6 +9,7 @@
     python -m kinc_gb300 run export-emx --input a.emx --output b.txt --nan NA --names a.genes
     python -m kinc_gb300 run import-cmx --input a.txt --ccm a.ccm --cmx a.cmx --genes 100 --maxclusters 5 \\
         --samples 40 --corrname pearson
+    python -m kinc_gb300 run merge --output a.cmx --inputs rank0.cmx rank1.cmx
 
 Analytic names follow src/core/analyticfactory.cpp:49-55; arguments follow each
 analytic's input class (src/core/similarity_input.cpp, exportcorrelationmatrix_input.cpp,
@@ -126,6 +127,11 @@ def _parser():
     icm.add_argument("--samples", type=int, required=True)
     icm.add_argument("--corrname", required=True, help="correlation name (KINC metadata; not stored in the files)")
     common(icm)
+
+    mrg = an.add_parser("merge", help="the CCM or CMX files of a sharded run -> one file, in rank order")
+    mrg.add_argument("--output", required=True)
+    mrg.add_argument("--inputs", required=True, nargs="+", help="the ranks' files, in rank order")
+    common(mrg)
     return ap
 
 
@@ -171,6 +177,8 @@ def main(argv=None):
             pm.export_emx_text(args.input, args.output, nan=args.nan, transform=args.transform,
                                gene_names_path=args.names, sample_names_path=args.sample_names,
                                little_endian=args.little_endian)
+        elif args.analytic == "merge":
+            pm.concat(args.output, args.inputs, little_endian=args.little_endian)
         elif args.analytic == "import-cmx":
             pm.import_text(args.input, args.ccm, args.cmx, args.genes, args.maxclusters, args.samples,
                            little_endian=args.little_endian)

@@ -85,6 +85,7 @@ const std::map<std::string, std::vector<std::string>> KEYS = {
    { "import-emx", { "input", "output", "nan", "samples", "transform", "names", "sample-names", "little-endian" } },
    { "export-emx", { "input", "output", "nan", "transform", "names", "sample-names", "little-endian" } },
    { "import-cmx", { "input", "ccm", "cmx", "genes", "maxclusters", "samples", "corrname", "little-endian" } },
+   { "merge", { "output", "inputs", "little-endian" } },
 };
 
 const std::vector<std::string> BOOLEANS = { "preout", "postout", "little-endian" };
@@ -115,6 +116,7 @@ int usage()
            "           [--sample-names TXT]\n"
            "       kinc-gb300 run import-cmx --input TXT --ccm CCM --cmx CMX --genes N --maxclusters N --samples N\n"
            "           --corrname NAME\n"
+           "       kinc-gb300 run merge --output CCM|CMX --inputs RANK0,RANK1,...\n"
            "  (every analytic takes --little-endian; --transform: none, \"natural logarithm\", \"logarithm base 2\",\n"
            "   \"logarithm base 10\")\n");
    return 2;
@@ -358,6 +360,30 @@ int run_import_cmx(const Args& a)
    return rc == KINC_SIM_OK ? 0 : 1;
 }
 
+int run_merge(const Args& a)
+{
+   if ( !a.has("output") || !a.has("inputs") )
+   {
+      fprintf(stderr, "merge: --output and --inputs (comma-separated, in rank order) are required\n");
+      return 2;
+   }
+   std::vector<std::string> ins;
+   const std::string list = a.str("inputs");
+   for ( size_t b = 0;; )
+   {
+      const size_t e = list.find(',', b);
+      ins.push_back(list.substr(b, e == std::string::npos ? std::string::npos : e - b));
+      if ( e == std::string::npos ) break;
+      b = e + 1;
+   }
+   std::vector<const char*> ptrs;
+   for ( const auto& p : ins ) ptrs.push_back(p.c_str());
+   const int rc = kinc_pm_concat(a.str("output").c_str(), ptrs.data(), (int32_t)ptrs.size(),
+                                 a.str("little-endian", "0") == "1");
+   if ( rc != KINC_SIM_OK ) fprintf(stderr, "merge: %s\n", kinc_pm_last_error());
+   return rc == KINC_SIM_OK ? 0 : 1;
+}
+
 }  // namespace
 
 int main(int argc, char** argv)
@@ -394,6 +420,7 @@ int main(int argc, char** argv)
    if ( an == "import-emx" ) return run_import_emx(a);
    if ( an == "export-emx" ) return run_export_emx(a);
    if ( an == "import-cmx" ) return run_import_cmx(a);
+   if ( an == "merge" ) return run_merge(a);
    fprintf(stderr, "unknown analytic %s\n", an.c_str());
    return usage();
 }

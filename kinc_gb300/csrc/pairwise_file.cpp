@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -411,6 +412,67 @@ extern "C" int kinc_emx_read(const char* path, int32_t little_endian, float* gem
    Endian e { little_endian != 0 };
    for ( int64_t i = 0; i < (int64_t)g * s; ++i ) gem[i] = e.get<float>(b.data() + 4 * i);
    return KINC_SIM_OK;
+}
+
+/*
+ * The files of a sharded run joined into one: each rank wrote the items of a contiguous range of
+ * work blocks, so the joined file is the inputs' items back to back, in the order given.  The
+ * inputs must agree on type, genes, maximum clusters and payload size, and their items must stay
+ * in strictly increasing indent order across the joins (Matrix::write's rule); the header counts
+ * are recomputed (a pair continued across a join counts once).
+ */
+extern "C" int kinc_pm_concat(const char* out_path, const char* const* in_paths, int32_t n, int32_t little_endian)
+{
+   if ( !out_path || !in_paths || n < 1 ) return pm_fail(KINC_SIM_EINVAL, "Did not get valid input and/or output arguments.");
+   for ( int32_t i = 0; i < n; ++i )
+   {
+      if ( !in_paths[i] ) return pm_fail(KINC_SIM_EINVAL, "input %d is NULL", i);
+      char a[4096], b[4096];
+      if ( realpath(in_paths[i], a) && realpath(out_path, b) && strcmp(a, b) == 0 )
+         return pm_fail(KINC_SIM_EINVAL, "the output %s is also input %d", out_path, i);
+   }
+   int type = 0;
+   int32_t G = 0, K = 0, sub = 0;
+   for ( int t : { KINC_PM_CCM, KINC_PM_CMX } )
+   {
+      kinc_pm* m = nullptr;
+      if ( kinc_pm_open(in_paths[0], t, little_endian, &m, &G, &K, &sub, nullptr, nullptr) == KINC_SIM_OK )
+      {
+         kinc_pm_close(m);
+         type = t;
+         break;
+      }
+   }
+   if ( !type ) return pm_fail(KINC_SIM_EINVAL, "%s is neither a CCM nor a CMX file in this byte order", in_paths[0]);
+   kinc_pm* out = nullptr;
+   int rc = kinc_pm_create(out_path, type, G, K, sub, little_endian, &out);
+   if ( rc ) return rc;
+   const size_t per = type == KINC_PM_CCM ? (size_t)sub : (size_t)sub * sizeof(float);
+   const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(1 << 16, (int64_t)((64u << 20) / std::max<size_t>(per, 1))));
+   std::vector<int32_t> x((size_t)chunk), y((size_t)chunk);
+   std::vector<int8_t> c((size_t)chunk);
+   std::vector<unsigned char> payload((size_t)chunk * per);
+   for ( int32_t i = 0; i < n && rc == KINC_SIM_OK; ++i )
+   {
+      kinc_pm* m = nullptr;
+      int32_t g = 0, k = 0, s2 = 0;
+      int64_t items = 0;
+      if ( (rc = kinc_pm_open(in_paths[i], type, little_endian, &m, &g, &k, &s2, nullptr, &items)) ) break;
+      if ( g != G || k != K || s2 != sub )
+      {
+         rc = pm_fail(KINC_SIM_EINVAL, "%s (%d genes, %d clusters, %d per item) does not match %s (%d, %d, %d)",
+                      in_paths[i], g, k, s2, in_paths[0], G, K, sub);
+      }
+      for ( int64_t first = 0; rc == KINC_SIM_OK && first < items; first += chunk )
+      {
+         const int64_t len = std::min(chunk, items - first);
+         rc = kinc_pm_read_items(m, first, len, x.data(), y.data(), c.data(), payload.data());
+         if ( rc == KINC_SIM_OK ) rc = kinc_pm_write_items(out, len, x.data(), y.data(), c.data(), payload.data());
+      }
+      kinc_pm_close(m);
+   }
+   const int rc2 = kinc_pm_close(out);
+   return rc ? rc : rc2;
 }
 
 /*

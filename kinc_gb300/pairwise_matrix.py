@@ -69,6 +69,12 @@ def read_emx(path, little_endian=False):
     return gem
 
 
+def concat(out_path, in_paths, little_endian=False):
+    """The CCM or CMX files of a sharded run joined into one, in rank order."""
+    arr = (ctypes.c_char_p * len(in_paths))(*[str(p).encode() for p in in_paths])
+    _check(_native.load().kinc_pm_concat(str(out_path).encode(), arr, len(in_paths), int(little_endian)))
+
+
 def export_text(ccm_path, cmx_path, out_path, little_endian=False):
     """ExportCorrelationMatrix: the CMX/CCM pair as tab-separated text (one line per CMX cluster)."""
     _check(_native.load().kinc_pm_export_text(str(ccm_path).encode(), str(cmx_path).encode(), int(little_endian),

@@ -136,3 +136,19 @@ def test_python_command_line_rejects_what_the_native_one_rejects(argv):
     with pytest.raises(SystemExit) as e:
         cli._parser().parse_args(argv)
     assert e.value.code == 2
+
+
+def test_merge_through_both_command_lines(tmp_path, native):
+    import subprocess
+    x, y, c = [2, 3, 3, 5], [1, 0, 0, 4], [0, 0, 1, 0]
+    r = np.array([[0.9], [-0.8], [0.7], [0.6]], np.float32)
+    pm.write(tmp_path / "all.cmx", pm.CMX, 6, 2, 1, x, y, c, r)
+    pm.write(tmp_path / "r0.cmx", pm.CMX, 6, 2, 1, x[:2], y[:2], c[:2], r[:2])
+    pm.write(tmp_path / "r1.cmx", pm.CMX, 6, 2, 1, x[2:], y[2:], c[2:], r[2:])
+    ins = [str(tmp_path / "r0.cmx"), str(tmp_path / "r1.cmx")]
+    assert cli.main(["run", "merge", "--output", str(tmp_path / "py.cmx"), "--inputs", *ins]) == 0
+    res = subprocess.run([_native_cli(), "run", "merge", "--output", str(tmp_path / "nat.cmx"), "--inputs",
+                          ",".join(ins)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr
+    want = (tmp_path / "all.cmx").read_bytes()
+    assert (tmp_path / "py.cmx").read_bytes() == want and (tmp_path / "nat.cmx").read_bytes() == want

@@ -256,3 +256,44 @@ def test_unwritable_output_is_an_io_error(tmp_path, native):
     with pytest.raises(_native.SimError) as err:
         pm.write(target, pm.CMX, 4, 2, 1, [1], [0], [0], np.array([[0.5]], np.float32))
     assert err.value.code in (_native.EINVAL, _native.EIO)
+
+
+@pytest.mark.parametrize("little", [False, True])
+@pytest.mark.parametrize("kind", ["ccm", "cmx"])
+def test_concat_rejoins_split_files(tmp_path, native, little, kind):
+    """A file cut into three item ranges (one cut inside a pair's clusters) and joined again is
+    byte for byte the original; the header counts are recomputed."""
+    rng = np.random.default_rng(6)
+    genes, maxk, samples = 14, 4, 9
+    x, y, c, codes, corr = _random_items(rng, genes, maxk, samples)
+    t = pm.CCM if kind == "ccm" else pm.CMX
+    payload = codes if kind == "ccm" else corr
+    sub = samples if kind == "ccm" else 1
+    pm.write(tmp_path / f"a.{kind}", t, genes, maxk, sub, x, y, c, payload, little_endian=little)
+    multi = [i for i in range(1, len(x)) if (x[i], y[i]) == (x[i - 1], y[i - 1])]
+    cuts = [0, multi[len(multi) // 2], 2 * len(x) // 3, len(x)]
+    parts = []
+    for k in range(3):
+        sl = slice(cuts[k], cuts[k + 1])
+        parts.append(tmp_path / f"p{k}.{kind}")
+        pm.write(parts[-1], t, genes, maxk, sub, x[sl], y[sl], c[sl], payload[sl], little_endian=little)
+    pm.concat(tmp_path / f"b.{kind}", parts, little_endian=little)
+    assert (tmp_path / f"b.{kind}").read_bytes() == (tmp_path / f"a.{kind}").read_bytes()
+
+
+def test_concat_errors(tmp_path, native):
+    rng = np.random.default_rng(7)
+    x, y, c, codes, corr = _random_items(rng, 10, 3, 5)
+    pm.write(tmp_path / "a.cmx", pm.CMX, 10, 3, 1, x, y, c, corr)
+    pm.write(tmp_path / "b.cmx", pm.CMX, 11, 3, 1, x, y, c, corr)
+    pm.write(tmp_path / "a.ccm", pm.CCM, 10, 3, 5, x, y, c, codes)
+    with pytest.raises(_native.SimError, match="does not match"):
+        pm.concat(tmp_path / "o.cmx", [tmp_path / "a.cmx", tmp_path / "b.cmx"])
+    with pytest.raises(_native.SimError) as e:      # the same items twice: out of order at the join
+        pm.concat(tmp_path / "o.cmx", [tmp_path / "a.cmx", tmp_path / "a.cmx"])
+    assert e.value.code == _native.EORDER
+    with pytest.raises(_native.SimError, match="not a CMX"):     # a CCM among CMX files
+        pm.concat(tmp_path / "o.cmx", [tmp_path / "a.cmx", tmp_path / "a.ccm"])
+    with pytest.raises(_native.SimError, match="is also input"):
+        pm.concat(tmp_path / "a.cmx", [tmp_path / "a.cmx"])
+    assert pm.read(tmp_path / "a.cmx", pm.CMX)["x"].size == len(x)    # the input was left alone

@@ -82,6 +82,54 @@ def test_two_ranks_equal_one(kw):
         assert list(ccm[k]) == list(one_ccm[k]), k
 
 
+def _write_files(path_ccm, path_cmx, genes, samples, maxk, cmx, ccm):
+    from kinc_gb300 import pairwise_matrix as pm
+    pm.write(path_cmx, pm.CMX, genes, maxk, 1, cmx["x"], cmx["y"], cmx["c"],
+             np.array(cmx["r"], np.float32).reshape(-1, 1))
+    codes = np.frombuffer(b"".join(ccm["codes"]), np.int8).reshape(-1, samples)
+    pm.write(path_ccm, pm.CCM, genes, maxk, samples, ccm["x"], ccm["y"], ccm["c"], codes)
+
+
+def _file_worker(rank, world, port, genes, samples, kw, out_dir):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    gem = synthetic.generate(2, genes=genes, samples=samples)
+    sh = shard.shard_pairs_by_cost(shard.block_costs(gem, block=64), genes, world, rank, block=64)
+    cmx, ccm = _items(gem, sh.start, sh.size, kw)
+    _write_files(os.path.join(out_dir, f"r{rank}.ccm"), os.path.join(out_dir, f"r{rank}.cmx"), genes, samples,
+                 kw.get("max_clusters", 5), cmx, ccm)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_rank_files_merge_into_the_single_run_files(tmp_path, native):
+    """Each of three ranks writes the CCM/CMX files of its range of work blocks; joined in rank
+    order (kinc_pm_concat) they are byte for byte the files of a single-process run."""
+    import torch.multiprocessing as mp
+
+    from kinc_gb300 import pairwise_matrix as pm
+    genes, samples, world = 30, 50, 3
+    kw = dict(clus_method=1, corr_method=1, criterion=0, pre_out=1)
+    ctx = mp.get_context("spawn")
+    port = _free_port()
+    procs = [ctx.Process(target=_file_worker, args=(r, world, port, genes, samples, kw, str(tmp_path)))
+             for r in range(world)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=300)
+        assert p.exitcode == 0
+    for ext in ("ccm", "cmx"):
+        pm.concat(tmp_path / f"all.{ext}", [tmp_path / f"r{r}.{ext}" for r in range(world)])
+    gem = synthetic.generate(2, genes=genes, samples=samples)
+    cmx, ccm = _items(gem, 0, shard.total_pairs(genes), kw)
+    _write_files(tmp_path / "one.ccm", tmp_path / "one.cmx", genes, samples, 5, cmx, ccm)
+    for ext in ("ccm", "cmx"):
+        assert (tmp_path / f"all.{ext}").read_bytes() == (tmp_path / f"one.{ext}").read_bytes(), ext
+
+
 def test_shards_cover_all_pairs():
     for genes in (2, 3, 100, 5000):
         for world in (1, 2, 3, 8):
