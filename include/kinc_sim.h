@@ -209,6 +209,19 @@ int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes, int32_t sa
                                    const kinc_sim_params* params, int64_t start, int64_t size, int8_t* d_K,
                                    int8_t* d_labels, float* d_corr, void* stream);
 
+/*
+ * Sharding across processes (one per GPU): the contiguous range of whole work blocks
+ * [*first_block, *first_block + *nblocks) that rank `rank` of `world` runs, for
+ * kinc_sim_run_to_files(..., first_block, nblocks); the ranks' ranges cover every block once,
+ * in rank order.  by_cost 0: equal block counts.  by_cost 1: equal estimated cost, a block
+ * costing the sum over its pairs of n_x * n_y / samples (n_g: gene g's samples that are present
+ * and not below min_expr), the expected usable count every per-pair pass is proportional to;
+ * gem is the host matrix, row-major [genes][samples] (unused for by_cost 0).  Replaces the
+ * block farming of ACE's MPI runner with a static partition; no counterpart in KINC itself.
+ */
+int kinc_shard_blocks(const float* gem, int32_t genes, int32_t samples, float min_expr, int32_t world,
+                      int32_t rank, int32_t by_cost, int64_t* first_block, int64_t* nblocks);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,10 @@ def _parser():
                      help="glibc: KINC's serial path; lcg: KINC's OpenCL worker (per-fit LCG GMM)")
     sim.add_argument("--first-block", type=int, default=0, help="first work block (for a shard)")
     sim.add_argument("--blocks", type=int, default=-1, help="work blocks to run (-1: to the end)")
+    sim.add_argument("--world", type=int, help="ranks of a sharded run (with --rank): this rank's work blocks")
+    sim.add_argument("--rank", type=int, default=0)
+    sim.add_argument("--by-cost", nargs="?", const=True, default=False, type=_bool,
+                     help="cut the ranks' ranges by estimated cost instead of block count")
     common(sim)
 
     exp = an.add_parser("export-cmx", help="CMX + CCM -> text")
@@ -147,6 +151,12 @@ def main(argv=None):
             if not args.ccm and not args.cmx:
                 raise SystemExit("similarity: give --ccm and/or --cmx")
             gem = pm.read_emx(args.input, little_endian=args.little_endian)
+            if args.world is not None:
+                from .shard import shard_blocks
+                if args.first_block or args.blocks != -1:
+                    raise SystemExit("similarity: give --world/--rank or --first-block/--blocks, not both")
+                args.first_block, args.blocks = shard_blocks(gem, args.world, args.rank, by_cost=args.by_cost,
+                                                             min_expr=args.minexpr)
             sim = Similarity(np.ascontiguousarray(gem), clusmethod=args.clusmethod, corrmethod=args.corrmethod,
                              minexpr=args.minexpr, minsamp=args.minsamp, minclus=args.minclus, maxclus=args.maxclus,
                              crit=args.crit, preout=args.preout, postout=args.postout, mincorr=args.mincorr,

@@ -32,6 +32,7 @@ UNITS = [
     ("compact.cu", []),
     ("pairwise_file.cpp", []),
     ("text_io.cpp", []),
+    ("shard.cpp", []),
     ("rmt.cu", []),
 ]
 

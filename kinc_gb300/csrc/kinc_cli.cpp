@@ -78,7 +78,7 @@ private:
 const std::map<std::string, std::vector<std::string>> KEYS = {
    { "similarity", { "input", "ccm", "cmx", "clusmethod", "corrmethod", "minexpr", "minsamp", "minclus", "maxclus",
                      "crit", "preout", "postout", "mincorr", "maxcorr", "ksize", "semantics", "precision",
-                     "rand", "first-block", "blocks", "little-endian" } },
+                     "rand", "first-block", "blocks", "world", "rank", "by-cost", "little-endian" } },
    { "export-cmx", { "ccm", "cmx", "output", "little-endian" } },
    { "extract", { "emx", "ccm", "cmx", "output", "graphml", "mincorr", "maxcorr", "names", "little-endian" } },
    { "rmt", { "input", "log", "tstart", "tstep", "tstop", "minpace", "maxpace", "bins", "little-endian" } },
@@ -88,7 +88,7 @@ const std::map<std::string, std::vector<std::string>> KEYS = {
    { "merge", { "output", "inputs", "little-endian" } },
 };
 
-const std::vector<std::string> BOOLEANS = { "preout", "postout", "little-endian" };
+const std::vector<std::string> BOOLEANS = { "preout", "postout", "little-endian", "by-cost" };
 
 bool is_bool(const std::string& k)
 {
@@ -104,7 +104,7 @@ int usage()
            "           [--corrmethod pearson|spearman|both] [--minexpr F] [--minsamp N] [--minclus N] [--maxclus N]\n"
            "           [--crit BIC|ICL] [--preout [true|false]] [--postout [true|false]] [--mincorr F] [--maxcorr F]\n"
            "           [--ksize N] [--semantics reference|fixed] [--precision fp32|tf32|3xbf16] [--rand glibc|lcg]\n"
-           "           [--first-block N] [--blocks N] [--little-endian]\n"
+           "           [--first-block N] [--blocks N | --world N --rank R [--by-cost]] [--little-endian]\n"
            "       kinc-gb300 run export-cmx --ccm CCM --cmx CMX --output TXT\n"
            "       kinc-gb300 run extract --emx EMX --ccm CCM --cmx CMX [--output TXT] [--graphml XML] [--mincorr F]\n"
            "           [--maxcorr F] [--names TXT]\n"
@@ -205,8 +205,24 @@ int run_similarity(const Args& a)
    p.min_corr = (float)a.real("mincorr", 0.5);
    p.max_corr = (float)a.real("maxcorr", 1.0);
    p.ksize = a.int32("ksize", 4096);
-   const long long first_block = a.integer("first-block", 0), blocks = a.integer("blocks", -1);
+   long long first_block = a.integer("first-block", 0), blocks = a.integer("blocks", -1);
+   const int world = a.int32("world", 0), rank = a.int32("rank", 0);
    if ( !a.ok ) return 2;
+   if ( (a.has("world") || a.has("rank") || a.has("by-cost")) && (a.has("first-block") || a.has("blocks")) )
+   {
+      fprintf(stderr, "similarity: give --world/--rank or --first-block/--blocks, not both\n");
+      return 2;
+   }
+   if ( (a.has("rank") || a.has("by-cost")) && !a.has("world") )
+   {
+      fprintf(stderr, "similarity: --rank and --by-cost need --world\n");
+      return 2;
+   }
+   if ( a.has("world") && (world < 1 || rank < 0 || rank >= world) )
+   {
+      fprintf(stderr, "similarity: rank %d outside a world of %d\n", rank, world);
+      return 2;
+   }
    const int le = a.str("little-endian", "0") == "1";
    int32_t G = 0, S = 0;
    if ( kinc_emx_read_header(a.str("input").c_str(), le, &G, &S) != KINC_SIM_OK )
@@ -219,6 +235,18 @@ int run_similarity(const Args& a)
    {
       fprintf(stderr, "similarity: %s\n", kinc_pm_last_error());
       return 1;
+   }
+   if ( a.has("world") )
+   {
+      int64_t fb = 0, nb = 0;
+      if ( kinc_shard_blocks(gem.data(), G, S, p.min_expr, world, rank, a.str("by-cost", "0") == "1", &fb, &nb)
+           != KINC_SIM_OK )
+      {
+         fprintf(stderr, "similarity: cannot shard %d genes over %d ranks\n", G, world);
+         return 2;
+      }
+      first_block = fb;
+      blocks = nb;
    }
    kinc_sim_ctx* ctx = nullptr;
    int rc = kinc_sim_create(gem.data(), G, S, &p, &ctx);

@@ -114,3 +114,22 @@ def merge_items(per_rank):
         for k in keys:
             out[k].extend(list(items[k]))
     return out
+
+
+def shard_blocks(gem, world, rank, by_cost=False, min_expr=float("-inf")):
+    """The native partition (include/kinc_sim.h: kinc_shard_blocks): (first_block, nblocks) of
+    KINC's 32,768-pair work blocks for `rank`, by block count or by estimated cost -- the same
+    cut as shard_pairs / shard_pairs_by_cost at that block size."""
+    import ctypes
+
+    import numpy as np
+
+    from . import _native
+    gem = np.ascontiguousarray(gem, np.float32)
+    first, n = ctypes.c_int64(), ctypes.c_int64()
+    rc = _native.load().kinc_shard_blocks(gem.ctypes.data_as(ctypes.c_void_p), gem.shape[0], gem.shape[1],
+                                          float(min_expr), int(world), int(rank), int(bool(by_cost)),
+                                          ctypes.byref(first), ctypes.byref(n))
+    if rc != _native.OK:
+        raise ValueError(f"rank {rank} outside world of {world}, or a matrix of fewer than 2 genes")
+    return first.value, n.value

@@ -112,6 +112,13 @@ def test_native_program_export_and_extract(tmp_path, native):
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--minsamp", "3x"], 2),
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--blocks", ""], 2),
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--rand", "mt"], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--world", "2",
+                                         "--rank", "2"], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--world", "2",
+                                         "--first-block", "1"], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--by-cost"], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--world", "2",
+                                         "--rank", "1", "--by-cost"], 1),
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--rand", "lcg"], 1),
                                        (["run", "extract", "--emx", "a", "--ccm", "b", "--cmx", "c", "--output", "d",
                                          "--mincorr", "high"], 2),

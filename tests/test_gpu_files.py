@@ -208,6 +208,33 @@ def test_command_line_similarity_and_rmt(tmp_path, capsys):
         assert "rmt:" in out.err
 
 
+@pytest.mark.parametrize("by_cost", [False, True])
+def test_sharded_command_line_runs_merge_into_the_single_run(tmp_path, by_cost):
+    """kinc-gb300 run similarity --world 3 --rank r on each rank, then run merge: the joined
+    CCM/CMX files are byte for byte the files of one unsharded run."""
+    import subprocess
+
+    from kinc_gb300 import build
+    G, S = 400, 48                        # 79,800 pairs: three work blocks
+    gem = synthetic.generate(4, genes=G, samples=S)
+    pm.write_emx(tmp_path / "g.emx", gem)
+    common = ["--input", str(tmp_path / "g.emx"), "--clusmethod", "gmm", "--corrmethod", "pearson", "--crit",
+              "BIC", "--postout", "--mincorr", "0.3"]
+    r = subprocess.run([build.CLI, "run", "similarity", *common, "--ccm", str(tmp_path / "one.ccm"), "--cmx",
+                        str(tmp_path / "one.cmx")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for rank in range(3):
+        r = subprocess.run([build.CLI, "run", "similarity", *common, "--ccm", str(tmp_path / f"r{rank}.ccm"),
+                            "--cmx", str(tmp_path / f"r{rank}.cmx"), "--world", "3", "--rank", str(rank),
+                            *(["--by-cost"] if by_cost else [])], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+    for ext in ("ccm", "cmx"):
+        r = subprocess.run([build.CLI, "run", "merge", "--output", str(tmp_path / f"all.{ext}"), "--inputs",
+                            ",".join(str(tmp_path / f"r{k}.{ext}") for k in range(3))], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        assert (tmp_path / f"all.{ext}").read_bytes() == (tmp_path / f"one.{ext}").read_bytes(), ext
+
+
 @pytest.mark.parametrize("precision", ["tf32", "3xbf16"])
 def test_run_to_files_tensor_core_matches_execute(tmp_path, precision):
     """The tensor-core form through the file runner keeps exactly the correlations execute() returns

@@ -168,3 +168,24 @@ def test_cost_shards_cover_and_balance(world):
     share_count = [costs[s.start // 512:(s.end + 511) // 512].sum() / costs.sum() for s in by_count]
     assert max(share) - min(share) <= max(share_count) - min(share_count) + 1e-12
     assert max(share) - 1 / world < 2 * costs.max() / costs.sum()
+
+
+@pytest.mark.parametrize("by_cost", [False, True])
+def test_native_shards_equal_the_python_cuts(native, by_cost):
+    """kinc_shard_blocks cuts where shard_pairs / shard_pairs_by_cost cut at KINC's block size."""
+    gem = synthetic.generate(4, genes=900, samples=60)
+    G = gem.shape[0]
+    costs = shard.block_costs(gem, min_expr=5.0) if by_cost else None
+    for world in (1, 2, 3, 5, 8):
+        got = []
+        for rank in range(world):
+            first, n = shard.shard_blocks(gem, world, rank, by_cost=by_cost, min_expr=5.0)
+            want = (shard.shard_pairs_by_cost(costs, G, world, rank) if by_cost
+                    else shard.shard_pairs(G, world, rank))
+            assert first * shard.WORK_BLOCK_SIZE == want.start
+            assert min((first + n) * shard.WORK_BLOCK_SIZE, shard.total_pairs(G)) == want.end
+            got.append((first, n))
+        assert got[0][0] == 0 and all(a[0] + a[1] == b[0] for a, b in zip(got, got[1:]))
+        assert sum(n for _, n in got) == -(-shard.total_pairs(G) // shard.WORK_BLOCK_SIZE)
+    with pytest.raises(ValueError):
+        shard.shard_blocks(gem, 2, 2)
