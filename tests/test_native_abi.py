@@ -1,4 +1,4 @@
-"""The C ABI library: it loads, exports every symbol include/kinc_sim.h
+"""The C ABI library: it loads, exports every function include/*.h
 declares, validates arguments, and its host-only filter (Similarity::process)
 matches the oracle.  No kernel is launched here."""
 import ctypes
@@ -19,7 +19,7 @@ def declared_symbols():
     for f in sorted(os.listdir(INCLUDE)):
         if f.endswith(".h"):
             text = re.sub(r"/\*.*?\*/", "", open(os.path.join(INCLUDE, f)).read(), flags=re.S)
-            names |= set(re.findall(r"\b(kinc_(?:sim|pm|emx)_\w+)\s*\(", text))
+            names |= set(re.findall(r"\b(kinc_\w+)\s*\(", text))
     return sorted(names)
 
 
