@@ -151,19 +151,14 @@ def main(argv=None):
             if not args.ccm and not args.cmx:
                 raise SystemExit("similarity: give --ccm and/or --cmx")
             gem = pm.read_emx(args.input, little_endian=args.little_endian)
-            if args.world is not None:
-                from .shard import shard_blocks
-                if args.first_block or args.blocks != -1:
-                    raise SystemExit("similarity: give --world/--rank or --first-block/--blocks, not both")
-                args.first_block, args.blocks = shard_blocks(gem, args.world, args.rank, by_cost=args.by_cost,
-                                                             min_expr=args.minexpr)
             sim = Similarity(np.ascontiguousarray(gem), clusmethod=args.clusmethod, corrmethod=args.corrmethod,
                              minexpr=args.minexpr, minsamp=args.minsamp, minclus=args.minclus, maxclus=args.maxclus,
                              crit=args.crit, preout=args.preout, postout=args.postout, mincorr=args.mincorr,
                              maxcorr=args.maxcorr, ksize=args.ksize, semantics=args.semantics,
                              precision=args.precision, rand=args.rand)
             sim.run(ccm_path=args.ccm, cmx_path=args.cmx, little_endian=args.little_endian,
-                    first_block=args.first_block, nblocks=args.blocks)
+                    first_block=args.first_block, nblocks=args.blocks, world=args.world, rank=args.rank,
+                    by_cost=args.by_cost)
             sim.close()
         elif args.analytic == "export-cmx":
             pm.export_text(args.ccm, args.cmx, args.output, little_endian=args.little_endian)

@@ -238,11 +238,20 @@ class Similarity:
             matrix.write_pair(int(x[i]), int(y[i]), payloads[i:j])
             i = j
 
-    def run(self, ccm_path=None, cmx_path=None, little_endian=False, first_block=0, nblocks=-1, device_block=0):
-        """Run work blocks [first_block, first_block + nblocks) in order (all of them by default).
-        With file paths, the native runner writes the CCM/CMX files (include/kinc_pairwise_matrix.h)
-        in device blocks of `device_block` pairs (0 = the largest the worker holds); otherwise the
-        items are kept in memory and (ccm, cmx) PairwiseMatrix objects are returned."""
+    def run(self, ccm_path=None, cmx_path=None, little_endian=False, first_block=0, nblocks=-1, device_block=0,
+            world=None, rank=0, by_cost=False):
+        """Run work blocks [first_block, first_block + nblocks) in order (all of them by default),
+        or, with `world`, the share of rank `rank` (kinc_shard_blocks: equal block counts, or equal
+        estimated cost with by_cost).  With file paths, the native runner writes the CCM/CMX files
+        (include/kinc_pairwise_matrix.h) in device blocks of `device_block` pairs (0 = the largest
+        the worker holds); otherwise the items are kept in memory and (ccm, cmx) PairwiseMatrix
+        objects are returned."""
+        if world is not None:
+            from .shard import shard_blocks
+            if first_block or nblocks != -1:
+                raise InvalidArgument("give world/rank or first_block/nblocks, not both")
+            first_block, nblocks = shard_blocks(self.expressions, world, rank, by_cost=by_cost,
+                                                min_expr=self.params.min_expr)
         self.initialize()
         if ccm_path is not None or cmx_path is not None:
             L = _native.load()
