@@ -146,6 +146,7 @@ def parity_block(gpu, cpu):
             "label_agreement": float(labels_eq.mean()) if len(labels_eq) else 1.0,
             "label_rows": int(rows.sum()), "correlations": int(mask.sum()),
             "nan_mismatches": int((nan_a != nan_b).sum()), "max_abs_dr": dr,
+            "k_histogram": np.bincount(np.asarray(Kc, np.int64)).tolist(),
             "bit_exact": bool(np.array_equal(Kg, Kc) and (not rows.any() or labels_eq.all())
                               and np.array_equal(a.view(np.uint32), b.view(np.uint32))),
             "vs": "oracle: C restatement of KINC's serial path, pinned bit-exact to KINC's compiled Pairwise code"}

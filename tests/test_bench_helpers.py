@@ -24,6 +24,7 @@ def test_parity_block_identical():
     assert p["bit_exact"] and p["k_agreement"] == 1.0 and p["label_agreement"] == 1.0
     assert p["max_abs_dr"] == 0.0 and p["nan_mismatches"] == 0
     assert p["correlations"] == int(r[0].sum())
+    assert sum(p["k_histogram"]) == len(r[0]) and p["k_histogram"][1] == int((r[0] == 1).sum())
 
 
 def test_parity_block_reports_differences():
