@@ -72,6 +72,19 @@ int kinc_emx_read_header(const char* path, int32_t little_endian, int32_t* genes
 int kinc_emx_read(const char* path, int32_t little_endian, float* gem, int64_t capacity);
 
 /*
+ * Resume an interrupted kinc_sim_run_to_files: the runner appends work blocks in pair order and
+ * rewrites the header counts only when it finishes, so an interrupted CCM/CMX file holds the
+ * items of the finished blocks and possibly part of the next.  *resume_block is the work block of
+ * the last whole item on disk -- the smallest over the two files -- or first_block for a file
+ * without items or not yet created (either path may be NULL: that file is not written);
+ * both files are cut back to the items of the blocks before *resume_block and their header
+ * counts rewritten.  Running blocks [*resume_block, end) into new files and joining them after
+ * these with kinc_pm_concat gives the files of the uninterrupted run.
+ */
+int kinc_pm_resume_point(const char* ccm_path, const char* cmx_path, int32_t little_endian, int64_t first_block,
+                         int64_t* resume_block);
+
+/*
  * The CCM or CMX files of a sharded run (each rank's contiguous range of work blocks) joined into
  * one, in the order given: the inputs must be of one type (detected from the first), agree on
  * genes, maximum clusters and payload size, and keep strictly increasing indent order across the

@@ -71,6 +71,8 @@ def _parser():
     sim.add_argument("--rank", type=int, default=0)
     sim.add_argument("--by-cost", nargs="?", const=True, default=False, type=_bool,
                      help="cut the ranks' ranges by estimated cost instead of block count")
+    sim.add_argument("--resume", nargs="?", const=True, default=False, type=_bool,
+                     help="continue an interrupted run: keep the files' whole work blocks, run the rest")
     common(sim)
 
     exp = an.add_parser("export-cmx", help="CMX + CCM -> text")
@@ -158,7 +160,7 @@ def main(argv=None):
                              precision=args.precision, rand=args.rand)
             sim.run(ccm_path=args.ccm, cmx_path=args.cmx, little_endian=args.little_endian,
                     first_block=args.first_block, nblocks=args.blocks, world=args.world, rank=args.rank,
-                    by_cost=args.by_cost)
+                    by_cost=args.by_cost, resume=args.resume)
             sim.close()
         elif args.analytic == "export-cmx":
             pm.export_text(args.ccm, args.cmx, args.output, little_endian=args.little_endian)

@@ -95,6 +95,8 @@ SIGNATURES = {
     "kinc_pm_export_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _I32, ctypes.c_char_p]),
     "kinc_shard_blocks": (ctypes.c_int, [_VP, _I32, _I32, ctypes.c_float, _I32, _I32, _I32,
                                          ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]),
+    "kinc_pm_resume_point": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _I32, _I64,
+                                            ctypes.POINTER(ctypes.c_int64)]),
     "kinc_pm_concat": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p), _I32, _I32]),
     "kinc_pm_import_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, _I32, _I32, _I32, _I32]),
     "kinc_emx_import_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, _I32, _I32, _I32, ctypes.c_char_p,

@@ -12,6 +12,7 @@
 #include "../../include/kinc_rmt.h"
 #include "../../include/kinc_sim.h"
 
+#include <algorithm>
 #include <cctype>
 #include <cerrno>
 #include <climits>
@@ -23,6 +24,8 @@
 #include <map>
 #include <string>
 #include <vector>
+
+#include <unistd.h>
 
 namespace {
 
@@ -78,7 +81,7 @@ private:
 const std::map<std::string, std::vector<std::string>> KEYS = {
    { "similarity", { "input", "ccm", "cmx", "clusmethod", "corrmethod", "minexpr", "minsamp", "minclus", "maxclus",
                      "crit", "preout", "postout", "mincorr", "maxcorr", "ksize", "semantics", "precision",
-                     "rand", "first-block", "blocks", "world", "rank", "by-cost", "little-endian" } },
+                     "rand", "first-block", "blocks", "world", "rank", "by-cost", "resume", "little-endian" } },
    { "export-cmx", { "ccm", "cmx", "output", "little-endian" } },
    { "extract", { "emx", "ccm", "cmx", "output", "graphml", "mincorr", "maxcorr", "names", "little-endian" } },
    { "rmt", { "input", "log", "tstart", "tstep", "tstop", "minpace", "maxpace", "bins", "little-endian" } },
@@ -88,7 +91,7 @@ const std::map<std::string, std::vector<std::string>> KEYS = {
    { "merge", { "output", "inputs", "little-endian" } },
 };
 
-const std::vector<std::string> BOOLEANS = { "preout", "postout", "little-endian", "by-cost" };
+const std::vector<std::string> BOOLEANS = { "preout", "postout", "little-endian", "by-cost", "resume" };
 
 bool is_bool(const std::string& k)
 {
@@ -104,7 +107,7 @@ int usage()
            "           [--corrmethod pearson|spearman|both] [--minexpr F] [--minsamp N] [--minclus N] [--maxclus N]\n"
            "           [--crit BIC|ICL] [--preout [true|false]] [--postout [true|false]] [--mincorr F] [--maxcorr F]\n"
            "           [--ksize N] [--semantics reference|fixed] [--precision fp32|tf32|3xbf16] [--rand glibc|lcg]\n"
-           "           [--first-block N] [--blocks N | --world N --rank R [--by-cost]] [--little-endian]\n"
+           "           [--first-block N] [--blocks N | --world N --rank R [--by-cost]] [--resume] [--little-endian]\n"
            "       kinc-gb300 run export-cmx --ccm CCM --cmx CMX --output TXT\n"
            "       kinc-gb300 run extract --emx EMX --ccm CCM --cmx CMX [--output TXT] [--graphml XML] [--mincorr F]\n"
            "           [--maxcorr F] [--names TXT]\n"
@@ -177,6 +180,51 @@ int choice(const std::string& v, const std::vector<std::string>& names, const ch
    fprintf(stderr, "\n");
    ok = false;
    return 0;
+}
+
+/* --resume: cut the files an interrupted run left back to their whole work blocks
+ * (kinc_pm_resume_point), run the remaining blocks into part files and join them after the kept
+ * items (kinc_pm_concat); a file not yet created takes the part file as it is. */
+int resume_to_files(kinc_sim_ctx* ctx, const std::string* ccm, const std::string* cmx, int le, int32_t G,
+                    long long first_block, long long blocks)
+{
+   const long long B = KINC_SIM_WORK_BLOCK_SIZE;
+   const long long total = (long long)G * (G - 1) / 2;
+   const long long all = (total + B - 1) / B;
+   const long long end = blocks < 0 ? all : std::min(all, first_block + blocks);
+   int64_t start = 0;
+   int rc = kinc_pm_resume_point(ccm ? ccm->c_str() : nullptr, cmx ? cmx->c_str() : nullptr, le, first_block, &start);
+   if ( rc != KINC_SIM_OK ) return rc;
+   if ( start > end )
+   {
+      fprintf(stderr, "similarity: the files hold work blocks past block %lld\n", end);
+      return KINC_SIM_EINVAL;
+   }
+   const std::string ccm_part = ccm ? *ccm + ".part" : "", cmx_part = cmx ? *cmx + ".part" : "";
+   rc = kinc_sim_run_to_files_ex(ctx, ccm ? ccm_part.c_str() : nullptr, cmx ? cmx_part.c_str() : nullptr, le, start,
+                                 end - start, 0);
+   if ( rc != KINC_SIM_OK ) return rc;
+   for ( const std::string* final : { ccm, cmx } )
+   {
+      if ( !final ) continue;
+      const std::string part = *final + ".part", joined = *final + ".joined";
+      if ( access(final->c_str(), F_OK) == 0 )
+      {
+         const char* ins[2] = { final->c_str(), part.c_str() };
+         if ( (rc = kinc_pm_concat(joined.c_str(), ins, 2, le)) != KINC_SIM_OK ) return rc;
+         if ( std::rename(joined.c_str(), final->c_str()) != 0 || std::remove(part.c_str()) != 0 )
+         {
+            fprintf(stderr, "similarity: cannot replace %s\n", final->c_str());
+            return KINC_SIM_EIO;
+         }
+      }
+      else if ( std::rename(part.c_str(), final->c_str()) != 0 )
+      {
+         fprintf(stderr, "similarity: cannot create %s\n", final->c_str());
+         return KINC_SIM_EIO;
+      }
+   }
+   return KINC_SIM_OK;
 }
 
 int run_similarity(const Args& a)
@@ -255,9 +303,13 @@ int run_similarity(const Args& a)
       fprintf(stderr, "similarity: %s\n", kinc_sim_last_error(nullptr));
       return 1;
    }
-   rc = kinc_sim_run_to_files_ex(ctx, a.has("ccm") ? a.str("ccm").c_str() : nullptr,
-                                 a.has("cmx") ? a.str("cmx").c_str() : nullptr, le,
-                                 first_block, blocks, 0);
+   const std::string ccm = a.str("ccm"), cmx = a.str("cmx");
+   if ( a.str("resume", "0") == "1" )
+      rc = resume_to_files(ctx, a.has("ccm") ? &ccm : nullptr, a.has("cmx") ? &cmx : nullptr, le, G, first_block,
+                           blocks);
+   else
+      rc = kinc_sim_run_to_files_ex(ctx, a.has("ccm") ? ccm.c_str() : nullptr, a.has("cmx") ? cmx.c_str() : nullptr,
+                                    le, first_block, blocks, 0);
    if ( rc != KINC_SIM_OK ) fprintf(stderr, "similarity: %s\n", kinc_pm_last_error());
    kinc_sim_destroy(ctx);
    return rc == KINC_SIM_OK ? 0 : 1;

@@ -11,6 +11,7 @@
 #include "sim_internal.h"
 
 #include <cuda_runtime.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <cmath>
@@ -411,6 +412,141 @@ extern "C" int kinc_emx_read(const char* path, int32_t little_endian, float* gem
    if ( !ok ) return pm_fail(KINC_SIM_EINVAL, "%s: truncated EMX data", path);
    Endian e { little_endian != 0 };
    for ( int64_t i = 0; i < (int64_t)g * s; ++i ) gem[i] = e.get<float>(b.data() + 4 * i);
+   return KINC_SIM_OK;
+}
+
+/*
+ * Resume point of an interrupted run (the runner writes work blocks in pair order and rewrites
+ * the header counts only when it finishes, so an interrupted file holds a valid header, the
+ * items of the finished blocks and possibly part of the next).  For each file that exists: the
+ * items on disk are those that fit whole in its length; the work block of the last one may be
+ * incomplete.  The resume block is the smallest such block over the files (first_block for a
+ * file without items); both files are cut back to the items of the blocks before it and their
+ * header counts are rewritten, so they are valid, finished files again.
+ */
+namespace {
+
+int cut_back(const char* path, int type, bool little, int64_t* last_block_out, int64_t keep_before_pair,
+             bool apply)
+{
+   FILE* f = fopen(path, apply ? "r+b" : "rb");
+   if ( !f ) return pm_fail(KINC_SIM_EINVAL, "cannot open %s", path);
+   Endian e { little };
+   unsigned char h[HEADER + 4];
+   const size_t hb = HEADER + (type == KINC_PM_CCM ? 4 : 1);
+   if ( fread(h, 1, hb, f) != hb )
+   {
+      fclose(f);
+      return pm_fail(KINC_SIM_EINVAL, "%s: truncated header", path);
+   }
+   const int32_t data_size = e.get<int32_t>(h + 8);
+   const int16_t offset = e.get<int16_t>(h + 28);
+   const int32_t subsize = type == KINC_PM_CCM ? e.get<int32_t>(h + 30) : (int32_t)(int8_t)h[30];
+   if ( offset != offset_of(type) || data_size != data_size_of(type, subsize) )
+   {
+      fclose(f);
+      return pm_fail(KINC_SIM_EINVAL, "%s: not a %s file with this byte order", path, type == KINC_PM_CCM ? "CCM" : "CMX");
+   }
+   const int64_t item = ITEM_HEADER + data_size;
+   const int64_t base = HEADER + offset;
+   fseek(f, 0, SEEK_END);
+   const int64_t size = (int64_t)ftell(f);
+   const int64_t n = size > base ? (size - base) / item : 0;
+   auto pair_at = [&](int64_t i, int32_t* xo, int32_t* yo) -> int64_t {
+      unsigned char b[8];
+      if ( fseek(f, (long)(base + i * item), SEEK_SET) != 0 || fread(b, 1, 8, f) != 8 ) return -1;
+      const int32_t x = e.get<int32_t>(b), y = e.get<int32_t>(b + 4);
+      if ( xo ) *xo = x;
+      if ( yo ) *yo = y;
+      return (int64_t)x * (x - 1) / 2 + y;
+   };
+   if ( !apply )
+   {
+      int64_t last = -1;
+      if ( n > 0 )
+      {
+         const int64_t p = pair_at(n - 1, nullptr, nullptr);
+         if ( p < 0 )
+         {
+            fclose(f);
+            return pm_fail(KINC_SIM_EIO, "cannot read %s", path);
+         }
+         last = p / KINC_SIM_WORK_BLOCK_SIZE;
+      }
+      *last_block_out = last;
+      fclose(f);
+      return KINC_SIM_OK;
+   }
+   /* keep the items whose pair is below keep_before_pair (items are in pair order) */
+   int64_t lo = 0, hi = n;
+   while ( lo < hi )
+   {
+      const int64_t mid = lo + (hi - lo) / 2;
+      const int64_t p = pair_at(mid, nullptr, nullptr);
+      if ( p < 0 )
+      {
+         fclose(f);
+         return pm_fail(KINC_SIM_EIO, "cannot read %s", path);
+      }
+      if ( p < keep_before_pair ) lo = mid + 1;
+      else hi = mid;
+   }
+   const int64_t keep = lo;
+   int64_t pairs = 0, prev = -1;
+   for ( int64_t i = 0; i < keep; ++i )
+   {
+      const int64_t p = pair_at(i, nullptr, nullptr);
+      if ( p < 0 )
+      {
+         fclose(f);
+         return pm_fail(KINC_SIM_EIO, "cannot read %s", path);
+      }
+      pairs += p != prev;
+      prev = p;
+   }
+   std::vector<unsigned char> counts;
+   e.put<int64_t>(counts, pairs);
+   e.put<int64_t>(counts, keep);
+   fflush(f);
+   const bool ok = fseek(f, 12, SEEK_SET) == 0 && fwrite(counts.data(), 1, counts.size(), f) == counts.size()
+                   && fflush(f) == 0 && ftruncate(fileno(f), (off_t)(base + keep * item)) == 0;
+   fclose(f);
+   return ok ? KINC_SIM_OK : pm_fail(KINC_SIM_EIO, "cannot cut %s back", path);
+}
+
+}  // namespace
+
+extern "C" int kinc_pm_resume_point(const char* ccm_path, const char* cmx_path, int32_t little_endian,
+                                    int64_t first_block, int64_t* resume_block)
+{
+   if ( !resume_block || first_block < 0 ) return pm_fail(KINC_SIM_EINVAL, "Did not get valid input and/or output arguments.");
+   const char* paths[2] = { ccm_path, cmx_path };
+   const int types[2] = { KINC_PM_CCM, KINC_PM_CMX };
+   int64_t R = INT64_MAX;
+   bool any = false;
+   for ( int k = 0; k < 2; ++k )
+   {
+      if ( !paths[k] ) continue;
+      if ( access(paths[k], F_OK) != 0 )
+      {
+         R = std::min(R, first_block);   /* nothing of this file was written */
+         continue;
+      }
+      int64_t last = -1;
+      const int rc = cut_back(paths[k], types[k], little_endian != 0, &last, 0, false);
+      if ( rc ) return rc;
+      any = true;
+      R = std::min(R, last < 0 ? first_block : std::max(last, first_block));
+   }
+   if ( !any ) R = first_block;
+   for ( int k = 0; k < 2; ++k )
+   {
+      if ( !paths[k] || access(paths[k], F_OK) != 0 ) continue;
+      int64_t unused = 0;
+      const int rc = cut_back(paths[k], types[k], little_endian != 0, &unused, R * KINC_SIM_WORK_BLOCK_SIZE, true);
+      if ( rc ) return rc;
+   }
+   *resume_block = R;
    return KINC_SIM_OK;
 }
 

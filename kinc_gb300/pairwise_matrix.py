@@ -69,6 +69,16 @@ def read_emx(path, little_endian=False):
     return gem
 
 
+def resume_point(ccm_path, cmx_path, first_block=0, little_endian=False):
+    """Cut an interrupted run's CCM/CMX files back to their finished work blocks; returns the
+    block to resume from (include/kinc_pairwise_matrix.h: kinc_pm_resume_point)."""
+    enc = lambda p: str(p).encode() if p is not None else None  # noqa: E731
+    r = ctypes.c_int64()
+    _check(_native.load().kinc_pm_resume_point(enc(ccm_path), enc(cmx_path), int(little_endian), int(first_block),
+                                               ctypes.byref(r)))
+    return r.value
+
+
 def concat(out_path, in_paths, little_endian=False):
     """The CCM or CMX files of a sharded run joined into one, in rank order."""
     arr = (ctypes.c_char_p * len(in_paths))(*[str(p).encode() for p in in_paths])

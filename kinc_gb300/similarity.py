@@ -239,29 +239,62 @@ class Similarity:
             i = j
 
     def run(self, ccm_path=None, cmx_path=None, little_endian=False, first_block=0, nblocks=-1, device_block=0,
-            world=None, rank=0, by_cost=False):
+            world=None, rank=0, by_cost=False, resume=False):
         """Run work blocks [first_block, first_block + nblocks) in order (all of them by default),
         or, with `world`, the share of rank `rank` (kinc_shard_blocks: equal block counts, or equal
         estimated cost with by_cost).  With file paths, the native runner writes the CCM/CMX files
         (include/kinc_pairwise_matrix.h) in device blocks of `device_block` pairs (0 = the largest
-        the worker holds); otherwise the items are kept in memory and (ccm, cmx) PairwiseMatrix
-        objects are returned."""
+        the worker holds); with resume, files an interrupted run left are cut back to their whole
+        work blocks and only the rest is run and appended.  Without file paths the items are kept
+        in memory and (ccm, cmx) PairwiseMatrix objects are returned."""
         if world is not None:
             from .shard import shard_blocks
             if first_block or nblocks != -1:
                 raise InvalidArgument("give world/rank or first_block/nblocks, not both")
             first_block, nblocks = shard_blocks(self.expressions, world, rank, by_cost=by_cost,
                                                 min_expr=self.params.min_expr)
-        self.initialize()
         if ccm_path is not None or cmx_path is not None:
-            L = _native.load()
-            rc = L.kinc_sim_run_to_files_ex(self._ctx, str(ccm_path).encode() if ccm_path else None,
-                                            str(cmx_path).encode() if cmx_path else None, int(little_endian),
-                                            int(first_block), int(nblocks), int(device_block))
-            if rc != _native.OK:
-                raise _native.SimError(rc, L.kinc_pm_last_error().decode())
+            if resume:
+                self._resume_to_files(ccm_path, cmx_path, little_endian, first_block, nblocks, device_block)
+            else:
+                self._run_to_files(ccm_path, cmx_path, little_endian, first_block, nblocks, device_block)
             return ccm_path, cmx_path
+        self.initialize()
         last = self.size() if nblocks < 0 else min(self.size(), first_block + nblocks)
         for b in range(first_block, last):
             self.process(self.execute(self.make_work(b)))
         return self.ccm, self.cmx
+
+    def _run_to_files(self, ccm_path, cmx_path, little_endian, first_block, nblocks, device_block):
+        """kinc_sim_run_to_files_ex: blocks [first_block, first_block + nblocks) into new files."""
+        self.initialize()
+        L = _native.load()
+        rc = L.kinc_sim_run_to_files_ex(self._ctx, str(ccm_path).encode() if ccm_path else None,
+                                        str(cmx_path).encode() if cmx_path else None, int(little_endian),
+                                        int(first_block), int(nblocks), int(device_block))
+        if rc != _native.OK:
+            raise _native.SimError(rc, L.kinc_pm_last_error().decode())
+
+    def _resume_to_files(self, ccm_path, cmx_path, little_endian, first_block, nblocks, device_block):
+        """Cut the files back to their whole work blocks (kinc_pm_resume_point), run the remaining
+        blocks into part files and join them after the kept items (kinc_pm_concat)."""
+        import os
+
+        from . import pairwise_matrix as pm
+        end = self.size() if nblocks < 0 else min(self.size(), first_block + nblocks)
+        start = pm.resume_point(ccm_path, cmx_path, first_block=first_block, little_endian=little_endian)
+        if start > end:
+            raise InvalidArgument(f"the files hold work blocks past block {end}: not an interrupted run of "
+                                  f"these blocks")
+        finals = [str(p) for p in (ccm_path, cmx_path) if p is not None]
+        parts = {f: f + ".part" for f in finals}
+        self._run_to_files(parts.get(str(ccm_path)) if ccm_path is not None else None,
+                           parts.get(str(cmx_path)) if cmx_path is not None else None,
+                           little_endian, start, end - start, device_block)
+        for final, part in parts.items():
+            if os.path.exists(final):
+                pm.concat(final + ".joined", [final, part], little_endian=little_endian)
+                os.replace(final + ".joined", final)
+                os.remove(part)
+            else:
+                os.replace(part, final)

@@ -25,6 +25,11 @@ def test_boolean_arguments(argv, want):
     assert _args("run", "similarity", "--input", "x", "--cmx", "y", *argv).preout is want
 
 
+def test_resume_argument():
+    assert _args("run", "similarity", "--input", "x", "--cmx", "y").resume is False
+    assert _args("run", "similarity", "--input", "x", "--cmx", "y", "--resume").resume is True
+
+
 def test_rand_mode_argument():
     assert _args("run", "similarity", "--input", "x", "--cmx", "y").rand == "glibc"
     assert _args("run", "similarity", "--input", "x", "--cmx", "y", "--rand", "lcg").rand == "lcg"
@@ -117,6 +122,9 @@ def test_native_program_export_and_extract(tmp_path, native):
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--world", "2",
                                          "--first-block", "1"], 2),
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--by-cost"], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--resume",
+                                         "maybe"], 2),
+                                       (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--resume"], 1),
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--world", "2",
                                          "--rank", "1", "--by-cost"], 1),
                                        (["run", "similarity", "--input", "x.emx", "--cmx", "y", "--rand", "lcg"], 1),

@@ -297,3 +297,68 @@ def test_concat_errors(tmp_path, native):
     with pytest.raises(_native.SimError, match="is also input"):
         pm.concat(tmp_path / "a.cmx", [tmp_path / "a.cmx"])
     assert pm.read(tmp_path / "a.cmx", pm.CMX)["x"].size == len(x)    # the input was left alone
+
+
+def _blocks_of_items(rng, genes, samples, maxk=3):
+    """CMX items for every pair (1..maxk clusters), CCM items for the multi-cluster pairs."""
+    xs, ys = np.tril_indices(genes, -1)
+    k = rng.integers(1, maxk + 1, size=len(xs))
+    X, Y = np.repeat(xs, k).astype(np.int32), np.repeat(ys, k).astype(np.int32)
+    C = np.concatenate([np.arange(kk) for kk in k]).astype(np.int8)
+    R = rng.uniform(-1, 1, (len(X), 1)).astype(np.float32)
+    multi = np.repeat(k, k) > 1
+    codes = rng.choice(np.array([0, 1, 6, 7, 8, 9], np.int8), size=(int(multi.sum()), samples))
+    return (X, Y, C, R), (X[multi], Y[multi], C[multi], codes)
+
+
+@pytest.mark.parametrize("little", [False, True])
+def test_resume_point_cuts_back_to_whole_blocks(tmp_path, native, little):
+    """An interrupted run (header counts still those of a new file, the last item cut short):
+    the files are cut back to the work blocks before the one holding the last whole item, and
+    the rest of the run joined after them gives the files of the uninterrupted run."""
+    rng = np.random.default_rng(8)
+    genes, samples, maxk = 450, 6, 3                 # 100,925 pairs: four work blocks
+    cmx, ccm = _blocks_of_items(rng, genes, samples, maxk)
+    full = {}
+    for kind, items, t, sub in (("cmx", cmx, pm.CMX, 1), ("ccm", ccm, pm.CCM, samples)):
+        pm.write(tmp_path / f"full.{kind}", t, genes, maxk, sub, *items, little_endian=little)
+        full[kind] = (tmp_path / f"full.{kind}").read_bytes()
+    B = 32768
+    # interrupt: CMX written up to the middle of block 2 (plus half an item), CCM to block 1
+    for kind, items, cut_pair, sub in (("cmx", cmx, 2 * B + 5000, 1), ("ccm", ccm, B + 700, samples)):
+        x, y = items[0].astype(np.int64), items[1].astype(np.int64)
+        n_keep = int(np.searchsorted(x * (x - 1) // 2 + y, cut_pair))
+        head = 30 + (1 if kind == "cmx" else 4)
+        item = 9 + (4 if kind == "cmx" else (samples + 1) // 2)
+        raw = bytearray(full[kind][:head + n_keep * item + item // 2])
+        raw[12:28] = bytes(16)                          # counts as kinc_pm_create wrote them
+        (tmp_path / f"run.{kind}").write_bytes(bytes(raw))
+    R = pm.resume_point(tmp_path / "run.ccm", tmp_path / "run.cmx", little_endian=little)
+    assert R == 1                                       # the CCM's last whole item is in block 1
+    for kind, items, t, sub in (("cmx", cmx, pm.CMX, 1), ("ccm", ccm, pm.CCM, samples)):
+        x, y = items[0].astype(np.int64), items[1].astype(np.int64)
+        keep = (x * (x - 1) // 2 + y) < R * B
+        pm.write(tmp_path / f"want.{kind}", t, genes, maxk, sub, *[a[keep] for a in items], little_endian=little)
+        assert (tmp_path / f"run.{kind}").read_bytes() == (tmp_path / f"want.{kind}").read_bytes(), kind
+        pm.write(tmp_path / f"part.{kind}", t, genes, maxk, sub, *[a[~keep] for a in items], little_endian=little)
+        pm.concat(tmp_path / f"joined.{kind}", [tmp_path / f"run.{kind}", tmp_path / f"part.{kind}"],
+                  little_endian=little)
+        assert (tmp_path / f"joined.{kind}").read_bytes() == full[kind], kind
+
+
+def test_resume_point_edge_cases(tmp_path, native):
+    # no files yet: start at the shard's first block
+    assert pm.resume_point(tmp_path / "none.ccm", tmp_path / "none.cmx", first_block=5) == 5
+    # a file without items, the other file not written
+    pm.write(tmp_path / "e.cmx", pm.CMX, 10, 2, 1, [], [], [], np.zeros((0, 1), np.float32))
+    assert pm.resume_point(None, tmp_path / "e.cmx", first_block=3) == 3
+    # a file not created yet: everything runs again, the other file is cut back to the start
+    pm.write(tmp_path / "f.cmx", pm.CMX, 10, 2, 1, [3, 5], [1, 2], [0, 0], np.array([[0.5], [0.6]], np.float32))
+    assert pm.resume_point(tmp_path / "missing.ccm", tmp_path / "f.cmx", first_block=0) == 0
+    assert pm.read(tmp_path / "f.cmx", pm.CMX)["x"].size == 0
+    # items of blocks below the shard's first block are never the resume point
+    pm.write(tmp_path / "s.cmx", pm.CMX, 10, 2, 1, [3], [1], [0], np.array([[0.5]], np.float32))
+    assert pm.resume_point(None, tmp_path / "s.cmx", first_block=2) == 2
+    assert pm.read(tmp_path / "s.cmx", pm.CMX)["x"].size == 1
+    with pytest.raises(_native.SimError, match="not a CCM"):
+        pm.resume_point(tmp_path / "s.cmx", None)

@@ -46,3 +46,62 @@ def test_pairwise_matrix_order_is_enforced():
         m.write_pair(9, 8, [0.1] * 6)
     x, y, c, r = m.arrays()
     assert list(c) == [0, 0, 1] and m.pairs == 2
+
+
+def test_resume_runs_only_the_missing_blocks(tmp_path, native, monkeypatch):
+    """Similarity.run(resume=True) on files an interrupted run left: they are cut back to whole
+    work blocks, only the blocks from there on run again (into part files), and the joined files
+    equal those of the uninterrupted run.  The worker is replaced by a deterministic item
+    generator, so this checks the orchestration on the CPU."""
+    import numpy as np
+
+    from kinc_gb300 import Similarity, pairwise_matrix as pm
+    B, S, maxk = 32768, 8, 3
+    gem = np.zeros((450, S), np.float32)                 # 100,925 pairs: four work blocks
+    G = gem.shape[0]
+    total = G * (G - 1) // 2
+    ran = []
+
+    def fake_run(self, ccm, cmx, le, first, n, dev):
+        if n < 0:                                        # the runner's "all remaining blocks"
+            n = -(-total // B) - first
+        ran.append((first, n))
+        lo, hi = first * B, min(total, (first + n) * B)
+        p = np.arange(lo, hi, dtype=np.int64)
+        x = np.floor((1 + np.sqrt(1 + 8 * p.astype(np.float64))) / 2).astype(np.int64)
+        x -= (x * (x - 1) // 2 > p)
+        y = p - x * (x - 1) // 2
+        k = (p * 7919) % (maxk + 1)
+        X, Y = np.repeat(x, k), np.repeat(y, k)
+        C = np.concatenate([np.arange(kk) for kk in k]) if len(k) else np.zeros(0, np.int64)
+        R = ((np.repeat(p, k) % 1000) / 1000.0).astype(np.float32).reshape(-1, 1)
+        m = np.repeat(k, k) > 1
+        codes = (np.repeat(p, k)[m][:, None] + np.arange(S)[None, :]) % 2
+        if cmx is not None:
+            pm.write(cmx, pm.CMX, G, maxk, 1, X, Y, C, R, little_endian=le)
+        if ccm is not None:
+            pm.write(ccm, pm.CCM, G, maxk, S, X[m], Y[m], C[m], codes.astype(np.int8), little_endian=le)
+
+    monkeypatch.setattr(Similarity, "_run_to_files", fake_run)
+    sim = Similarity(gem, clusmethod="gmm", maxclus=maxk)
+    sim.run(ccm_path=tmp_path / "full.ccm", cmx_path=tmp_path / "full.cmx")
+    full = {e: (tmp_path / f"full.{e}").read_bytes() for e in ("ccm", "cmx")}
+    # the interrupted run: both files cut inside block 2 (CMX further than CCM), counts as at creation
+    for e, cut in (("cmx", 0.9), ("ccm", 0.7)):
+        raw = bytearray(full[e][:int(len(full[e]) * cut)])
+        raw[12:28] = bytes(16)
+        (tmp_path / f"run.{e}").write_bytes(bytes(raw))
+    ran.clear()
+    sim.run(ccm_path=tmp_path / "run.ccm", cmx_path=tmp_path / "run.cmx", resume=True)
+    assert ran == [(2, 2)]                               # blocks 2 and 3 only
+    for e in ("ccm", "cmx"):
+        assert (tmp_path / f"run.{e}").read_bytes() == full[e], e
+        assert not (tmp_path / f"run.{e}.part").exists()
+    # a rank's share: the interrupted files of rank 1 of 2 resume inside its own range
+    sim.run(ccm_path=tmp_path / "r1.ccm", cmx_path=tmp_path / "r1.cmx", world=2, rank=1)
+    r1 = (tmp_path / "r1.cmx").read_bytes()
+    (tmp_path / "r1.cmx").write_bytes(r1[:len(r1) // 2])
+    ran.clear()
+    sim.run(ccm_path=tmp_path / "r1.ccm", cmx_path=tmp_path / "r1.cmx", world=2, rank=1, resume=True)
+    assert ran[0][0] >= 2 and ran[0][0] + ran[0][1] == 4
+    assert (tmp_path / "r1.cmx").read_bytes() == r1
