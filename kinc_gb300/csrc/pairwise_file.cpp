@@ -492,17 +492,33 @@ int cut_back(const char* path, int type, bool little, int64_t* last_block_out, i
       else hi = mid;
    }
    const int64_t keep = lo;
+   /* the kept items' distinct pairs, read sequentially a chunk of items at a time */
    int64_t pairs = 0, prev = -1;
-   for ( int64_t i = 0; i < keep; ++i )
    {
-      const int64_t p = pair_at(i, nullptr, nullptr);
-      if ( p < 0 )
+      const int64_t per = std::max<int64_t>(1, (int64_t)(16u << 20) / item);
+      std::vector<unsigned char> buf((size_t)(per * item));
+      if ( fseek(f, (long)base, SEEK_SET) != 0 )
       {
          fclose(f);
          return pm_fail(KINC_SIM_EIO, "cannot read %s", path);
       }
-      pairs += p != prev;
-      prev = p;
+      for ( int64_t i = 0; i < keep; i += per )
+      {
+         const int64_t len = std::min(per, keep - i);
+         if ( fread(buf.data(), 1, (size_t)(len * item), f) != (size_t)(len * item) )
+         {
+            fclose(f);
+            return pm_fail(KINC_SIM_EIO, "cannot read %s", path);
+         }
+         for ( int64_t j = 0; j < len; ++j )
+         {
+            const unsigned char* b = buf.data() + j * item;
+            const int32_t x = e.get<int32_t>(b), y = e.get<int32_t>(b + 4);
+            const int64_t p = (int64_t)x * (x - 1) / 2 + y;
+            pairs += p != prev;
+            prev = p;
+         }
+      }
    }
    std::vector<unsigned char> counts;
    e.put<int64_t>(counts, pairs);
