@@ -573,6 +573,48 @@ extern "C" int kinc_pm_resume_point(const char* ccm_path, const char* cmx_path, 
  * in strictly increasing indent order across the joins (Matrix::write's rule); the header counts
  * are recomputed (a pair continued across a join counts once).
  */
+namespace {
+
+/* Append n items already encoded in the file's byte order (as another file of the same kind
+ * holds them), with write_items' checks and bookkeeping. */
+int append_raw_items(kinc_pm* m, const unsigned char* raw, int64_t n)
+{
+   const size_t item = ITEM_HEADER + (size_t)m->data_size;
+   int64_t last = m->last_indent, last_pair = m->last_pair, pairs = m->pairs;
+   for ( int64_t i = 0; i < n; ++i )
+   {
+      const unsigned char* o = raw + (size_t)i * item;
+      const int32_t x = m->e.get<int32_t>(o), y = m->e.get<int32_t>(o + 4);
+      const int c = (int8_t)o[8];
+      if ( x < 1 || y < 0 || x <= y || x >= m->genes )
+         return pm_fail(KINC_SIM_EINVAL, "Cannot initialize pairwise index (%d, %d).", x, y);
+      if ( c < 0 || c >= MAX_CLUSTER_SIZE || c >= m->max_clusters )
+         return pm_fail(KINC_SIM_EINVAL, "Cluster %d is outside limits.", c);
+      const int64_t pair = (int64_t)x * (x - 1) / 2 + y;
+      const int64_t indent = pair * MAX_CLUSTER_SIZE + c;
+      if ( indent <= last )
+         return pm_fail(KINC_SIM_EORDER, "Attempting to write indent %lld when last written is %lld.",
+                        (long long)(pair * MAX_CLUSTER_SIZE), (long long)last);
+      last = indent;
+      if ( pair != last_pair )
+      {
+         ++pairs;
+         last_pair = pair;
+      }
+   }
+   const long pos = (long)(HEADER + m->offset) + (long)(m->clusters * (int64_t)item);
+   const size_t bytes = (size_t)n * item;
+   if ( fseek(m->f, pos, SEEK_SET) != 0 || (bytes > 0 && fwrite(raw, 1, bytes, m->f) != bytes) )
+      return pm_fail(KINC_SIM_EIO, "write failed");
+   m->last_indent = last;
+   m->last_pair = last_pair;
+   m->pairs = pairs;
+   m->clusters += n;
+   return KINC_SIM_OK;
+}
+
+}  // namespace
+
 extern "C" int kinc_pm_concat(const char* out_path, const char* const* in_paths, int32_t n, int32_t little_endian)
 {
    if ( !out_path || !in_paths || n < 1 ) return pm_fail(KINC_SIM_EINVAL, "Did not get valid input and/or output arguments.");
@@ -599,11 +641,10 @@ extern "C" int kinc_pm_concat(const char* out_path, const char* const* in_paths,
    kinc_pm* out = nullptr;
    int rc = kinc_pm_create(out_path, type, G, K, sub, little_endian, &out);
    if ( rc ) return rc;
-   const size_t per = type == KINC_PM_CCM ? (size_t)sub : (size_t)sub * sizeof(float);
-   const int64_t chunk = std::max<int64_t>(1, std::min<int64_t>(1 << 16, (int64_t)((64u << 20) / std::max<size_t>(per, 1))));
-   std::vector<int32_t> x((size_t)chunk), y((size_t)chunk);
-   std::vector<int8_t> c((size_t)chunk);
-   std::vector<unsigned char> payload((size_t)chunk * per);
+   /* items are copied as they are encoded (the files share one byte order), a chunk at a time */
+   const int64_t item = ITEM_HEADER + (int64_t)out->data_size;
+   const int64_t chunk = std::max<int64_t>(1, (int64_t)(32u << 20) / item);
+   std::vector<unsigned char> buf((size_t)(chunk * item));
    for ( int32_t i = 0; i < n && rc == KINC_SIM_OK; ++i )
    {
       kinc_pm* m = nullptr;
@@ -615,11 +656,15 @@ extern "C" int kinc_pm_concat(const char* out_path, const char* const* in_paths,
          rc = pm_fail(KINC_SIM_EINVAL, "%s (%d genes, %d clusters, %d per item) does not match %s (%d, %d, %d)",
                       in_paths[i], g, k, s2, in_paths[0], G, K, sub);
       }
+      if ( rc == KINC_SIM_OK && fseek(m->f, (long)(HEADER + m->offset), SEEK_SET) != 0 )
+         rc = pm_fail(KINC_SIM_EIO, "cannot read %s", in_paths[i]);
       for ( int64_t first = 0; rc == KINC_SIM_OK && first < items; first += chunk )
       {
          const int64_t len = std::min(chunk, items - first);
-         rc = kinc_pm_read_items(m, first, len, x.data(), y.data(), c.data(), payload.data());
-         if ( rc == KINC_SIM_OK ) rc = kinc_pm_write_items(out, len, x.data(), y.data(), c.data(), payload.data());
+         if ( fread(buf.data(), 1, (size_t)(len * item), m->f) != (size_t)(len * item) )
+            rc = pm_fail(KINC_SIM_EINVAL, "%s: truncated items", in_paths[i]);
+         else
+            rc = append_raw_items(out, buf.data(), len);
       }
       kinc_pm_close(m);
    }
