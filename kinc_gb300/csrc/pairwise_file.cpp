@@ -216,7 +216,7 @@ static int write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y
       }
    }
    /* items are laid out straight into the buffer: 4-byte fields byte-swapped when the file's
-    * order differs from the host's (both hosts this builds for are little-endian) */
+    * order differs from the host's (x86-64 and aarch64, the hosts compiled for, are little-endian) */
    if ( (size_t)n * item > m->items_cap )
    {
       m->items.reset(new unsigned char[(size_t)n * item]);
