@@ -1,7 +1,7 @@
 """Build recipe for the checkers under oracle/ (TEST INFRASTRUCTURE ONLY).
 
 * ``oracle/_build/libkinc_oracle.so`` -- the plain-C restatement
-  (kinc_oracle.c).  Builds anywhere (x86 container or the Arm GPU host).
+  (kinc_oracle.c).  Builds on any host (x86-64 or aarch64).
 * ``oracle/_ref/libkinc_ocl.so`` -- KINC's OpenCL kernels compiled as C++ for
   the host (ref_shim/ocl_shim.h) and driven as the OpenCL worker drives them
   (ocl_driver.cpp); also only with the KINC tree.
