@@ -88,7 +88,8 @@ int kinc_pm_resume_point(const char* ccm_path, const char* cmx_path, int32_t lit
  * The CCM or CMX files of a sharded run (each rank's contiguous range of work blocks) joined into
  * one, in the order given: the inputs must be of one type (detected from the first), agree on
  * genes, maximum clusters and payload size, and keep strictly increasing indent order across the
- * joins (else KINC_SIM_EINVAL / KINC_SIM_EORDER).  The output may not be one of the inputs.
+ * joins (else KINC_SIM_EINVAL / KINC_SIM_EORDER, and no output file is left).  The output may not
+ * be one of the inputs.
  */
 int kinc_pm_concat(const char* out_path, const char* const* in_paths, int32_t n, int32_t little_endian);
 

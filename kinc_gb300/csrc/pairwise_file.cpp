@@ -669,6 +669,7 @@ extern "C" int kinc_pm_concat(const char* out_path, const char* const* in_paths,
       kinc_pm_close(m);
    }
    const int rc2 = kinc_pm_close(out);
+   if ( rc || rc2 ) remove(out_path);   /* no half-joined file is left behind */
    return rc ? rc : rc2;
 }
 

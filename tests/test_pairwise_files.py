@@ -289,6 +289,7 @@ def test_concat_errors(tmp_path, native):
     pm.write(tmp_path / "a.ccm", pm.CCM, 10, 3, 5, x, y, c, codes)
     with pytest.raises(_native.SimError, match="does not match"):
         pm.concat(tmp_path / "o.cmx", [tmp_path / "a.cmx", tmp_path / "b.cmx"])
+    assert not (tmp_path / "o.cmx").exists()
     with pytest.raises(_native.SimError) as e:      # the same items twice: out of order at the join
         pm.concat(tmp_path / "o.cmx", [tmp_path / "a.cmx", tmp_path / "a.cmx"])
     assert e.value.code == _native.EORDER
