@@ -245,8 +245,10 @@ static int write_items(kinc_pm* m, int64_t n, const int32_t* x, const int32_t* y
          const int8_t* codes = (const int8_t*)payload + (size_t)i * m->subsize;
          for ( int s = 0; s < m->subsize; s += 2 )
          {
-            int8_t v = (int8_t)(codes[s] & 0x0F);
-            if ( s + 1 < m->subsize ) v = (int8_t)(v | (int8_t)(codes[s + 1] << 4));
+            /* sample s in the low nibble, s + 1 in the high one (shifted as unsigned: a code
+             * outside 0..15, such as a non-digit mask character's -1, keeps its low 4 bits) */
+            unsigned v = (unsigned)(uint8_t)codes[s] & 0x0Fu;
+            if ( s + 1 < m->subsize ) v |= ((unsigned)(uint8_t)codes[s + 1] << 4) & 0xF0u;
             d[s / 2] = (unsigned char)v;
          }
       }
