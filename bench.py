@@ -152,6 +152,39 @@ def parity_block(gpu, cpu):
             "vs": "oracle: C restatement of KINC's serial path, pinned bit-exact to KINC's compiled Pairwise code"}
 
 
+def libm_leg():
+    """The GPU on the clustering workloads' 64-gene matrices (tests/golden/libm: 2,016 pairs each, GMM
+    k <= 5 + Spearman at 1,000 samples, K-means k <= 3 + Pearson at 4,000, GMM ICL + both correlations
+    at 500): bit-exactness against KINC's own code with the portable exp/log (math mode 0), and the
+    agreement with KINC built against glibc's float (mode 1) and double (mode 2) exp/log -- and of
+    those two builds with each other, the spread that is the reference's own."""
+    from kinc_gb300 import Similarity
+    from oracle import agreement
+    names = {0: "none", 1: "gmm", 2: "kmeans"}
+    out = {}
+    for name, path in agreement.cases().items():
+        fx = agreement.load(path)
+        a = fx["params"]
+        sim = Similarity(fx["gem"], clusmethod=names[a["clus_method"]],
+                         corrmethod=2 if fx["ncorr"] == 2 else a["corr_method"], minsamp=a.get("min_samples", 30),
+                         minclus=a.get("min_clusters", 1), maxclus=a["max_clusters"], crit=a["criterion"],
+                         preout=a.get("pre_out", 0), postout=a.get("post_out", 0))
+        sim.initialize()
+        res = sim.execute(None, start=0, size=len(fx["K0"]))
+        sim.close()
+        exact = bool(np.array_equal(res.K, fx["K0"])
+                     and np.array_equal(agreement.row_hashes(res.labels), fx["hash0"])
+                     and np.array_equal(np.nan_to_num(res.corr, nan=9.0).view(np.uint32),
+                                        np.nan_to_num(fx["corr0"], nan=9.0).view(np.uint32)))
+        entry = {"pairs": int(len(res.K)), "samples": int(fx["gem"].shape[1]),
+                 "k_histogram": np.bincount(res.K.astype(np.int64)).tolist(), "bit_exact_vs_mode0": exact}
+        for mode in (1, 2):
+            entry[f"vs_mode{mode}"] = agreement.compare(res.K, res.labels, res.corr, fx, mode)
+        entry["mode1_vs_mode2"] = agreement.compare_modes(fx)
+        out[name] = entry
+    return out
+
+
 def run_reference(args, gem):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -425,6 +458,7 @@ def main():
     ap.add_argument("--no-dense", action="store_true")
     ap.add_argument("--no-kmeans", action="store_true")
     ap.add_argument("--no-rmt", action="store_true")
+    ap.add_argument("--no-libm", action="store_true")
     ap.add_argument("--dense-check-pairs", type=int, default=1000000)
     ap.add_argument("--stream-blocks", type=int, default=2,
                     help="device blocks of 2^22 pairs in the streamed 30000x500 leg (0 = skip)")
@@ -582,12 +616,13 @@ def main():
                 "peak_source": f"nominal FP32 FMA rate: {props.multi_processor_count} SMs x 128 lanes x 2 flops x "
                                f"{sm_max:.0f} MHz (MEASURED_PEAKS.json holds no FP32 figure)",
                 "kernel": "k_similarity", "units": units, "flops_per_unit": FLOPS_PER_UNIT, "fits": fits,
-                "issue": issue}
+                "issue_frac": issue["frac"] if issue else None, "issue": issue}
 
     tensor_core = None if args.no_dense else dense_leg(L, vp, args.dense_check_pairs)
     kmeans = None if args.no_kmeans else kmeans_leg(L, vp, cpu=not args.no_cpu)
     streamed = None if args.stream_blocks <= 0 else stream_leg(1 << 22, args.stream_blocks)
     rmt = None if args.no_rmt else rmt_leg(cpu=not args.no_cpu)
+    libm = None if args.no_libm else libm_leg()
 
     cpu = None
     parity = None
@@ -610,7 +645,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded; no public dataset)",
             "config": config_dict(args, gem), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "cpu_baseline": cpu, "parity": parity, "clocks": clk, "tensor_core": tensor_core, "kmeans_uneven": kmeans,
-            "streamed_30000x500": streamed, "rmt": rmt}
+            "streamed_30000x500": streamed, "rmt": rmt, "libm_agreement": libm}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

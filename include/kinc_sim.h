@@ -84,7 +84,8 @@ int kinc_sim_create(const float* gem, int32_t genes, int32_t samples, const kinc
 
 void kinc_sim_destroy(kinc_sim_ctx* ctx);
 
-/* Message of the last failed call on `ctx` (or of the last failed kinc_sim_create if ctx is NULL). */
+/* Message of the last failed call on `ctx`; with ctx NULL, of the calling thread's last failed call
+ * that has no context (kinc_sim_create, kinc_sim_execute_block_noalloc). */
 const char* kinc_sim_last_error(const kinc_sim_ctx* ctx);
 
 /* The context's arguments and matrix shape (any output may be NULL). */
@@ -195,15 +196,19 @@ int kinc_sim_work_counters(kinc_sim_ctx* ctx, uint64_t* out, int reset);
  * kinc_sim_execute_block.  All working memory is a 64 MiB static device array
  * inside the library, which every GPU that loads the library holds until the
  * process exits.  Limits: samples <= 4096 and size <= 262144 pairs per call,
- * and the per-gene masks, per-pair arrays and at least one 4-warp block of
- * working space must fit in the 64 MiB; larger requests are rejected with
- * KINC_SIM_EINVAL and a message from kinc_sim_last_error(NULL).  precision must be 0.
+ * and the per-gene masks, per-pair arrays and the working space of at least
+ * one 16-warp block must fit in the 64 MiB; precision must be 0 (the per-pair FP32
+ * path; corr_method 0, 1 or 2 as in kinc_sim_create).  Other requests are
+ * rejected with KINC_SIM_EINVAL and a message from kinc_sim_last_error(NULL).
  *
- * The first call on a device looks up the array's device address and uploads
- * the rand() jump table; make that first call before any stream capture.
- * Every call shares the one array, so calls that overlap on the GPU race:
- * the function serialises host callers and waits for its own work on
- * `stream` (a cudaStream_t, 0 = default stream) before returning.
+ * The first call on a device does a one-time set-up with that device current:
+ * it looks up the array's device address and uploads the rand() jump table,
+ * so make that first call before any stream capture begins.  Every call runs
+ * its kernels on `stream` (a cudaStream_t, 0 = default stream), then waits
+ * for them with cudaStreamSynchronize and copies a status word back to the
+ * host before returning.  Every call shares the one array, which keeps the
+ * last call's contents, so calls that overlap on the GPU race; the function
+ * serialises callers on the host side.
  */
 int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes, int32_t samples,
                                    const kinc_sim_params* params, int64_t start, int64_t size, int8_t* d_K,

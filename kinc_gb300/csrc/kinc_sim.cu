@@ -302,16 +302,20 @@ struct kinc_sim_ctx
 
 namespace {
 
-std::string g_create_error;
+/* message of the calling thread's last failure that had no context (kinc_sim_create, the
+ * allocation-free entry point): a fixed per-thread buffer, so threads do not race on it and
+ * reporting an error allocates nothing */
+constexpr size_t ERROR_CHARS = 512;
+thread_local char g_create_error[ERROR_CHARS] = "";
 
 int fail(kinc_sim_ctx* ctx, int code, const char* fmt, ...)
 {
-   char buf[512];
+   char buf[ERROR_CHARS];
    va_list ap;
    va_start(ap, fmt);
    vsnprintf(buf, sizeof buf, fmt, ap);
    va_end(ap);
-   if ( ctx ) ctx->err = buf; else g_create_error = buf;
+   if ( ctx ) ctx->err = buf; else memcpy(g_create_error, buf, sizeof buf);
    return code;
 }
 
@@ -443,7 +447,7 @@ extern "C" int kinc_sim_params_default(kinc_sim_params* p)
 
 extern "C" const char* kinc_sim_last_error(const kinc_sim_ctx* ctx)
 {
-   return ctx ? ctx->err.c_str() : g_create_error.c_str();
+   return ctx ? ctx->err.c_str() : g_create_error;
 }
 
 extern "C" int kinc_sim_get_params(const kinc_sim_ctx* ctx, kinc_sim_params* params, int32_t* genes, int32_t* samples)
@@ -523,7 +527,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    const int S = samples;
    const int W = ctx->W;
    auto bail = [&](int code) {
-      g_create_error = ctx->err;
+      snprintf(g_create_error, ERROR_CHARS, "%s", ctx->err.c_str());
       release(ctx);
       delete ctx;
       return code;
@@ -1069,12 +1073,6 @@ double g_noalloc_host_logn[NOALLOC_MAX_SAMPLES + 1];
 bool g_noalloc_tables = false;
 std::mutex g_noalloc_mutex;
 
-/* error messages are written into reserved capacity, so reporting one does not allocate */
-struct NoallocErrorReserve
-{
-   NoallocErrorReserve() { g_create_error.reserve(1024); }
-} g_noalloc_error_reserve;
-
 /* the glibc rand() tables of glibc_rng_tables, computed into fixed storage */
 void noalloc_rng_tables()
 {
@@ -1118,7 +1116,8 @@ const char* noalloc_check(const kinc_sim_params* p, int32_t G, int32_t S)
    if ( G < 2 ) return "genes must be >= 2";
    if ( S < 1 ) return "samples must be >= 1";
    if ( p->clus_method < 0 || p->clus_method > 2 ) return "clus_method must be 0 (none), 1 (gmm) or 2 (kmeans)";
-   if ( p->corr_method < 0 || p->corr_method > 1 ) return "corr_method must be 0 (pearson) or 1 (spearman)";
+   if ( p->corr_method < 0 || p->corr_method > 2 )
+      return "corr_method must be 0 (pearson), 1 (spearman) or 2 (both)";
    if ( p->min_samples < 1 ) return "min_samples must be >= 1";
    if ( p->min_clusters < 1 || p->min_clusters > 64 ) return "min_clusters must be in 1..64";
    if ( p->max_clusters < 1 || p->max_clusters > 64 ) return "max_clusters must be in 1..64";
@@ -1138,7 +1137,8 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
                                               const kinc_sim_params* params, int64_t start, int64_t size,
                                               int8_t* d_K, int8_t* d_labels, float* d_corr, void* stream)
 {
-   kinc_sim_ctx* ctx = nullptr;   /* errors go to kinc_sim_last_error(NULL) */
+   kinc_sim_ctx* ctx = nullptr;   /* errors go to kinc_sim_last_error(NULL) of the calling thread */
+   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
    if ( !d_gem || !params ) return fail(nullptr, KINC_SIM_EINVAL, "d_gem and params must not be NULL");
    const char* bad = noalloc_check(params, genes, samples);
    if ( bad ) return fail(nullptr, KINC_SIM_EINVAL, "%s", bad);
@@ -1159,7 +1159,6 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    if ( dev < 0 || dev >= NOALLOC_MAX_DEVICES )
       return fail(nullptr, KINC_SIM_EINVAL, "device %d beyond the supported %d", dev, NOALLOC_MAX_DEVICES);
    cudaStream_t st = (cudaStream_t)stream;
-   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
 
    /* set-up, once per device, with that device current */
    NoallocDevice& nd = g_noalloc_dev[dev];
@@ -1196,19 +1195,19 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    dp.c2 = 2 * std::log(2.0f * M_PI);
    dp.P2 = next_pow2_host(std::max(S, 2));
    const bool need_sort = (params->clus_method != 0 && (params->pre_out || params->post_out))
-                          || params->corr_method == 1;
-   dp.sort_floats = params->corr_method == 1 ? 3 * dp.P2 : (need_sort ? dp.P2 : 0);
+                          || params->corr_method >= 1;
+   dp.sort_floats = params->corr_method >= 1 ? 3 * dp.P2 : (need_sort ? dp.P2 : 0);
    /* room for the GMM responsibilities the fit keeps between its two M passes (as in kinc_sim_create) */
    dp.gam_k = (KINC_STORE_GAMMA && params->clus_method == 1)
                  ? (params->max_clusters <= 3 ? 3 : params->max_clusters <= 5 ? 5 : 0) : 0;
-   dp.ncorr = 1;
+   dp.ncorr = params->corr_method == 2 ? 2 : 1;
    const size_t sort_bytes_warp = (size_t)dp.sort_floats * sizeof(float);
    const SimKernel kern = params->clus_method == 0 ? sim_kernel_none()
                         : params->clus_method == 1 ? sim_kernel_gmm(params->max_clusters, params->rand_mode == 1)
                                                    : sim_kernel_kmeans(params->max_clusters);
    const size_t param_bytes_warp = (KINC_GMM_PARAMS_SMEM && kern.clus == 1 && kern.ks > 0)
                                       ? (size_t)7 * kern.ks * TILE * sizeof(float) : 0;
-   const int smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * WARPS_PER_BLOCK <= 160 * 1024;
+   const int smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * WARPS_PER_BLOCK <= 200 * 1024;
    const int smem_bytes = (int)((smem_sort ? sort_bytes_warp : 0) + param_bytes_warp) * WARPS_PER_BLOCK;
    if ( smem_bytes > 0 )
       CK(cudaFuncSetAttribute(kern.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
@@ -1296,7 +1295,7 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
       k_scan_blocks<<<1, SCAN_THREADS, 0, st>>>(d_bsum, nscan, d_qbase);
       k_scan_apply<<<nscan, SCAN_THREADS, 0, st>>>(d_N, offq, size, dp.min_samples, d_bsum, d_qpos);
    }
-   if ( dp.corr == 0 && dp.semantics == 0 )
+   if ( (dp.corr == 0 || dp.corr == 2) && dp.semantics == 0 )
    {
       const int64_t nwb = (end - 1) / KINC_SIM_WORK_BLOCK_SIZE - lo / KINC_SIM_WORK_BLOCK_SIZE + 1;
       k_prev<<<(int)((nwb + 63) / 64), 64, 0, st>>>(d_N, lo, end, d_pg);

@@ -8,7 +8,8 @@
 * ``oracle/_ref/libkinc_ref{0,1,2}.so`` -- KINC's own CPU Pairwise:: sources,
   compiled unmodified from the KINC source tree with the stand-in ACE header
   in ref_shim/ and the restated serial driver ref_driver.cpp.  Only built when
-  the KINC tree is present (``KINC_REFERENCE_DIR``, default /root/reference).
+  ``KINC_REFERENCE_DIR`` names a KINC tree; without it, libraries built earlier
+  are used as they are, and none is built.
   The suffix is the math resolution (ref_shim/ace/core/core.h): 0 = the
   portable kinc_expf/kinc_logf the GPU uses, 1 = glibc float expf/logf,
   2 = the C library's double functions.
@@ -22,7 +23,6 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
-REF_DIR = os.environ.get("KINC_REFERENCE_DIR", "/root/reference")
 REF_SOURCES = ["pairwise_linalg.cpp", "pairwise_clustering.cpp", "pairwise_gmm.cpp",
                "pairwise_kmeans.cpp", "pairwise_correlation.cpp", "pairwise_pearson.cpp",
                "pairwise_spearman.cpp"]
@@ -49,15 +49,27 @@ def build_oracle():
     return out
 
 
+def ref_dir():
+    """The KINC source tree named by KINC_REFERENCE_DIR, or None."""
+    return os.environ.get("KINC_REFERENCE_DIR") or None
+
+
 def reference_available():
-    return os.path.isfile(os.path.join(REF_DIR, "src", "core", "pairwise_gmm.cpp"))
+    d = ref_dir()
+    return d is not None and os.path.isfile(os.path.join(d, "src", "core", "pairwise_gmm.cpp"))
+
+
+def _prebuilt(name):
+    """A library built earlier from the KINC tree, when the tree is not named now."""
+    path = os.path.join(HERE, "_ref", name)
+    return path if os.path.isfile(path) else None
 
 
 def build_ref(math_mode=0):
     """Compile the KINC Pairwise:: sources where they lie; returns the .so path or None."""
     if not reference_available():
-        return None
-    core = os.path.join(REF_DIR, "src", "core")
+        return _prebuilt(f"libkinc_ref{math_mode}.so")
+    core = os.path.join(ref_dir(), "src", "core")
     out_dir = os.path.join(HERE, "_ref")
     os.makedirs(out_dir, exist_ok=True)
     out = os.path.join(out_dir, f"libkinc_ref{math_mode}.so")
@@ -91,8 +103,8 @@ def build_ocl():
     OpenCL-only construct in them, the vector literal "(float2) (a, b)"
     (src/opencl/fetchpair.cl:62), is rewritten to a constructor call on the way."""
     if not reference_available():
-        return None
-    cl_dir = os.path.join(REF_DIR, "src", "opencl")
+        return _prebuilt("libkinc_ocl.so")
+    cl_dir = os.path.join(ref_dir(), "src", "opencl")
     out_dir = os.path.join(HERE, "_ref")
     os.makedirs(out_dir, exist_ok=True)
     out = os.path.join(out_dir, "libkinc_ocl.so")

@@ -21,6 +21,10 @@ CASES = [
     ("gmm_spearman_prepost", 2, 60, 120, dict(clusmethod="gmm", corrmethod="spearman", crit="BIC", preout=True,
                                               postout=True)),
     ("none_pearson", 1, 300, 50, dict()),
+    ("kmeans_pearson", 4, 40, 400, dict(clusmethod="kmeans", corrmethod="pearson", maxclus=3, crit="BIC")),
+    ("gmm_both_icl", 5, 50, 200, dict(clusmethod="gmm", corrmethod="both", crit="ICL", preout=True,
+                                      postout=True)),
+    ("none_spearman_3000_samples", 1, 24, 3000, dict(corrmethod="spearman")),
 ]
 
 
@@ -28,7 +32,8 @@ def _run_noalloc(L, d_gem, G, S, params, start, size, maxk):
     import torch
     dK = torch.empty(size, dtype=torch.int8, device="cuda")
     dL = torch.empty((size, S), dtype=torch.int8, device="cuda")
-    dC = torch.empty((size, maxk), dtype=torch.float32, device="cuda")
+    dC = torch.empty((size, maxk, 2) if params.corr_method == 2 else (size, maxk), dtype=torch.float32,
+                     device="cuda")
     torch.cuda.synchronize()
     vp = ctypes.c_void_p
     rc = L.kinc_sim_execute_block_noalloc(vp(d_gem.data_ptr()), G, S, ctypes.byref(params), start, size,
@@ -69,3 +74,19 @@ def test_noalloc_rejects_sizes_beyond_its_limit():
                                           (1 << 18) + 1, None, None, None, None)
     assert rc == _native.EINVAL
     assert b"allocation-free limit" in L.kinc_sim_last_error(None)
+
+
+def test_noalloc_rejects_work_that_does_not_fit_its_array():
+    """GMM k <= 5 at 4,096 samples needs about 4.7 MB of working space per warp: one 16-warp block
+    no longer fits the 64 MiB array, so the call is refused before anything runs."""
+    import torch
+    gem = synthetic.generate(2, genes=40, samples=4096)
+    params = Similarity(gem, clusmethod="gmm", corrmethod="spearman", maxclus=5).params
+    L = _native.load()
+    d_gem = torch.from_numpy(gem).cuda()
+    d_out = torch.empty(1 << 16, dtype=torch.uint8, device="cuda")
+    vp = ctypes.c_void_p
+    rc = L.kinc_sim_execute_block_noalloc(vp(d_gem.data_ptr()), 40, 4096, ctypes.byref(params), 0, 10,
+                                          vp(d_out.data_ptr()), vp(d_out.data_ptr()), vp(d_out.data_ptr()), None)
+    assert rc == _native.EINVAL
+    assert b"do not fit" in L.kinc_sim_last_error(None)
