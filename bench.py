@@ -459,6 +459,7 @@ def main():
     ap.add_argument("--no-kmeans", action="store_true")
     ap.add_argument("--no-rmt", action="store_true")
     ap.add_argument("--no-libm", action="store_true")
+    ap.add_argument("--no-tune-cache", action="store_true", help="time the launch shapes even if cached")
     ap.add_argument("--dense-check-pairs", type=int, default=1000000)
     ap.add_argument("--stream-blocks", type=int, default=2,
                     help="device blocks of 2^22 pairs in the streamed 30000x500 leg (0 = skip)")
@@ -503,6 +504,11 @@ def main():
     sim.initialize()
     ctx = sim._ctx
     maxk = sim.params.max_clusters
+    # launch shape picked by the autotuner (kinc_sim_autotune, cached per shape and GPU) before any timing
+    t0 = time.perf_counter()
+    chosen, timed = sim.autotune(use_cache=not args.no_tune_cache)
+    autotune = {"chosen": chosen, "candidates": timed, "seconds": time.perf_counter() - t0,
+                "sample_pairs": 4 * 32 * 16 * 152, "from_cache": len(timed) == 0}
     dK = torch.empty(B, dtype=torch.int8, device="cuda")
     dL = torch.empty((B, S), dtype=torch.int8, device="cuda")
     dC = torch.empty((B, maxk), dtype=torch.float32, device="cuda")
@@ -645,7 +651,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded; no public dataset)",
             "config": config_dict(args, gem), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "cpu_baseline": cpu, "parity": parity, "clocks": clk, "tensor_core": tensor_core, "kmeans_uneven": kmeans,
-            "streamed_30000x500": streamed, "rmt": rmt, "libm_agreement": libm}
+            "streamed_30000x500": streamed, "rmt": rmt, "libm_agreement": libm, "autotune": autotune}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

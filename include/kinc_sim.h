@@ -179,6 +179,54 @@ int kinc_sim_pair_counts(kinc_sim_ctx* ctx, int64_t start, int64_t size, int32_t
 /* Kernel launches made by the last kinc_sim_execute_block* call (for accounting). */
 int32_t kinc_sim_last_launch_count(const kinc_sim_ctx* ctx);
 
+/*
+ * Launch shape of the per-pair kernel.  Every shape computes the same bits;
+ * only the speed differs, so the shape is picked by measurement
+ * (kinc_sim_autotune) rather than fixed.  Replaces the hand-set work-item
+ * count of KINC's OpenCL worker (--ksize, src/core/similarity_input.cpp:241-251),
+ * which this worker does not need for correctness.
+ *   warps_per_cta  4, 8 or 16: warps of one CTA (the SM holds 16 warps either way)
+ *   rounds         1: a CTA's warps take their 32-pair tiles together, round by
+ *                  round (they then run the same code region at the same time);
+ *                  0: every warp takes its next tile as soon as it is done
+ *   prefetch       0, 4, 8 or 16: samples ahead the GMM sweeps prefetch into L2
+ */
+typedef struct kinc_sim_launch
+{
+   int32_t warps_per_cta;
+   int32_t rounds;
+   int32_t prefetch;
+   int32_t reserved;
+} kinc_sim_launch;
+
+/* One timed candidate of kinc_sim_autotune. */
+typedef struct kinc_sim_tune_entry
+{
+   kinc_sim_launch launch;
+   double ms;             /* device time of the sample block */
+} kinc_sim_tune_entry;
+
+int kinc_sim_get_launch(const kinc_sim_ctx* ctx, kinc_sim_launch* launch);
+/* KINC_SIM_EINVAL for a shape outside the values above */
+int kinc_sim_set_launch(kinc_sim_ctx* ctx, const kinc_sim_launch* launch);
+
+/*
+ * Pick the launch shape by timing: the pairs [start, start + size) (size is
+ * capped at kinc_sim_max_device_block) run once per candidate on the context's
+ * stream, timed with CUDA events, in a coordinate descent from the current
+ * shape over prefetch (GMM only), warps_per_cta and rounds; the fastest is
+ * applied.  With use_cache, the shape is first looked up -- and afterwards
+ * stored -- in a small text cache keyed by the clustering and correlation
+ * arguments, max_clusters, the sample count rounded up to a power of two and
+ * the GPU (file: $KINC_TUNE_CACHE, else $XDG_CACHE_HOME/kinc_gb300/launch.txt,
+ * else ~/.cache/kinc_gb300/launch.txt); a cache hit times nothing.  Up to
+ * `cap` timed candidates are written to `entries` (may be NULL) and their
+ * count to *n.  Synchronises the context's stream; the per-pair outputs of the
+ * timed runs are discarded.  Not available for the tensor-core precisions.
+ */
+int kinc_sim_autotune(kinc_sim_ctx* ctx, int64_t start, int64_t size, int32_t use_cache, kinc_sim_launch* chosen,
+                      kinc_sim_tune_entry* entries, int32_t cap, int32_t* n);
+
 /* Work done since the last reset: out[0] = clustering model units (sum over
  * fits of iterations x N x K), out[1] = fits run, out[2..3] reserved.
  * Synchronises the context's stream. */

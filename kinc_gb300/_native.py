@@ -37,6 +37,20 @@ class RmtParams(ctypes.Structure):
 
 RMT_ENOTHRESHOLD, RMT_ESPLINE = 6, 7
 
+
+class Launch(ctypes.Structure):
+    """kinc_sim_launch (include/kinc_sim.h): the per-pair kernel's launch shape."""
+    _fields_ = [("warps_per_cta", ctypes.c_int32), ("rounds", ctypes.c_int32), ("prefetch", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {"warps_per_cta": self.warps_per_cta, "rounds": self.rounds, "prefetch": self.prefetch}
+
+
+class TuneEntry(ctypes.Structure):
+    """kinc_sim_tune_entry: one timed candidate of the autotuner."""
+    _fields_ = [("launch", Launch), ("ms", ctypes.c_double)]
+
 # name -> (restype, argtypes); every symbol include/kinc_sim.h declares
 _VP = ctypes.c_void_p
 _I64 = ctypes.c_int64
@@ -106,6 +120,10 @@ SIGNATURES = {
     "kinc_sim_run_to_files_ex": (ctypes.c_int, [_VP, ctypes.c_char_p, ctypes.c_char_p, _I32, _I64, _I64, _I64]),
     "kinc_sim_execute_block_noalloc": (ctypes.c_int, [_VP, _I32, _I32, ctypes.POINTER(SimParams), _I64, _I64,
                                                       _VP, _VP, _VP, _VP]),
+    "kinc_sim_get_launch": (ctypes.c_int, [_VP, ctypes.POINTER(Launch)]),
+    "kinc_sim_set_launch": (ctypes.c_int, [_VP, ctypes.POINTER(Launch)]),
+    "kinc_sim_autotune": (ctypes.c_int, [_VP, _I64, _I64, _I32, ctypes.POINTER(Launch), ctypes.POINTER(TuneEntry),
+                                         _I32, ctypes.POINTER(_I32)]),
 }
 
 

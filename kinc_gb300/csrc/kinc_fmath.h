@@ -17,19 +17,31 @@
  * a*b+c on their own (host: -ffp-contract=off; device: --fmad=false).
  *
  * Methods (written from the mathematics, not from any vendor library):
- *   exp:  n = rint(x/ln2) by the 1.5*2^23 shifter; Cody-Waite argument
- *         reduction x = n*ln2 + r with a two-part ln2
- *         whose leading part has 16 significant bits (so n*LN2_HI and
- *         x - n*LN2_HI are exact for |n| <= 2^8), |r| <= ln2/2; then the
- *         degree-7 Taylor polynomial of e^r by Horner's rule in fused
- *         multiply-adds; then scaling by 2^n through the exponent field,
- *         split in two steps when 2^n itself is not a normal float.
- *   log:  x = 2^e * m with m in [sqrt(1/2), sqrt(2)); with f = m - 1 and
- *         s = f/(2+f), log(m) = 2 atanh(s) = f - (f^2/2 - s*(f^2/2 + R)),
- *         R = sum_{k>=1} 2 s^{2k}/(2k+1) (Taylor series of atanh, truncated
- *         after s^10), and log(x) = e*ln2 + log(m) with the same two-part ln2.
- * Both are within ~1 ulp of the true value (checked against libm double in
- * the CPU tests and against all float inputs of the used range on the GPU).
+ *   exp:  n = rint(x/ln2) by the 1.5*2^23 shifter (one fused multiply-add,
+ *         whose sum also holds n in its low mantissa bits); Cody-Waite
+ *         argument reduction x = n*ln2 + r with a two-part ln2 whose leading
+ *         part has 16 significant bits (so n*LN2_HI and x - n*LN2_HI are
+ *         exact for |n| <= 2^8), |r| <= ln2/2; then
+ *         e^r ~ 1 + r + r^2 (c2 + c3 r + ... + c6 r^4), the coefficients a
+ *         minimax fit of the relative error on [-ln2/2, ln2/2] found with
+ *         the Remez exchange algorithm (max relative error 4.3e-9 before
+ *         rounding), evaluated by Horner's rule in fused multiply-adds; then
+ *         scaling by 2^n with one integer add of n to the exponent field
+ *         when the result is a normal float, in two steps otherwise.
+ *         Max error 0.92 ulp over every float input with a normal result;
+ *         99.52 % of results are correctly rounded.
+ *   log:  the table-driven method of P. T. P. Tang (ACM TOMS 16(4), 1990)
+ *         in single precision: x = 2^e * m with m in [0.703125, 1.40625),
+ *         the reduction offset chosen so that 1.0 starts one of 32 equal
+ *         steps of the mantissa bits; entry i holds c_i = 1/invc_i with invc_i
+ *         a multiple of 1/64 (1 on the two steps around 1), and
+ *         log(c_i) = hi_i + lo_i with hi_i a multiple of 2^-16.  Then
+ *         z = m * invc_i - 1 is exact (|z| < 2^-5 and a multiple of 2^-30),
+ *         e*LN2_HI + hi_i is exact, that sum plus z is carried as a
+ *         two-float sum, and log1p(z) = z + z^2 (-1/2 + z/3 - z^2/4 + z^3/5)
+ *         supplies the rest (Taylor series, truncation below 2^-27
+ *         relative).  No division.  Max error 0.60 ulp over every positive
+ *         normal float; all but 0.0005 % correctly rounded.
  */
 #ifndef KINC_FMATH_H
 #define KINC_FMATH_H
@@ -56,6 +68,54 @@
 #define KINC_F_LN2_HI 0.693145751953125f             /* 0x3f317200 */
 #define KINC_F_LN2_LO 1.428606765330187045037746429e-06f /* ln2 - LN2_HI */
 #define KINC_F_SQRT2 1.41421353816986083984375f      /* float nearest to sqrt(2) */
+
+/* kinc_logf's reduction table: { invc_i, hi_i, lo_i, 0 } for the 32 steps of
+ * the mantissa bits above 0x3f340000 (see the method note above) */
+#define KINC_LOG_TABLE_INIT \
+   { \
+   { 1.40625f, -0.3409271240234375f, 5.370528697e-07f, 0.0f }, \
+   { 1.375f, -0.318450927734375f, -2.803384177e-06f, 0.0f }, \
+   { 1.34375f, -0.29547119140625f, 6.978512374e-06f, 0.0f }, \
+   { 1.3125f, -0.2719268798828125f, -6.835600743e-06f, 0.0f }, \
+   { 1.296875f, -0.2599639892578125f, 6.464820672e-06f, 0.0f }, \
+   { 1.265625f, -0.235565185546875f, -8.857658713e-07f, 0.0f }, \
+   { 1.25f, -0.22314453125f, 9.799357485e-07f, 0.0f }, \
+   { 1.21875f, -0.1978302001953125f, 4.456865554e-06f, 0.0f }, \
+   { 1.203125f, -0.1849212646484375f, -1.073845624e-06f, 0.0f }, \
+   { 1.171875f, -0.158599853515625f, -5.176661034e-06f, 0.0f }, \
+   { 1.15625f, -0.1451873779296875f, 5.368085112e-06f, 0.0f }, \
+   { 1.125f, -0.1177825927734375f, -4.428829357e-07f, 0.0f }, \
+   { 1.109375f, -0.103790283203125f, -6.510478670e-06f, 0.0f }, \
+   { 1.09375f, -0.0896148681640625f, 2.709474302e-06f, 0.0f }, \
+   { 1.078125f, -0.075225830078125f, 2.408840601e-06f, 0.0f }, \
+   { 1.0625f, -0.0606231689453125f, -1.452871174e-06f, 0.0f }, \
+   { 1.046875f, -0.045806884765625f, -2.651265731e-06f, 0.0f }, \
+   { 1.03125f, -0.0307769775390625f, 5.318872354e-06f, 0.0f }, \
+   { 1.0f, 0.0f, 0.0f, 0.0f }, \
+   { 1.0f, 0.0f, 0.000000000e+00f, 0.0f }, \
+   { 0.953125f, 0.048004150390625f, 5.068795872e-06f, 0.0f }, \
+   { 0.921875f, 0.0813446044921875f, 1.034961770e-06f, 0.0f }, \
+   { 0.90625f, 0.0984344482421875f, 5.624571259e-06f, 0.0f }, \
+   { 0.875f, 0.1335296630859375f, 1.729538553e-06f, 0.0f }, \
+   { 0.859375f, 0.15155029296875f, -3.948415497e-07f, 0.0f }, \
+   { 0.828125f, 0.1885986328125f, -7.463004749e-06f, 0.0f }, \
+   { 0.8125f, 0.2076416015625f, -2.236784212e-06f, 0.0f }, \
+   { 0.796875f, 0.22705078125f, 6.669385129e-06f, 0.0f }, \
+   { 0.765625f, 0.267059326171875f, 3.459077107e-06f, 0.0f }, \
+   { 0.75f, 0.287689208984375f, -7.136532531e-06f, 0.0f }, \
+   { 0.734375f, 0.3087310791015625f, 4.402548257e-06f, 0.0f }, \
+   { 0.71875f, 0.3302459716796875f, -4.284809165e-06f, 0.0f }, \
+   }
+
+typedef struct
+{
+   float inv, hi, lo, pad;
+} kinc_log_entry;
+
+#ifdef __CUDACC__
+static __device__ const __align__(16) kinc_log_entry kinc_log_table_d[32] = KINC_LOG_TABLE_INIT;
+#endif
+static const kinc_log_entry kinc_log_table_h[32] = KINC_LOG_TABLE_INIT;
 
 KINC_HD uint32_t kinc_f2u(float x)
 {
@@ -114,31 +174,27 @@ KINC_HD float kinc_expf(float x)
    /* n = rint(x / ln2): adding and removing 1.5 * 2^23 rounds to the nearest
     * integer (ties to even) for |x / ln2| < 2^22, which covers every x that
     * reaches the scaling below; the sum's low mantissa bits hold n itself */
-#ifdef __CUDA_ARCH__
-   const float shifted = __fadd_rn(__fmul_rn(x, KINC_F_LOG2E), 12582912.0f);   /* never contracted */
-#else
-   const float shifted = x * KINC_F_LOG2E + 12582912.0f;   /* hosts build with -ffp-contract=off */
-#endif
+   const float shifted = KINC_FMAF(x, KINC_F_LOG2E, 12582912.0f);
    const float n = shifted - 12582912.0f;
    float r = KINC_FMAF(-n, KINC_F_LN2_HI, x);
    r = KINC_FMAF(-n, KINC_F_LN2_LO, r);
 
-   /* 1 + r + r^2/2! + ... + r^7/7! */
-   float p = 1.98412698412698412698e-4f;                /* 1/5040 */
-   p = KINC_FMAF(p, r, 1.38888888888888888889e-3f);     /* 1/720 */
-   p = KINC_FMAF(p, r, 8.33333333333333333333e-3f);     /* 1/120 */
-   p = KINC_FMAF(p, r, 4.16666666666666666667e-2f);     /* 1/24 */
-   p = KINC_FMAF(p, r, 1.66666666666666666667e-1f);     /* 1/6 */
-   p = KINC_FMAF(p, r, 0.5f);
+   /* 1 + r + r^2 (c2 + r (c3 + r (c4 + r (c5 + r c6)))) */
+   float p = 1.3893402647227049e-3f;
+   p = KINC_FMAF(p, r, 8.370262570679188e-3f);
+   p = KINC_FMAF(p, r, 4.1667088866233826e-2f);
+   p = KINC_FMAF(p, r, 1.6666506230831146e-1f);
+   p = KINC_FMAF(p, r, 4.999999701976776e-1f);
    p = KINC_FMAF(p, r, 1.0f);
    p = KINC_FMAF(p, r, 1.0f);
 
-   /* |x| <= 87 keeps n in [-126, 126]: 2^n is a normal float and the product
-    * rounds once (NaN fails the comparison and takes the tail) */
-   if ( (x < 0.0f ? -x : x) <= 87.0f )
+   /* |x| <= 86 keeps n in [-125, 125] and p in [0.70, 1.42]: p * 2^n is a
+    * normal float, formed exactly by adding n to p's exponent field -- the
+    * low bits of `shifted` shifted up by 23 are n * 2^23 modulo 2^32 (NaN
+    * fails the comparison and takes the tail) */
+   if ( (x < 0.0f ? -x : x) <= 86.0f )
    {
-      /* bits(shifted) - bits(1.5 * 2^23) = n; 2^n has exponent field n + 127 */
-      return p * kinc_u2f((kinc_f2u(shifted) - 0x4b400000u + 127u) << 23);
+      return kinc_u2f(kinc_f2u(p) + (kinc_f2u(shifted) << 23));
    }
    return kinc_expf_tail(x, n, p);
 }
@@ -146,30 +202,28 @@ KINC_HD float kinc_expf(float x)
 /* natural logarithm of the positive normal float with bits b, times 2^eoff */
 KINC_HD float kinc_logf_normal(uint32_t b, int eoff)
 {
-   int e = (int)(b >> 23) - 127 + eoff;
-   float m = kinc_u2f((b & 0x007fffffu) | 0x3f800000u);
-   if ( m > KINC_F_SQRT2 )
-   {
-      m = m * 0.5f;
-      e += 1;
-   }
-
-   const float f = m - 1.0f;                 /* exact: m in [0.70, 1.42] */
-   const float s = f / (2.0f + f);
-   const float z = s * s;
-   float R = 0.181818181818181818182f;                   /* 2/11 */
-   R = KINC_FMAF(R, z, 0.222222222222222222222f);        /* 2/9 */
-   R = KINC_FMAF(R, z, 0.285714285714285714286f);        /* 2/7 */
-   R = KINC_FMAF(R, z, 0.4f);                            /* 2/5 */
-   R = KINC_FMAF(R, z, 0.666666666666666666667f);        /* 2/3 */
-   R = R * z;
-   const float hfsq = (0.5f * f) * f;
+   const uint32_t tmp = b - 0x3f340000u;
+   const int e = (int)((int32_t)tmp >> 23) + eoff;
+   const int i = (int)((tmp >> 18) & 31u);
+   const float m = kinc_u2f(b - (tmp & 0xff800000u));   /* in [0.703125, 1.40625) */
+#ifdef __CUDA_ARCH__
+   const kinc_log_entry t = kinc_log_table_d[i];
+#else
+   const kinc_log_entry t = kinc_log_table_h[i];
+#endif
+   const float z = KINC_FMAF(m, t.inv, -1.0f);           /* exact */
+   float q = 0.2f;
+   q = KINC_FMAF(q, z, -0.25f);
+   q = KINC_FMAF(q, z, 0.333333343267440796f);          /* float nearest to 1/3 */
+   q = KINC_FMAF(q, z, -0.5f);
+   const float z2 = z * z;
    const float ef = (float)e;
-
-   /* log(m) = f - (hfsq - s*(hfsq + R)); the e*ln2 tail joins the small terms */
-   const float small = KINC_FMAF(s, hfsq + R, ef * KINC_F_LN2_LO);
-   const float logm = f - (hfsq - small);
-   return KINC_FMAF(ef, KINC_F_LN2_HI, logm);
+   const float hi = KINC_FMAF(ef, KINC_F_LN2_HI, t.hi);   /* exact: a multiple of 2^-16 below 2^7 */
+   /* hi + z as s + err (|hi| >= |z| or hi = 0: Dekker's fast two-sum) */
+   const float s = hi + z;
+   const float err = (hi - s) + z;
+   const float lo = KINC_FMAF(ef, KINC_F_LN2_LO, t.lo) + err;
+   return s + KINC_FMAF(z2, q, lo);
 }
 
 /* natural logarithm, single precision. */

@@ -33,6 +33,8 @@
 #include <string>
 #include <vector>
 
+#include <sys/stat.h>
+
 using namespace kinc;
 
 /* compact.cu */
@@ -268,9 +270,14 @@ struct kinc_sim_ctx
    SimKernel kern {};
    TcState tc;                      /* tensor-core Pearson form (precision != 0) */
    bool use_tc = false;
-   int grid = 0;
-   int smem_bytes = 0;
+   int grid = 0;                    /* CTAs of the current launch shape */
+   int smem_bytes = 0;              /* dynamic shared memory of one CTA of the current shape */
    int smem_sort = 0;
+   int smem_warp = 0;               /* dynamic shared memory per warp */
+   int sms = 0;
+   int64_t slots = 0;               /* warp scratch slots allocated */
+   kinc_sim_launch launch {};
+   char gpu_name[256] = "";
    int64_t max_block = 0;
    /* device allocations */
    float* d_gem = nullptr;
@@ -509,6 +516,50 @@ extern "C" void kinc_sim_destroy(kinc_sim_ctx* ctx)
    delete ctx;
 }
 
+/* ---------------------------------------------------------- launch shape */
+
+/* the shape measured best on the clustering workloads: 16-warp CTAs, rounds for GMM and no
+ * clustering, free-running warps for K-means, GMM prefetch 8 samples ahead */
+static kinc_sim_launch default_launch(int clus)
+{
+   kinc_sim_launch l {};
+   l.warps_per_cta = WARPS_PER_BLOCK;
+   l.rounds = ((KINC_CTA_ROUNDS) >> clus) & 1;
+   l.prefetch = 8;
+   return l;
+}
+
+static bool launch_valid(const kinc_sim_launch& l)
+{
+   const bool w = l.warps_per_cta == 4 || l.warps_per_cta == 8 || l.warps_per_cta == 16;
+   const bool r = l.rounds == 0 || l.rounds == 1;
+   const bool f = l.prefetch == 0 || l.prefetch == 4 || l.prefetch == 8 || l.prefetch == 16;
+   return w && WARPS_PER_BLOCK % l.warps_per_cta == 0 && r && f;
+}
+
+/* the grid and shared memory of a shape: as many CTAs per SM as fit, within the warp scratch
+ * slots the context holds */
+static int apply_launch(kinc_sim_ctx* ctx, const kinc_sim_launch& l)
+{
+   if ( !launch_valid(l) )
+      return fail(ctx, KINC_SIM_EINVAL, "launch shape warps_per_cta %d rounds %d prefetch %d not supported",
+                  l.warps_per_cta, l.rounds, l.prefetch);
+   const int nw = l.warps_per_cta;
+   const int smem = ctx->smem_warp * nw;
+   int per_sm = 0;
+   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ctx->kern.fn, nw * 32, smem));
+   per_sm = std::max(1, per_sm);
+   const int64_t by_slots = ctx->slots / nw;
+   const int64_t grid = std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->sms * per_sm, by_slots));
+   ctx->grid = (int)grid;
+   ctx->smem_bytes = smem;
+   ctx->launch = l;
+   ctx->dp.warps = nw;
+   ctx->dp.rounds = l.rounds;
+   ctx->dp.prefetch = l.prefetch;
+   return KINC_SIM_OK;
+}
+
 extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples, const kinc_sim_params* params,
                                kinc_sim_ctx** out)
 {
@@ -624,8 +675,11 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    const size_t scratch_cap = free_b / 4;
    while ( grid > prop.multiProcessorCount && (size_t)grid * WARPS_PER_BLOCK * slot_bytes > scratch_cap )
       grid -= prop.multiProcessorCount;
-   ctx->grid = grid;
    const size_t slots = (size_t)grid * WARPS_PER_BLOCK;
+   ctx->sms = prop.multiProcessorCount;
+   snprintf(ctx->gpu_name, sizeof ctx->gpu_name, "%s", prop.name);
+   ctx->slots = (int64_t)slots;
+   ctx->smem_warp = (int)((ctx->smem_sort ? sort_bytes_warp : 0) + param_bytes_warp);
    {
       size_t off = 0;
       auto take = [&](size_t bytes) {
@@ -711,6 +765,12 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    ctx->dd.logn = ctx->d_logn;
    ctx->dd.jump = ctx->d_jump;
    ctx->dd.rng0 = ctx->d_rng0;
+   if ( params->precision == 0 )
+   {
+      const kinc_sim_launch def = default_launch(params->clus_method);
+      const int rc = apply_launch(ctx, def);
+      if ( rc ) return bail(rc);
+   }
    CKC(cudaStreamSynchronize(ctx->stream));
    *out = ctx;
    return KINC_SIM_OK;
@@ -851,6 +911,181 @@ extern "C" int kinc_sim_execute_block_device(kinc_sim_ctx* ctx, int64_t start, i
    ctx->launches = 0;
    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
    return enqueue_block(ctx, start, size, d_K, d_labels, d_corr, st);
+}
+
+/* ------------------------------------------------------------- autotuner */
+
+extern "C" int kinc_sim_get_launch(const kinc_sim_ctx* ctx, kinc_sim_launch* launch)
+{
+   if ( !ctx || !launch ) return KINC_SIM_EINVAL;
+   *launch = ctx->launch;
+   return KINC_SIM_OK;
+}
+
+extern "C" int kinc_sim_set_launch(kinc_sim_ctx* ctx, const kinc_sim_launch* launch)
+{
+   if ( !ctx || !launch ) return KINC_SIM_EINVAL;
+   if ( ctx->use_tc ) return fail(ctx, KINC_SIM_EINVAL, "the tensor-core precisions have no per-pair launch shape");
+   return apply_launch(ctx, *launch);
+}
+
+namespace {
+
+/* the cache file named in include/kinc_sim.h */
+std::string tune_cache_path()
+{
+   if ( const char* p = getenv("KINC_TUNE_CACHE") ) return p;
+   if ( const char* x = getenv("XDG_CACHE_HOME") ) return std::string(x) + "/kinc_gb300/launch.txt";
+   if ( const char* h = getenv("HOME") ) return std::string(h) + "/.cache/kinc_gb300/launch.txt";
+   return "";
+}
+
+std::string tune_key(const kinc_sim_ctx* ctx)
+{
+   const kinc_sim_params& p = ctx->params;
+   char buf[400];
+   snprintf(buf, sizeof buf, "clus=%d ks=%d ocl=%d corr=%d sem=%d pre=%d post=%d maxk=%d S<=%d gpu=%s sms=%d",
+            p.clus_method, ctx->kern.ks, (int)ctx->kern.ocl, p.corr_method, p.semantics, p.pre_out, p.post_out,
+            p.max_clusters, next_pow2_host(std::max(ctx->S, 2)), ctx->gpu_name, ctx->sms);
+   for ( char* c = buf; *c; ++c )
+      if ( *c == '\t' || *c == '\n' ) *c = ' ';
+   return buf;
+}
+
+bool tune_cache_lookup(const std::string& key, kinc_sim_launch& out)
+{
+   const std::string path = tune_cache_path();
+   if ( path.empty() ) return false;
+   FILE* f = fopen(path.c_str(), "r");
+   if ( !f ) return false;
+   char line[1024];
+   bool found = false;
+   while ( fgets(line, sizeof line, f) )
+   {
+      char* tab = strchr(line, '\t');
+      if ( !tab ) continue;
+      *tab = 0;
+      kinc_sim_launch l {};
+      if ( key == line && sscanf(tab + 1, "%d %d %d", &l.warps_per_cta, &l.rounds, &l.prefetch) == 3
+           && launch_valid(l) )
+      {
+         out = l;          /* the last entry for a key wins */
+         found = true;
+      }
+   }
+   fclose(f);
+   return found;
+}
+
+void tune_cache_store(const std::string& key, const kinc_sim_launch& l, double ms, int64_t pairs)
+{
+   const std::string path = tune_cache_path();
+   if ( path.empty() ) return;
+   /* create the directory chain of the file if needed */
+   for ( size_t i = 1; i < path.size(); ++i )
+   {
+      if ( path[i] != '/' ) continue;
+      const std::string dir = path.substr(0, i);
+      mkdir(dir.c_str(), 0755);
+   }
+   FILE* f = fopen(path.c_str(), "a");
+   if ( !f ) return;
+   fprintf(f, "%s\t%d %d %d\t%.4f ms for %lld pairs\n", key.c_str(), l.warps_per_cta, l.rounds, l.prefetch, ms,
+           (long long)pairs);
+   fclose(f);
+}
+
+}  // namespace
+
+static int time_launch(kinc_sim_ctx* ctx, const kinc_sim_launch& l, int64_t start, int64_t size, double& ms)
+{
+   int rc = apply_launch(ctx, l);
+   if ( rc ) return rc;
+   cudaEvent_t e0 = nullptr, e1 = nullptr;
+   CK(cudaEventCreate(&e0));
+   CK(cudaEventCreate(&e1));
+   cudaError_t err = cudaEventRecord(e0, ctx->stream);
+   rc = err == cudaSuccess ? enqueue_block(ctx, start, size, ctx->d_K, ctx->d_labels, ctx->d_corr, ctx->stream)
+                           : KINC_SIM_ECUDA;
+   if ( rc == KINC_SIM_OK ) err = cudaEventRecord(e1, ctx->stream);
+   if ( rc == KINC_SIM_OK && err == cudaSuccess ) err = cudaEventSynchronize(e1);
+   float t = 0.f;
+   if ( rc == KINC_SIM_OK && err == cudaSuccess ) err = cudaEventElapsedTime(&t, e0, e1);
+   cudaEventDestroy(e0);
+   cudaEventDestroy(e1);
+   if ( rc ) return rc;
+   if ( err != cudaSuccess ) return fail(ctx, KINC_SIM_ECUDA, "autotune timing: %s", cudaGetErrorString(err));
+   ms = t;
+   return kinc_sim_synchronize(ctx);
+}
+
+extern "C" int kinc_sim_autotune(kinc_sim_ctx* ctx, int64_t start, int64_t size, int32_t use_cache,
+                                 kinc_sim_launch* chosen, kinc_sim_tune_entry* entries, int32_t cap, int32_t* n)
+{
+   if ( !ctx ) return KINC_SIM_EINVAL;
+   if ( n ) *n = 0;
+   if ( ctx->use_tc ) return fail(ctx, KINC_SIM_EINVAL, "the tensor-core precisions have no per-pair launch shape");
+   int rc = check_range(ctx, start, size);
+   if ( rc ) return rc;
+   size = std::min(size, ctx->max_block);
+   if ( size <= 0 ) return fail(ctx, KINC_SIM_EINVAL, "autotune needs at least one pair");
+   const std::string key = tune_key(ctx);
+   kinc_sim_launch best = ctx->launch;
+   if ( use_cache && tune_cache_lookup(key, best) )
+   {
+      rc = apply_launch(ctx, best);
+      if ( rc == KINC_SIM_OK && chosen ) *chosen = best;
+      return rc;
+   }
+   CK(cudaStreamSynchronize(ctx->stream));
+   int32_t count = 0;
+   auto record = [&](const kinc_sim_launch& l, double ms) {
+      if ( entries && count < cap ) entries[count] = kinc_sim_tune_entry { l, ms };
+      ++count;
+   };
+   /* warm-up of the current shape (module load, caches), then the timed descent */
+   double best_ms = 0;
+   rc = time_launch(ctx, best, start, size, best_ms);
+   if ( rc ) return rc;
+   rc = time_launch(ctx, best, start, size, best_ms);
+   if ( rc ) return rc;
+   record(best, best_ms);
+   const int warps_v[] = { 4, 8, 16 };
+   const int pf_v[] = { 0, 4, 8, 16 };
+   for ( int pass = 0; pass < 2; ++pass )
+   {
+      const kinc_sim_launch start_best = best;
+      for ( int knob = 0; knob < 3; ++knob )
+      {
+         if ( knob == 0 && ctx->params.clus_method != 1 ) continue;   /* prefetch: the GMM sweeps only */
+         const int nv = knob == 0 ? 4 : knob == 1 ? 3 : 2;
+         const kinc_sim_launch base = best;
+         for ( int v = 0; v < nv; ++v )
+         {
+            kinc_sim_launch c = base;
+            if ( knob == 0 ) c.prefetch = pf_v[v];
+            else if ( knob == 1 ) c.warps_per_cta = warps_v[v];
+            else c.rounds = v;
+            if ( memcmp(&c, &base, sizeof c) == 0 ) continue;
+            double ms = 0;
+            rc = time_launch(ctx, c, start, size, ms);
+            if ( rc ) return rc;
+            record(c, ms);
+            if ( ms < best_ms )
+            {
+               best_ms = ms;
+               best = c;
+            }
+         }
+      }
+      if ( memcmp(&best, &start_best, sizeof best) == 0 ) break;
+   }
+   rc = apply_launch(ctx, best);
+   if ( rc ) return rc;
+   if ( use_cache ) tune_cache_store(key, best, best_ms, size);
+   if ( chosen ) *chosen = best;
+   if ( n ) *n = count;
+   return KINC_SIM_OK;
 }
 
 extern "C" int kinc_sim_execute_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t* out_K,
@@ -1201,6 +1436,12 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    dp.gam_k = (KINC_STORE_GAMMA && params->clus_method == 1)
                  ? (params->max_clusters <= 3 ? 3 : params->max_clusters <= 5 ? 5 : 0) : 0;
    dp.ncorr = params->corr_method == 2 ? 2 : 1;
+   {
+      const kinc_sim_launch l = default_launch(params->clus_method);
+      dp.warps = l.warps_per_cta;
+      dp.rounds = l.rounds;
+      dp.prefetch = l.prefetch;
+   }
    const size_t sort_bytes_warp = (size_t)dp.sort_floats * sizeof(float);
    const SimKernel kern = params->clus_method == 0 ? sim_kernel_none()
                         : params->clus_method == 1 ? sim_kernel_gmm(params->max_clusters, params->rand_mode == 1)

@@ -47,7 +47,8 @@ constexpr int TILE = 32;            /* pairs per warp tile */
 #endif
 constexpr int SAMPLE_UNROLL = KINC_SAMPLE_UNROLL;   /* unroll factor of the EM sample loops */
 #ifndef KINC_PREFETCH
-#define KINC_PREFETCH 8             /* samples ahead the EM / Lloyd sweeps prefetch into L2 (0: none) */
+#define KINC_PREFETCH 8             /* samples ahead the Lloyd sweeps prefetch into L2 (0: none); the EM
+                                       sweeps take theirs from DevParams::prefetch */
 #endif
 #ifndef KINC_KM_RING
 #define KINC_KM_RING 2              /* samples the Lloyd sweep keeps in flight in registers */
@@ -99,6 +100,10 @@ struct DevParams
    int32_t sort_floats;             /* floats of sort buffer per warp */
    int32_t gam_k;                   /* components per sample in DevScratch::gam (0: none) */
    int32_t ncorr;                   /* correlations per cluster: 1, or 2 for Pearson and Spearman */
+   /* launch shape (results are the same for every choice) */
+   int32_t warps;                   /* warps per CTA */
+   int32_t rounds;                  /* 1: a CTA's warps take their tiles together, round by round */
+   int32_t prefetch;                /* samples ahead the EM sweeps prefetch into L2 (0: none) */
 };
 
 struct DevData
@@ -231,9 +236,9 @@ struct LaneRng
    }
 };
 
-/* Jump the glibc state to output position `pos` (warp-cooperative: lane r < 31
- * holds word r) and store it interleaved for lane `slot`. */
-__device__ inline void warp_rng_jump(const DevData& D, uint64_t pos, uint32_t* ring, int slot, int lane)
+/* The glibc state at output position `pos`, warp-cooperatively: lane r < 31
+ * returns word r. */
+__device__ inline uint32_t warp_rng_state(const DevData& D, uint64_t pos, int lane)
 {
    uint32_t s = lane < RNG_WORDS ? D.rng0[lane] : 0u;
    for ( int b = 0; b < RNG_BITS && pos; ++b, pos >>= 1 )
@@ -248,12 +253,21 @@ __device__ inline void warp_rng_jump(const DevData& D, uint64_t pos, uint32_t* r
       }
       s = acc;
    }
+   return s;
+}
+
+/* Jump the glibc state to output position `pos` and store it interleaved for lane `slot`. */
+__device__ inline void warp_rng_jump(const DevData& D, uint64_t pos, uint32_t* ring, int slot, int lane)
+{
+   const uint32_t s = warp_rng_state(D, pos, lane);
    if ( lane < RNG_WORDS ) ring[lane * TILE + slot] = s;
 }
 
 /* ------------------------------------------------------ warp-coop steps */
 
-/* fetchPair for pair (x, y) into column `j` of the tile's interleaved arrays. */
+/* fetchPair for pair (x, y) into column `j` of the tile's interleaved arrays
+ * (STR = TILE), or into the pair's own contiguous arrays (STR = 1, j = 0). */
+template <int STR = TILE>
 __device__ inline int warp_fetch(const DevParams& P, const DevData& D, int32_t x, int32_t y, float2* X,
                           int8_t* lbl, int j, int lane)
 {
@@ -271,11 +285,11 @@ __device__ inline int warp_fetch(const DevParams& P, const DevData& D, int32_t x
          v2 = g2[s];
          const bool nanb = isnan(v1) || isnan(v2);
          const bool low = v1 < P.min_expr || v2 < P.min_expr;
-         lbl[s * TILE + j] = nanb ? (int8_t)-9 : (low ? (int8_t)-6 : (int8_t)0);
+         lbl[s * STR + j] = nanb ? (int8_t)-9 : (low ? (int8_t)-6 : (int8_t)0);
          use = !nanb && !low;
       }
       const unsigned bal = __ballot_sync(0xffffffffu, use);
-      if ( use ) X[(n + __popc(bal & lanemask_lt())) * TILE + j] = make_float2(v1, v2);
+      if ( use ) X[(n + __popc(bal & lanemask_lt())) * STR + j] = make_float2(v1, v2);
       n += __popc(bal);
    }
    __syncwarp();
@@ -283,7 +297,9 @@ __device__ inline int warp_fetch(const DevParams& P, const DevData& D, int32_t x
 }
 
 /* Clustering::markOutliers on column j of the tile (labels by sample position
- * i < N, values from the packed array at i, as in the reference). */
+ * i < N, values from the packed array at i, as in the reference); STR as in
+ * warp_fetch. */
+template <int STR = TILE>
 __device__ inline void warp_mark_outliers(const float2* X, int N, int col, int8_t* lbl, int8_t cluster,
                                    int8_t marker, float* buf, int j, int lane)
 {
@@ -295,11 +311,11 @@ __device__ inline void warp_mark_outliers(const float2* X, int N, int col, int8_
       float v = 0.f;
       if ( i < N )
       {
-         const int8_t l = lbl[i * TILE + j];
+         const int8_t l = lbl[i * STR + j];
          sel = l == cluster || l == marker;
          if ( sel )
          {
-            const float2 xv = X[i * TILE + j];
+            const float2 xv = X[i * STR + j];
             v = col == 0 ? xv.x : xv.y;
          }
       }
@@ -323,17 +339,18 @@ __device__ inline void warp_mark_outliers(const float2* X, int N, int col, int8_
    __syncwarp();
    for ( int i = lane; i < N; i += 32 )
    {
-      if ( lbl[i * TILE + j] == cluster )
+      if ( lbl[i * STR + j] == cluster )
       {
-         const float2 xv = X[i * TILE + j];
+         const float2 xv = X[i * STR + j];
          const float v = col == 0 ? xv.x : xv.y;
-         if ( v < T_min || T_max < v ) lbl[i * TILE + j] = marker;
+         if ( v < T_min || T_max < v ) lbl[i * STR + j] = marker;
       }
    }
    __syncwarp();
 }
 
-/* Spearman::computeCluster for column j, cluster k. */
+/* Spearman::computeCluster for column j, cluster k; STR as in warp_fetch. */
+template <int STR = TILE>
 __device__ inline float warp_spearman(const DevParams& P, const DevData& D, const float2* X, const int8_t* lbl,
                                int32_t x, int32_t y, int8_t k, float* buf, int j, int lane)
 {
@@ -347,7 +364,7 @@ __device__ inline float warp_spearman(const DevParams& P, const DevData& D, cons
    for ( int base = 0; base < P.S; base += 32 )
    {
       const int i = base + lane;
-      const int8_t l = i < P.S ? lbl[i * TILE + j] : (int8_t)-1;
+      const int8_t l = i < P.S ? lbl[i * STR + j] : (int8_t)-1;
       const bool nonneg = l >= 0;
       const bool incl = l == k;
       const unsigned bn = __ballot_sync(0xffffffffu, nonneg);
@@ -358,7 +375,7 @@ __device__ inline float warp_spearman(const DevParams& P, const DevData& D, cons
          float2 v;
          if ( P.semantics == 0 )
          {
-            v = X[(jw + __popc(bn & lanemask_lt())) * TILE + j];
+            v = X[(jw + __popc(bn & lanemask_lt())) * STR + j];
          }
          else
          {
@@ -464,7 +481,7 @@ __device__ __forceinline__ bool prepare_cov(float s00, float s01, float s11, dou
  */
 template <int KT, bool OCL>
 __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int N, int Kr, LaneRng& rng,
-                        double c2, float& out_logL, float& out_E, unsigned long long& units, float* pbuf)
+                        double c2, float& out_logL, float& out_E, unsigned long long& units, float* pbuf, int pd)
 {
    const int K = (KINC_STATIC_K && KT > 0) ? KT : Kr;
    /* KT > 0: up to KT components in registers (K <= KT at run time);
@@ -521,7 +538,7 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
       {
          const float2 xv = xn;
          if ( i + 1 < N ) xn = X[(i + 1) * TILE];
-         if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N ) prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
+         if ( pd > 0 && i + pd < N ) prefetch_l2(&X[(i + pd) * TILE]);
          float lg[KA];
          float m = -INFINITY;
 #pragma unroll UF
@@ -581,21 +598,21 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
                xn = X[(i + 1) * TILE];
                if ( !STORE_V ) ln = lpx[(i + 1) * TILE];
             }
-            if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N )
+            if ( pd > 0 && i + pd < N )
             {
-               prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
+               prefetch_l2(&X[(i + pd) * TILE]);
                if ( STORE_V )
                {
 #pragma unroll UF
                   for ( int k = 0; k < KA; ++k )
                   {
                      if ( k >= K ) continue;
-                     prefetch_l2(&gam[((i + KINC_PREFETCH) * KA + k) * TILE]);
+                     prefetch_l2(&gam[((i + pd) * KA + k) * TILE]);
                   }
                }
                else
                {
-                  prefetch_l2(&lpx[(i + KINC_PREFETCH) * TILE]);
+                  prefetch_l2(&lpx[(i + pd) * TILE]);
                }
             }
 #pragma unroll UF
@@ -661,21 +678,21 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
             xn = X[(i + 1) * TILE];
             ln = lpx[(i + 1) * TILE];
          }
-         if ( KINC_PREFETCH > 0 && i + KINC_PREFETCH < N )
+         if ( pd > 0 && i + pd < N )
          {
-            prefetch_l2(&X[(i + KINC_PREFETCH) * TILE]);
+            prefetch_l2(&X[(i + pd) * TILE]);
             if ( STORE_G )
             {
 #pragma unroll UF
                for ( int k = 0; k < KA; ++k )
                {
                   if ( k >= K ) continue;
-                  prefetch_l2(&gam[((i + KINC_PREFETCH) * KA + k) * TILE]);
+                  prefetch_l2(&gam[((i + pd) * KA + k) * TILE]);
                }
             }
             else
             {
-               prefetch_l2(&lpx[(i + KINC_PREFETCH) * TILE]);
+               prefetch_l2(&lpx[(i + pd) * TILE]);
             }
          }
 #pragma unroll UF

@@ -72,7 +72,9 @@ struct PackedCursor
    }
 };
 
-/* Pearson::computeCluster for this lane's pair (pairwise_pearson.cpp:12-52). */
+/* Pearson::computeCluster for this lane's pair (pairwise_pearson.cpp:12-52); X and lbl step
+ * by STR per sample (TILE: the tile's interleaved arrays, 1: a pair's own arrays). */
+template <int STR = TILE>
 __device__ inline float lane_pearson(const DevParams& P, const DevData& D, const DevBlock& B, const float2* X,
                                      const int8_t* lbl, int64_t p, int32_t x, int32_t y, int N, int8_t k)
 {
@@ -85,9 +87,9 @@ __device__ inline float lane_pearson(const DevParams& P, const DevData& D, const
        * usable samples left there (zero if none) */
       for ( int i = 0; i < N; ++i )
       {
-         if ( lbl[i * TILE] == k )
+         if ( lbl[i * STR] == k )
          {
-            const float2 v = X[i * TILE];
+            const float2 v = X[i * STR];
             sumx += v.x; sumy += v.y; sumx2 += v.x * v.x; sumy2 += v.y * v.y; sumxy += v.x * v.y;
             ++n;
          }
@@ -100,7 +102,7 @@ __device__ inline float lane_pearson(const DevParams& P, const DevData& D, const
       PackedCursor cur;
       for ( int i = N; i < P.S; ++i )
       {
-         if ( lbl[i * TILE] != k ) continue;
+         if ( lbl[i * STR] != k ) continue;
          while ( c >= 0 && B.N[c] <= i )
          {
             const int32_t nxt = B.pg[c];
@@ -117,7 +119,7 @@ __device__ inline float lane_pearson(const DevParams& P, const DevData& D, const
       const float* g2 = D.gem + (size_t)y * P.S;
       for ( int i = 0; i < P.S; ++i )
       {
-         if ( lbl[i * TILE] == k )
+         if ( lbl[i * STR] == k )
          {
             const float vx = g1[i];
             const float vy = g2[i];
@@ -161,7 +163,7 @@ __device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, co
 {
    if ( CLUS == 1 || CLUS == 3 )
    {
-      return gmm_fit<KT, CLUS == 3>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units, pbuf);
+      return gmm_fit<KT, CLUS == 3>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units, pbuf, P.prefetch);
    }
 #if KINC_KMEANS_PIPELINE
 #if KINC_KMEANS_LANE_MAJOR
@@ -232,7 +234,8 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
    extern __shared__ float smem[];
    const int lane = threadIdx.x & 31;
    const int warp = threadIdx.x >> 5;
-   const int64_t slot = blockIdx.x * (int64_t)WARPS_PER_BLOCK + warp;
+   const int nwarps = blockDim.x >> 5;          /* warps per CTA: a launch-shape choice, up to WARPS_PER_BLOCK */
+   const int64_t slot = blockIdx.x * (int64_t)nwarps + warp;
    const size_t col = (size_t)P.S * TILE;
 
    float2* X = W.X + slot * col;
@@ -247,19 +250,19 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
    float* sbuf = smem_sort ? smem + (size_t)warp * P.sort_floats : W.sortbuf + slot * (size_t)P.sort_floats;
    /* GMM parameters in shared memory (KINC_GMM_PARAMS_SMEM): 7 arrays of KS x 32 floats per warp */
    float* pbuf = (CM == 1 && KINC_GMM_PARAMS_SMEM && KS > 0)
-                    ? smem + (smem_sort ? (size_t)WARPS_PER_BLOCK * P.sort_floats : 0) + (size_t)warp * 7 * KS * TILE
+                    ? smem + (smem_sort ? (size_t)nwarps * P.sort_floats : 0) + (size_t)warp * 7 * KS * TILE
                     : nullptr;
 
    const int64_t ntiles = (B.size + TILE - 1) / TILE;
-   constexpr bool ROUNDS = ((KINC_CTA_ROUNDS) >> CM) & 1;
+   const bool rounds = P.rounds != 0;         /* uniform over the launch */
    __shared__ unsigned long long round_base;
    for ( ;; )
    {
       unsigned long long t = 0;
-      if constexpr ( ROUNDS )
+      if ( rounds )
       {
          __syncthreads();                       /* every warp is done with the previous round */
-         if ( threadIdx.x == 0 ) round_base = atomicAdd(B.tiles, (unsigned long long)WARPS_PER_BLOCK);
+         if ( threadIdx.x == 0 ) round_base = atomicAdd(B.tiles, (unsigned long long)nwarps);
          __syncthreads();
          const unsigned long long base = round_base;
          if ( (int64_t)base >= ntiles ) break;  /* uniform over the CTA */
@@ -422,11 +425,13 @@ inline SimKernel sim_kernel_handle()
    return SimKernel { (const void*)&k_similarity<CLUS, KS>, CLUS == 3 ? 1 : CLUS, KS, CLUS == 3 };
 }
 
+/* launch with P.warps warps per CTA (the host keeps it in 1..WARPS_PER_BLOCK and sizes grid, smem
+ * and the scratch slots for it) */
 template <int CLUS, int KS>
 inline cudaError_t sim_kernel_launch(int grid, int smem, cudaStream_t st, const DevParams& P, const DevData& D,
                                      const DevScratch& W, const DevBlock& B, int smem_sort)
 {
-   k_similarity<CLUS, KS><<<grid, WARPS_PER_BLOCK * 32, smem, st>>>(P, D, W, B, smem_sort);
+   k_similarity<CLUS, KS><<<grid, P.warps * 32, smem, st>>>(P, D, W, B, smem_sort);
    return cudaGetLastError();
 }
 

@@ -164,6 +164,44 @@ class Similarity:
         self.ccm = PairwiseMatrix("ccm", self.genes, p.max_clusters, self.samples)
         self.cmx = PairwiseMatrix("cmx", self.genes, p.max_clusters, self.samples)
 
+    def launch(self):
+        """The per-pair kernel's launch shape (kinc_sim_get_launch) as a dict."""
+        if self._ctx is None:
+            self.initialize()
+        L = _native.load()
+        out = _native.Launch()
+        _native.check(L.kinc_sim_get_launch(self._ctx, ctypes.byref(out)), self._ctx)
+        return out.as_dict()
+
+    def set_launch(self, warps_per_cta, rounds, prefetch):
+        """Fix the launch shape (kinc_sim_set_launch); every shape gives the same results."""
+        if self._ctx is None:
+            self.initialize()
+        L = _native.load()
+        _native.check(L.kinc_sim_set_launch(self._ctx, ctypes.byref(_native.Launch(warps_per_cta, rounds, prefetch,
+                                                                                       0))), self._ctx)
+
+    def autotune(self, start=None, size=None, use_cache=True, cap=64):
+        """Pick the launch shape by timing candidates on pairs [start, start+size)
+        (kinc_sim_autotune; default: the middle of the pairs, 4 x 32 pairs per resident warp of
+        the GPU, at most one device block).  Returns (chosen shape, timed candidates)."""
+        if self._ctx is None:
+            self.initialize()
+        L = _native.load()
+        total = self.total_pairs()
+        if size is None:
+            size = 4 * 32 * 16 * 152
+        size = int(min(size, total, L.kinc_sim_max_device_block(self._ctx)))
+        if start is None:
+            start = max(0, total // 2 - size // 2)
+        chosen = _native.Launch()
+        entries = (_native.TuneEntry * cap)()
+        n = ctypes.c_int32(0)
+        _native.check(L.kinc_sim_autotune(self._ctx, int(start), size, int(bool(use_cache)), ctypes.byref(chosen),
+                                          entries, cap, ctypes.byref(n)), self._ctx)
+        timed = [dict(entries[i].launch.as_dict(), ms=entries[i].ms) for i in range(min(n.value, cap))]
+        return chosen.as_dict(), timed
+
     def close(self):
         if self._ctx is not None:
             _native.load().kinc_sim_destroy(self._ctx)

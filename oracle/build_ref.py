@@ -59,24 +59,25 @@ def reference_available():
     return d is not None and os.path.isfile(os.path.join(d, "src", "core", "pairwise_gmm.cpp"))
 
 
-def _prebuilt(name):
-    """A library built earlier from the KINC tree, when the tree is not named now."""
+def _prebuilt(name, own_deps):
+    """A library built earlier from the KINC tree, when the tree is not named now; None when it is
+    missing or older than this repository's files it was built from."""
     path = os.path.join(HERE, "_ref", name)
-    return path if os.path.isfile(path) else None
+    return path if _newer(path, own_deps) else None
 
 
 def build_ref(math_mode=0):
     """Compile the KINC Pairwise:: sources where they lie; returns the .so path or None."""
+    own = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "ref_shim", "ace", "core", "core.h"),
+           os.path.join(HERE, "ref_shim", "pre.h"), os.path.join(REPO, "kinc_gb300", "csrc", "kinc_fmath.h")]
     if not reference_available():
-        return _prebuilt(f"libkinc_ref{math_mode}.so")
+        return _prebuilt(f"libkinc_ref{math_mode}.so", own)
     core = os.path.join(ref_dir(), "src", "core")
     out_dir = os.path.join(HERE, "_ref")
     os.makedirs(out_dir, exist_ok=True)
     out = os.path.join(out_dir, f"libkinc_ref{math_mode}.so")
     srcs = [os.path.join(core, s) for s in REF_SOURCES] + [os.path.join(HERE, "ref_driver.cpp")]
-    deps = srcs + [os.path.join(HERE, "ref_shim", "ace", "core", "core.h"),
-                   os.path.join(HERE, "ref_shim", "pre.h"),
-                   os.path.join(REPO, "kinc_gb300", "csrc", "kinc_fmath.h")]
+    deps = srcs + own
     if _newer(out, deps):
         return out
     cmd = ["g++", "-std=c++14", "-shared", *FP_FLAGS, "-w",
@@ -102,15 +103,16 @@ def build_ocl():
     KINC tree.  The kernels are read where they lie and piped to the compiler; the one
     OpenCL-only construct in them, the vector literal "(float2) (a, b)"
     (src/opencl/fetchpair.cl:62), is rewritten to a constructor call on the way."""
+    own = [os.path.join(HERE, "ocl_driver.cpp"), os.path.join(HERE, "ref_shim", "ocl_shim.h"),
+           os.path.join(REPO, "kinc_gb300", "csrc", "kinc_fmath.h")]
     if not reference_available():
-        return _prebuilt("libkinc_ocl.so")
+        return _prebuilt("libkinc_ocl.so", own)
     cl_dir = os.path.join(ref_dir(), "src", "opencl")
     out_dir = os.path.join(HERE, "_ref")
     os.makedirs(out_dir, exist_ok=True)
     out = os.path.join(out_dir, "libkinc_ocl.so")
     srcs = [os.path.join(cl_dir, s) for s in OCL_SOURCES]
-    deps = srcs + [os.path.join(HERE, "ocl_driver.cpp"), os.path.join(HERE, "ref_shim", "ocl_shim.h"),
-                   os.path.join(REPO, "kinc_gb300", "csrc", "kinc_fmath.h")]
+    deps = srcs + own
     if _newer(out, deps):
         return out
     import re

@@ -1,7 +1,7 @@
 """The oracle (oracle/kinc_oracle.c) pinned against KINC's own code.
 
 * glibc rand(): the restatement equals the C library's rand() stream.
-* kinc_expf / kinc_logf: within 1 ulp of the correctly rounded value.
+* kinc_expf / kinc_logf: within 0.93 / 0.61 ulp of the true value.
 * the restatement reproduces the golden fixtures (generated by KINC's own
   Pairwise:: sources, and by KINC's OpenCL kernels compiled for the host for
   the rand="lcg" mode, tests/golden/make_golden.py) bit for bit;
@@ -69,7 +69,9 @@ def test_fmath_accuracy():
     H = ctypes.CDLL(so)
     rng = np.random.default_rng(0)
     x = np.concatenate([rng.uniform(-104, 89, 200000), rng.uniform(-2, 2, 200000),
-                        np.exp(rng.uniform(-100, 88, 200000))]).astype(np.float32)
+                        np.exp(rng.uniform(-100, 88, 200000)), rng.uniform(0.98, 1.03, 200000),
+                        np.nextafter(np.float32(1), np.float32(0)) - np.arange(2000, dtype=np.float32) * 2 ** -24,
+                        np.float32(1) + np.arange(2000, dtype=np.float32) * 2 ** -23]).astype(np.float32)
     e = np.empty_like(x)
     lg = np.empty_like(x)
     P = ctypes.c_void_p
@@ -78,12 +80,12 @@ def test_fmath_accuracy():
         ex = np.exp(x.astype(np.float64))
         ulp = np.spacing(ex.astype(np.float32)).astype(np.float64)
     ok = (ex < 3.4e38) & (ex > 1.2e-38)
-    assert np.max(np.abs(e[ok] - ex[ok]) / ulp[ok]) < 1.0
+    assert np.max(np.abs(e[ok] - ex[ok]) / ulp[ok]) < 0.93
     pos = x > 0
     lx = np.log(x[pos].astype(np.float64))
     ulp = np.spacing(np.abs(lx).astype(np.float32)).astype(np.float64)
     nz = lx != 0
-    assert np.max(np.abs(lg[pos][nz] - lx[nz]) / ulp[nz]) < 1.0
+    assert np.max(np.abs(lg[pos][nz] - lx[nz]) / ulp[nz]) < 0.61
     specials = np.array([0.0, -0.0, 1.0, np.inf, -np.inf, np.nan, -1.0, 1e-45], np.float32)
     e = np.empty_like(specials)
     lg = np.empty_like(specials)
