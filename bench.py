@@ -138,6 +138,8 @@ def parity_block(gpu, cpu):
     rows = same_k & (Kc > 1)
     labels_eq = np.all(Lg[rows] == Lc[rows], axis=1) if rows.any() else np.ones(0, bool)
     mask = (np.arange(Cc.shape[1])[None, :] < Kc[:, None]) & same_k[:, None]
+    if Cc.ndim == 3:                      # [pair][k][Pearson, Spearman]
+        mask = np.broadcast_to(mask[:, :, None], Cc.shape)
     a, b = Cg[mask], Cc[mask]
     nan_a, nan_b = np.isnan(a), np.isnan(b)
     both = ~nan_a & ~nan_b
@@ -216,7 +218,8 @@ def run_reference(args, gem):
 def dense_leg(L, vp, check_pairs=1000000):
     """Pearson without clustering on the dense 20,000 x 2,000 workload (kinc_gb300.synthetic workload 3:
     rank-50 factors + noise, per-gene NaN rate ~U(0,0.2)): all 199,990,000 pairs with the tcgen05 tensor-core
-    form (TF32 and 3xBF16) and a 1,048,576-pair block with the plain per-pair FP32 kernel, both
+    form (TF32 and 3xBF16), the same contraction tiled in FP32 on the CUDA cores (the comparator
+    for the tensor-core forms), and a 1,048,576-pair block with the plain per-pair FP32 kernel, all
     device-resident and timed with CUDA events; max |r - r_fp64| over a seeded random subset."""
     import ctypes
 
@@ -236,7 +239,7 @@ def dense_leg(L, vp, check_pairs=1000000):
                        "per-gene NaN rate ~U(0,0.2), pairwise-complete (semantics fixed)",
            "pairs": total, "fp64_check_pairs": int(len(idx))}
     stream = torch.cuda.Stream()
-    for prec in ("tf32", "3xbf16", "fp32"):
+    for prec in ("tf32", "3xbf16", "fp32tiled", "fp32"):
         sim = Similarity(gem, semantics="fixed", precision=prec, maxclus=1)
         sim.initialize()
         ctx = sim._ctx
@@ -263,7 +266,7 @@ def dense_leg(L, vp, check_pairs=1000000):
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
-            reps = 3 if prec != "fp32" else 1
+            reps = 3 if prec in ("tf32", "3xbf16") else 1
             e0.record(stream)
             for _ in range(reps):
                 run(False)
@@ -293,8 +296,98 @@ def dense_leg(L, vp, check_pairs=1000000):
     out["3xbf16"]["frac_of_bf16_peak"] = out["3xbf16"]["executed_tflops"] / bf16
     out["peak_note"] = (f"TF32 dense peak taken as half the measured bf16 burst ({bf16:.0f} TFLOP/s, "
                         "MEASURED_PEAKS.json); 3xBF16 executes 2x the useful flops of the TF32 form")
+    sm_max = 2070.0
+    if os.path.exists(peaks):
+        with open(peaks) as fh:
+            sm_max = float(json.load(fh).get("sm_max_mhz", sm_max))
+    fp32_peak = torch.cuda.get_device_properties(0).multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    out["fp32tiled"]["frac_of_fp32_peak"] = out["fp32tiled"]["useful_tflops"] / fp32_peak
+    out["fp32tiled"]["peak_note"] = (f"nominal FP32 FMA rate {fp32_peak:.1f} TFLOP/s; 12 useful flops per pair and "
+                                     f"sample are 6 FFMA")
+    out["speedup_tf32_vs_fp32_tiled"] = out["tf32"]["pairs_per_s"] / out["fp32tiled"]["pairs_per_s"]
+    out["speedup_3xbf16_vs_fp32_tiled"] = out["3xbf16"]["pairs_per_s"] / out["fp32tiled"]["pairs_per_s"]
     out["speedup_tf32_vs_fp32_per_pair"] = out["tf32"]["pairs_per_s"] / out["fp32"]["pairs_per_s"]
     out["speedup_3xbf16_vs_fp32_per_pair"] = out["3xbf16"]["pairs_per_s"] / out["fp32"]["pairs_per_s"]
+    return out
+
+
+def pearson_leg(L, vp, cpu=True):
+    """Pearson without clustering on the 1,000 x 200 workload (kinc_gb300.synthetic workload 1: gene means
+    ~U(4,12), N(mean, 2), 5% NaN; minsamp 30, mincorr 0.5), reference semantics -- KINC's packed-array
+    reads, stale values of earlier pairs of the work block included: all 499,500 pairs as one device block
+    timed with CUDA events, and end to end into CCM/CMX files; the oracle over all pairs on the host cores
+    (one thread per 32,768-pair work block), its CMX/CCM items compared with the files bit for bit."""
+    import shutil
+    import tempfile
+
+    import torch
+
+    from kinc_gb300 import Similarity, _native, pairwise_matrix as pm, synthetic
+    from oracle import pyoracle
+    gem = synthetic.generate(1)
+    G, S = gem.shape
+    total = G * (G - 1) // 2
+    args = dict(clusmethod="none", corrmethod="pearson", minsamp=30, mincorr=0.5, maxcorr=1.0, maxclus=1)
+    sim = Similarity(gem, **args)
+    sim.initialize()
+    ctx = sim._ctx
+    dK = torch.empty(total, dtype=torch.int8, device="cuda")
+    dL = torch.empty((total, S), dtype=torch.int8, device="cuda")
+    dC = torch.empty((total, 1), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    reps = 5
+    with torch.cuda.stream(stream):
+        def once():
+            _native.check(L.kinc_sim_execute_block_device(ctx, 0, total, vp(dK.data_ptr()), vp(dL.data_ptr()),
+                                                          vp(dC.data_ptr()), vp(stream.cuda_stream)), ctx)
+        once()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            once()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    _native.check(L.kinc_sim_synchronize(ctx), ctx)
+    tmp = tempfile.mkdtemp(prefix="kinc_cfg1_")
+    try:
+        ccm, cmx = os.path.join(tmp, "a.ccm"), os.path.join(tmp, "a.cmx")
+        t0 = time.perf_counter()
+        sim.run(ccm_path=ccm, cmx_path=cmx)
+        e2e_s = time.perf_counter() - t0
+        got_cmx, got_ccm = pm.read(cmx, pm.CMX), pm.read(ccm, pm.CCM)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+        sim.close()
+    # per (pair, sample) 8 flops: n, sums of x, y, x^2, y^2, xy
+    out = {"workload": "Pearson only, GEM 1000x200 float32, gene means ~U(4,12), 5% NaN, minsamp 30, mincorr 0.5, "
+                       "reference semantics (stale packed-array reads), all pairs",
+           "pairs": total, "ms": ms, "pairs_per_s": total / (ms / 1e3),
+           "e2e": {"seconds": e2e_s, "pairs_per_s": total / e2e_s,
+                   "includes": "kinc_sim_run_to_files: compute, device process(), items to CCM/CMX files"},
+           "achieved_tflops": 8.0 * S * total / (ms / 1e3) / 1e12, "cmx_items": int(len(got_cmx["x"]))}
+    if cpu:
+        threads = os.cpu_count() or 1
+        nblk = (total + 32767) // 32768
+        starts = np.arange(nblk, dtype=np.int64) * 32768
+        sizes = np.minimum(32768, total - starts).astype(np.int64)
+        p = pyoracle.params(clus_method=0, corr_method=0, min_samples=30, max_clusters=1, min_corr=0.5,
+                            max_corr=1.0)
+        done, secs, ref = pyoracle.run_segments_parallel(gem, p, starts, sizes, threads, outputs=True)
+        out["cpu_baseline"] = {"value": done / secs, "unit": "pairs/s", "cores": min(threads, nblk), "kind": "port",
+                               "sample": f"all {done} pairs, one thread per work block, {secs:.2f} s"}
+        out["gpu_over_cpu"] = out["pairs_per_s"] / out["cpu_baseline"]["value"]
+        want_cmx, want_ccm = pyoracle.process_block(S, p, 0, *ref)
+        same_cmx = (np.array_equal(got_cmx["x"], want_cmx["x"]) and np.array_equal(got_cmx["y"], want_cmx["y"])
+                    and np.array_equal(got_cmx["c"], want_cmx["c"])
+                    and np.array_equal(got_cmx["payload"][:, 0].view(np.uint32), want_cmx["r"].view(np.uint32)))
+        same_ccm = len(got_ccm["x"]) == len(want_ccm["x"]) and np.array_equal(got_ccm["x"], want_ccm["x"]) \
+            and np.array_equal(got_ccm["y"], want_ccm["y"])
+        out["parity"] = {"cmx_items_gpu": int(len(got_cmx["x"])), "cmx_items_oracle": int(len(want_cmx["x"])),
+                         "cmx_bit_exact": bool(same_cmx), "ccm_pairs_equal": bool(same_ccm),
+                         "vs": "oracle: C restatement of KINC's serial path and Similarity::process"}
     return out
 
 
@@ -345,11 +438,11 @@ def kmeans_leg(L, vp, cpu=True):
         rng = np.random.default_rng(11)
         starts = rng.choice((total - 1) // 32768, size=threads, replace=False).astype(np.int64) * 32768
         p = pyoracle.params(clus_method=2, corr_method=0, min_clusters=1, max_clusters=3, criterion=0, min_samples=30)
-        sizes = np.full(threads, 6, np.int64)
+        sizes = np.full(threads, max(1, 2048 // threads), np.int64)
         done, secs, ref = pyoracle.run_segments_parallel(gem, p, starts, sizes, threads, outputs=True)
         out["cpu_baseline"] = {"value": done / secs, "unit": "pairs/s", "cores": threads, "kind": "port",
-                               "sample": f"{done} pairs: {threads} threads x 6 consecutive pairs from seeded "
-                                         f"random work blocks, {secs:.1f} s"}
+                               "sample": f"{done} pairs: {threads} threads x {int(sizes[0])} consecutive pairs "
+                                         f"from seeded random work blocks, {secs:.1f} s"}
         out["gpu_over_cpu"] = out["pairs_per_s"] / out["cpu_baseline"]["value"]
         chk = Similarity(gem, **args)
         parts = [chk.execute(None, int(a), int(b)) for a, b in zip(starts, sizes)]
@@ -359,7 +452,7 @@ def kmeans_leg(L, vp, cpu=True):
     return out
 
 
-def stream_leg(device_block, nblk):
+def stream_leg(device_block, nblk, cpu=True):
     """The large streamed run (kinc_gb300.synthetic workload 5: GEM 30,000 x 500, 8% NaN, 5% planted
     2-4 component mixture pairs; GMM k <= 5, ICL, pre+post outliers, Pearson and Spearman per cluster)
     end to end through kinc_sim_run_to_files_ex: `nblk` device blocks of `device_block` pairs from the
@@ -390,7 +483,32 @@ def stream_leg(device_block, nblk):
         shutil.rmtree(tmp, ignore_errors=True)
         sim.close()
     rate = pairs / secs
-    return {"workload": "GMM k<=5 (ICL) + pre/post outliers + Pearson and Spearman per cluster, GEM 30000x500 "
+    extra = {}
+    if cpu:
+        # the oracle on the host cores over seeded random work blocks of the same workload, and the GPU on the
+        # same pairs through the host-buffer entry point
+        from oracle import pyoracle
+        threads = os.cpu_count() or 1
+        total = sim.total_pairs()
+        rng = np.random.default_rng(55)
+        starts = rng.choice((total - 1) // 32768, size=threads, replace=False).astype(np.int64) * 32768
+        sizes = np.full(threads, max(1, 2048 // threads), np.int64)
+        p = pyoracle.params(clus_method=1, corr_method=2, min_clusters=1, max_clusters=5, criterion=1, pre_out=1,
+                            post_out=1, min_samples=30)
+        done, csecs, ref = pyoracle.run_segments_parallel(gem, p, starts, sizes, threads, outputs=True)
+        chk = Similarity(gem, clusmethod="gmm", corrmethod="both", minclus=1, maxclus=5, crit="ICL", preout=True,
+                         postout=True, minsamp=30)
+        parts = [chk.execute(None, int(a), int(b)) for a, b in zip(starts, sizes)]
+        chk.close()
+        gpu = (np.concatenate([r.K for r in parts]), np.concatenate([r.labels for r in parts]),
+               np.concatenate([r.corr for r in parts]))
+        extra["cpu_baseline"] = {"value": done / csecs, "unit": "pairs/s", "cores": threads, "kind": "port",
+                                 "sample": f"{done} pairs: {threads} threads x {int(sizes[0])} consecutive pairs "
+                                           f"from seeded random work blocks, both correlations, {csecs:.1f} s"}
+        extra["gpu_over_cpu"] = rate / extra["cpu_baseline"]["value"]
+        extra["parity"] = parity_block(gpu, ref)
+    return {**extra,
+            "workload": "GMM k<=5 (ICL) + pre/post outliers + Pearson and Spearman per cluster, GEM 30000x500 "
                         "float32, 8% NaN, 5% planted 2-4 component mixture pairs, minsamp 30, mincorr 0.5",
             "pairs": int(pairs), "first_pair": int(first * 32768), "device_block": device_block,
             "device_blocks": nblk, "seconds": secs, "pairs_per_s": rate,
@@ -451,7 +569,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--block", type=int, default=1048576)
-    ap.add_argument("--ref-pairs-per-thread", type=int, default=64)
+    ap.add_argument("--ref-pairs-per-thread", type=int, default=128)
     ap.add_argument("--cpu-pairs-per-thread", type=int, default=512)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -459,6 +577,7 @@ def main():
     ap.add_argument("--no-kmeans", action="store_true")
     ap.add_argument("--no-rmt", action="store_true")
     ap.add_argument("--no-libm", action="store_true")
+    ap.add_argument("--no-pearson", action="store_true")
     ap.add_argument("--no-tune-cache", action="store_true", help="time the launch shapes even if cached")
     ap.add_argument("--dense-check-pairs", type=int, default=1000000)
     ap.add_argument("--stream-blocks", type=int, default=2,
@@ -626,7 +745,8 @@ def main():
 
     tensor_core = None if args.no_dense else dense_leg(L, vp, args.dense_check_pairs)
     kmeans = None if args.no_kmeans else kmeans_leg(L, vp, cpu=not args.no_cpu)
-    streamed = None if args.stream_blocks <= 0 else stream_leg(1 << 22, args.stream_blocks)
+    pearson = None if args.no_pearson else pearson_leg(L, vp, cpu=not args.no_cpu)
+    streamed = None if args.stream_blocks <= 0 else stream_leg(1 << 22, args.stream_blocks, cpu=not args.no_cpu)
     rmt = None if args.no_rmt else rmt_leg(cpu=not args.no_cpu)
     libm = None if args.no_libm else libm_leg()
 
@@ -651,7 +771,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded; no public dataset)",
             "config": config_dict(args, gem), "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "cpu_baseline": cpu, "parity": parity, "clocks": clk, "tensor_core": tensor_core, "kmeans_uneven": kmeans,
-            "streamed_30000x500": streamed, "rmt": rmt, "libm_agreement": libm, "autotune": autotune}
+            "streamed_30000x500": streamed, "rmt": rmt, "libm_agreement": libm, "autotune": autotune,
+            "pearson_1000x200": pearson}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -62,7 +62,8 @@ def _parser():
     sim.add_argument("--maxcorr", type=float, default=1.0)
     sim.add_argument("--ksize", type=int, default=4096)
     sim.add_argument("--semantics", default="reference", choices=["reference", "fixed"])
-    sim.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "3xbf16"])
+    sim.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "3xbf16", "fp32tiled"])
+    sim.add_argument("--autotune", action="store_true", help="pick the kernel launch shape by timing (cached)")
     sim.add_argument("--rand", default="glibc", choices=["glibc", "lcg"],
                      help="glibc: KINC's serial path; lcg: KINC's OpenCL worker (per-fit LCG GMM)")
     sim.add_argument("--first-block", type=int, default=0, help="first work block (for a shard)")
@@ -158,6 +159,8 @@ def main(argv=None):
                              crit=args.crit, preout=args.preout, postout=args.postout, mincorr=args.mincorr,
                              maxcorr=args.maxcorr, ksize=args.ksize, semantics=args.semantics,
                              precision=args.precision, rand=args.rand)
+            if args.autotune and args.precision == "fp32":
+                sim.autotune()
             sim.run(ccm_path=args.ccm, cmx_path=args.cmx, little_endian=args.little_endian,
                     first_block=args.first_block, nblocks=args.blocks, world=args.world, rank=args.rank,
                     by_cost=args.by_cost, resume=args.resume)

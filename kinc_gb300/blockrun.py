@@ -33,6 +33,8 @@ def main(argv=None):
     ap.add_argument("--start", default="0", help="first pair, or 'mid'")
     ap.add_argument("--blocks", default="32768,262144", help="comma-separated device block sizes")
     ap.add_argument("--repeat", type=int, default=1, help="run each block this many times from the same pair")
+    ap.add_argument("--launch", default="", help="launch shape warps_per_cta,rounds,prefetch (default: the "
+                                                 "worker's); 'tune' = kinc_sim_autotune with its cache")
     args = ap.parse_args(argv)
 
     import torch
@@ -43,6 +45,10 @@ def main(argv=None):
                      minclus=args.minclus, maxclus=args.maxclus, minsamp=args.minsamp, preout=args.preout,
                      postout=args.postout, semantics=args.semantics, precision=args.precision)
     sim.initialize()
+    if args.launch == "tune":
+        sim.autotune()
+    elif args.launch:
+        sim.set_launch(*[int(v) for v in args.launch.split(",")])
     L = _native.load()
     ctx = sim._ctx
     vp = ctypes.c_void_p
@@ -69,7 +75,8 @@ def main(argv=None):
         _native.check(L.kinc_sim_synchronize(ctx), ctx)
         _native.check(L.kinc_sim_work_counters(ctx, counters, 1), ctx)
         ms = e0.elapsed_time(e1)
-        print(json.dumps({"workload": args.workload, "start": pos, "pairs": size, "ms": ms,
+        print(json.dumps({"workload": args.workload, "launch": sim.launch() if args.precision == "fp32" else None,
+                          "start": pos, "pairs": size, "ms": ms,
                           "pairs_per_s": size / (ms / 1e3), "units": int(counters[0]), "fits": int(counters[1]),
                           "launches": int(L.kinc_sim_last_launch_count(ctx))}), flush=True)
         if args.repeat <= 1:

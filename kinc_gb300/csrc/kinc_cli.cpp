@@ -81,7 +81,8 @@ private:
 const std::map<std::string, std::vector<std::string>> KEYS = {
    { "similarity", { "input", "ccm", "cmx", "clusmethod", "corrmethod", "minexpr", "minsamp", "minclus", "maxclus",
                      "crit", "preout", "postout", "mincorr", "maxcorr", "ksize", "semantics", "precision",
-                     "rand", "first-block", "blocks", "world", "rank", "by-cost", "resume", "little-endian" } },
+                     "rand", "first-block", "blocks", "world", "rank", "by-cost", "resume", "little-endian",
+                     "autotune" } },
    { "export-cmx", { "ccm", "cmx", "output", "little-endian" } },
    { "extract", { "emx", "ccm", "cmx", "output", "graphml", "mincorr", "maxcorr", "names", "little-endian" } },
    { "rmt", { "input", "log", "tstart", "tstep", "tstop", "minpace", "maxpace", "bins", "little-endian" } },
@@ -91,7 +92,7 @@ const std::map<std::string, std::vector<std::string>> KEYS = {
    { "merge", { "output", "inputs", "little-endian" } },
 };
 
-const std::vector<std::string> BOOLEANS = { "preout", "postout", "little-endian", "by-cost", "resume" };
+const std::vector<std::string> BOOLEANS = { "preout", "postout", "little-endian", "by-cost", "resume", "autotune" };
 
 bool is_bool(const std::string& k)
 {
@@ -106,8 +107,9 @@ int usage()
            "usage: kinc-gb300 run similarity --input EMX [--ccm CCM] [--cmx CMX] [--clusmethod none|gmm|kmeans]\n"
            "           [--corrmethod pearson|spearman|both] [--minexpr F] [--minsamp N] [--minclus N] [--maxclus N]\n"
            "           [--crit BIC|ICL] [--preout [true|false]] [--postout [true|false]] [--mincorr F] [--maxcorr F]\n"
-           "           [--ksize N] [--semantics reference|fixed] [--precision fp32|tf32|3xbf16] [--rand glibc|lcg]\n"
-           "           [--first-block N] [--blocks N | --world N --rank R [--by-cost]] [--resume] [--little-endian]\n"
+           "           [--ksize N] [--semantics reference|fixed] [--precision fp32|tf32|3xbf16|fp32tiled]\n"
+           "           [--rand glibc|lcg] [--first-block N] [--blocks N | --world N --rank R [--by-cost]] [--resume]\n"
+           "           [--autotune] [--little-endian]\n"
            "       kinc-gb300 run export-cmx --ccm CCM --cmx CMX --output TXT\n"
            "       kinc-gb300 run extract --emx EMX --ccm CCM --cmx CMX [--output TXT] [--graphml XML] [--mincorr F]\n"
            "           [--maxcorr F] [--names TXT]\n"
@@ -241,7 +243,7 @@ int run_similarity(const Args& a)
    p.corr_method = choice(a.str("corrmethod", "pearson"), { "pearson", "spearman", "both" }, "corrmethod", ok);
    p.criterion = choice(a.str("crit", "ICL"), { "BIC", "ICL" }, "crit", ok);
    p.semantics = choice(a.str("semantics", "reference"), { "reference", "fixed" }, "semantics", ok);
-   p.precision = choice(a.str("precision", "fp32"), { "fp32", "tf32", "3xbf16" }, "precision", ok);
+   p.precision = choice(a.str("precision", "fp32"), { "fp32", "tf32", "3xbf16", "fp32tiled" }, "precision", ok);
    p.rand_mode = choice(a.str("rand", "glibc"), { "glibc", "lcg" }, "rand", ok);
    if ( !ok ) return 2;
    p.min_expr = (float)a.real("minexpr", p.min_expr);
@@ -302,6 +304,23 @@ int run_similarity(const Args& a)
    {
       fprintf(stderr, "similarity: %s\n", kinc_sim_last_error(nullptr));
       return 1;
+   }
+   if ( a.str("autotune", "0") == "1" && p.precision == 0 )
+   {
+      /* launch shape timed on pairs from the middle of the matrix (or taken from the tuning cache) */
+      const int64_t total = kinc_sim_total_pairs(ctx);
+      const int64_t size = std::min<int64_t>(total, (int64_t)4 * 32 * 16 * 152);
+      kinc_sim_launch chosen {};
+      int32_t n = 0;
+      rc = kinc_sim_autotune(ctx, total / 2 - size / 2, size, 1, &chosen, nullptr, 0, &n);
+      if ( rc != KINC_SIM_OK )
+      {
+         fprintf(stderr, "similarity: %s\n", kinc_sim_last_error(ctx));
+         kinc_sim_destroy(ctx);
+         return 1;
+      }
+      fprintf(stderr, "similarity: launch shape %d warps per CTA, rounds %d, prefetch %d (%s)\n",
+              chosen.warps_per_cta, chosen.rounds, chosen.prefetch, n ? "timed" : "cached");
    }
    const std::string ccm = a.str("ccm"), cmx = a.str("cmx");
    if ( a.str("resume", "0") == "1" )

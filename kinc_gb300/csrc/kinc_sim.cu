@@ -417,10 +417,10 @@ int validate(const kinc_sim_params* p, int32_t G, int32_t S, std::string& why)
    }
    if ( p->semantics < 0 || p->semantics > 1 ) { why = "semantics must be 0 or 1"; return 0; }
    if ( p->rand_mode < 0 || p->rand_mode > 1 ) { why = "rand_mode must be 0 or 1"; return 0; }
-   if ( p->precision < 0 || p->precision > 2 ) { why = "precision must be 0, 1 or 2"; return 0; }
+   if ( p->precision < 0 || p->precision > 3 ) { why = "precision must be 0, 1, 2 or 3"; return 0; }
    if ( p->precision != 0 && (p->clus_method != 0 || p->corr_method != 0 || p->semantics != 1) )
    {
-      why = "precision TF32/3xBF16 is the tensor-core pairwise-complete Pearson: it needs clus_method none, "
+      why = "precision TF32/3xBF16/FP32-tiled is the pairwise-complete Pearson contraction: it needs clus_method none, "
             "corr_method pearson and semantics 1 (each sample's own values)";
       return 0;
    }
@@ -514,6 +514,25 @@ extern "C" void kinc_sim_destroy(kinc_sim_ctx* ctx)
    if ( !ctx ) return;
    release(ctx);
    delete ctx;
+}
+
+/* per warp slot scratch of the K-means task pool (kinc::kmeans_pool) */
+struct KmPool
+{
+   int dmax = 0, tmax = 0, rs = 0;
+   size_t bytes = 0;
+};
+
+static KmPool km_pool_sizes(const kinc_sim_params& p, const SimKernel& k)
+{
+   KmPool m;
+   if ( p.clus_method != 2 || k.ks == 0 ) return m;
+   m.dmax = km_draws_per_pair(p.min_clusters, p.max_clusters);
+   m.tmax = TILE * (p.max_clusters - p.min_clusters + 1) * 10;
+   m.rs = k.ks == 3 ? km_record_floats<3>() : km_record_floats<5>();
+   m.bytes = (((size_t)m.dmax * TILE * sizeof(int32_t) + 255) & ~(size_t)255)
+             + (((size_t)m.tmax * m.rs * sizeof(float) + 255) & ~(size_t)255);
+   return m;
 }
 
 /* ---------------------------------------------------------- launch shape */
@@ -664,11 +683,16 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    const size_t col = (size_t)S * TILE;
    dp.gam_k = (KINC_STORE_GAMMA && params->clus_method == 1)
                  ? (params->max_clusters <= 3 ? 3 : params->max_clusters <= 5 ? 5 : 0) : 0;
-   /* K-means sweeps read each lane's samples from its own contiguous copy */
-   const bool lane_major = params->clus_method == 2 && KINC_KMEANS_LANE_MAJOR;
+   /* K-means with register-resident means (up to 3 or 5 clusters) runs the tile as a task pool
+    * (draws and task records per slot); beyond that, per-lane fits over a contiguous copy of the
+    * lane's samples */
+   const KmPool km = km_pool_sizes(*params, ctx->kern);
+   dp.km_dmax = km.dmax;
+   dp.km_tmax = km.tmax;
+   const bool lane_major = params->clus_method == 2 && KINC_KMEANS_LANE_MAJOR && ctx->kern.ks == 0;
    const size_t slot_bytes = col * sizeof(float2) * (lane_major ? 2 : 1) + col * sizeof(float) * (1 + dp.gam_k)
                              + 5 * col + (size_t)RNG_WORDS * TILE * sizeof(uint32_t)
-                             + (ctx->smem_sort ? 0 : sort_bytes_warp) + 256 * 8;
+                             + (ctx->smem_sort ? 0 : sort_bytes_warp) + km.bytes + 256 * 10;
    size_t free_b = 0, total_b = 0;
    CKC(cudaMemGetInfo(&free_b, &total_b));
    int grid = prop.multiProcessorCount * per_sm;
@@ -698,6 +722,8 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
       const size_t oR = take(slots * RNG_WORDS * TILE * sizeof(uint32_t));
       const size_t oS = take(ctx->smem_sort ? 0 : slots * sort_bytes_warp);
       const size_t oXl = take(lane_major ? slots * col * sizeof(float2) : 0);
+      const size_t oKd = take(slots * (size_t)km.dmax * TILE * sizeof(int32_t));
+      const size_t oKr = take(slots * (size_t)km.tmax * km.rs * sizeof(float));
       CKC(cudaMalloc(&ctx->d_scratch, off));
       char* base = (char*)ctx->d_scratch;
       ctx->ds.X = (float2*)(base + oX);
@@ -711,6 +737,8 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
       ctx->ds.rng = (uint32_t*)(base + oR);
       ctx->ds.sortbuf = ctx->smem_sort ? nullptr : (float*)(base + oS);
       ctx->ds.Xl = lane_major ? (float2*)(base + oXl) : nullptr;
+      ctx->ds.kmd = km.bytes ? (int32_t*)(base + oKd) : nullptr;
+      ctx->ds.kmr = km.bytes ? (float*)(base + oKr) : nullptr;
    }
 
    /* one device block of pairs (the tensor-core form writes no labels, so its blocks can be far larger) */
@@ -1448,6 +1476,9 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
                                                    : sim_kernel_kmeans(params->max_clusters);
    const size_t param_bytes_warp = (KINC_GMM_PARAMS_SMEM && kern.clus == 1 && kern.ks > 0)
                                       ? (size_t)7 * kern.ks * TILE * sizeof(float) : 0;
+   const KmPool km = km_pool_sizes(*params, kern);
+   dp.km_dmax = km.dmax;
+   dp.km_tmax = km.tmax;
    const int smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * WARPS_PER_BLOCK <= 200 * 1024;
    const int smem_bytes = (int)((smem_sort ? sort_bytes_warp : 0) + param_bytes_warp) * WARPS_PER_BLOCK;
    if ( smem_bytes > 0 )
@@ -1477,8 +1508,9 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
                              + 5 * ((col + 255) & ~(size_t)255)
                              + (((size_t)RNG_WORDS * TILE * sizeof(uint32_t) + 255) & ~(size_t)255)
                              + (smem_sort ? 0 : ((sort_bytes_warp + 255) & ~(size_t)255))
-                             + ((params->clus_method == 2 && KINC_KMEANS_LANE_MAJOR)
-                                   ? ((col * sizeof(float2) + 255) & ~(size_t)255) : 0);
+                             + ((params->clus_method == 2 && KINC_KMEANS_LANE_MAJOR && kern.ks == 0)
+                                   ? ((col * sizeof(float2) + 255) & ~(size_t)255) : 0)
+                             + km.bytes;
    if ( off >= NOALLOC_SCRATCH_BYTES || (NOALLOC_SCRATCH_BYTES - off) / slot_bytes < (size_t)WARPS_PER_BLOCK )
       return fail(nullptr, KINC_SIM_EINVAL,
                   "%d genes x %d samples and %lld pairs do not fit the %zu-byte allocation-free scratch",
@@ -1503,8 +1535,10 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
       ds.yc = (int8_t*)carve(nslots * col);
       ds.rng = (uint32_t*)carve(nslots * RNG_WORDS * TILE * sizeof(uint32_t));
       ds.sortbuf = smem_sort ? nullptr : (float*)carve(nslots * sort_bytes_warp);
-      ds.Xl = (params->clus_method == 2 && KINC_KMEANS_LANE_MAJOR) ? (float2*)carve(nslots * col * sizeof(float2))
-                                                                  : nullptr;
+      ds.Xl = (params->clus_method == 2 && KINC_KMEANS_LANE_MAJOR && kern.ks == 0)
+                 ? (float2*)carve(nslots * col * sizeof(float2)) : nullptr;
+      ds.kmd = km.bytes ? (int32_t*)carve(nslots * (size_t)km.dmax * TILE * sizeof(int32_t)) : nullptr;
+      ds.kmr = km.bytes ? (float*)carve(nslots * (size_t)km.tmax * km.rs * sizeof(float)) : nullptr;
       if ( o > NOALLOC_SCRATCH_BYTES )
          return fail(nullptr, KINC_SIM_EINVAL, "allocation-free scratch layout overflow");
    }

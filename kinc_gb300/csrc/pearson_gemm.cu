@@ -1,6 +1,8 @@
 /*
  * pearson_gemm.cu -- pairwise-complete Pearson for clusmethod none as a dense
- * masked contraction on the tcgen05 tensor cores (precision TF32 or 3xBF16).
+ * masked contraction on the tcgen05 tensor cores (precision TF32 or 3xBF16),
+ * and the same contraction tiled on the CUDA cores in FP32 (precision 3, the
+ * comparator for the tensor-core forms).
  *
  * For genes x, y with usable-sample masks m and centred values a (a = v - mean
  * over the gene's usable samples, 0 where unusable), every sum Pearson needs
@@ -287,7 +289,14 @@ __global__ void k_tc_prep(const float* __restrict__ gem, int G, int S, int Gp, i
       }
       const float a2 = a * a;
       const size_t o = (size_t)warp * Sp + s;
-      if ( MODE == 1 )
+      if ( MODE == 3 )
+      {
+         float* f = (float*)ops;
+         f[o] = a;
+         f[plane + o] = a2;
+         f[2 * plane + o] = m;
+      }
+      else if ( MODE == 1 )
       {
          float* f = (float*)ops;
          uint32_t t;
@@ -576,6 +585,141 @@ __global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant
    }
 }
 
+/*
+ * The same contraction on the CUDA cores in FP32 (precision 3): the comparator
+ * for the tensor-core forms.  A CTA of 256 threads computes a 64 x 64 tile of
+ * pairs; each thread a 4 x 4 block with the six sums in registers (96 FFMA
+ * per sample, fed by six 128-bit shared-memory reads).  The operand chunks
+ * (3 planes x 32 samples x 64 genes per side) are staged transposed in shared
+ * memory -- [plane][sample][gene], so a thread's four genes are one float4 --
+ * double-buffered through registers: the next chunk is read from global
+ * memory while the current one is multiplied.
+ */
+constexpr int SB = 64;                /* genes per tile side */
+constexpr int SK = 32;                /* samples per chunk */
+constexpr int STHREADS = 256;
+constexpr int SIMT_SMEM = 2 * 2 * 3 * SK * SB * (int)sizeof(float);   /* two stages, two sides, three planes */
+
+__global__ void __launch_bounds__(STHREADS, 1) k_pearson_simt(const float* __restrict__ ops, int Gp, int Sp,
+                                                             TcArgs args)
+{
+   extern __shared__ __align__(16) float sm[];
+   const int I = args.I0 + (int)blockIdx.y;
+   const int J = (int)blockIdx.x;
+   const int64_t rowmax = (int64_t)(I + 1) * SB - 1;
+   const int64_t xmax = rowmax < args.xb ? rowmax : args.xb;
+   if ( (int64_t)J * SB >= xmax ) return;    /* no pair x > y in this tile */
+   const int t = threadIdx.x;
+   const int tx = t & 15, ty = t >> 4;       /* this thread's genes: x rows 4tx.., y rows 4ty.. */
+   const int lr = t & 31, lg = t >> 5;       /* loader: rows lr and lr + 32, samples 4lg..4lg+3 */
+   const size_t plane = (size_t)Gp * Sp;
+   const float* xsrc = ops + (size_t)I * SB * Sp;
+   const float* ysrc = ops + (size_t)J * SB * Sp;
+
+   float4 stage[2][3][2];
+   auto fetch = [&](int kc) {
+#pragma unroll
+      for ( int m = 0; m < 3; ++m )
+#pragma unroll
+         for ( int h = 0; h < 2; ++h )
+         {
+            const size_t o = m * plane + (size_t)(lr + 32 * h) * Sp + (size_t)kc * SK + 4 * lg;
+            stage[0][m][h] = *reinterpret_cast<const float4*>(xsrc + o);
+            stage[1][m][h] = *reinterpret_cast<const float4*>(ysrc + o);
+         }
+   };
+   auto put = [&](int buf) {
+#pragma unroll
+      for ( int side = 0; side < 2; ++side )
+#pragma unroll
+         for ( int m = 0; m < 3; ++m )
+#pragma unroll
+            for ( int h = 0; h < 2; ++h )
+            {
+               float* d = sm + (((buf * 2 + side) * 3 + m) * SK + 4 * lg) * SB + lr + 32 * h;
+               const float4 v = stage[side][m][h];
+               d[0 * SB] = v.x;
+               d[1 * SB] = v.y;
+               d[2 * SB] = v.z;
+               d[3 * SB] = v.w;
+            }
+   };
+
+   float sxy[4][4] = {}, sx[4][4] = {}, sy[4][4] = {}, sxx[4][4] = {}, syy[4][4] = {}, nn[4][4] = {};
+   const int K = args.kchunks;
+   fetch(0);
+   put(0);
+   __syncthreads();
+   for ( int kc = 0; kc < K; ++kc )
+   {
+      const int buf = kc & 1;
+      if ( kc + 1 < K ) fetch(kc + 1);
+      const float* xa = sm + ((buf * 2 + 0) * 3 + 0) * SK * SB + 4 * tx;
+      const float* xq = xa + SK * SB;
+      const float* xm = xq + SK * SB;
+      const float* ya = sm + ((buf * 2 + 1) * 3 + 0) * SK * SB + 4 * ty;
+      const float* yq = ya + SK * SB;
+      const float* ym = yq + SK * SB;
+#pragma unroll 4
+      for ( int k = 0; k < SK; ++k )
+      {
+         const float4 a4 = *reinterpret_cast<const float4*>(xa + k * SB);
+         const float4 q4 = *reinterpret_cast<const float4*>(xq + k * SB);
+         const float4 m4 = *reinterpret_cast<const float4*>(xm + k * SB);
+         const float4 b4 = *reinterpret_cast<const float4*>(ya + k * SB);
+         const float4 r4 = *reinterpret_cast<const float4*>(yq + k * SB);
+         const float4 n4 = *reinterpret_cast<const float4*>(ym + k * SB);
+         const float ax[4] = { a4.x, a4.y, a4.z, a4.w }, qx[4] = { q4.x, q4.y, q4.z, q4.w };
+         const float mx[4] = { m4.x, m4.y, m4.z, m4.w };
+         const float ay[4] = { b4.x, b4.y, b4.z, b4.w }, qy[4] = { r4.x, r4.y, r4.z, r4.w };
+         const float my[4] = { n4.x, n4.y, n4.z, n4.w };
+#pragma unroll
+         for ( int i = 0; i < 4; ++i )
+#pragma unroll
+            for ( int j = 0; j < 4; ++j )
+            {
+               sxy[i][j] = fmaf(ax[i], ay[j], sxy[i][j]);
+               sx[i][j] = fmaf(ax[i], my[j], sx[i][j]);
+               sy[i][j] = fmaf(mx[i], ay[j], sy[i][j]);
+               sxx[i][j] = fmaf(qx[i], my[j], sxx[i][j]);
+               syy[i][j] = fmaf(mx[i], qy[j], syy[i][j]);
+               nn[i][j] = fmaf(mx[i], my[j], nn[i][j]);
+            }
+      }
+      if ( kc + 1 < K )
+      {
+         put(buf ^ 1);          /* the other buffer: last read before the previous barrier */
+         __syncthreads();
+      }
+   }
+
+#pragma unroll
+   for ( int i = 0; i < 4; ++i )
+   {
+      const int64_t x = (int64_t)I * SB + 4 * tx + i;
+      if ( x >= args.G ) continue;
+      const int64_t pbase = x * (x - 1) / 2;
+#pragma unroll
+      for ( int j = 0; j < 4; ++j )
+      {
+         const int64_t y = (int64_t)J * SB + 4 * ty + j;
+         if ( y >= x ) continue;
+         const int64_t p = pbase + y;
+         if ( p < args.start || p >= args.end ) continue;
+         const float n = nn[i][j];
+         float r = __int_as_float(0x7fc00000);
+         if ( n >= (float)args.min_samples && n > 0.f )
+         {
+            const float num = diff_of_products(n, sxy[i][j], sx[i][j], sy[i][j]);
+            const float dx = diff_of_products(n, sxx[i][j], sx[i][j], sx[i][j]);
+            const float dy = diff_of_products(n, syy[i][j], sy[i][j], sy[i][j]);
+            r = num * rsqrtf(dx) * rsqrtf(dy);
+         }
+         args.out_corr[(p - args.start) * args.max_k] = r;
+      }
+   }
+}
+
 /* K = 1 and NaN beyond column 0 for the pairs of the range (clusmethod none) */
 __global__ void k_tc_fill(int64_t size, int max_k, int8_t* __restrict__ K, float* __restrict__ corr)
 {
@@ -617,8 +761,8 @@ cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_e
    t.mode = mode;
    t.Gp = (G + BM - 1) / BM * BM;
    t.Sp = (S + 63) / 64 * 64;
-   const int elem = mode == 1 ? 4 : 2;
-   const int nmat = mode == 1 ? 3 : 5;
+   const int elem = mode == 2 ? 2 : 4;
+   const int nmat = mode == 2 ? 5 : 3;
    const size_t plane = (size_t)t.Gp * t.Sp * elem;
    cudaError_t e = cudaMalloc(&t.ops, plane * nmat);
    if ( e != cudaSuccess ) return e;
@@ -627,12 +771,17 @@ cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_e
    {
       k_tc_prep<1><<<blocks, 256, 0, st>>>(d_gem, G, S, t.Gp, t.Sp, min_expr, t.ops);
    }
-   else
+   else if ( mode == 2 )
    {
       k_tc_prep<2><<<blocks, 256, 0, st>>>(d_gem, G, S, t.Gp, t.Sp, min_expr, t.ops);
    }
+   else
+   {
+      k_tc_prep<3><<<blocks, 256, 0, st>>>(d_gem, G, S, t.Gp, t.Sp, min_expr, t.ops);
+   }
    e = cudaGetLastError();
    if ( e != cudaSuccess ) return e;
+   if ( mode == 3 ) return cudaSuccess;      /* the CUDA-core form reads the planes directly */
    EncodeTiledFn enc = encode_fn();
    if ( !enc )
    {
@@ -683,8 +832,9 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
    };
    const int64_t xa = row_of(start);
    const int64_t xb = row_of(end - 1);
-   const int Ia = (int)(xa / BM), Ib = (int)(xb / BM);
-   const int Jn = (int)((xb + BN - 1) / BN);
+   const int tile_x = t.mode == 3 ? SB : BM, tile_y = t.mode == 3 ? SB : BN;
+   const int Ia = (int)(xa / tile_x), Ib = (int)(xb / tile_x);
+   const int Jn = (int)((xb + tile_y - 1) / tile_y);
    if ( Jn < 1 ) return cudaSuccess;
    k_tc_fill<<<(int)std::min<int64_t>((size + 255) / 256, 65535), 256, 0, st>>>(size, max_k, d_K, d_corr);
    TcArgs a;
@@ -698,7 +848,14 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
    a.out_corr = d_corr;
    a.status = d_status;
    a.kchunks = t.Sp / 32;
-   if ( t.mode == 1 )
+   if ( t.mode == 3 )
+   {
+      a.kchunks = t.Sp / SK;
+      cudaFuncSetAttribute(k_pearson_simt, cudaFuncAttributeMaxDynamicSharedMemorySize, SIMT_SMEM);
+      k_pearson_simt<<<dim3((unsigned)Jn, (unsigned)(Ib - Ia + 1)), STHREADS, SIMT_SMEM, st>>>(
+         (const float*)t.ops, t.Gp, t.Sp, a);
+   }
+   else if ( t.mode == 1 )
    {
       const int smem = Layout<1>::SMEM;
       cudaFuncSetAttribute(k_pearson_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

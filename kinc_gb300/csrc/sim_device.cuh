@@ -104,6 +104,7 @@ struct DevParams
    int32_t warps;                   /* warps per CTA */
    int32_t rounds;                  /* 1: a CTA's warps take their tiles together, round by round */
    int32_t prefetch;                /* samples ahead the EM sweeps prefetch into L2 (0: none) */
+   int32_t km_dmax, km_tmax;        /* K-means task pool: draws per pair, tasks per tile */
 };
 
 struct DevData
@@ -128,6 +129,8 @@ struct DevScratch
    uint32_t* rng;                   /* per warp slot: [31][32] */
    float* sortbuf;                  /* per warp slot: sort_floats, used when not in shared memory */
    float2* Xl;                      /* K-means: per lane [S], the lane's samples contiguous */
+   int32_t* kmd;                    /* K-means task pool: per warp slot [km_dmax][32] rand() draws */
+   float* kmr;                      /* K-means task pool: per warp slot [km_tmax][record floats] */
 };
 
 struct DevBlock

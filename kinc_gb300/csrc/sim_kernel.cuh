@@ -226,6 +226,12 @@ __device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* 
    return bestK;
 }
 
+} /* namespace kinc */
+
+#include "sim_kmeans_pool.cuh"
+
+namespace kinc {
+
 template <int CLUS, int KS>
 __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32, KINC_MIN_BLOCKS)
 k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
@@ -316,7 +322,20 @@ k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
       {
          unsigned long long units = 0, fits = 0;
          K = 0;
-         if ( lane < npairs )
+         if constexpr ( CLUS == 2 && KS > 0 )
+         {
+            /* the tile's runs as one pool of tasks, every lane busy until it is empty */
+            LaneRng rng;
+            rng.ring = ring + lane;
+            rng.head = 0;
+            rng.mode = P.rand_mode;
+            rng.lcg = 1;
+            constexpr int RS = km_record_floats<KS>();
+            K = kmeans_pool<KS>(P, D, X, lbl, ya + lane, yb + lane, wl + lane, lpx + lane,
+                                W.kmd + (size_t)slot * P.km_dmax * TILE, W.kmr + (size_t)slot * P.km_tmax * RS,
+                                npairs, myN, rng, lane, units, fits);
+         }
+         else if ( lane < npairs )
          {
             LaneRng rng;
             rng.ring = ring + lane;

@@ -889,7 +889,24 @@ int ko_run_block(const float* gem, int32_t G, int32_t S, const ko_params* p, ko_
       {
          K = cluster_pair(p, &w, N, &rnd);
       }
-      if ( out_corr )
+      if ( out_corr && p->corr_method == 2 )
+      {
+         /* both methods of one clustering, [k][0] Pearson and [k][1] Spearman: what two KINC runs
+          * with the same arguments and the two --corrmethod values give (the worker computes both
+          * in one pass) */
+         for ( k = 0; k < maxK; ++k )
+         {
+            float rp = NAN, rs = NAN;
+            if ( k < K )
+            {
+               rp = pearson_cluster(p, &w, g1, g2, S, (int8_t)k);
+               rs = spearman_cluster(p, &w, g1, g2, S, (int8_t)k);
+            }
+            out_corr[(q * maxK + k) * 2] = rp;
+            out_corr[(q * maxK + k) * 2 + 1] = rs;
+         }
+      }
+      else if ( out_corr )
       {
          for ( k = 0; k < maxK; ++k )
          {
@@ -1006,7 +1023,8 @@ static void* par_worker(void* argp)
       ko_run_block(st->gem, st->G, st->S, st->p, &rngs[s], st->starts[s], st->sizes[s],
                    st->out_K ? st->out_K + o : NULL,
                    st->out_labels ? st->out_labels + o * st->S : NULL,
-                   st->out_corr ? st->out_corr + o * st->p->max_clusters : NULL, NULL);
+                   st->out_corr ? st->out_corr + o * st->p->max_clusters * (st->p->corr_method == 2 ? 2 : 1)
+                                : NULL, NULL);
       pthread_mutex_lock(&st->lock);
       st->done += st->sizes[s];
       pthread_mutex_unlock(&st->lock);

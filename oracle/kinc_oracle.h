@@ -24,7 +24,7 @@ extern "C" {
 typedef struct ko_params
 {
    int32_t clus_method;   /* 0 none, 1 gmm, 2 kmeans */
-   int32_t corr_method;   /* 0 pearson, 1 spearman */
+   int32_t corr_method;   /* 0 pearson, 1 spearman, 2 both ([k][0] Pearson, [k][1] Spearman) */
    float   min_expr;
    int32_t min_samples;
    int32_t min_clusters;

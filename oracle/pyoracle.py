@@ -175,7 +175,7 @@ def run_block(gem, p, start, size, rand_pos=None):
     G, S = gem.shape
     K = np.zeros(size, np.int8)
     labels = np.zeros((size, S), np.int8)
-    corr = np.zeros((size, p.max_clusters), np.float32)
+    corr = np.zeros((size, p.max_clusters, 2) if p.corr_method == 2 else (size, p.max_clusters), np.float32)
     N = np.zeros(size, np.int32)
     g = KoRand()
     L.ko_rand_seed(ctypes.byref(g), 1)
@@ -242,7 +242,7 @@ def run_segments_parallel(gem, p, starts, sizes, threads, outputs=False):
     n = int(sizes.sum())
     K = np.zeros(n, np.int8)
     labels = np.zeros((n, S), np.int8)
-    corr = np.zeros((n, p.max_clusters), np.float32)
+    corr = np.zeros((n, p.max_clusters, 2) if p.corr_method == 2 else (n, p.max_clusters), np.float32)
     done = L.ko_run_segments_parallel_out(_ptr(gem), G, S, ctypes.byref(p), _ptr(starts), _ptr(sizes), _ptr(pos),
                                           len(starts), threads, ctypes.byref(secs), _ptr(K), _ptr(labels),
                                           _ptr(corr))

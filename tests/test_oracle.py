@@ -191,3 +191,16 @@ def test_oracle_equals_compiled_reference_on_edge_inputs(case):
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[3], b[3])
     assert np.array_equal(a[1][a[0] > 1], b[1][b[0] > 1])
     assert same_corr(a[2], b[2])
+
+
+def test_oracle_both_correlations_equal_two_runs():
+    """corr_method 2 (Pearson and Spearman from one clustering, what the worker's corrmethod both
+    computes) equals the two single-method runs a KINC user would make."""
+    from kinc_gb300 import synthetic
+    gem = synthetic.generate(5, genes=30, samples=90)
+    kw = dict(clus_method=1, criterion=1, pre_out=1, post_out=1)
+    Kb, Lb, Cb, Nb = pyoracle.run_block(gem, pyoracle.params(corr_method=2, **kw), 0, 300)
+    for c in (0, 1):
+        K, L, C, N = pyoracle.run_block(gem, pyoracle.params(corr_method=c, **kw), 0, 300)
+        assert np.array_equal(K, Kb) and np.array_equal(L, Lb) and np.array_equal(N, Nb)
+        assert np.array_equal(np.nan_to_num(C, nan=9.0), np.nan_to_num(Cb[:, :, c], nan=9.0))
