@@ -438,7 +438,7 @@ def kmeans_leg(L, vp, cpu=True):
         rng = np.random.default_rng(11)
         starts = rng.choice((total - 1) // 32768, size=threads, replace=False).astype(np.int64) * 32768
         p = pyoracle.params(clus_method=2, corr_method=0, min_clusters=1, max_clusters=3, criterion=0, min_samples=30)
-        sizes = np.full(threads, max(1, 2048 // threads), np.int64)
+        sizes = np.full(threads, max(1, 16384 // threads), np.int64)      # ~20 s on 16 cores
         done, secs, ref = pyoracle.run_segments_parallel(gem, p, starts, sizes, threads, outputs=True)
         out["cpu_baseline"] = {"value": done / secs, "unit": "pairs/s", "cores": threads, "kind": "port",
                                "sample": f"{done} pairs: {threads} threads x {int(sizes[0])} consecutive pairs "
@@ -492,7 +492,7 @@ def stream_leg(device_block, nblk, cpu=True):
         total = sim.total_pairs()
         rng = np.random.default_rng(55)
         starts = rng.choice((total - 1) // 32768, size=threads, replace=False).astype(np.int64) * 32768
-        sizes = np.full(threads, max(1, 2048 // threads), np.int64)
+        sizes = np.full(threads, max(1, 24576 // threads), np.int64)      # ~15 s on 16 cores
         p = pyoracle.params(clus_method=1, corr_method=2, min_clusters=1, max_clusters=5, criterion=1, pre_out=1,
                             post_out=1, min_samples=30)
         done, csecs, ref = pyoracle.run_segments_parallel(gem, p, starts, sizes, threads, outputs=True)
@@ -570,7 +570,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--block", type=int, default=1048576)
     ap.add_argument("--ref-pairs-per-thread", type=int, default=128)
-    ap.add_argument("--cpu-pairs-per-thread", type=int, default=512)
+    ap.add_argument("--cpu-pairs-per-thread", type=int, default=3072, help="headline CPU sample (~60 s on 16 cores)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-dense", action="store_true")

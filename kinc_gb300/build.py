@@ -20,6 +20,9 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc" if os.path.exists("/usr
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-I", os.path.join(REPO, "include"), "-I", CSRC]
+# extra nvcc flags for the CUDA units, e.g. KINC_BUILD_FLAGS="-DKINC_GMM_PACKED=0" to time a compile-time
+# variant (every variant gives the same results); pass force=True after changing it
+EXTRA = os.environ.get("KINC_BUILD_FLAGS", "").split()
 
 # (source, extra flags); kinc_cli.cpp is the command-line program, linked against the library
 CLI_SRC = "kinc_cli.cpp"
@@ -68,7 +71,7 @@ def build(force=False, verbose=False):
         if not os.path.exists(path):
             continue
         obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
-        cmd = [NVCC, *ARCH, *COMMON, *flags, "-c", path, "-o", obj]
+        cmd = [NVCC, *ARCH, *COMMON, *flags, *EXTRA, "-c", path, "-o", obj]
         jobs.append((cmd, obj))
 
     def run(job):

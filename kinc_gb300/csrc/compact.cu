@@ -32,7 +32,8 @@ __device__ __forceinline__ bool keep(const float* r, int nc, float lo, float hi)
 
 __device__ __forceinline__ void pair_of(int64_t p, int32_t& x, int32_t& y)
 {
-   int64_t xx = (int64_t)((1.0 + sqrt(1.0 + 8.0 * (double)p)) * 0.5);
+   /* float estimate (GB300's FP64 rate is a small fraction of FP32), corrected exactly below */
+   int64_t xx = (int64_t)((1.0f + sqrtf(1.0f + 8.0f * (float)p)) * 0.5f);
    while ( xx * (xx - 1) / 2 > p ) --xx;
    while ( (xx + 1) * xx / 2 <= p ) ++xx;
    x = (int32_t)xx;

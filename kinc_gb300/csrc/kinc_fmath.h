@@ -68,6 +68,12 @@
 #define KINC_F_LN2_HI 0.693145751953125f             /* 0x3f317200 */
 #define KINC_F_LN2_LO 1.428606765330187045037746429e-06f /* ln2 - LN2_HI */
 #define KINC_F_SQRT2 1.41421353816986083984375f      /* float nearest to sqrt(2) */
+/* kinc_expf's polynomial (minimax on [-ln2/2, ln2/2], see the method note) */
+#define KINC_EXP_C6 1.3893402647227049e-3f
+#define KINC_EXP_C5 8.370262570679188e-3f
+#define KINC_EXP_C4 4.1667088866233826e-2f
+#define KINC_EXP_C3 1.6666506230831146e-1f
+#define KINC_EXP_C2 4.999999701976776e-1f
 
 /* kinc_logf's reduction table: { invc_i, hi_i, lo_i, 0 } for the 32 steps of
  * the mantissa bits above 0x3f340000 (see the method note above) */
@@ -180,11 +186,11 @@ KINC_HD float kinc_expf(float x)
    r = KINC_FMAF(-n, KINC_F_LN2_LO, r);
 
    /* 1 + r + r^2 (c2 + r (c3 + r (c4 + r (c5 + r c6)))) */
-   float p = 1.3893402647227049e-3f;
-   p = KINC_FMAF(p, r, 8.370262570679188e-3f);
-   p = KINC_FMAF(p, r, 4.1667088866233826e-2f);
-   p = KINC_FMAF(p, r, 1.6666506230831146e-1f);
-   p = KINC_FMAF(p, r, 4.999999701976776e-1f);
+   float p = KINC_EXP_C6;
+   p = KINC_FMAF(p, r, KINC_EXP_C5);
+   p = KINC_FMAF(p, r, KINC_EXP_C4);
+   p = KINC_FMAF(p, r, KINC_EXP_C3);
+   p = KINC_FMAF(p, r, KINC_EXP_C2);
    p = KINC_FMAF(p, r, 1.0f);
    p = KINC_FMAF(p, r, 1.0f);
 

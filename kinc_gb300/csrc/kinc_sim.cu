@@ -186,24 +186,59 @@ __global__ void k_scan_apply(const int32_t* __restrict__ N, int64_t offset, int6
    if ( t < count ) qpos[t] = boff[blockIdx.x] + ex;
 }
 
-/* previous pair (same 32768-pair work block) with a strictly larger N, by
- * jumping along already computed links; one thread per work block.  Links
- * are offsets from lo (-1 = none). */
-__global__ void k_prev(const int32_t* __restrict__ N, int64_t lo, int64_t end, int32_t* __restrict__ pg)
+/* previous pair (same 32768-pair work block) with a strictly larger N: one CTA
+ * per work block builds a max-tree of the block's N in shared memory (internal
+ * nodes 1..WB-1; leaf i is N of the block's i-th pair, -1 past its end) and
+ * every pair searches it independently -- up the tree until a left sibling
+ * holds a larger maximum, then down that subtree keeping to the right.  Links
+ * are offsets from lo (-1 = none); lo is a work-block boundary. */
+constexpr int PREV_THREADS = 1024;
+constexpr int PREV_SMEM = KINC_SIM_WORK_BLOCK_SIZE * (int)sizeof(int32_t);
+
+__global__ void __launch_bounds__(PREV_THREADS) k_prev(const int32_t* __restrict__ N, int64_t lo, int64_t end,
+                                                       int32_t* __restrict__ pg)
 {
-   const int64_t wb = lo / KINC_SIM_WORK_BLOCK_SIZE + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-   int64_t b0 = wb * KINC_SIM_WORK_BLOCK_SIZE;
-   int64_t b1 = (wb + 1) * KINC_SIM_WORK_BLOCK_SIZE;
-   b0 = b0 < lo ? lo : b0;
-   b1 = b1 > end ? end : b1;
-   const int64_t o0 = b0 - lo;
-   for ( int64_t o = o0; o < b1 - lo; ++o )
+   constexpr int WB = KINC_SIM_WORK_BLOCK_SIZE;
+   extern __shared__ int32_t tree[];
+   const int64_t b0 = lo + (int64_t)blockIdx.x * WB;
+   const int64_t n64 = end - b0 < WB ? end - b0 : WB;
+   const int n = (int)n64;
+   const int32_t* Nb = N + (b0 - lo);
+   auto leaf = [&](int i) -> int32_t { return i < n ? Nb[i] : -1; };
+   auto node = [&](int k) -> int32_t { return k >= WB ? leaf(k - WB) : tree[k]; };
+
+   for ( int k = WB / 2 + threadIdx.x; k < WB; k += PREV_THREADS )
+      tree[k] = max(leaf(2 * k - WB), leaf(2 * k + 1 - WB));
+   __syncthreads();
+   for ( int level = WB / 4; level >= 1; level >>= 1 )
    {
-      const int32_t np = N[o];
-      int64_t c = o - 1;
-      while ( c >= o0 && N[c] <= np ) c = pg[c];
-      pg[o] = c >= o0 ? (int32_t)c : -1;
+      for ( int k = level + threadIdx.x; k < 2 * level; k += PREV_THREADS ) tree[k] = max(tree[2 * k], tree[2 * k + 1]);
+      __syncthreads();
    }
+   for ( int o = threadIdx.x; o < n; o += PREV_THREADS )
+   {
+      const int32_t v = Nb[o];
+      int ans = -1;
+      for ( int idx = WB + o; idx > 1; idx >>= 1 )
+      {
+         if ( !(idx & 1) || node(idx - 1) <= v ) continue;
+         int s = idx - 1;            /* the nearest range to the left with a larger N */
+         while ( s < WB ) s = node(2 * s + 1) > v ? 2 * s + 1 : 2 * s;
+         ans = s - WB;
+         break;
+      }
+      pg[(b0 - lo) + o] = ans >= 0 ? (int32_t)((b0 - lo) + ans) : -1;
+   }
+}
+
+/* the links of every work block of [lo, end) (lo a work-block boundary) */
+cudaError_t launch_prev(const int32_t* N, int64_t lo, int64_t end, int32_t* pg, cudaStream_t st)
+{
+   const cudaError_t attr = cudaFuncSetAttribute(k_prev, cudaFuncAttributeMaxDynamicSharedMemorySize, PREV_SMEM);
+   if ( attr != cudaSuccess ) return attr;
+   const int64_t nwb = (end - 1) / KINC_SIM_WORK_BLOCK_SIZE - lo / KINC_SIM_WORK_BLOCK_SIZE + 1;
+   k_prev<<<(int)nwb, PREV_THREADS, PREV_SMEM, st>>>(N, lo, end, pg);
+   return cudaGetLastError();
 }
 
 /* counting sort of a block's pairs by usable-sample count, largest first, so a
@@ -538,7 +573,7 @@ static KmPool km_pool_sizes(const kinc_sim_params& p, const SimKernel& k)
 /* ---------------------------------------------------------- launch shape */
 
 /* the shape measured best on the clustering workloads: 16-warp CTAs, rounds for GMM and no
- * clustering, free-running warps for K-means, GMM prefetch 8 samples ahead */
+ * clustering, free-running warps for K-means, the sweeps prefetching 8 samples ahead */
 static kinc_sim_launch default_launch(int clus)
 {
    kinc_sim_launch l {};
@@ -655,6 +690,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    dp.semantics = params->semantics; dp.rand_mode = params->rand_mode;
    dp.draws_per_pair = draws_per_pair(*params);
    dp.c2 = 2 * std::log(2.0f * M_PI);
+   dp.neg_zero = -0.0f;
    dp.P2 = next_pow2_host(std::max(S, 2));
    const bool need_sort = (params->clus_method != 0 && (params->pre_out || params->post_out))
                           || params->corr_method >= 1;
@@ -851,11 +887,12 @@ static int enqueue_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t*
    if ( (dp.corr == 0 || dp.corr == 2) && dp.semantics == 0 )
    {
       /* every Pearson run with the reference's packed-array reads needs the links */
-      const int64_t nwb = (end - 1) / KINC_SIM_WORK_BLOCK_SIZE - lo / KINC_SIM_WORK_BLOCK_SIZE + 1;
-      k_prev<<<(int)((nwb + 63) / 64), 64, 0, st>>>(ctx->d_N, lo, end, ctx->d_pg);
+      CK(launch_prev(ctx->d_N, lo, end, ctx->d_pg, st));
       ++launches;
    }
-   if ( ctx->d_order && size > TILE )
+   /* Pearson without clustering runs one thread per pair straight from the matrix (no tiles) */
+   const bool lanes = dp.clus == 0 && dp.corr == 0;
+   if ( ctx->d_order && size > TILE && !lanes )
    {
       const int64_t off = start - lo;
       const int g = (int)std::min<int64_t>((size + BIN_THREADS - 1) / BIN_THREADS, 1024);
@@ -880,6 +917,11 @@ static int enqueue_block(kinc_sim_ctx* ctx, int64_t start, int64_t size, int8_t*
    B.tiles = ctx->d_tiles;
    B.status = ctx->d_status;
    B.work = ctx->d_work;
+   if ( lanes )
+   {
+      CK(sim_launch_pearson_lanes(ctx->sms, st, dp, ctx->dd, B));
+   }
+   else
    {
       const SimKernel& k = ctx->kern;
       cudaError_t e = k.clus == 0 ? sim_launch_none(k, ctx->grid, ctx->smem_bytes, st, dp, ctx->dd, ctx->ds, B,
@@ -1085,7 +1127,7 @@ extern "C" int kinc_sim_autotune(kinc_sim_ctx* ctx, int64_t start, int64_t size,
       const kinc_sim_launch start_best = best;
       for ( int knob = 0; knob < 3; ++knob )
       {
-         if ( knob == 0 && ctx->params.clus_method != 1 ) continue;   /* prefetch: the GMM sweeps only */
+         if ( knob == 0 && ctx->params.clus_method == 0 ) continue;   /* prefetch: the clustering sweeps only */
          const int nv = knob == 0 ? 4 : knob == 1 ? 3 : 2;
          const kinc_sim_launch base = best;
          for ( int v = 0; v < nv; ++v )
@@ -1456,6 +1498,7 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    dp.semantics = params->semantics; dp.rand_mode = params->rand_mode;
    dp.draws_per_pair = draws_per_pair(*params);
    dp.c2 = 2 * std::log(2.0f * M_PI);
+   dp.neg_zero = -0.0f;
    dp.P2 = next_pow2_host(std::max(S, 2));
    const bool need_sort = (params->clus_method != 0 && (params->pre_out || params->post_out))
                           || params->corr_method >= 1;
@@ -1572,8 +1615,7 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    }
    if ( (dp.corr == 0 || dp.corr == 2) && dp.semantics == 0 )
    {
-      const int64_t nwb = (end - 1) / KINC_SIM_WORK_BLOCK_SIZE - lo / KINC_SIM_WORK_BLOCK_SIZE + 1;
-      k_prev<<<(int)((nwb + 63) / 64), 64, 0, st>>>(d_N, lo, end, d_pg);
+      CK(launch_prev(d_N, lo, end, d_pg, st));
    }
    CK(cudaGetLastError());
    DevData dd {};

@@ -45,7 +45,6 @@ constexpr int BN = 64;                /* pair-tile columns (genes y) */
 constexpr int NACC = 6;               /* Sxy, Sx, Sy, Sxx, Syy, n */
 constexpr int TMEM_COLS = 512;
 constexpr int STAGES = 3;
-constexpr int THREADS = 128;
 constexpr long long WAIT_CYCLES = 4ll << 30;  /* ~2 s of SM clock before a wait gives up */
 
 constexpr int ST_TIMEOUT = 10;        /* an mbarrier wait expired */
@@ -324,7 +323,7 @@ __global__ void k_tc_prep(const float* __restrict__ gem, int G, int S, int Gp, i
 
 struct TcArgs
 {
-   int I0;                            /* first row tile (blockIdx.y = I - I0, blockIdx.x = J) */
+   int I0;                            /* CUDA-core form: first row tile (blockIdx.y = I - I0, blockIdx.x = J) */
    int64_t xb;                        /* last row of the pair range */
    int G;
    int min_samples;
@@ -344,33 +343,139 @@ __device__ __forceinline__ float diff_of_products(float a, float b, float c, flo
    return dop + err;
 }
 
+/* MMAs of one K-chunk in ring stage `stage` (see the TF32 / 3xBF16 notes above); acc0: 0 on the
+ * tile's first chunk (the accumulators start from zero) */
 template <int MODE>
-__global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant__ TcMaps maps, TcArgs args)
+__device__ __forceinline__ void issue_chunk(uint32_t tmem, uint32_t stage, bool first)
+{
+   using C = Cfg<MODE>;
+   using L = Layout<MODE>;
+   const uint32_t ysb = stage + C::NMAT * L::XMAT;
+#pragma unroll
+   for ( int ks = 0; ks < C::BK / C::UMMA_K; ++ks )
+   {
+      const uint32_t koff = ks * C::UMMA_K * C::ELEM;   /* byte step along K inside the row */
+      const uint32_t acc = (!first || ks > 0) ? 1u : 0u;
+      if ( merged<MODE>() && MODE == 2 )
+      {
+         /* x side: 0 Ah, 1 Al, 2 Qh, 3 Ql, 4 M; y side in slots [Ql][Qh][Ah][M][Al] */
+         const uint64_t xah = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
+         const uint64_t xal = smem_desc<MODE>(stage + 1 * L::XMAT + koff);
+         const uint64_t xqh = smem_desc<MODE>(stage + 2 * L::XMAT + koff);
+         const uint64_t xql = smem_desc<MODE>(stage + 3 * L::XMAT + koff);
+         const uint64_t xm = smem_desc<MODE>(stage + 4 * L::XMAT + koff);
+         const uint64_t y_ql = smem_desc<MODE>(ysb + 0 * L::YMAT + koff);
+         const uint64_t y_qh_ah_m = smem_desc<MODE>(ysb + 1 * L::YMAT + koff);
+         const uint64_t y_ah_m_al = smem_desc<MODE>(ysb + 2 * L::YMAT + koff);
+         const uint64_t y_m = smem_desc<MODE>(ysb + 3 * L::YMAT + koff);
+         const uint64_t y_al = smem_desc<MODE>(ysb + 4 * L::YMAT + koff);
+         mma<MODE, 3 * BN>(tmem + 0, xah, y_ah_m_al, acc);      /* Sxy(hh) | Sx(h) | Sxy(hl) */
+         mma<MODE, 2 * BN>(tmem + 0, xal, y_ah_m_al, 1u);       /* += Sxy(lh) | Sx(l) */
+         mma<MODE, BN>(tmem + acc_col<MODE>(3), xqh, y_m, acc); /* Sxx */
+         mma<MODE, BN>(tmem + acc_col<MODE>(3), xql, y_m, 1u);
+         mma<MODE, 3 * BN>(tmem + acc_col<MODE>(4), xm, y_qh_ah_m, acc);   /* Syy(h) | Sy(h) | n */
+         mma<MODE, BN>(tmem + acc_col<MODE>(4), xm, y_ql, 1u);             /* Syy += l */
+         mma<MODE, BN>(tmem + acc_col<MODE>(2), xm, y_al, 1u);             /* Sy += l */
+      }
+      else if ( merged<MODE>() )
+      {
+         const uint64_t xa = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
+         const uint64_t xq = smem_desc<MODE>(stage + 1 * L::XMAT + koff);
+         const uint64_t xm = smem_desc<MODE>(stage + 2 * L::XMAT + koff);
+         const uint64_t y_q_a_m = smem_desc<MODE>(ysb + 0 * L::YMAT + koff);   /* [A2_y; A_y; M_y] */
+         const uint64_t y_a_m = smem_desc<MODE>(ysb + 1 * L::YMAT + koff);     /* [A_y; M_y] */
+         const uint64_t y_m = smem_desc<MODE>(ysb + 2 * L::YMAT + koff);       /* M_y */
+         mma<MODE, 2 * BN>(tmem + acc_col<MODE>(0), xa, y_a_m, acc);     /* Sxy | Sx */
+         mma<MODE, BN>(tmem + acc_col<MODE>(3), xq, y_m, acc);           /* Sxx */
+         mma<MODE, 3 * BN>(tmem + acc_col<MODE>(4), xm, y_q_a_m, acc);   /* Syy | Sy | n */
+      }
+      else if ( MODE == 1 )
+      {
+         /* x side: 0 A, 1 A2, 2 M; y side likewise */
+         const uint64_t xa = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
+         const uint64_t xq = smem_desc<MODE>(stage + 1 * L::XMAT + koff);
+         const uint64_t xm = smem_desc<MODE>(stage + 2 * L::XMAT + koff);
+         const uint64_t ya = smem_desc<MODE>(ysb + 0 * L::YMAT + koff);
+         const uint64_t yq = smem_desc<MODE>(ysb + 1 * L::YMAT + koff);
+         const uint64_t ym = smem_desc<MODE>(ysb + 2 * L::YMAT + koff);
+         mma<MODE>(tmem + 0 * BN, xa, ya, acc);   /* Sxy */
+         mma<MODE>(tmem + 1 * BN, xa, ym, acc);   /* Sx */
+         mma<MODE>(tmem + 2 * BN, xm, ya, acc);   /* Sy */
+         mma<MODE>(tmem + 3 * BN, xq, ym, acc);   /* Sxx */
+         mma<MODE>(tmem + 4 * BN, xm, yq, acc);   /* Syy */
+         mma<MODE>(tmem + 5 * BN, xm, ym, acc);   /* n */
+      }
+      else
+      {
+         /* 0 A_hi, 1 A_lo, 2 A2_hi, 3 A2_lo, 4 M */
+         uint64_t xd[5], yd[5];
+#pragma unroll
+         for ( int m = 0; m < 5; ++m )
+         {
+            xd[m] = smem_desc<MODE>(stage + m * L::XMAT + koff);
+            yd[m] = smem_desc<MODE>(ysb + m * L::YMAT + koff);
+         }
+         mma<MODE>(tmem + 0 * BN, xd[0], yd[0], acc);   /* Sxy: hi.hi + hi.lo + lo.hi */
+         mma<MODE>(tmem + 0 * BN, xd[0], yd[1], 1u);
+         mma<MODE>(tmem + 0 * BN, xd[1], yd[0], 1u);
+         mma<MODE>(tmem + 1 * BN, xd[0], yd[4], acc);   /* Sx */
+         mma<MODE>(tmem + 1 * BN, xd[1], yd[4], 1u);
+         mma<MODE>(tmem + 2 * BN, xd[4], yd[0], acc);   /* Sy */
+         mma<MODE>(tmem + 2 * BN, xd[4], yd[1], 1u);
+         mma<MODE>(tmem + 3 * BN, xd[2], yd[4], acc);   /* Sxx */
+         mma<MODE>(tmem + 3 * BN, xd[3], yd[4], 1u);
+         mma<MODE>(tmem + 4 * BN, xd[4], yd[2], acc);   /* Syy */
+         mma<MODE>(tmem + 4 * BN, xd[4], yd[3], 1u);
+         mma<MODE>(tmem + 5 * BN, xd[4], yd[4], acc);   /* n */
+      }
+   }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+/*
+ * Persistent form: one CTA per SM walks its share of the tile list (tile t = blockIdx.x,
+ * blockIdx.x + gridDim.x, ...; the host orders the list in bands of TILE_GROUP row tiles, column
+ * by column, so the CTAs running at one time share their x- and y-side operand panels in L2).
+ * Warp 0 streams the K-chunks of its tiles through the ring without stopping at tile boundaries;
+ * warp 1 issues a tile's MMAs once the epilogue has released TMEM from the previous tile and
+ * signals `tfull` when the accumulators are final; warps 2..9 (two per TMEM lane quarter, each
+ * half of the 64 columns) read them back, form r, write it and signal `tempty`.  So the next
+ * tile's operand loads overlap this tile's epilogue, and TMEM, barriers and the ring are set up
+ * once per CTA.  Every mbarrier wait is bounded: on expiry the CTA records an error, every role
+ * stops, the CTA drains its own copies (bounded), frees its TMEM and returns.
+ */
+constexpr int EPI_WARPS = 8;
+constexpr int TC_THREADS = (2 + EPI_WARPS) * 32;
+
+template <int MODE>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+   k_pearson_tc(const __grid_constant__ TcMaps maps, TcArgs args, const int2* __restrict__ tiles, int ntiles)
 {
    using C = Cfg<MODE>;
    using L = Layout<MODE>;
    extern __shared__ __align__(1024) unsigned char smem_raw[];
-   /* 1024-byte aligned ring (swizzle atoms), barriers after it */
    unsigned char* ring = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
    uint64_t* bars = (uint64_t*)(ring + L::RING);
-   uint32_t* tmem_holder = (uint32_t*)(bars + 2 * STAGES + 1);
+   uint32_t* tmem_holder = (uint32_t*)(bars + 2 * STAGES + 2);
    __shared__ int s_fail;
 
-   const int I = args.I0 + (int)blockIdx.y;
-   const int J = (int)blockIdx.x;
-   /* tiles entirely on or above the diagonal (y >= x) or past the range hold no pair */
-   const int64_t rowmax = (int64_t)(I + 1) * BM - 1;
-   const int64_t xmax = rowmax < args.xb ? rowmax : args.xb;
-   if ( (int64_t)J * BN >= xmax ) return;
-   /* a CTA that failed earlier in this launch stops the rest from starting */
-   if ( *(volatile int*)args.status != 0 ) return;
+   /* a CTA that failed earlier in this launch stops the rest from starting (decided once, for
+    * the whole CTA) */
+   if ( threadIdx.x == 0 ) s_fail = *(volatile int*)args.status != 0;
+   __syncthreads();
+   if ( s_fail ) return;
    const int warp = threadIdx.x >> 5;
    const int lane = threadIdx.x & 31;
-
    const uint32_t full0 = smem_u32(&bars[0]);
    const uint32_t empty0 = smem_u32(&bars[STAGES]);
-   const uint32_t done = smem_u32(&bars[2 * STAGES]);
+   const uint32_t tfull = smem_u32(&bars[2 * STAGES]);
+   const uint32_t tempty = smem_u32(&bars[2 * STAGES + 1]);
 
+   __syncthreads();                     /* every thread has read s_fail before it is reused */
    if ( threadIdx.x == 0 )
    {
       s_fail = 0;
@@ -379,10 +484,11 @@ __global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant
          mbar_init(full0 + 8 * s, 1);
          mbar_init(empty0 + 8 * s, 1);
       }
-      mbar_init(done, 1);
+      mbar_init(tfull, 1);
+      mbar_init(tempty, EPI_WARPS);
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
    }
-   if ( warp == 0 )
+   if ( warp == 1 )
    {
       asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
                    "r"(TMEM_COLS));
@@ -394,173 +500,140 @@ __global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant
    const uint32_t tmem = *tmem_holder;
 
    const int K = args.kchunks;
-   int issued = 0;                      /* TMA chunks issued (producer) */
-   if ( warp == 0 && lane == 0 )
+   int issued = 0;                      /* producer: TMA chunks issued */
+   if ( warp == 0 )
    {
-      /* ---- producer: TMA into the ring */
-      for ( int kc = 0; kc < K; ++kc )
+      if ( lane == 0 )
       {
-         const int s = kc % STAGES;
-         if ( kc >= STAGES && !mbar_wait(empty0 + 8 * s, ((kc / STAGES) - 1) & 1) )
+         /* ---- producer: the chunks of every tile of this CTA, back to back */
+         for ( int t = blockIdx.x; t < ntiles && !*(volatile int*)&s_fail; t += gridDim.x )
          {
-            atomicExch(&s_fail, 1);
-            break;
+            const int2 ij = tiles[t];
+            for ( int kc = 0; kc < K; ++kc, ++issued )
+            {
+               const int s = issued % STAGES;
+               if ( issued >= STAGES && !mbar_wait(empty0 + 8 * s, ((issued / STAGES) - 1) & 1) )
+               {
+                  atomicExch(&s_fail, 1);
+                  break;
+               }
+               if ( *(volatile int*)&s_fail ) break;
+               const uint32_t stage = smem_u32(ring + s * L::STAGE);
+               mbar_expect_tx(full0 + 8 * s, L::STAGE);
+               for ( int m = 0; m < C::NMAT; ++m )
+               {
+                  tma_load_2d(stage + m * L::XMAT, &maps.x[m], kc * C::BK, ij.x * BM, full0 + 8 * s);
+                  tma_load_2d(stage + C::NMAT * L::XMAT + yslot<MODE>(m) * L::YMAT, &maps.y[m], kc * C::BK,
+                              ij.y * BN, full0 + 8 * s);
+               }
+            }
          }
-         if ( *(volatile int*)&s_fail ) break;
-         const uint32_t stage = smem_u32(ring + s * L::STAGE);
-         mbar_expect_tx(full0 + 8 * s, L::STAGE);
-         for ( int m = 0; m < C::NMAT; ++m )
-         {
-            tma_load_2d(stage + m * L::XMAT, &maps.x[m], kc * C::BK, I * BM, full0 + 8 * s);
-            tma_load_2d(stage + C::NMAT * L::XMAT + yslot<MODE>(m) * L::YMAT, &maps.y[m], kc * C::BK, J * BN,
-                        full0 + 8 * s);
-         }
-         ++issued;
       }
    }
-   else if ( warp == 1 && lane == 0 )
+   else if ( warp == 1 )
    {
-      /* ---- MMA issuer */
-      for ( int kc = 0; kc < K; ++kc )
+      if ( lane == 0 )
       {
-         const int s = kc % STAGES;
-         if ( !mbar_wait(full0 + 8 * s, (kc / STAGES) & 1) )
+         /* ---- MMA issuer */
+         int used = 0, tl = 0;
+         for ( int t = blockIdx.x; t < ntiles && !*(volatile int*)&s_fail; t += gridDim.x, ++tl )
          {
-            atomicExch(&s_fail, 1);
+            if ( tl > 0 && !mbar_wait(tempty, (tl - 1) & 1) )
+            {
+               atomicExch(&s_fail, 1);
+               break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            bool ok = true;
+            for ( int kc = 0; kc < K; ++kc, ++used )
+            {
+               const int s = used % STAGES;
+               if ( !mbar_wait(full0 + 8 * s, (used / STAGES) & 1) )
+               {
+                  ok = false;
+                  break;
+               }
+               asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+               issue_chunk<MODE>(tmem, smem_u32(ring + s * L::STAGE), kc == 0);
+               mma_commit(empty0 + 8 * s);      /* frees the stage when these MMAs have read it */
+            }
+            if ( !ok )
+            {
+               atomicExch(&s_fail, 1);
+               break;
+            }
+            mma_commit(tfull);                  /* the tile's accumulators are final */
+         }
+      }
+   }
+   else
+   {
+      /* ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. (its quarter of the tile's rows) and
+       * columns 32 h .. 32 h + 31, h = (w - 2) / 4 */
+      const int quarter = warp & 3;
+      const int half = (warp - 2) >> 2;
+      int tl = 0;
+      for ( int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl )
+      {
+         /* one lane waits and the warp follows its verdict, so the warp stays converged for the
+          * .sync.aligned TMEM loads */
+         int go = 0;
+         if ( lane == 0 ) go = !*(volatile int*)&s_fail && mbar_wait(tfull, tl & 1);
+         go = __shfl_sync(0xffffffffu, go, 0);
+         if ( !go )
+         {
+            if ( lane == 0 ) atomicExch(&s_fail, 1);
             break;
          }
          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-         const uint32_t stage = smem_u32(ring + s * L::STAGE);
-         const uint32_t ysb = stage + C::NMAT * L::XMAT;
-         for ( int ks = 0; ks < C::BK / C::UMMA_K; ++ks )
+         const int2 ij = tiles[t];
+         const int row = quarter * 32 + lane;
+         const int64_t x = (int64_t)ij.x * BM + row;
+         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+         const int64_t pbase = x * (x - 1) / 2;
+#pragma unroll 1
+         for ( int c = 2 * half; c < 2 * half + 2; ++c )
          {
-            const uint32_t koff = ks * C::UMMA_K * C::ELEM;   /* byte step along K inside the row */
-            const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
-            if ( merged<MODE>() && MODE == 2 )
-            {
-               /* x side: 0 Ah, 1 Al, 2 Qh, 3 Ql, 4 M; y side in slots [Ql][Qh][Ah][M][Al] */
-               const uint64_t xah = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
-               const uint64_t xal = smem_desc<MODE>(stage + 1 * L::XMAT + koff);
-               const uint64_t xqh = smem_desc<MODE>(stage + 2 * L::XMAT + koff);
-               const uint64_t xql = smem_desc<MODE>(stage + 3 * L::XMAT + koff);
-               const uint64_t xm = smem_desc<MODE>(stage + 4 * L::XMAT + koff);
-               const uint64_t y_ql = smem_desc<MODE>(ysb + 0 * L::YMAT + koff);
-               const uint64_t y_qh_ah_m = smem_desc<MODE>(ysb + 1 * L::YMAT + koff);
-               const uint64_t y_ah_m_al = smem_desc<MODE>(ysb + 2 * L::YMAT + koff);
-               const uint64_t y_m = smem_desc<MODE>(ysb + 3 * L::YMAT + koff);
-               const uint64_t y_al = smem_desc<MODE>(ysb + 4 * L::YMAT + koff);
-               mma<MODE, 3 * BN>(tmem + 0, xah, y_ah_m_al, acc);      /* Sxy(hh) | Sx(h) | Sxy(hl) */
-               mma<MODE, 2 * BN>(tmem + 0, xal, y_ah_m_al, 1u);       /* += Sxy(lh) | Sx(l) */
-               mma<MODE, BN>(tmem + acc_col<MODE>(3), xqh, y_m, acc); /* Sxx */
-               mma<MODE, BN>(tmem + acc_col<MODE>(3), xql, y_m, 1u);
-               mma<MODE, 3 * BN>(tmem + acc_col<MODE>(4), xm, y_qh_ah_m, acc);   /* Syy(h) | Sy(h) | n */
-               mma<MODE, BN>(tmem + acc_col<MODE>(4), xm, y_ql, 1u);             /* Syy += l */
-               mma<MODE, BN>(tmem + acc_col<MODE>(2), xm, y_al, 1u);             /* Sy += l */
-            }
-            else if ( merged<MODE>() )
-            {
-               const uint64_t xa = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
-               const uint64_t xq = smem_desc<MODE>(stage + 1 * L::XMAT + koff);
-               const uint64_t xm = smem_desc<MODE>(stage + 2 * L::XMAT + koff);
-               const uint64_t y_q_a_m = smem_desc<MODE>(ysb + 0 * L::YMAT + koff);   /* [A2_y; A_y; M_y] */
-               const uint64_t y_a_m = smem_desc<MODE>(ysb + 1 * L::YMAT + koff);     /* [A_y; M_y] */
-               const uint64_t y_m = smem_desc<MODE>(ysb + 2 * L::YMAT + koff);       /* M_y */
-               mma<MODE, 2 * BN>(tmem + acc_col<MODE>(0), xa, y_a_m, acc);     /* Sxy | Sx */
-               mma<MODE, BN>(tmem + acc_col<MODE>(3), xq, y_m, acc);           /* Sxx */
-               mma<MODE, 3 * BN>(tmem + acc_col<MODE>(4), xm, y_q_a_m, acc);   /* Syy | Sy | n */
-            }
-            else if ( MODE == 1 )
-            {
-               /* x side: 0 A, 1 A2, 2 M; y side likewise */
-               const uint64_t xa = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
-               const uint64_t xq = smem_desc<MODE>(stage + 1 * L::XMAT + koff);
-               const uint64_t xm = smem_desc<MODE>(stage + 2 * L::XMAT + koff);
-               const uint64_t ya = smem_desc<MODE>(ysb + 0 * L::YMAT + koff);
-               const uint64_t yq = smem_desc<MODE>(ysb + 1 * L::YMAT + koff);
-               const uint64_t ym = smem_desc<MODE>(ysb + 2 * L::YMAT + koff);
-               mma<MODE>(tmem + 0 * BN, xa, ya, acc);   /* Sxy */
-               mma<MODE>(tmem + 1 * BN, xa, ym, acc);   /* Sx */
-               mma<MODE>(tmem + 2 * BN, xm, ya, acc);   /* Sy */
-               mma<MODE>(tmem + 3 * BN, xq, ym, acc);   /* Sxx */
-               mma<MODE>(tmem + 4 * BN, xm, yq, acc);   /* Syy */
-               mma<MODE>(tmem + 5 * BN, xm, ym, acc);   /* n */
-            }
-            else
-            {
-               /* 0 A_hi, 1 A_lo, 2 A2_hi, 3 A2_lo, 4 M */
-               uint64_t xd[5], yd[5];
+            float v[NACC][16];
 #pragma unroll
-               for ( int m = 0; m < 5; ++m )
+            for ( int a = 0; a < NACC; ++a ) tmem_ld16(lane_base + acc_col<MODE>(a) + c * 16, v[a]);
+            if constexpr ( sxy2_col<MODE>() >= 0 )
+            {
+               float w2[16];
+               tmem_ld16(lane_base + (uint32_t)sxy2_col<MODE>() + c * 16, w2);
+#pragma unroll
+               for ( int jj = 0; jj < 16; ++jj ) v[0][jj] += w2[jj];
+            }
+            if ( x < args.G )
+            {
+#pragma unroll
+               for ( int jj = 0; jj < 16; ++jj )
                {
-                  xd[m] = smem_desc<MODE>(stage + m * L::XMAT + koff);
-                  yd[m] = smem_desc<MODE>(ysb + m * L::YMAT + koff);
+                  const int64_t y = (int64_t)ij.y * BN + c * 16 + jj;
+                  if ( y >= x ) continue;
+                  const int64_t p = pbase + y;
+                  if ( p < args.start || p >= args.end ) continue;
+                  const float sxy = v[0][jj], sx = v[1][jj], sy = v[2][jj], sxx = v[3][jj], syy = v[4][jj];
+                  const float n = v[5][jj];
+                  float r = __int_as_float(0x7fc00000);
+                  if ( n >= (float)args.min_samples && n > 0.f )
+                  {
+                     const float num = diff_of_products(n, sxy, sx, sy);
+                     const float dx = diff_of_products(n, sxx, sx, sx);
+                     const float dy = diff_of_products(n, syy, sy, sy);
+                     r = num * rsqrtf(dx) * rsqrtf(dy);
+                  }
+                  args.out_corr[(p - args.start) * args.max_k] = r;
                }
-               mma<MODE>(tmem + 0 * BN, xd[0], yd[0], acc);   /* Sxy: hi.hi + hi.lo + lo.hi */
-               mma<MODE>(tmem + 0 * BN, xd[0], yd[1], 1u);
-               mma<MODE>(tmem + 0 * BN, xd[1], yd[0], 1u);
-               mma<MODE>(tmem + 1 * BN, xd[0], yd[4], acc);   /* Sx */
-               mma<MODE>(tmem + 1 * BN, xd[1], yd[4], 1u);
-               mma<MODE>(tmem + 2 * BN, xd[4], yd[0], acc);   /* Sy */
-               mma<MODE>(tmem + 2 * BN, xd[4], yd[1], 1u);
-               mma<MODE>(tmem + 3 * BN, xd[2], yd[4], acc);   /* Sxx */
-               mma<MODE>(tmem + 3 * BN, xd[3], yd[4], 1u);
-               mma<MODE>(tmem + 4 * BN, xd[4], yd[2], acc);   /* Syy */
-               mma<MODE>(tmem + 4 * BN, xd[4], yd[3], 1u);
-               mma<MODE>(tmem + 5 * BN, xd[4], yd[4], acc);   /* n */
             }
          }
-         mma_commit(empty0 + 8 * s);      /* frees the stage when these MMAs have read it */
+         /* every TMEM read of this warp is complete (tmem_ld16 waits): hand TMEM back */
+         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+         __syncwarp();
+         if ( lane == 0 ) mbar_arrive(tempty);
       }
-      mma_commit(done);                   /* all accumulators final */
    }
    __syncwarp();
-
-   /* ---- epilogue: every warp reads its 32 TMEM lanes (tile rows) */
-   bool ok = mbar_wait(done, 0);
-   if ( !ok ) atomicExch(&s_fail, 1);
-   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-   if ( ok && !*(volatile int*)&s_fail )
-   {
-      const int row = warp * 32 + lane;
-      const int64_t x = (int64_t)I * BM + row;
-      const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-      const int64_t pbase = x * (x - 1) / 2;
-      for ( int c = 0; c < BN / 16; ++c )
-      {
-         float v[NACC][16];
-#pragma unroll
-         for ( int a = 0; a < NACC; ++a ) tmem_ld16(lane_base + acc_col<MODE>(a) + c * 16, v[a]);
-         if constexpr ( sxy2_col<MODE>() >= 0 )
-         {
-            float w[16];
-            tmem_ld16(lane_base + (uint32_t)sxy2_col<MODE>() + c * 16, w);
-#pragma unroll
-            for ( int jj = 0; jj < 16; ++jj ) v[0][jj] += w[jj];
-         }
-         if ( x < args.G )
-         {
-#pragma unroll
-            for ( int jj = 0; jj < 16; ++jj )
-            {
-               const int64_t y = (int64_t)J * BN + c * 16 + jj;
-               if ( y >= x ) continue;
-               const int64_t p = pbase + y;
-               if ( p < args.start || p >= args.end ) continue;
-               const float sxy = v[0][jj], sx = v[1][jj], sy = v[2][jj], sxx = v[3][jj], syy = v[4][jj];
-               const float n = v[5][jj];
-               float r = __int_as_float(0x7fc00000);
-               if ( n >= (float)args.min_samples && n > 0.f )
-               {
-                  const float num = diff_of_products(n, sxy, sx, sy);
-                  const float dx = diff_of_products(n, sxx, sx, sx);
-                  const float dy = diff_of_products(n, syy, sy, sy);
-                  r = num * rsqrtf(dx) * rsqrtf(dy);
-               }
-               args.out_corr[(p - args.start) * args.max_k] = r;
-            }
-         }
-      }
-   }
 
    /* ---- teardown: on failure drain this CTA's copies (bounded), then free TMEM */
    __syncthreads();
@@ -569,9 +642,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant
       if ( threadIdx.x == 0 )
       {
          atomicCAS(args.status, 0, ST_TIMEOUT);
-         for ( int kc = (issued > STAGES ? issued - STAGES : 0); kc < issued; ++kc )
+         for ( int g = (issued > STAGES ? issued - STAGES : 0); g < issued; ++g )
          {
-            mbar_wait(full0 + 8 * (kc % STAGES), (kc / STAGES) & 1);
+            mbar_wait(full0 + 8 * (g % STAGES), (g / STAGES) & 1);
          }
       }
       __syncthreads();
@@ -579,7 +652,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_pearson_tc(const __grid_constant
    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
    __syncthreads();
    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-   if ( warp == 0 )
+   if ( warp == 1 )
    {
       asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
    }
@@ -816,6 +889,81 @@ void tc_release(TcState& t)
 {
    if ( t.ops ) cudaFree(t.ops);
    t.ops = nullptr;
+   if ( t.d_tiles ) cudaFree(t.d_tiles);
+   if ( t.h_tiles ) cudaFreeHost(t.h_tiles);
+   if ( t.tiles_ev ) cudaEventDestroy(t.tiles_ev);
+   t.d_tiles = nullptr;
+   t.h_tiles = nullptr;
+   t.tiles_ev = nullptr;
+   t.tiles_cap = 0;
+   t.tiles_ia = t.tiles_ib = -1;
+   t.tiles_xb = -1;
+}
+
+/*
+ * The tensor-core form's tile list for row tiles Ia..Ib (rows up to xb): every 128 x 64 tile
+ * (I, J) with a pair y < x, in bands of TILE_GROUP row tiles, column by column within a band and
+ * row by row within a column.  The persistent CTAs take the list round robin, so the tiles
+ * running at one time lie in one band and a few columns: TILE_GROUP x-side row panels and a few
+ * y-side column panels, which stay in L2 while the band's rows reuse them.  Built on the host into
+ * pinned memory and copied on the stream; the copy of the previous list must be complete before
+ * the host buffer is rewritten.
+ */
+constexpr int TILE_GROUP = 8;
+
+static cudaError_t tc_tile_list(TcState& t, int Ia, int Ib, int64_t xb, cudaStream_t st)
+{
+   if ( t.tiles_ia == Ia && t.tiles_ib == Ib && t.tiles_xb == xb ) return cudaSuccess;
+   auto jhi = [&](int I) {
+      const int64_t rowmax = std::min<int64_t>((int64_t)(I + 1) * BM - 1, xb);
+      return rowmax >= 1 ? (int)((rowmax - 1) / BN) : -1;   /* last column tile holding some y < x */
+   };
+   int64_t n = 0;
+   for ( int I = Ia; I <= Ib; ++I ) n += jhi(I) + 1;
+   if ( n > INT32_MAX ) return cudaErrorInvalidValue;
+   cudaError_t e;
+   if ( t.tiles_ev )
+   {
+      e = cudaEventSynchronize(t.tiles_ev);
+      if ( e != cudaSuccess ) return e;
+   }
+   else
+   {
+      e = cudaEventCreateWithFlags(&t.tiles_ev, cudaEventDisableTiming);
+      if ( e != cudaSuccess ) return e;
+   }
+   if ( n > t.tiles_cap )
+   {
+      /* the device list may still be read by an earlier launch on this stream */
+      e = cudaStreamSynchronize(st);
+      if ( e != cudaSuccess ) return e;
+      if ( t.d_tiles ) cudaFree(t.d_tiles);
+      if ( t.h_tiles ) cudaFreeHost(t.h_tiles);
+      t.d_tiles = nullptr;
+      t.h_tiles = nullptr;
+      t.tiles_cap = 0;
+      e = cudaMalloc(&t.d_tiles, (size_t)n * sizeof(int2));
+      if ( e != cudaSuccess ) return e;
+      e = cudaMallocHost(&t.h_tiles, (size_t)n * sizeof(int2));
+      if ( e != cudaSuccess ) return e;
+      t.tiles_cap = n;
+   }
+   int64_t k = 0;
+   for ( int b0 = Ia; b0 <= Ib; b0 += TILE_GROUP )
+   {
+      const int b1 = std::min(Ib, b0 + TILE_GROUP - 1);
+      for ( int J = 0; J <= jhi(b1); ++J )
+         for ( int I = b0; I <= b1; ++I )
+            if ( J <= jhi(I) ) t.h_tiles[k++] = make_int2(I, J);
+   }
+   t.ntiles = (int)k;
+   t.tiles_ia = Ia;
+   t.tiles_ib = Ib;
+   t.tiles_xb = xb;
+   if ( k == 0 ) return cudaSuccess;
+   e = cudaMemcpyAsync(t.d_tiles, t.h_tiles, (size_t)k * sizeof(int2), cudaMemcpyHostToDevice, st);
+   if ( e != cudaSuccess ) return e;
+   return cudaEventRecord(t.tiles_ev, st);
 }
 
 /* enqueue the pairs [start, start+size): K = 1, corr[.][0] = r, NaN elsewhere */
@@ -855,17 +1003,27 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
       k_pearson_simt<<<dim3((unsigned)Jn, (unsigned)(Ib - Ia + 1)), STHREADS, SIMT_SMEM, st>>>(
          (const float*)t.ops, t.Gp, t.Sp, a);
    }
-   else if ( t.mode == 1 )
-   {
-      const int smem = Layout<1>::SMEM;
-      cudaFuncSetAttribute(k_pearson_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      k_pearson_tc<1><<<dim3((unsigned)Jn, (unsigned)(Ib - Ia + 1)), THREADS, smem, st>>>(t.maps, a);
-   }
    else
    {
-      const int smem = Layout<2>::SMEM;
-      cudaFuncSetAttribute(k_pearson_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      k_pearson_tc<2><<<dim3((unsigned)Jn, (unsigned)(Ib - Ia + 1)), THREADS, smem, st>>>(t.maps, a);
+      const cudaError_t e = tc_tile_list(t, Ia, Ib, xb, st);
+      if ( e != cudaSuccess ) return e;
+      if ( t.ntiles == 0 ) return cudaGetLastError();
+      int sms = 0, dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      const int grid = std::max(1, std::min(sms, t.ntiles));
+      if ( t.mode == 1 )
+      {
+         const int smem = Layout<1>::SMEM;
+         cudaFuncSetAttribute(k_pearson_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+         k_pearson_tc<1><<<grid, TC_THREADS, smem, st>>>(t.maps, a, t.d_tiles, t.ntiles);
+      }
+      else
+      {
+         const int smem = Layout<2>::SMEM;
+         cudaFuncSetAttribute(k_pearson_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+         k_pearson_tc<2><<<grid, TC_THREADS, smem, st>>>(t.maps, a, t.d_tiles, t.ntiles);
+      }
    }
    if ( launches ) *launches += 2;
    (void)S;

@@ -27,6 +27,14 @@ struct TcState
    int Gp = 0, Sp = 0;                /* padded genes (x128) and samples (x64) */
    void* ops = nullptr;               /* operand planes [Gp][Sp] */
    kinc_tc::TcMaps maps;
+   /* tensor-core tile list of the last range enqueued (row tiles tiles_ia..tiles_ib, rows to tiles_xb) */
+   int2* d_tiles = nullptr;
+   int2* h_tiles = nullptr;           /* pinned */
+   int64_t tiles_cap = 0;
+   int ntiles = 0;
+   int tiles_ia = -1, tiles_ib = -1;
+   int64_t tiles_xb = -1;
+   cudaEvent_t tiles_ev = nullptr;    /* the list's host-to-device copy */
 };
 
 /* centred/masked operands and their tensor maps for d_gem [G][S] */

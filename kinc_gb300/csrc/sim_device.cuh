@@ -30,6 +30,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "kinc_f2.h"
 #include "kinc_fmath.h"
 
 namespace kinc {
@@ -77,6 +78,10 @@ constexpr int KM_RING = KINC_KM_RING;
 #ifndef KINC_STORE_LOGGAMMA
 #define KINC_STORE_LOGGAMMA 0
 #endif
+/* 1: GMM fits with K >= 2 pair their components in packed FP32 registers (gmm_fit_packed) */
+#ifndef KINC_GMM_PACKED
+#define KINC_GMM_PACKED 1
+#endif
 #ifndef KINC_STORE_GAMMA
 #define KINC_STORE_GAMMA 1          /* 1: keep the M1 responsibilities for M2 instead of recomputing them */
 #endif
@@ -105,6 +110,7 @@ struct DevParams
    int32_t rounds;                  /* 1: a CTA's warps take their tiles together, round by round */
    int32_t prefetch;                /* samples ahead the EM sweeps prefetch into L2 (0: none) */
    int32_t km_dmax, km_tmax;        /* K-means task pool: draws per pair, tasks per tile */
+   float neg_zero;                  /* -0.0f, a value the compiler cannot see (kinc_f2.h: mulz) */
 };
 
 struct DevData
@@ -155,7 +161,8 @@ struct DevBlock
 __device__ __forceinline__ void pair_xy(int64_t p, int32_t& x, int32_t& y)
 {
    /* inverse of p = x(x-1)/2 + y, x > y >= 0 (src/core/pairwise_index.cpp:32-57) */
-   int64_t xx = (int64_t)((1.0 + sqrt(1.0 + 8.0 * (double)p)) * 0.5);
+   /* float estimate (GB300's FP64 rate is a small fraction of FP32), corrected exactly below */
+   int64_t xx = (int64_t)((1.0f + sqrtf(1.0f + 8.0f * (float)p)) * 0.5f);
    while ( xx * (xx - 1) / 2 > p ) --xx;
    while ( (xx + 1) * xx / 2 <= p ) ++xx;
    x = (int32_t)xx;
@@ -276,24 +283,35 @@ __device__ inline int warp_fetch(const DevParams& P, const DevData& D, int32_t x
 {
    const float* g1 = D.gem + (size_t)x * P.S;
    const float* g2 = D.gem + (size_t)y * P.S;
+   constexpr int CH = 4;            /* 32-sample chunks whose loads are in flight together */
    int n = 0;
-   for ( int base = 0; base < P.S; base += 32 )
+   for ( int base = 0; base < P.S; base += CH * 32 )
    {
-      const int s = base + lane;
-      bool use = false;
-      float v1 = 0.f, v2 = 0.f;
-      if ( s < P.S )
+      float v1[CH], v2[CH];
+#pragma unroll
+      for ( int u = 0; u < CH; ++u )
       {
-         v1 = g1[s];
-         v2 = g2[s];
-         const bool nanb = isnan(v1) || isnan(v2);
-         const bool low = v1 < P.min_expr || v2 < P.min_expr;
-         lbl[s * STR + j] = nanb ? (int8_t)-9 : (low ? (int8_t)-6 : (int8_t)0);
-         use = !nanb && !low;
+         const int s = base + u * 32 + lane;
+         v1[u] = s < P.S ? __ldg(g1 + s) : 0.f;
+         v2[u] = s < P.S ? __ldg(g2 + s) : 0.f;
       }
-      const unsigned bal = __ballot_sync(0xffffffffu, use);
-      if ( use ) X[(n + __popc(bal & lanemask_lt())) * STR + j] = make_float2(v1, v2);
-      n += __popc(bal);
+#pragma unroll
+      for ( int u = 0; u < CH; ++u )
+      {
+         if ( base + u * 32 >= P.S ) break;   /* uniform over the warp */
+         const int s = base + u * 32 + lane;
+         bool use = false;
+         if ( s < P.S )
+         {
+            const bool nanb = isnan(v1[u]) || isnan(v2[u]);
+            const bool low = v1[u] < P.min_expr || v2[u] < P.min_expr;
+            lbl[s * STR + j] = nanb ? (int8_t)-9 : (low ? (int8_t)-6 : (int8_t)0);
+            use = !nanb && !low;
+         }
+         const unsigned bal = __ballot_sync(0xffffffffu, use);
+         if ( use ) X[(n + __popc(bal & lanemask_lt())) * STR + j] = make_float2(v1[u], v2[u]);
+         n += __popc(bal);
+      }
    }
    __syncwarp();
    return n;
@@ -762,6 +780,322 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
             v = log_mvn(xv.x, xv.y, m0[k], m1[k], ia[k], ib[k], ic[k], nrm[k]) + (-logpx);
             if ( !converged ) v = kinc_expf(v);
          }
+         if ( max_g < v )
+         {
+            max_k = k;
+            max_g = v;
+         }
+      }
+      wl[i * TILE] = (int8_t)max_k;
+      E += max_k >= 0 ? kinc_logf(max_g) : __int_as_float(0x7fc00000);
+   }
+   out_E = E;
+   return true;
+}
+
+/* calcLogMvNorm for one component (float) or two (F2), the operations of log_mvn; every product
+ * that feeds a sum goes through mulz, so it is rounded on its own as in the reference */
+template <class T>
+__device__ __forceinline__ T log_mvn_t(T x0, T x1, T m0, T m1, T a, T b, T c, T nrm, T z)
+{
+   const T xm0 = x0 - m0;
+   const T xm1 = x1 - m1;
+   const T b0 = mulz(a, xm0, z) + mulz(b, xm1, z);
+   const T b1 = mulz(b, xm0, z) + mulz(c, xm1, z);
+   const T dot = mulz(xm0, b0, z) + mulz(xm1, b1, z);
+   return nrm - mulz(cst<T>(0.5f), dot, z);
+}
+
+/* K per-component floats held as K/2 packed pairs (components 2q, 2q+1) and, for odd K, one
+ * float (component K-1); element access with a compile-time k reads or writes half a register */
+template <int K>
+struct PArr
+{
+   static constexpr int NP = K / 2;
+   F2 p[NP > 0 ? NP : 1];
+   float o;
+   __device__ __forceinline__ float get(int k) const
+   {
+      if ( k == K - 1 && (K & 1) ) return o;
+      return (k & 1) ? hi(p[k >> 1]) : lo(p[k >> 1]);
+   }
+   __device__ __forceinline__ void set(int k, float v)
+   {
+      if ( k == K - 1 && (K & 1) )
+         o = v;
+      else if ( k & 1 )
+         p[k >> 1] = f2(lo(p[k >> 1]), v);
+      else
+         p[k >> 1] = f2(v, hi(p[k >> 1]));
+   }
+   __device__ __forceinline__ void fill(float v)
+   {
+#pragma unroll
+      for ( int q = 0; q < NP; ++q ) p[q] = f2(v);
+      o = v;
+   }
+};
+
+/*
+ * gmm_fit with the mixture components paired in packed FP32 registers: components (2q, 2q+1)
+ * share one F2 for every per-component value of the three EM passes, and an odd last component
+ * runs in plain floats.  Every per-component operation is the one gmm_fit performs, on each half,
+ * every accumulator is still summed in sample order, and the cross-component steps (maximum,
+ * the log-sum-exp sum in component order, the E-step's log) stay scalar, so the results are
+ * gmm_fit's bit for bit with about half the floating-point instructions issued.
+ * Responsibilities are kept between M1 and M2 as gmm_fit keeps them, laid out per sample as
+ * [pair q][lane][2] followed by the odd component's [lane] (KT x 32 floats per sample as before).
+ */
+template <int KT, bool OCL>
+__device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* wl, int N, LaneRng& rng, double c2,
+                               float& out_logL, float& out_E, unsigned long long& units, int pd, float neg_zero)
+{
+   static_assert(KT >= 2, "one component has nothing to pair");
+   constexpr int K = KT;
+   constexpr int NP = KT / 2;
+   constexpr bool ODD = (KT & 1) != 0;
+   constexpr int GS = KT * TILE;               /* floats of gam per sample */
+   const int lane = threadIdx.x & 31;
+   /* gam = slot base + lane: pair q of sample i at base + i*GS + q*64 + 2*lane, the odd
+    * component at base + i*GS + NP*64 + lane */
+   float* gpair = gam + lane;
+   float* godd = gam + NP * 2 * TILE;
+   const F2 z = f2(neg_zero);
+
+   PArr<K> m0, m1, ia, ib, ic, nrm, logpi;
+   if ( rng.mode == 1 ) rng.lcg = 1;
+   {
+      float a0, b0, c0, n0;
+      prepare_cov<OCL>(1.f, 0.f, 1.f, c2, a0, b0, c0, n0);
+      ia.fill(a0); ib.fill(b0); ic.fill(c0); nrm.fill(n0);
+      logpi.fill(kinc_logf(1.0f / K));
+#pragma unroll
+      for ( int k = 0; k < K; ++k )
+      {
+         const int ii = rng.next() % N;
+         const float2 xv = X[ii * TILE];
+         m0.set(k, xv.x);
+         m1.set(k, xv.y);
+      }
+   }
+
+   float prevL = -INFINITY;
+   float curL = -INFINITY;
+   bool converged = false;
+   for ( int t = 0; t < 100; ++t )
+   {
+      units += (unsigned long long)N * K;
+
+      /* ---- E step */
+      float logL = 0.0f;
+      PArr<K> maxG;
+      maxG.fill(-INFINITY);
+      float2 xn = X[0];
+      for ( int i = 0; i < N; ++i )
+      {
+         const float2 xv = xn;
+         if ( i + 1 < N ) xn = X[(i + 1) * TILE];
+         if ( pd > 0 && i + pd < N ) prefetch_l2(&X[(i + pd) * TILE]);
+         const F2 x0 = f2(xv.x), x1 = f2(xv.y);
+         F2 lg[NP], lp[NP];
+         float lgo = 0.f, lpo = 0.f;
+         float m = -INFINITY;
+#pragma unroll
+         for ( int q = 0; q < NP; ++q )
+         {
+            lg[q] = log_mvn_t(x0, x1, m0.p[q], m1.p[q], ia.p[q], ib.p[q], ic.p[q], nrm.p[q], z);
+            lp[q] = logpi.p[q] + lg[q];
+            float a, b;
+            split(lp[q], a, b);
+            if ( a > m ) m = a;
+            if ( b > m ) m = b;
+         }
+         if ( ODD )
+         {
+            lgo = log_mvn(xv.x, xv.y, m0.o, m1.o, ia.o, ib.o, ic.o, nrm.o);
+            lpo = logpi.o + lgo;
+            if ( lpo > m ) m = lpo;
+         }
+         float sum = 0.0f;
+         const F2 mm = f2(m);
+#pragma unroll
+         for ( int q = 0; q < NP; ++q )
+         {
+            float a, b;
+            split(kinc_expf2(lp[q] - mm), a, b);
+            sum += a;
+            sum += b;
+         }
+         if ( ODD ) sum += kinc_expf(lpo - m);
+         const float logpx = m + kinc_logf(sum);
+         logL += logpx;
+         lpx[i * TILE] = logpx;
+         const F2 nl = f2(-logpx);
+#pragma unroll
+         for ( int q = 0; q < NP; ++q )
+         {
+            float a, b, ga, gb;
+            split(lg[q] + nl, a, b);
+            split(maxG.p[q], ga, gb);
+            if ( a > ga ) ga = a;
+            if ( b > gb ) gb = b;
+            maxG.p[q] = f2(ga, gb);
+         }
+         if ( ODD )
+         {
+            const float v = lgo + (-logpx);
+            if ( v > maxG.o ) maxG.o = v;
+         }
+      }
+      prevL = curL;
+      curL = logL;
+      if ( fabsf(curL - prevL) < 1e-8f )
+      {
+         converged = true;
+         break;
+      }
+
+      /* ---- M step, pass 1: logGamma sums and mean sums */
+      PArr<K> nm0, nm1, Gam;
+      {
+         PArr<K> sG;
+         sG.fill(0.f);
+         nm0.fill(0.f);
+         nm1.fill(0.f);
+         xn = X[0];
+         float ln = lpx[0];
+         for ( int i = 0; i < N; ++i )
+         {
+            const float2 xv = xn;
+            const float logpx = ln;
+            if ( i + 1 < N )
+            {
+               xn = X[(i + 1) * TILE];
+               ln = lpx[(i + 1) * TILE];
+            }
+            if ( pd > 0 && i + pd < N )
+            {
+               prefetch_l2(&X[(i + pd) * TILE]);
+               prefetch_l2(&lpx[(i + pd) * TILE]);
+            }
+            const F2 x0 = f2(xv.x), x1 = f2(xv.y), nl = f2(-logpx);
+#pragma unroll
+            for ( int q = 0; q < NP; ++q )
+            {
+               const F2 lgk = log_mvn_t(x0, x1, m0.p[q], m1.p[q], ia.p[q], ib.p[q], ic.p[q], nrm.p[q], z) + nl;
+               sG.p[q] += kinc_expf2(lgk - maxG.p[q]);
+               const F2 g = kinc_expf2(lgk);
+               *reinterpret_cast<unsigned long long*>(gpair + i * GS + q * 2 * TILE) = g.v;
+               nm0.p[q] += mulz(g, x0, z);
+               nm1.p[q] += mulz(g, x1, z);
+            }
+            if ( ODD )
+            {
+               const float lgk = log_mvn(xv.x, xv.y, m0.o, m1.o, ia.o, ib.o, ic.o, nrm.o) + (-logpx);
+               sG.o += kinc_expf(lgk - maxG.o);
+               const float g = kinc_expf(lgk);
+               godd[i * GS] = g;
+               nm0.o += g * xv.x;
+               nm1.o += g * xv.y;
+            }
+         }
+         float logGamma[K];
+         float mx = -INFINITY;
+#pragma unroll
+         for ( int k = 0; k < K; ++k )
+         {
+            logGamma[k] = maxG.get(k) + kinc_logf(sG.get(k));
+            const float arg = logpi.get(k) + logGamma[k];
+            if ( arg > mx ) mx = arg;
+         }
+         float s = 0.f;
+#pragma unroll
+         for ( int k = 0; k < K; ++k ) s += kinc_expf((logpi.get(k) + logGamma[k]) - mx);
+         const float lgs = mx + kinc_logf(s);
+#pragma unroll
+         for ( int k = 0; k < K; ++k )
+         {
+            logpi.set(k, logpi.get(k) + (logGamma[k] - lgs));
+            const float G = kinc_expf(logGamma[k]);
+            Gam.set(k, G);
+            const float sc = 1.0f / G;
+            nm0.set(k, nm0.get(k) * sc);
+            nm1.set(k, nm1.get(k) * sc);
+         }
+      }
+
+      /* ---- M step, pass 2: covariance sums around the new means */
+      PArr<K> s00, s01, s11;
+      s00.fill(0.f);
+      s01.fill(0.f);
+      s11.fill(0.f);
+      xn = X[0];
+      for ( int i = 0; i < N; ++i )
+      {
+         const float2 xv = xn;
+         if ( i + 1 < N ) xn = X[(i + 1) * TILE];
+         if ( pd > 0 && i + pd < N )
+         {
+            prefetch_l2(&X[(i + pd) * TILE]);
+#pragma unroll
+            for ( int q = 0; q < NP; ++q ) prefetch_l2(gpair + (i + pd) * GS + q * 2 * TILE);
+            if ( ODD ) prefetch_l2(godd + (i + pd) * GS);
+         }
+         const F2 x0 = f2(xv.x), x1 = f2(xv.y);
+#pragma unroll
+         for ( int q = 0; q < NP; ++q )
+         {
+            F2 g;
+            g.v = *reinterpret_cast<const unsigned long long*>(gpair + i * GS + q * 2 * TILE);
+            const F2 xm0 = x0 - nm0.p[q];
+            const F2 xm1 = x1 - nm1.p[q];
+            s00.p[q] += mulz(g, xm0 * xm0, z);
+            s01.p[q] += mulz(g, xm0 * xm1, z);
+            s11.p[q] += mulz(g, xm1 * xm1, z);
+         }
+         if ( ODD )
+         {
+            const float g = godd[i * GS];
+            const float xm0 = xv.x - nm0.o;
+            const float xm1 = xv.y - nm1.o;
+            s00.o += g * (xm0 * xm0);
+            s01.o += g * (xm0 * xm1);
+            s11.o += g * (xm1 * xm1);
+         }
+      }
+      bool ok = true;
+      const bool last = t == 99;
+#pragma unroll
+      for ( int k = 0; k < K; ++k )
+      {
+         const float sc = 1.0f / Gam.get(k);
+         float a, b, c, n;
+         ok = prepare_cov<OCL>(s00.get(k) * sc, s01.get(k) * sc, s11.get(k) * sc, c2, a, b, c, n) && ok;
+         if ( !last )
+         {
+            m0.set(k, nm0.get(k));
+            m1.set(k, nm1.get(k));
+            ia.set(k, a); ib.set(k, b); ic.set(k, c); nrm.set(k, n);
+         }
+      }
+      if ( !ok ) return false;
+   }
+
+   /* ---- calcLabels + calcEntropy, as gmm_fit */
+   out_logL = curL;
+   float E = 0.f;
+   for ( int i = 0; i < N; ++i )
+   {
+      const float2 xv = X[i * TILE];
+      const float logpx = lpx[i * TILE];
+      int max_k = -1;
+      float max_g = -INFINITY;
+#pragma unroll
+      for ( int k = 0; k < K; ++k )
+      {
+         float v = log_mvn(xv.x, xv.y, m0.get(k), m1.get(k), ia.get(k), ib.get(k), ic.get(k), nrm.get(k)) +
+                   (-logpx);
+         if ( !converged ) v = kinc_expf(v);
          if ( max_g < v )
          {
             max_k = k;

@@ -72,6 +72,17 @@ struct PackedCursor
    }
 };
 
+/* the closing formula of Pearson::computeCluster (pairwise_pearson.cpp:44-51): NaN below min_samples */
+__device__ __forceinline__ float pearson_value(const DevParams& P, int n, float sumx, float sumy, float sumx2,
+                                               float sumy2, float sumxy)
+{
+   if ( n >= P.min_samples )
+   {
+      return (n * sumxy - sumx * sumy) / sqrtf((n * sumx2 - sumx * sumx) * (n * sumy2 - sumy * sumy));
+   }
+   return __int_as_float(0x7fc00000);
+}
+
 /* Pearson::computeCluster for this lane's pair (pairwise_pearson.cpp:12-52); X and lbl step
  * by STR per sample (TILE: the tile's interleaved arrays, 1: a pair's own arrays). */
 template <int STR = TILE>
@@ -85,11 +96,14 @@ __device__ inline float lane_pearson(const DevParams& P, const DevData& D, const
       /* positions i < N read the pair's own packed array at i; positions i >= N
        * read what the last earlier pair of the work block with more than i
        * usable samples left there (zero if none) */
+#pragma unroll 4
       for ( int i = 0; i < N; ++i )
       {
-         if ( lbl[i * STR] == k )
+         /* both loads unconditional (X holds N packed points), so several samples are in flight */
+         const int8_t l = lbl[i * STR];
+         const float2 v = X[i * STR];
+         if ( l == k )
          {
-            const float2 v = X[i * STR];
             sumx += v.x; sumy += v.y; sumx2 += v.x * v.x; sumy2 += v.y * v.y; sumxy += v.x * v.y;
             ++n;
          }
@@ -128,11 +142,7 @@ __device__ inline float lane_pearson(const DevParams& P, const DevData& D, const
          }
       }
    }
-   if ( n >= P.min_samples )
-   {
-      return (n * sumxy - sumx * sumy) / sqrtf((n * sumx2 - sumx * sumx) * (n * sumy2 - sumy * sumy));
-   }
-   return __int_as_float(0x7fc00000);
+   return pearson_value(P, n, sumx, sumy, sumx2, sumy2, sumxy);
 }
 
 /* computeBIC / computeICL (pairwise_clustering.cpp:155-172): log of the int N
@@ -163,7 +173,11 @@ __device__ __forceinline__ bool lane_fit(const DevParams& P, const float2* X, co
 {
    if ( CLUS == 1 || CLUS == 3 )
    {
-      return gmm_fit<KT, CLUS == 3>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units, pbuf, P.prefetch);
+      if constexpr ( KINC_GMM_PACKED && KT >= 2 && KINC_STATIC_K && KINC_STORE_GAMMA && !KINC_STORE_LOGGAMMA &&
+                     !KINC_GMM_PARAMS_SMEM )
+         return gmm_fit_packed<KT, CLUS == 3>(X, lpx, gam, wl, N, rng, P.c2, logL, E, units, P.prefetch, P.neg_zero);
+      else
+         return gmm_fit<KT, CLUS == 3>(X, lpx, gam, wl, N, K, rng, P.c2, logL, E, units, pbuf, P.prefetch);
    }
 #if KINC_KMEANS_PIPELINE
 #if KINC_KMEANS_LANE_MAJOR
@@ -459,6 +473,9 @@ SimKernel sim_kernel_select(int clus, int max_k);
 cudaError_t sim_kernel_launch_any(const SimKernel& k, int grid, int smem, cudaStream_t st, const DevParams& P,
                                   const DevData& D, const DevScratch& W, const DevBlock& B, int smem_sort);
 SimKernel sim_kernel_none();
+/* Pearson without clustering, one thread per pair (sim_none.cu) */
+cudaError_t sim_launch_pearson_lanes(int sms, cudaStream_t st, const DevParams& P, const DevData& D,
+                                     const DevBlock& B);
 SimKernel sim_kernel_gmm(int max_k, bool opencl);
 SimKernel sim_kernel_kmeans(int max_k);
 cudaError_t sim_launch_none(const SimKernel& k, int grid, int smem, cudaStream_t st, const DevParams& P,

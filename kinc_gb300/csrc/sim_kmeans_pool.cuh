@@ -117,6 +117,7 @@ __device__ int kmeans_pool(const DevParams& P, const DevData& D, const float2* X
    const int kmin = P.min_k, kmax = P.max_k;
    const int nK = kmax - kmin + 1;
    const bool qual = lane < npairs && myN >= P.min_samples;
+   const int pd = P.prefetch;          /* samples ahead the sweeps prefetch into L2 (0: none) */
 
    /* the pair's rand() draws, in the reference's order (the LCG restarts at every fit) */
    if ( qual )
@@ -195,6 +196,7 @@ __device__ int kmeans_pool(const DevParams& P, const DevData& D, const float2* X
          {
             const float2 xv = xn;
             if ( i + 1 < lim ) xn = X[(i + 1) * TILE + j];
+            if ( pd > 0 && i + pd < lim ) prefetch_l2(&X[(i + pd) * TILE + j]);
             float md;
             const int min_k = km_assign<KT>(xv.x, xv.y, mu0, mu1, K, md);
             yb[i * TILE] = (int8_t)min_k;
@@ -311,6 +313,7 @@ __device__ int kmeans_pool(const DevParams& P, const DevData& D, const float2* X
          if ( i < lim )
          {
             const float2 xv = X[i * TILE + c.j];
+            if ( pd > 0 && i + pd < lim ) prefetch_l2(&X[(i + pd) * TILE + c.j]);
             float md;
             const int l = km_assign<KT>(xv.x, xv.y, a0, a1, c.K, md);
             float c0 = 0.f, c1 = 0.f;
