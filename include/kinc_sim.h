@@ -190,7 +190,10 @@ int32_t kinc_sim_last_launch_count(const kinc_sim_ctx* ctx);
  *   rounds         1: a CTA's warps take their 32-pair tiles together, round by
  *                  round (they then run the same code region at the same time);
  *                  0: every warp takes its next tile as soon as it is done
- *   prefetch       0, 4, 8 or 16: samples ahead the GMM sweeps prefetch into L2
+ *   prefetch       0, 4, 8 or 16: samples ahead the clustering sweeps (GMM EM passes,
+ *                  K-means Lloyd and log-likelihood passes) prefetch into L2
+ * Pearson without clustering (clusmethod none, corrmethod pearson) runs one thread
+ * per pair and takes no shape.
  */
 typedef struct kinc_sim_launch
 {
@@ -215,7 +218,7 @@ int kinc_sim_set_launch(kinc_sim_ctx* ctx, const kinc_sim_launch* launch);
  * Pick the launch shape by timing: the pairs [start, start + size) (size is
  * capped at kinc_sim_max_device_block) run once per candidate on the context's
  * stream, timed with CUDA events, in a coordinate descent from the current
- * shape over prefetch (GMM only), warps_per_cta and rounds; the fastest is
+ * shape over prefetch (clustering only), warps_per_cta and rounds; the fastest is
  * applied.  With use_cache, the shape is first looked up -- and afterwards
  * stored -- in a small text cache keyed by the clustering and correlation
  * arguments, max_clusters, the sample count rounded up to a power of two and
@@ -227,6 +230,16 @@ int kinc_sim_set_launch(kinc_sim_ctx* ctx, const kinc_sim_launch* launch);
  */
 int kinc_sim_autotune(kinc_sim_ctx* ctx, int64_t start, int64_t size, int32_t use_cache, kinc_sim_launch* chosen,
                       kinc_sim_tune_entry* entries, int32_t cap, int32_t* n);
+
+/*
+ * Dense tcgen05 MMA rate of the current device, in TFLOP/s, for the operand type of
+ * precision 1 (TF32) or 2 (BF16): one CTA per SM issuing 128 x 256 MMAs back to back
+ * on operands resident in shared memory, timed with CUDA events (best of two after a
+ * warm-up).  The ceiling the tensor-core Pearson form is measured against.  No
+ * counterpart in the reference (its OpenCL worker has no tensor-core path).
+ * Synchronises the device.
+ */
+int kinc_sim_tensor_peak(int32_t precision, double* tflops);
 
 /* Work done since the last reset: out[0] = clustering model units (sum over
  * fits of iterations x N x K), out[1] = fits run, out[2..3] reserved.

@@ -56,6 +56,7 @@ _VP = ctypes.c_void_p
 _I64 = ctypes.c_int64
 _I32 = ctypes.c_int32
 SIGNATURES = {
+    "kinc_sim_tensor_peak": (ctypes.c_int, [_I32, ctypes.POINTER(ctypes.c_double)]),
     "kinc_sim_params_default": (ctypes.c_int, [ctypes.POINTER(SimParams)]),
     "kinc_sim_create": (ctypes.c_int, [_VP, _I32, _I32, ctypes.POINTER(SimParams), ctypes.POINTER(_VP)]),
     "kinc_sim_destroy": (None, [_VP]),

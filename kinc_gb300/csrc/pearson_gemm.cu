@@ -227,18 +227,20 @@ __device__ __forceinline__ void mma_commit(uint32_t bar)
                 : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v)
+/* 16 consecutive TMEM columns of this warp's 32 lanes into r (asynchronous: tmem_wait_ld before use) */
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t* r)
 {
-   uint32_t r[16];
    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15},"
                 " [%16];"
                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
                   "=r"(r[15])
                 : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld()
+{
    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-   for ( int i = 0; i < 16; ++i ) v[i] = __uint_as_float(r[i]);
 }
 
 /* ------------------------------------------------------------ kernels */
@@ -594,15 +596,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll 1
          for ( int c = 2 * half; c < 2 * half + 2; ++c )
          {
+            /* all of the chunk's accumulators in flight at once, then one wait */
+            uint32_t u[NACC + 1][16];
+#pragma unroll
+            for ( int a = 0; a < NACC; ++a ) tmem_ld16_async(lane_base + acc_col<MODE>(a) + c * 16, u[a]);
+            if constexpr ( sxy2_col<MODE>() >= 0 ) tmem_ld16_async(lane_base + (uint32_t)sxy2_col<MODE>() + c * 16, u[NACC]);
+            tmem_wait_ld();
             float v[NACC][16];
 #pragma unroll
-            for ( int a = 0; a < NACC; ++a ) tmem_ld16(lane_base + acc_col<MODE>(a) + c * 16, v[a]);
+            for ( int a = 0; a < NACC; ++a )
+#pragma unroll
+               for ( int jj = 0; jj < 16; ++jj ) v[a][jj] = __uint_as_float(u[a][jj]);
             if constexpr ( sxy2_col<MODE>() >= 0 )
             {
-               float w2[16];
-               tmem_ld16(lane_base + (uint32_t)sxy2_col<MODE>() + c * 16, w2);
 #pragma unroll
-               for ( int jj = 0; jj < 16; ++jj ) v[0][jj] += w2[jj];
+               for ( int jj = 0; jj < 16; ++jj ) v[0][jj] += __uint_as_float(u[NACC][jj]);
             }
             if ( x < args.G )
             {
@@ -627,7 +635,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                }
             }
          }
-         /* every TMEM read of this warp is complete (tmem_ld16 waits): hand TMEM back */
+         /* every TMEM read of this warp is complete (tmem_wait_ld): hand TMEM back */
          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
          __syncwarp();
          if ( lane == 0 ) mbar_arrive(tempty);
@@ -656,6 +664,55 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    {
       asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
    }
+}
+
+/*
+ * The dense tcgen05 MMA rate of one operand type (MODE 1 TF32, 2 BF16) with nothing else in the
+ * way: one CTA per SM, operands resident in shared memory, one thread issuing M = 128, N = 256 MMAs
+ * (4 K-steps of a 128-byte-swizzled chunk) back to back into TMEM, then one commit and a bounded
+ * wait.  The ceiling the tensor-core Pearson form is measured against (the library GEMM rate
+ * includes its memory traffic).
+ */
+template <int MODE>
+__global__ void __launch_bounds__(128, 1) k_tensor_peak(int iters, int* status)
+{
+   extern __shared__ __align__(1024) unsigned char smem_raw[];
+   unsigned char* ops = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+   __shared__ uint64_t bar;
+   __shared__ uint32_t holder;
+   constexpr int A_BYTES = BM * 128, B_BYTES = 256 * 128;
+   for ( int i = threadIdx.x; i < (A_BYTES + B_BYTES) / 4; i += blockDim.x )
+      ((uint32_t*)ops)[i] = 0x3f800000u ^ ((uint32_t)i * 2654435761u & 0x007fffffu);   /* values in [1, 2) */
+   if ( threadIdx.x == 0 )
+   {
+      mbar_init(smem_u32(&bar), 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+   }
+   if ( threadIdx.x < 32 )
+   {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&holder)),
+                   "r"(TMEM_COLS));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+   }
+   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   /* the operands, to the tensor core */
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   const uint32_t tmem = holder;
+   if ( threadIdx.x == 0 )
+   {
+      const uint32_t a = smem_u32(ops), b = smem_u32(ops + A_BYTES);
+      for ( int it = 0; it < iters; ++it )
+         for ( int ks = 0; ks < 4; ++ks )
+            mma<MODE, 256>(tmem, smem_desc<1>(a + ks * 32), smem_desc<1>(b + ks * 32), (it | ks) ? 1u : 0u);
+      mma_commit(smem_u32(&bar));
+      if ( !mbar_wait(smem_u32(&bar), 0) ) atomicExch(status, ST_TIMEOUT);
+   }
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   if ( threadIdx.x < 32 )
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
 }
 
 /*
@@ -1028,4 +1085,53 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
    if ( launches ) *launches += 2;
    (void)S;
    return cudaGetLastError();
+}
+
+/* dense tcgen05 MMA rate of the current device for precision 1 (TF32) or 2 (BF16), in TFLOP/s */
+extern "C" int kinc_sim_tensor_peak(int32_t precision, double* tflops)
+{
+   if ( (precision != 1 && precision != 2) || !tflops ) return KINC_SIM_EINVAL;
+   int dev = 0, sms = 0;
+   if ( cudaGetDevice(&dev) != cudaSuccess ) return KINC_SIM_ECUDA;
+   if ( cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ) return KINC_SIM_ECUDA;
+   int* d_status = nullptr;
+   if ( cudaMalloc(&d_status, sizeof(int)) != cudaSuccess ) return KINC_SIM_ENOMEM;
+   cudaEvent_t e0 = nullptr, e1 = nullptr;
+   const int smem = 160 * 1024;   /* one CTA per SM */
+   const int iters = 20000;
+   int rc = KINC_SIM_OK;
+   float best = 0.f;
+   if ( cudaMemset(d_status, 0, sizeof(int)) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess )
+      rc = KINC_SIM_ECUDA;
+   if ( rc == KINC_SIM_OK )
+   {
+      cudaFuncSetAttribute(k_tensor_peak<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      cudaFuncSetAttribute(k_tensor_peak<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      for ( int rep = 0; rep < 3 && rc == KINC_SIM_OK; ++rep )
+      {
+         cudaEventRecord(e0);
+         if ( precision == 1 )
+            k_tensor_peak<1><<<sms, 128, smem>>>(iters, d_status);
+         else
+            k_tensor_peak<2><<<sms, 128, smem>>>(iters, d_status);
+         cudaEventRecord(e1);
+         float ms = 0.f;
+         if ( cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess )
+            rc = KINC_SIM_ECUDA;
+         else if ( rep > 0 && (best == 0.f || ms < best) )
+            best = ms;   /* the first launch is the warm-up */
+      }
+   }
+   int st = 0;
+   if ( rc == KINC_SIM_OK && cudaMemcpy(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess )
+      rc = KINC_SIM_ECUDA;
+   if ( rc == KINC_SIM_OK && st != 0 ) rc = KINC_SIM_EKERNEL;
+   if ( e0 ) cudaEventDestroy(e0);
+   if ( e1 ) cudaEventDestroy(e1);
+   cudaFree(d_status);
+   if ( rc != KINC_SIM_OK ) return rc;
+   const double k = precision == 1 ? 8.0 : 16.0;
+   *tflops = 2.0 * BM * 256 * k * 4.0 * iters * sms / (best * 1e-3) / 1e12;
+   return KINC_SIM_OK;
 }

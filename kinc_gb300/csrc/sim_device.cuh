@@ -82,6 +82,12 @@ constexpr int KM_RING = KINC_KM_RING;
 #ifndef KINC_GMM_PACKED
 #define KINC_GMM_PACKED 1
 #endif
+#ifndef KINC_GMM_RING
+#define KINC_GMM_RING 1             /* gmm_fit_packed: samples the E and M1 sweeps load ahead into registers */
+#endif
+#ifndef KINC_GMM_PIPE_G
+#define KINC_GMM_PIPE_G 1           /* 1: gmm_fit's M2 loads the next sample's responsibilities a step ahead */
+#endif
 #ifndef KINC_STORE_GAMMA
 #define KINC_STORE_GAMMA 1          /* 1: keep the M1 responsibilities for M2 instead of recomputing them */
 #endif
@@ -689,15 +695,46 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
       }
       xn = X[0];
       float ln = lpx[0];
+      /* kept responsibilities of sample i+1 loaded while sample i is summed (static K only) */
+      constexpr bool PIPE_G = STORE_G && KT > 0 && KINC_GMM_PIPE_G;
+      float gn[PIPE_G ? KA : 1];
+      if ( PIPE_G )
+      {
+#pragma unroll UF
+         for ( int k = 0; k < KA; ++k )
+         {
+            if ( k >= K ) continue;
+            gn[k] = gam[k * TILE];
+         }
+      }
       #pragma unroll SU
       for ( int i = 0; i < N; ++i )
       {
          const float2 xv = xn;
          const float logpx = ln;
+         float gc[PIPE_G ? KA : 1];
+         if ( PIPE_G )
+         {
+#pragma unroll UF
+            for ( int k = 0; k < KA; ++k )
+            {
+               if ( k >= K ) continue;
+               gc[k] = gn[k];
+            }
+         }
          if ( i + 1 < N )
          {
             xn = X[(i + 1) * TILE];
             ln = lpx[(i + 1) * TILE];
+            if ( PIPE_G )
+            {
+#pragma unroll UF
+               for ( int k = 0; k < KA; ++k )
+               {
+                  if ( k >= K ) continue;
+                  gn[k] = gam[((i + 1) * KA + k) * TILE];
+               }
+            }
          }
          if ( pd > 0 && i + pd < N )
          {
@@ -721,7 +758,11 @@ __device__ bool gmm_fit(const float2* X, float* lpx, float* gam, int8_t* wl, int
          {
             if ( k >= K ) continue;
             float g;
-            if ( STORE_G )
+            if ( PIPE_G )
+            {
+               g = gc[k];
+            }
+            else if ( STORE_G )
             {
                g = gam[(i * KA + k) * TILE];
             }
@@ -861,6 +902,7 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
    float* gpair = gam + lane;
    float* godd = gam + NP * 2 * TILE;
    const F2 z = f2(neg_zero);
+   constexpr int GR = KINC_GMM_RING;           /* samples the E and M1 sweeps keep in flight */
 
    PArr<K> m0, m1, ia, ib, ic, nrm, logpi;
    if ( rng.mode == 1 ) rng.lcg = 1;
@@ -890,11 +932,16 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
       float logL = 0.0f;
       PArr<K> maxG;
       maxG.fill(-INFINITY);
-      float2 xn = X[0];
+      /* the next GR samples in flight in registers */
+      float2 xr[GR];
+#pragma unroll
+      for ( int d = 0; d < GR; ++d ) xr[d] = d < N ? X[d * TILE] : make_float2(0.f, 0.f);
       for ( int i = 0; i < N; ++i )
       {
-         const float2 xv = xn;
-         if ( i + 1 < N ) xn = X[(i + 1) * TILE];
+         const float2 xv = xr[0];
+#pragma unroll
+         for ( int d = 0; d + 1 < GR; ++d ) xr[d] = xr[d + 1];
+         if ( i + GR < N ) xr[GR - 1] = X[(i + GR) * TILE];
          if ( pd > 0 && i + pd < N ) prefetch_l2(&X[(i + pd) * TILE]);
          const F2 x0 = f2(xv.x), x1 = f2(xv.y);
          F2 lg[NP], lp[NP];
@@ -907,14 +954,15 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
             lp[q] = logpi.p[q] + lg[q];
             float a, b;
             split(lp[q], a, b);
-            if ( a > m ) m = a;
-            if ( b > m ) m = b;
+            /* fmaxf keeps m where a comparison would (m is never NaN; m's zero sign changes no result) */
+            m = fmaxf(m, a);
+            m = fmaxf(m, b);
          }
          if ( ODD )
          {
             lgo = log_mvn(xv.x, xv.y, m0.o, m1.o, ia.o, ib.o, ic.o, nrm.o);
             lpo = logpi.o + lgo;
-            if ( lpo > m ) m = lpo;
+            m = fmaxf(m, lpo);
          }
          float sum = 0.0f;
          const F2 mm = f2(m);
@@ -937,14 +985,11 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
             float a, b, ga, gb;
             split(lg[q] + nl, a, b);
             split(maxG.p[q], ga, gb);
-            if ( a > ga ) ga = a;
-            if ( b > gb ) gb = b;
-            maxG.p[q] = f2(ga, gb);
+            maxG.p[q] = f2(fmaxf(ga, a), fmaxf(gb, b));
          }
          if ( ODD )
          {
-            const float v = lgo + (-logpx);
-            if ( v > maxG.o ) maxG.o = v;
+            maxG.o = fmaxf(maxG.o, lgo + (-logpx));
          }
       }
       prevL = curL;
@@ -962,16 +1007,28 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
          sG.fill(0.f);
          nm0.fill(0.f);
          nm1.fill(0.f);
-         xn = X[0];
-         float ln = lpx[0];
+         float2 xr[GR];
+         float lr[GR];
+#pragma unroll
+         for ( int d = 0; d < GR; ++d )
+         {
+            xr[d] = d < N ? X[d * TILE] : make_float2(0.f, 0.f);
+            lr[d] = d < N ? lpx[d * TILE] : 0.f;
+         }
          for ( int i = 0; i < N; ++i )
          {
-            const float2 xv = xn;
-            const float logpx = ln;
-            if ( i + 1 < N )
+            const float2 xv = xr[0];
+            const float logpx = lr[0];
+#pragma unroll
+            for ( int d = 0; d + 1 < GR; ++d )
             {
-               xn = X[(i + 1) * TILE];
-               ln = lpx[(i + 1) * TILE];
+               xr[d] = xr[d + 1];
+               lr[d] = lr[d + 1];
+            }
+            if ( i + GR < N )
+            {
+               xr[GR - 1] = X[(i + GR) * TILE];
+               lr[GR - 1] = lpx[(i + GR) * TILE];
             }
             if ( pd > 0 && i + pd < N )
             {
@@ -1029,11 +1086,29 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
       s00.fill(0.f);
       s01.fill(0.f);
       s11.fill(0.f);
-      xn = X[0];
+      /* the pass does little arithmetic per sample, so sample i+1's point and responsibilities are
+       * loaded while sample i is summed */
+      float2 xn = X[0];
+      F2 gn[NP];
+      float gno = 0.f;
+#pragma unroll
+      for ( int q = 0; q < NP; ++q ) gn[q].v = *reinterpret_cast<const unsigned long long*>(gpair + q * 2 * TILE);
+      if ( ODD ) gno = godd[0];
       for ( int i = 0; i < N; ++i )
       {
          const float2 xv = xn;
-         if ( i + 1 < N ) xn = X[(i + 1) * TILE];
+         F2 gc[NP];
+#pragma unroll
+         for ( int q = 0; q < NP; ++q ) gc[q] = gn[q];
+         const float gco = gno;
+         if ( i + 1 < N )
+         {
+            xn = X[(i + 1) * TILE];
+#pragma unroll
+            for ( int q = 0; q < NP; ++q )
+               gn[q].v = *reinterpret_cast<const unsigned long long*>(gpair + (i + 1) * GS + q * 2 * TILE);
+            if ( ODD ) gno = godd[(i + 1) * GS];
+         }
          if ( pd > 0 && i + pd < N )
          {
             prefetch_l2(&X[(i + pd) * TILE]);
@@ -1045,8 +1120,7 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
 #pragma unroll
          for ( int q = 0; q < NP; ++q )
          {
-            F2 g;
-            g.v = *reinterpret_cast<const unsigned long long*>(gpair + i * GS + q * 2 * TILE);
+            const F2 g = gc[q];
             const F2 xm0 = x0 - nm0.p[q];
             const F2 xm1 = x1 - nm1.p[q];
             s00.p[q] += mulz(g, xm0 * xm0, z);
@@ -1055,7 +1129,7 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
          }
          if ( ODD )
          {
-            const float g = godd[i * GS];
+            const float g = gco;
             const float xm0 = xv.x - nm0.o;
             const float xm1 = xv.y - nm1.o;
             s00.o += g * (xm0 * xm0);

@@ -189,13 +189,18 @@ __device__ int kmeans_pool(const DevParams& P, const DevData& D, const float2* X
          s0[k] = 0.f; s1[k] = 0.f; nk[k] = 0;
       }
       const int lim = active ? N : 0;
-      float2 xn = lim > 0 ? X[j] : make_float2(0.f, 0.f);
+      /* the next KM_RING samples are in flight in registers */
+      float2 ring[KM_RING];
+#pragma unroll
+      for ( int d = 0; d < KM_RING; ++d ) ring[d] = d < lim ? X[d * TILE + j] : make_float2(0.f, 0.f);
       for ( int i = 0; i < maxN; ++i )
       {
          if ( i < lim )
          {
-            const float2 xv = xn;
-            if ( i + 1 < lim ) xn = X[(i + 1) * TILE + j];
+            const float2 xv = ring[0];
+#pragma unroll
+            for ( int d = 0; d + 1 < KM_RING; ++d ) ring[d] = ring[d + 1];
+            if ( i + KM_RING < lim ) ring[KM_RING - 1] = X[(i + KM_RING) * TILE + j];
             if ( pd > 0 && i + pd < lim ) prefetch_l2(&X[(i + pd) * TILE + j]);
             float md;
             const int min_k = km_assign<KT>(xv.x, xv.y, mu0, mu1, K, md);
@@ -308,11 +313,17 @@ __device__ int kmeans_pool(const DevParams& P, const DevData& D, const float2* X
          }
       }
       /* the final labels and each sample's distance to its cluster's final mean */
+      float2 ring[KM_RING];
+#pragma unroll
+      for ( int d = 0; d < KM_RING; ++d ) ring[d] = d < lim ? X[d * TILE + c.j] : make_float2(0.f, 0.f);
       for ( int i = 0; i < maxN; ++i )
       {
          if ( i < lim )
          {
-            const float2 xv = X[i * TILE + c.j];
+            const float2 xv = ring[0];
+#pragma unroll
+            for ( int d = 0; d + 1 < KM_RING; ++d ) ring[d] = ring[d + 1];
+            if ( i + KM_RING < lim ) ring[KM_RING - 1] = X[(i + KM_RING) * TILE + c.j];
             if ( pd > 0 && i + pd < lim ) prefetch_l2(&X[(i + pd) * TILE + c.j]);
             float md;
             const int l = km_assign<KT>(xv.x, xv.y, a0, a1, c.K, md);
@@ -331,12 +342,22 @@ __device__ int kmeans_pool(const DevParams& P, const DevData& D, const float2* X
       for ( int k = 0; k < kmax; ++k )
       {
          const int klim = k < c.K ? lim : 0;
+         /* label and distance of sample i+1 loaded (unconditionally, both written above for i < lim)
+          * while sample i is added */
+         int8_t ln = klim > 0 ? ya[0] : (int8_t)-1;
+         float dn = klim > 0 ? dbuf[0] : 0.f;
          for ( int i = 0; i < maxN; ++i )
          {
-            if ( i < klim && ya[i * TILE] == k )
+            if ( i < klim )
             {
-               const float d = dbuf[i * TILE];
-               S += d * d;
+               const int8_t l = ln;
+               const float d = dn;
+               if ( i + 1 < klim )
+               {
+                  ln = ya[(i + 1) * TILE];
+                  dn = dbuf[(i + 1) * TILE];
+               }
+               if ( l == k ) S += d * d;
             }
          }
       }

@@ -59,3 +59,20 @@ def test_plain_fp32_fixed_semantics_vs_fp64():
     ref = pyoracle.pearson_fp64_pairs(gem, x, y)
     both = ~np.isnan(ref)
     assert np.abs(res.corr[both, 0] - ref[both]).max() < 1e-4
+
+
+def test_tensor_peak_measures_both_operand_types():
+    """kinc_sim_tensor_peak: the dense tcgen05 rate the tensor-core form is compared with; BF16
+    (K = 16 per MMA) runs at about twice the TF32 rate (K = 8)."""
+    import ctypes
+
+    from kinc_gb300 import _native
+    L = _native.load()
+    rates = {}
+    for prec in (1, 2):
+        v = ctypes.c_double(0.0)
+        assert L.kinc_sim_tensor_peak(prec, ctypes.byref(v)) == 0
+        rates[prec] = v.value
+    assert 100.0 < rates[1] < 10000.0
+    assert 1.5 < rates[2] / rates[1] < 2.5
+    assert L.kinc_sim_tensor_peak(3, ctypes.byref(ctypes.c_double(0.0))) == _native.EINVAL
