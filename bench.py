@@ -427,6 +427,7 @@ def kmeans_leg(L, vp, cpu=True):
     args = dict(clusmethod="kmeans", corrmethod="pearson", minclus=1, maxclus=3, crit="BIC", minsamp=30)
     sim = Similarity(gem, **args)
     sim.initialize()
+    chosen, _ = sim.autotune()      # launch shape for this workload (kinc_sim_autotune, cached)
     ctx = sim._ctx
     n = 262144
     dK = torch.empty(n, dtype=torch.int8, device="cuda")
@@ -451,7 +452,7 @@ def kmeans_leg(L, vp, cpu=True):
     sim.close()
     out = {"workload": "K-means k<=3 (BIC) + Pearson, GEM 10000x4000 float32, per-gene NaN rate ~U(0,0.6), "
                        "5% planted 2-cluster pairs, minsamp 30", "pairs_per_step": n, "ms_per_step": ms,
-           "pairs_per_s": n / (ms / 1e3)}
+           "pairs_per_s": n / (ms / 1e3), "launch": chosen}
     if cpu:
         threads = os.cpu_count() or 1
         total = G * (G - 1) // 2
@@ -487,6 +488,7 @@ def stream_leg(device_block, nblk, cpu=True):
     sim = Similarity(gem, clusmethod="gmm", corrmethod="both", minclus=1, maxclus=5, crit="ICL", preout=True,
                      postout=True, minsamp=30, mincorr=0.5, maxcorr=1.0)
     sim.initialize()
+    chosen, _ = sim.autotune()      # launch shape for this workload (kinc_sim_autotune, cached)
     wb_per_dev = device_block // 32768
     first = (sim.size() // 2) // wb_per_dev * wb_per_dev
     pairs = min(sim.total_pairs(), (first + nblk * wb_per_dev) * 32768) - first * 32768
@@ -531,7 +533,7 @@ def stream_leg(device_block, nblk, cpu=True):
             "workload": "GMM k<=5 (ICL) + pre/post outliers + Pearson and Spearman per cluster, GEM 30000x500 "
                         "float32, 8% NaN, 5% planted 2-4 component mixture pairs, minsamp 30, mincorr 0.5",
             "pairs": int(pairs), "first_pair": int(first * 32768), "device_block": device_block,
-            "device_blocks": nblk, "seconds": secs, "pairs_per_s": rate,
+            "device_blocks": nblk, "seconds": secs, "pairs_per_s": rate, "launch": chosen,
             "cmx_items": int(items_cmx), "ccm_items": int(items_ccm), "bytes_written": int(ccm_bytes + cmx_bytes),
             "projected_full_run_s": sim.total_pairs() / rate,
             "includes": "kinc_sim_run_to_files_ex: compute, device-side process(), pinned D2H of kept items "

@@ -35,16 +35,26 @@ def main(argv=None):
     ap.add_argument("--repeat", type=int, default=1, help="run each block this many times from the same pair")
     ap.add_argument("--launch", default="", help="launch shape warps_per_cta,rounds,prefetch (default: the "
                                                  "worker's); 'tune' = kinc_sim_autotune with its cache")
+    ap.add_argument("--tune-grid", action="store_true",
+                    help="run kinc_sim_autotune (no cache) on its default sample block, then time every launch "
+                         "shape on that block and print the pick beside the best of the grid")
+    ap.add_argument("--genes", type=int, default=0, help="override the workload's gene count")
+    ap.add_argument("--samples", type=int, default=0, help="override the workload's sample count")
     args = ap.parse_args(argv)
 
     import torch
 
-    gem = synthetic.generate(args.workload)
+    over = {k: v for k, v in (("genes", args.genes), ("samples", args.samples)) if v}
+    gem = synthetic.generate(args.workload, **over)
     G, S = gem.shape
     sim = Similarity(gem, clusmethod=args.clusmethod, corrmethod=args.corrmethod, crit=args.crit,
                      minclus=args.minclus, maxclus=args.maxclus, minsamp=args.minsamp, preout=args.preout,
                      postout=args.postout, semantics=args.semantics, precision=args.precision)
     sim.initialize()
+    if args.tune_grid:
+        tune_grid(sim, args)
+        sim.close()
+        return
     if args.launch == "tune":
         sim.autotune()
     elif args.launch:
@@ -82,6 +92,47 @@ def main(argv=None):
         if args.repeat <= 1:
             pos += size
     sim.close()
+
+
+def tune_grid(sim, args):
+    """The autotuner's pick against every launch shape, on the sample block it times."""
+    import time
+
+    import torch
+    L = _native.load()
+    vp = ctypes.c_void_p
+    t0 = time.perf_counter()
+    chosen, cands = sim.autotune(use_cache=False)
+    tune_s = time.perf_counter() - t0
+    total = sim.total_pairs()
+    size = int(min(4 * 32 * 16 * 152, total, L.kinc_sim_max_device_block(sim._ctx)))
+    start = max(0, total // 2 - size // 2)          # Similarity.autotune's default block
+    G, S = sim.expressions.shape
+    nc = 2 if sim.params.corr_method == 2 else 1
+    dK = torch.empty(size, dtype=torch.int8, device="cuda")
+    dL = torch.empty((size, S), dtype=torch.int8, device="cuda")
+    dC = torch.empty((size, sim.params.max_clusters * nc), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    grid = {}
+    for w in (4, 8, 16):
+        for r in (0, 1):
+            for pf in (0, 4, 8, 16):
+                sim.set_launch(w, r, pf)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                _native.check(L.kinc_sim_execute_block_device(sim._ctx, start, size, vp(dK.data_ptr()),
+                                                              vp(dL.data_ptr()), vp(dC.data_ptr()),
+                                                              vp(stream.cuda_stream)), sim._ctx)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                grid[f"{w},{r},{pf}"] = e0.elapsed_time(e1)
+    best = min(grid, key=grid.get)
+    pick = f"{chosen['warps_per_cta']},{chosen['rounds']},{chosen['prefetch']}"
+    print(json.dumps({"workload": args.workload, "genes": int(G), "samples": int(S),
+                      "sample_pairs": size, "autotune_s": tune_s, "autotune_candidates": len(cands),
+                      "picked": pick, "picked_ms": grid[pick], "best": best, "best_ms": grid[best],
+                      "picked_over_best": grid[pick] / grid[best], "grid_ms": grid}), flush=True)
 
 
 if __name__ == "__main__":

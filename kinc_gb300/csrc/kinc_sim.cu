@@ -585,7 +585,8 @@ static kinc_sim_launch default_launch(int clus)
 
 static bool launch_valid(const kinc_sim_launch& l)
 {
-   const bool w = l.warps_per_cta == 4 || l.warps_per_cta == 8 || l.warps_per_cta == 16;
+   const bool w = l.warps_per_cta == 4 || l.warps_per_cta == 8 || l.warps_per_cta == 16 ||
+                  l.warps_per_cta == WARPS_PER_BLOCK;
    const bool r = l.rounds == 0 || l.rounds == 1;
    const bool f = l.prefetch == 0 || l.prefetch == 4 || l.prefetch == 8 || l.prefetch == 16;
    return w && WARPS_PER_BLOCK % l.warps_per_cta == 0 && r && f;
@@ -1136,7 +1137,7 @@ extern "C" int kinc_sim_autotune(kinc_sim_ctx* ctx, int64_t start, int64_t size,
             if ( knob == 0 ) c.prefetch = pf_v[v];
             else if ( knob == 1 ) c.warps_per_cta = warps_v[v];
             else c.rounds = v;
-            if ( memcmp(&c, &base, sizeof c) == 0 ) continue;
+            if ( memcmp(&c, &base, sizeof c) == 0 || !launch_valid(c) ) continue;
             double ms = 0;
             rc = time_launch(ctx, c, start, size, ms);
             if ( rc ) return rc;

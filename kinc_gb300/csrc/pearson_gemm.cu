@@ -41,33 +41,40 @@
 namespace kinc_tc {
 
 constexpr int BM = 128;               /* pair-tile rows (genes x) */
-constexpr int BN = 64;                /* pair-tile columns (genes y) */
 constexpr int NACC = 6;               /* Sxy, Sx, Sy, Sxx, Syy, n */
 constexpr int TMEM_COLS = 512;
-constexpr int STAGES = 3;
 constexpr long long WAIT_CYCLES = 4ll << 30;  /* ~2 s of SM clock before a wait gives up */
 
 constexpr int ST_TIMEOUT = 10;        /* an mbarrier wait expired */
 
 /* per precision: element type, elements per K-chunk row, swizzle, operands per side */
 template <int MODE> struct Cfg;
+/*
+ * Tiles are 128 x 64 pairs.  (128 x 80 TF32 tiles -- 480 TMEM columns, 16-sample chunks in a
+ * 5-stage ring of 64-byte rows -- were measured slower: 8.44 against 6.97 ms for the 20,000 x 2,000
+ * matrix.)
+ */
 template <> struct Cfg<1>             /* TF32: A, A2, M as fp32 rounded to tf32 */
 {
    static constexpr int ELEM = 4;
+   static constexpr int BN = 64;      /* pair-tile columns (genes y) */
    static constexpr int BK = 32;      /* 128-byte rows, SWIZZLE_128B */
    static constexpr int ROWB = 128;
    static constexpr int NMAT = 3;
    static constexpr int UMMA_K = 8;
+   static constexpr int STAGES = 3;
    static constexpr uint32_t A_FMT = 2, B_FMT = 2;   /* tf32 */
    static constexpr uint64_t LAYOUT = 2;              /* SWIZZLE_128B */
 };
 template <> struct Cfg<2>             /* 3xBF16: A_hi, A_lo, A2_hi, A2_lo, M as bf16 */
 {
    static constexpr int ELEM = 2;
+   static constexpr int BN = 64;
    static constexpr int BK = 32;      /* 64-byte rows, SWIZZLE_64B */
    static constexpr int ROWB = 64;
    static constexpr int NMAT = 5;
    static constexpr int UMMA_K = 16;
+   static constexpr int STAGES = 3;
    static constexpr uint32_t A_FMT = 1, B_FMT = 1;   /* bf16 */
    static constexpr uint64_t LAYOUT = 4;              /* SWIZZLE_64B */
 };
@@ -76,9 +83,9 @@ template <int MODE>
 struct Layout
 {
    static constexpr int XMAT = BM * Cfg<MODE>::ROWB;          /* bytes of one x-side operand chunk */
-   static constexpr int YMAT = BN * Cfg<MODE>::ROWB;
+   static constexpr int YMAT = Cfg<MODE>::BN * Cfg<MODE>::ROWB;
    static constexpr int STAGE = Cfg<MODE>::NMAT * (XMAT + YMAT);
-   static constexpr int RING = STAGES * STAGE;
+   static constexpr int RING = Cfg<MODE>::STAGES * STAGE;
    static constexpr int SMEM = RING + 1024 /* alignment slack */ + 256 /* barriers */;
 };
 
@@ -140,7 +147,7 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
 }
 
 /* instruction descriptor: D f32, A/B format, both K-major, N columns, M = BM */
-template <int MODE, int N = BN>
+template <int MODE, int N = Cfg<MODE>::BN>
 __host__ __device__ constexpr uint32_t instr_desc()
 {
    static_assert(N % 16 == 0 && N >= 16 && N <= 256, "M = 128 takes N in 16..256, a multiple of 16");
@@ -191,7 +198,7 @@ __host__ __device__ constexpr int yslot(int m)
 template <int MODE>
 __host__ __device__ constexpr int acc_col(int a)
 {
-   return !merged<MODE>() ? a * BN
+   return !merged<MODE>() ? a * Cfg<MODE>::BN
           : MODE == 1     ? (a == 0 ? 0 : a == 1 ? 64 : a == 2 ? 256 : a == 3 ? 128 : a == 4 ? 192 : 320)
                           : (a == 0 ? 0 : a == 1 ? 64 : a == 2 ? 320 : a == 3 ? 192 : a == 4 ? 256 : 384);
 }
@@ -203,7 +210,7 @@ __host__ __device__ constexpr int sxy2_col()
    return (merged<MODE>() && MODE == 2) ? 128 : -1;
 }
 
-template <int MODE, int N = BN>
+template <int MODE, int N = Cfg<MODE>::BN>
 __device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate)
 {
    constexpr uint32_t idesc = instr_desc<MODE, N>();
@@ -352,6 +359,7 @@ __device__ __forceinline__ void issue_chunk(uint32_t tmem, uint32_t stage, bool 
 {
    using C = Cfg<MODE>;
    using L = Layout<MODE>;
+   constexpr int BN = C::BN;
    const uint32_t ysb = stage + C::NMAT * L::XMAT;
 #pragma unroll
    for ( int ks = 0; ks < C::BK / C::UMMA_K; ++ks )
@@ -459,6 +467,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 {
    using C = Cfg<MODE>;
    using L = Layout<MODE>;
+   constexpr int BN = C::BN;
+   constexpr int STAGES = C::STAGES;
    extern __shared__ __align__(1024) unsigned char smem_raw[];
    unsigned char* ring = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
    uint64_t* bars = (uint64_t*)(ring + L::RING);
@@ -571,9 +581,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    else
    {
       /* ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. (its quarter of the tile's rows) and
-       * columns 32 h .. 32 h + 31, h = (w - 2) / 4 */
+       * half h = (w - 2) / 4 of the tile's 16-column chunks */
       const int quarter = warp & 3;
       const int half = (warp - 2) >> 2;
+      constexpr int NCH = BN / 16;                 /* 16-column chunks of a tile */
+      constexpr int HCH = (NCH + 1) / 2;           /* the first half's share */
+      const int c0 = half * HCH, c1 = half ? NCH : HCH;
       int tl = 0;
       for ( int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl )
       {
@@ -594,7 +607,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
          const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
          const int64_t pbase = x * (x - 1) / 2;
 #pragma unroll 1
-         for ( int c = 2 * half; c < 2 * half + 2; ++c )
+         for ( int c = c0; c < c1; ++c )
          {
             /* all of the chunk's accumulators in flight at once, then one wait */
             uint32_t u[NACC + 1][16];
@@ -673,6 +686,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
  * wait.  The ceiling the tensor-core Pearson form is measured against (the library GEMM rate
  * includes its memory traffic).
  */
+/* K-major, 128-byte swizzled rows in 8-row atoms (1,024-byte stride): the probe's operand layout */
+__device__ __forceinline__ uint64_t peak_desc(uint32_t addr)
+{
+   uint64_t d = 0;
+   d |= (uint64_t)((addr >> 4) & 0x3fff);
+   d |= (uint64_t)((1024 >> 4) & 0x3fff) << 32;
+   d |= (uint64_t)1 << 46;
+   d |= (uint64_t)2 << 61;
+   return d;
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(128, 1) k_tensor_peak(int iters, int* status)
 {
@@ -704,7 +728,7 @@ __global__ void __launch_bounds__(128, 1) k_tensor_peak(int iters, int* status)
       const uint32_t a = smem_u32(ops), b = smem_u32(ops + A_BYTES);
       for ( int it = 0; it < iters; ++it )
          for ( int ks = 0; ks < 4; ++ks )
-            mma<MODE, 256>(tmem, smem_desc<1>(a + ks * 32), smem_desc<1>(b + ks * 32), (it | ks) ? 1u : 0u);
+            mma<MODE, 256>(tmem, peak_desc(a + ks * 32), peak_desc(b + ks * 32), (it | ks) ? 1u : 0u);
       mma_commit(smem_u32(&bar));
       if ( !mbar_wait(smem_u32(&bar), 0) ) atomicExch(status, ST_TIMEOUT);
    }
@@ -918,7 +942,8 @@ cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_e
       snprintf(err, errlen, "cuTensorMapEncodeTiled is not available");
       return cudaErrorNotSupported;
    }
-   const int bk = 32;
+   const int bk = mode == 1 ? Cfg<1>::BK : Cfg<2>::BK;
+   const int bn = mode == 1 ? Cfg<1>::BN : Cfg<2>::BN;
    for ( int m = 0; m < nmat; ++m )
    {
       char* base = (char*)t.ops + m * plane;
@@ -928,7 +953,7 @@ cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_e
       const CUtensorMapDataType dt = mode == 1 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
       const CUtensorMapSwizzle sw = mode == 1 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
       const cuuint32_t boxx[2] = { (cuuint32_t)bk, (cuuint32_t)BM };
-      const cuuint32_t boxy[2] = { (cuuint32_t)bk, (cuuint32_t)BN };
+      const cuuint32_t boxy[2] = { (cuuint32_t)bk, (cuuint32_t)bn };
       CUresult r1 = enc(&t.maps.x[m], dt, 2, base, dims, strides, boxx, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
       CUresult r2 = enc(&t.maps.y[m], dt, 2, base, dims, strides, boxy, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
@@ -971,9 +996,10 @@ constexpr int TILE_GROUP = 8;
 static cudaError_t tc_tile_list(TcState& t, int Ia, int Ib, int64_t xb, cudaStream_t st)
 {
    if ( t.tiles_ia == Ia && t.tiles_ib == Ib && t.tiles_xb == xb ) return cudaSuccess;
+   const int bn = t.mode == 1 ? Cfg<1>::BN : Cfg<2>::BN;
    auto jhi = [&](int I) {
       const int64_t rowmax = std::min<int64_t>((int64_t)(I + 1) * BM - 1, xb);
-      return rowmax >= 1 ? (int)((rowmax - 1) / BN) : -1;   /* last column tile holding some y < x */
+      return rowmax >= 1 ? (int)((rowmax - 1) / bn) : -1;   /* last column tile holding some y < x */
    };
    int64_t n = 0;
    for ( int I = Ia; I <= Ib; ++I ) n += jhi(I) + 1;
@@ -1037,7 +1063,8 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
    };
    const int64_t xa = row_of(start);
    const int64_t xb = row_of(end - 1);
-   const int tile_x = t.mode == 3 ? SB : BM, tile_y = t.mode == 3 ? SB : BN;
+   const int tile_x = t.mode == 3 ? SB : BM;
+   const int tile_y = t.mode == 3 ? SB : t.mode == 1 ? Cfg<1>::BN : Cfg<2>::BN;
    const int Ia = (int)(xa / tile_x), Ib = (int)(xb / tile_x);
    const int Jn = (int)((xb + tile_y - 1) / tile_y);
    if ( Jn < 1 ) return cudaSuccess;
@@ -1052,7 +1079,7 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
    a.end = end;
    a.out_corr = d_corr;
    a.status = d_status;
-   a.kchunks = t.Sp / 32;
+   a.kchunks = t.Sp / (t.mode == 1 ? Cfg<1>::BK : Cfg<2>::BK);   /* Sp is a multiple of 64 */
    if ( t.mode == 3 )
    {
       a.kchunks = t.Sp / SK;
