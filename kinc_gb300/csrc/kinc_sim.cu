@@ -186,8 +186,8 @@ __global__ void k_scan_apply(const int32_t* __restrict__ N, int64_t offset, int6
    if ( t < count ) qpos[t] = boff[blockIdx.x] + ex;
 }
 
-/* previous pair (same 32768-pair work block) with a strictly larger N: one CTA
- * per work block builds a max-tree of the block's N in shared memory (internal
+/* previous pair (same 32768-pair work block) with a strictly larger N: a CTA
+ * builds a max-tree of its work block's N in shared memory (internal
  * nodes 1..WB-1; leaf i is N of the block's i-th pair, -1 past its end) and
  * every pair searches it independently -- up the tree until a left sibling
  * holds a larger maximum, then down that subtree keeping to the right.  Links
@@ -196,11 +196,13 @@ constexpr int PREV_THREADS = 1024;
 constexpr int PREV_SMEM = KINC_SIM_WORK_BLOCK_SIZE * (int)sizeof(int32_t);
 
 __global__ void __launch_bounds__(PREV_THREADS) k_prev(const int32_t* __restrict__ N, int64_t lo, int64_t end,
-                                                       int32_t* __restrict__ pg)
+                                                       int32_t* __restrict__ pg, int split)
 {
    constexpr int WB = KINC_SIM_WORK_BLOCK_SIZE;
    extern __shared__ int32_t tree[];
-   const int64_t b0 = lo + (int64_t)blockIdx.x * WB;
+   /* `split` CTAs per work block: each builds the block's tree and answers its share of the pairs */
+   const int part = (int)(blockIdx.x % split);
+   const int64_t b0 = lo + (int64_t)(blockIdx.x / split) * WB;
    const int64_t n64 = end - b0 < WB ? end - b0 : WB;
    const int n = (int)n64;
    const int32_t* Nb = N + (b0 - lo);
@@ -215,7 +217,9 @@ __global__ void __launch_bounds__(PREV_THREADS) k_prev(const int32_t* __restrict
       for ( int k = level + threadIdx.x; k < 2 * level; k += PREV_THREADS ) tree[k] = max(tree[2 * k], tree[2 * k + 1]);
       __syncthreads();
    }
-   for ( int o = threadIdx.x; o < n; o += PREV_THREADS )
+   const int share = (n + split - 1) / split;
+   const int o_end = min(n, (part + 1) * share);
+   for ( int o = part * share + threadIdx.x; o < o_end; o += PREV_THREADS )
    {
       const int32_t v = Nb[o];
       int ans = -1;
@@ -237,7 +241,12 @@ cudaError_t launch_prev(const int32_t* N, int64_t lo, int64_t end, int32_t* pg, 
    const cudaError_t attr = cudaFuncSetAttribute(k_prev, cudaFuncAttributeMaxDynamicSharedMemorySize, PREV_SMEM);
    if ( attr != cudaSuccess ) return attr;
    const int64_t nwb = (end - 1) / KINC_SIM_WORK_BLOCK_SIZE - lo / KINC_SIM_WORK_BLOCK_SIZE + 1;
-   k_prev<<<(int)nwb, PREV_THREADS, PREV_SMEM, st>>>(N, lo, end, pg);
+   int dev = 0, sms = 0;
+   cudaGetDevice(&dev);
+   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+   /* enough CTAs for two per SM: a few work blocks split their pairs over several CTAs */
+   const int split = (int)std::max<int64_t>(1, std::min<int64_t>(16, (2 * (int64_t)sms + nwb - 1) / nwb));
+   k_prev<<<(int)(nwb * split), PREV_THREADS, PREV_SMEM, st>>>(N, lo, end, pg, split);
    return cudaGetLastError();
 }
 

@@ -1183,6 +1183,17 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
    return true;
 }
 
+/* "no label changed": a lane's label columns ya and yb (stride TILE) agree on samples [0, N).
+ * The whole range is compared without an early exit, so the loads of several samples are in flight
+ * at once (the first mismatch decides nothing that the full comparison does not). */
+__device__ __forceinline__ bool labels_equal(const int8_t* ya, const int8_t* yb, int N)
+{
+   bool same = true;
+#pragma unroll 8
+   for ( int i = 0; i < N; ++i ) same &= ya[i * TILE] == yb[i * TILE];
+   return same;
+}
+
 /* vectorDiffNorm (pairwise_linalg.cpp:97-104) */
 __device__ __forceinline__ float diff_norm(float x0, float x1, float m0, float m1)
 {
@@ -1303,7 +1314,7 @@ __device__ float kmeans_fit_inits_in_step(const float2* X, int8_t*& cur, int8_t*
          }
          else if ( means_same )
          {
-            for ( int i = 0; i < N && same; ++i ) same = ya[i * TILE] == yb[i * TILE];
+            same = labels_equal(ya, yb, N);
          }
          else
          {
@@ -1566,7 +1577,7 @@ __device__ float kmeans_fit_pipelined(const float2* X, int8_t*& ya, int8_t*& yb,
       else if ( means_same )
       {
          same = true;
-         for ( int i = 0; i < N && same; ++i ) same = ya[i * TILE] == yb[i * TILE];
+         same = labels_equal(ya, yb, N);
       }
       else
       {

@@ -242,7 +242,7 @@ __device__ int kmeans_pool(const DevParams& P, const DevData& D, const float2* X
       else if ( means_same )
       {
          same = true;
-         for ( int i = 0; i < N && same; ++i ) same = ya[i * TILE] == yb[i * TILE];
+         same = labels_equal(ya, yb, N);
       }
       else
       {

@@ -63,7 +63,13 @@ __global__ void __launch_bounds__(256) k_pearson_lanes(DevParams P, DevData D, D
                }
                const int s = ws * 32 + __ffs(bs) - 1;
                bs &= bs - 1;
-               if ( (pos >> b) & 1u ) add(__ldg(g1 + s), __ldg(g2 + s));
+               /* an unusable position adds +0.0, which leaves every sum as it is (a sum of floats
+                * starting at +0.0 is never -0.0), so the lanes need not branch */
+               const bool use = (pos >> b) & 1u;
+               const float vx = use ? __ldg(g1 + s) : 0.f;
+               const float vy = use ? __ldg(g2 + s) : 0.f;
+               sumx += vx; sumy += vy; sumx2 += vx * vx; sumy2 += vy * vy; sumxy += vx * vy;
+               n += use;
             }
          }
          /* positions i >= N: stale points of earlier pairs of the work block (as lane_pearson) */

@@ -22,6 +22,11 @@ CASES = [
      dict(clusmethod="kmeans", corrmethod="pearson", crit="BIC", maxclus=3),
      dict(clus_method=2, corr_method=0, criterion=0, max_clusters=3)),
     ("none_pearson", 1, 300, 50, 0, 44850, dict(), dict()),
+    # ten work blocks from inside the second one: links searched by several CTAs per work block,
+    # packed-array reads of the one-thread-per-pair kernel, S above one mask word with a ragged tail
+    ("none_pearson_many_blocks", 1, 800, 100, 50000, 200000, dict(), dict()),
+    ("none_pearson_fixed_many_blocks", 1, 800, 100, 50000, 200000, dict(semantics="fixed"), dict(semantics=1)),
+    ("none_pearson_minexpr", 1, 400, 45, 1000, 60000, dict(minexpr=7.0), dict(min_expr=7.0)),
     ("none_spearman", 1, 200, 70, 0, 19900, dict(corrmethod="spearman"), dict(corr_method=1)),
     ("gmm_pearson_fixed_lcg", 2, 50, 100, 0, 1225,
      dict(clusmethod="gmm", corrmethod="pearson", crit="BIC", semantics="fixed", rand="lcg", postout=True),
