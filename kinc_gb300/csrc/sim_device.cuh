@@ -82,8 +82,11 @@ constexpr int KM_RING = KINC_KM_RING;
 #ifndef KINC_GMM_PACKED
 #define KINC_GMM_PACKED 1
 #endif
+#ifndef KINC_GMM_E_UNROLL
+#define KINC_GMM_E_UNROLL 1         /* gmm_fit_packed: unroll of the E-step sample loop (2: -3 %) */
+#endif
 #ifndef KINC_GMM_RING
-#define KINC_GMM_RING 1             /* gmm_fit_packed: samples the E and M1 sweeps load ahead into registers */
+#define KINC_GMM_RING 1             /* gmm_fit_packed: samples the E and M1 sweeps load ahead into registers (2: -0.7 %) */
 #endif
 #ifndef KINC_GMM_PIPE_G
 #define KINC_GMM_PIPE_G 1           /* 1: gmm_fit's M2 loads the next sample's responsibilities a step ahead */
@@ -903,6 +906,7 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
    float* godd = gam + NP * 2 * TILE;
    const F2 z = f2(neg_zero);
    constexpr int GR = KINC_GMM_RING;           /* samples the E and M1 sweeps keep in flight */
+   constexpr int EU = KINC_GMM_E_UNROLL;
 
    PArr<K> m0, m1, ia, ib, ic, nrm, logpi;
    if ( rng.mode == 1 ) rng.lcg = 1;
@@ -936,6 +940,7 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
       float2 xr[GR];
 #pragma unroll
       for ( int d = 0; d < GR; ++d ) xr[d] = d < N ? X[d * TILE] : make_float2(0.f, 0.f);
+#pragma unroll EU
       for ( int i = 0; i < N; ++i )
       {
          const float2 xv = xr[0];
