@@ -1017,8 +1017,8 @@ static cudaError_t tc_tile_list(TcState& t, int Ia, int Ib, int64_t xb, cudaStre
    }
    if ( n > t.tiles_cap )
    {
-      /* the device list may still be read by an earlier launch on this stream */
-      e = cudaStreamSynchronize(st);
+      /* the device list may still be read by an earlier launch (on any stream) */
+      e = cudaDeviceSynchronize();
       if ( e != cudaSuccess ) return e;
       if ( t.d_tiles ) cudaFree(t.d_tiles);
       if ( t.h_tiles ) cudaFreeHost(t.h_tiles);

@@ -82,6 +82,10 @@ constexpr int KM_RING = KINC_KM_RING;
 #ifndef KINC_GMM_PACKED
 #define KINC_GMM_PACKED 1
 #endif
+#ifndef KINC_GMM_M2_UNROLL
+#define KINC_GMM_M2_UNROLL 2        /* gmm_fit_packed: unroll of the M2 sample loop (its loads of several samples in
+                                       flight; 2: +0.5 %, 4: -0.6 %) */
+#endif
 #ifndef KINC_GMM_E_UNROLL
 #define KINC_GMM_E_UNROLL 1         /* gmm_fit_packed: unroll of the E-step sample loop (2: -3 %) */
 #endif
@@ -907,6 +911,7 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
    const F2 z = f2(neg_zero);
    constexpr int GR = KINC_GMM_RING;           /* samples the E and M1 sweeps keep in flight */
    constexpr int EU = KINC_GMM_E_UNROLL;
+   constexpr int M2U = KINC_GMM_M2_UNROLL;
 
    PArr<K> m0, m1, ia, ib, ic, nrm, logpi;
    if ( rng.mode == 1 ) rng.lcg = 1;
@@ -1099,6 +1104,7 @@ __device__ bool gmm_fit_packed(const float2* X, float* lpx, float* gam, int8_t* 
 #pragma unroll
       for ( int q = 0; q < NP; ++q ) gn[q].v = *reinterpret_cast<const unsigned long long*>(gpair + q * 2 * TILE);
       if ( ODD ) gno = godd[0];
+#pragma unroll M2U
       for ( int i = 0; i < N; ++i )
       {
          const float2 xv = xn;
