@@ -54,17 +54,28 @@ template <int MODE> struct Cfg;
  * 5-stage ring of 64-byte rows -- were measured slower: 8.44 against 6.97 ms for the 20,000 x 2,000
  * matrix.)
  */
+#ifndef KINC_TC_TF32_BK16
+#define KINC_TC_TF32_BK16 0           /* 1: TF32 K-chunks of 16 samples (64-byte rows) in a 6-stage ring:
+                                         measured slower, 8.2-8.6 vs 6.6-7.0 ms per 134M-pair block */
+#endif
 template <> struct Cfg<1>             /* TF32: A, A2, M as fp32 rounded to tf32 */
 {
    static constexpr int ELEM = 4;
    static constexpr int BN = 64;      /* pair-tile columns (genes y) */
+#if KINC_TC_TF32_BK16
+   static constexpr int BK = 16;      /* 64-byte rows, SWIZZLE_64B */
+   static constexpr int ROWB = 64;
+   static constexpr int STAGES = 6;
+   static constexpr uint64_t LAYOUT = 4;              /* SWIZZLE_64B */
+#else
    static constexpr int BK = 32;      /* 128-byte rows, SWIZZLE_128B */
    static constexpr int ROWB = 128;
+   static constexpr int STAGES = 3;
+   static constexpr uint64_t LAYOUT = 2;              /* SWIZZLE_128B */
+#endif
    static constexpr int NMAT = 3;
    static constexpr int UMMA_K = 8;
-   static constexpr int STAGES = 3;
    static constexpr uint32_t A_FMT = 2, B_FMT = 2;   /* tf32 */
-   static constexpr uint64_t LAYOUT = 2;              /* SWIZZLE_128B */
 };
 template <> struct Cfg<2>             /* 3xBF16: A_hi, A_lo, A2_hi, A2_lo, M as bf16 */
 {
@@ -951,7 +962,8 @@ cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_e
       const cuuint64_t strides[1] = { (cuuint64_t)t.Sp * elem };
       const cuuint32_t estr[2] = { 1, 1 };
       const CUtensorMapDataType dt = mode == 1 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-      const CUtensorMapSwizzle sw = mode == 1 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+      const CUtensorMapSwizzle sw = (mode == 1 && Cfg<1>::ROWB == 128) ? CU_TENSOR_MAP_SWIZZLE_128B
+                                                                        : CU_TENSOR_MAP_SWIZZLE_64B;
       const cuuint32_t boxx[2] = { (cuuint32_t)bk, (cuuint32_t)BM };
       const cuuint32_t boxy[2] = { (cuuint32_t)bk, (cuuint32_t)bn };
       CUresult r1 = enc(&t.maps.x[m], dt, 2, base, dims, strides, boxx, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
