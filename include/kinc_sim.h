@@ -264,8 +264,8 @@ int kinc_sim_work_counters(kinc_sim_ctx* ctx, uint64_t* out, int reset);
  * rejected with KINC_SIM_EINVAL and a message from kinc_sim_last_error(NULL).
  *
  * The first call on a device does a one-time set-up with that device current:
- * it looks up the array's device address and uploads the rand() jump table,
- * so make that first call before any stream capture begins.  Every call runs
+ * it looks up the array's device address and uploads the rand() jump table.
+ * Every call runs
  * its kernels on `stream` (a cudaStream_t, 0 = default stream), then waits
  * for them with cudaStreamSynchronize and copies a status word back to the
  * host before returning.  Every call shares the one array, which keeps the
