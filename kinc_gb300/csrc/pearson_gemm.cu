@@ -97,7 +97,10 @@ struct Layout
    static constexpr int YMAT = Cfg<MODE>::BN * Cfg<MODE>::ROWB;
    static constexpr int STAGE = Cfg<MODE>::NMAT * (XMAT + YMAT);
    static constexpr int RING = Cfg<MODE>::STAGES * STAGE;
-   static constexpr int SMEM = RING + 1024 /* alignment slack */ + 256 /* barriers */;
+   /* the epilogue warps' transposition tiles: 32 rows x 8 columns of r each */
+   static constexpr int EBUF = 8 /* epilogue warps */ * 32 * 8 * 4;
+   static constexpr int SMEM = RING + 1024 /* alignment slack */ + 256 /* barriers */ + EBUF;
+   static_assert(SMEM <= 227 * 1024, "ring, barriers and epilogue tiles fit the shared memory of one CTA");
 };
 
 /* ---------------------------------------------------------------- PTX */
@@ -141,6 +144,30 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
                 " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
                 "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
                 : "memory");
+}
+
+/* one read of the box from L2, written at shared-memory offset `dst` of every CTA in `mask` (bit r
+ * = cluster rank r) and counted on the mbarrier at offset `bar` of each of them */
+__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar,
+                                               uint16_t mask)
+{
+   asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
+                " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
+                "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar), "h"(mask)
+                : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+   uint32_t r;
+   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+   return r;
+}
+
+/* every thread of every CTA of the cluster; release/acquire orders shared-memory state across it */
+__device__ __forceinline__ void cluster_sync()
+{
+   asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
 
 /* shared-memory matrix descriptor: K-major, swizzled rows of ROWB bytes, 8-row atoms */
@@ -242,6 +269,14 @@ __device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uin
 __device__ __forceinline__ void mma_commit(uint32_t bar)
 {
    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                : "memory");
+}
+
+/* the same arrival on the mbarrier at offset `bar` of every CTA in `mask` */
+__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask)
+{
+   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+                ::"r"(bar), "h"(mask)
                 : "memory");
 }
 
@@ -468,11 +503,26 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
  * tile's operand loads overlap this tile's epilogue, and TMEM, barriers and the ring are set up
  * once per CTA.  Every mbarrier wait is bounded: on expiry the CTA records an error, every role
  * stops, the CTA drains its own copies (bounded), frees its TMEM and returns.
+ *
+ * CL = 2: CTA pairs (thread-block clusters of two) take units of two list entries with the same
+ * row tile and neighbouring column tiles.  Each CTA of the pair loads half of the shared x-side
+ * panel, 64 of its 128 rows, with one TMA multicast into both CTAs' ring, and its own y-side
+ * panel, so a K-chunk costs a CTA 2/3 of the L2-to-SM bytes (TF32: 24 + 24 of 72 KB).  A stage
+ * is refilled only when both CTAs' MMAs have read it: every MMA commit arrives on the stage's
+ * `empty` barrier in both CTAs (count 2).  A unit whose second column tile lies past the
+ * diagonal carries a placeholder entry (column -J-1): that CTA loads and multiplies tile J again
+ * to keep the pair in step and writes nothing.  Before it returns, each CTA waits until both
+ * CTAs' MMAs have released every stage its copies went into, then the pair meets at a cluster
+ * barrier, so neither leaves while the other can still write into it.
  */
 constexpr int EPI_WARPS = 8;
 constexpr int TC_THREADS = (2 + EPI_WARPS) * 32;
 
-template <int MODE>
+#ifndef KINC_TC_CLUSTER
+#define KINC_TC_CLUSTER 1             /* CTAs sharing an x-side panel by TMA multicast (1 or 2) */
+#endif
+
+template <int MODE, int CL>
 __global__ void __launch_bounds__(TC_THREADS, 1)
    k_pearson_tc(const __grid_constant__ TcMaps maps, TcArgs args, const int2* __restrict__ tiles, int ntiles)
 {
@@ -480,6 +530,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    using L = Layout<MODE>;
    constexpr int BN = C::BN;
    constexpr int STAGES = C::STAGES;
+   static_assert(CL == 1 || (CL == 2 && 2 * BN == BM), "a CTA pair loads the x panel as two y-sized boxes");
    extern __shared__ __align__(1024) unsigned char smem_raw[];
    unsigned char* ring = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
    uint64_t* bars = (uint64_t*)(ring + L::RING);
@@ -487,10 +538,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    __shared__ int s_fail;
 
    /* a CTA that failed earlier in this launch stops the rest from starting (decided once, for
-    * the whole CTA) */
-   if ( threadIdx.x == 0 ) s_fail = *(volatile int*)args.status != 0;
+    * the whole CTA; CTA pairs always start, so that both reach their cluster barriers) */
+   if ( threadIdx.x == 0 ) s_fail = CL == 1 && *(volatile int*)args.status != 0;
    __syncthreads();
    if ( s_fail ) return;
+   const int rank = CL > 1 ? (int)cluster_rank() : 0;
+   const int unit0 = blockIdx.x / CL, nunit_step = gridDim.x / CL;
+   const int nunits = ntiles / CL;
    const int warp = threadIdx.x >> 5;
    const int lane = threadIdx.x & 31;
    const uint32_t full0 = smem_u32(&bars[0]);
@@ -505,7 +559,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for ( int s = 0; s < STAGES; ++s )
       {
          mbar_init(full0 + 8 * s, 1);
-         mbar_init(empty0 + 8 * s, 1);
+         mbar_init(empty0 + 8 * s, CL);
       }
       mbar_init(tfull, 1);
       mbar_init(tempty, EPI_WARPS);
@@ -519,6 +573,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    }
    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
    __syncthreads();
+   if ( CL > 1 ) cluster_sync();        /* both CTAs' barriers are initialised before either signals the other */
    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
    const uint32_t tmem = *tmem_holder;
 
@@ -529,9 +584,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if ( lane == 0 )
       {
          /* ---- producer: the chunks of every tile of this CTA, back to back */
-         for ( int t = blockIdx.x; t < ntiles && !*(volatile int*)&s_fail; t += gridDim.x )
+         for ( int u = unit0; u < nunits && !*(volatile int*)&s_fail; u += nunit_step )
          {
-            const int2 ij = tiles[t];
+            const int2 ij = tiles[u * CL + rank];
+            const int jy = ij.y >= 0 ? ij.y : -ij.y - 1;
             for ( int kc = 0; kc < K; ++kc, ++issued )
             {
                const int s = issued % STAGES;
@@ -545,9 +601,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                mbar_expect_tx(full0 + 8 * s, L::STAGE);
                for ( int m = 0; m < C::NMAT; ++m )
                {
-                  tma_load_2d(stage + m * L::XMAT, &maps.x[m], kc * C::BK, ij.x * BM, full0 + 8 * s);
+                  if ( CL == 1 )
+                     tma_load_2d(stage + m * L::XMAT, &maps.x[m], kc * C::BK, ij.x * BM, full0 + 8 * s);
+                  else
+                     tma_load_2d_mc(stage + m * L::XMAT + rank * L::YMAT, &maps.y[m], kc * C::BK,
+                                    ij.x * BM + rank * BN, full0 + 8 * s, (uint16_t)0x3);
                   tma_load_2d(stage + C::NMAT * L::XMAT + yslot<MODE>(m) * L::YMAT, &maps.y[m], kc * C::BK,
-                              ij.y * BN, full0 + 8 * s);
+                              jy * BN, full0 + 8 * s);
+               }
+            }
+         }
+         /* a pair: every arrival on this CTA's stages (the other CTA's copies and MMA commits)
+          * has landed once both MMAs have released the last chunks */
+         if ( CL > 1 && !*(volatile int*)&s_fail )
+         {
+            for ( int g = (issued > STAGES ? issued - STAGES : 0); g < issued; ++g )
+            {
+               if ( !mbar_wait(empty0 + 8 * (g % STAGES), (g / STAGES) & 1) )
+               {
+                  atomicExch(&s_fail, 1);
+                  break;
                }
             }
          }
@@ -559,7 +632,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       {
          /* ---- MMA issuer */
          int used = 0, tl = 0;
-         for ( int t = blockIdx.x; t < ntiles && !*(volatile int*)&s_fail; t += gridDim.x, ++tl )
+         for ( int u = unit0; u < nunits && !*(volatile int*)&s_fail; u += nunit_step, ++tl )
          {
             if ( tl > 0 && !mbar_wait(tempty, (tl - 1) & 1) )
             {
@@ -578,7 +651,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                }
                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                issue_chunk<MODE>(tmem, smem_u32(ring + s * L::STAGE), kc == 0);
-               mma_commit(empty0 + 8 * s);      /* frees the stage when these MMAs have read it */
+               /* frees the stage when these MMAs have read it (in both CTAs of a pair) */
+               if ( CL == 1 )
+                  mma_commit(empty0 + 8 * s);
+               else
+                  mma_commit_mc(empty0 + 8 * s, (uint16_t)0x3);
             }
             if ( !ok )
             {
@@ -592,14 +669,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    else
    {
       /* ---- epilogue: warp w reads TMEM lanes 32 (w % 4) .. (its quarter of the tile's rows) and
-       * half h = (w - 2) / 4 of the tile's 16-column chunks */
+       * half h = (w - 2) / 4 of the tile's four 16-column chunks.  It forms r for its 32 x 32
+       * pairs, hands TMEM back to the MMA warp, and only then writes them: the writes overlap the
+       * next tile's MMAs instead of holding them up. */
       const int quarter = warp & 3;
       const int half = (warp - 2) >> 2;
-      constexpr int NCH = BN / 16;                 /* 16-column chunks of a tile */
-      constexpr int HCH = (NCH + 1) / 2;           /* the first half's share */
-      const int c0 = half * HCH, c1 = half ? NCH : HCH;
+      constexpr int WCH = BN / 32;                 /* 16-column chunks per warp */
+      static_assert(BN % 32 == 0, "two warps share a quarter's columns");
+      const int c0 = half * WCH;
+      float* ebuf = (float*)(ring + L::RING + 256) + (warp - 2) * (32 * 8);
       int tl = 0;
-      for ( int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl )
+      for ( int u = unit0; u < nunits; u += nunit_step, ++tl )
       {
          /* one lane waits and the warp follows its verdict, so the warp stays converged for the
           * .sync.aligned TMEM loads */
@@ -612,50 +692,39 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             break;
          }
          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-         const int2 ij = tiles[t];
-         const int row = quarter * 32 + lane;
-         const int64_t x = (int64_t)ij.x * BM + row;
+         const int2 ij = tiles[u * CL + rank];
          const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
-         const int64_t pbase = x * (x - 1) / 2;
-#pragma unroll 1
-         for ( int c = c0; c < c1; ++c )
+         /* r of this lane's row (TMEM lane = pair row) and the warp's columns */
+         float r[WCH][16];
+         if ( ij.y >= 0 )
          {
-            /* all of the chunk's accumulators in flight at once, then one wait */
-            uint32_t u[NACC + 1][16];
 #pragma unroll
-            for ( int a = 0; a < NACC; ++a ) tmem_ld16_async(lane_base + acc_col<MODE>(a) + c * 16, u[a]);
-            if constexpr ( sxy2_col<MODE>() >= 0 ) tmem_ld16_async(lane_base + (uint32_t)sxy2_col<MODE>() + c * 16, u[NACC]);
-            tmem_wait_ld();
-            float v[NACC][16];
-#pragma unroll
-            for ( int a = 0; a < NACC; ++a )
-#pragma unroll
-               for ( int jj = 0; jj < 16; ++jj ) v[a][jj] = __uint_as_float(u[a][jj]);
-            if constexpr ( sxy2_col<MODE>() >= 0 )
+            for ( int w = 0; w < WCH; ++w )
             {
+               const int c = c0 + w;
+               /* all of the chunk's accumulators in flight at once, then one wait */
+               uint32_t v[NACC + 1][16];
 #pragma unroll
-               for ( int jj = 0; jj < 16; ++jj ) v[0][jj] += __uint_as_float(u[NACC][jj]);
-            }
-            if ( x < args.G )
-            {
+               for ( int a = 0; a < NACC; ++a ) tmem_ld16_async(lane_base + acc_col<MODE>(a) + c * 16, v[a]);
+               if constexpr ( sxy2_col<MODE>() >= 0 )
+                  tmem_ld16_async(lane_base + (uint32_t)sxy2_col<MODE>() + c * 16, v[NACC]);
+               tmem_wait_ld();
 #pragma unroll
                for ( int jj = 0; jj < 16; ++jj )
                {
-                  const int64_t y = (int64_t)ij.y * BN + c * 16 + jj;
-                  if ( y >= x ) continue;
-                  const int64_t p = pbase + y;
-                  if ( p < args.start || p >= args.end ) continue;
-                  const float sxy = v[0][jj], sx = v[1][jj], sy = v[2][jj], sxx = v[3][jj], syy = v[4][jj];
-                  const float n = v[5][jj];
-                  float r = __int_as_float(0x7fc00000);
+                  float sxy = __uint_as_float(v[0][jj]);
+                  if constexpr ( sxy2_col<MODE>() >= 0 ) sxy += __uint_as_float(v[NACC][jj]);
+                  const float sx = __uint_as_float(v[1][jj]), sy = __uint_as_float(v[2][jj]);
+                  const float sxx = __uint_as_float(v[3][jj]), syy = __uint_as_float(v[4][jj]);
+                  const float n = __uint_as_float(v[5][jj]);
+                  r[w][jj] = __int_as_float(0x7fc00000);
                   if ( n >= (float)args.min_samples && n > 0.f )
                   {
                      const float num = diff_of_products(n, sxy, sx, sy);
                      const float dx = diff_of_products(n, sxx, sx, sx);
                      const float dy = diff_of_products(n, syy, sy, sy);
-                     r = num * rsqrtf(dx) * rsqrtf(dy);
+                     r[w][jj] = num * rsqrtf(dx) * rsqrtf(dy);
                   }
-                  args.out_corr[(p - args.start) * args.max_k] = r;
                }
             }
          }
@@ -663,6 +732,29 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
          __syncwarp();
          if ( lane == 0 ) mbar_arrive(tempty);
+         if ( ij.y < 0 ) continue;              /* the placeholder of a CTA pair: nothing to write */
+         /* written through a 32 x 8 shared-memory tile so that each store covers 8 neighbouring
+          * pairs of 4 rows (a lane's own row would put the warp's 32 stores in 32 rows); element
+          * (row, col) sits at row * 8 + (col ^ (row / 4)), conflict-free both ways */
+         const int64_t x0 = (int64_t)ij.x * BM + quarter * 32;   /* the warp's first row */
+#pragma unroll
+         for ( int g = 0; g < 2 * WCH; ++g )
+         {
+            __syncwarp();
+#pragma unroll
+            for ( int j = 0; j < 8; ++j ) ebuf[lane * 8 + (j ^ (lane >> 2))] = r[g >> 1][(g & 1) * 8 + j];
+            __syncwarp();
+#pragma unroll
+            for ( int i = 0; i < 8; ++i )
+            {
+               const int rr = 4 * i + (lane >> 3), cc = lane & 7;
+               const int64_t x = x0 + rr;
+               const int64_t y = (int64_t)ij.y * BN + c0 * 16 + g * 8 + cc;
+               const int64_t p = x * (x - 1) / 2 + y;
+               if ( x < args.G && y < x && p >= args.start && p < args.end )
+                  args.out_corr[(p - args.start) * args.max_k] = ebuf[rr * 8 + (cc ^ i)];
+            }
+         }
       }
    }
    __syncwarp();
@@ -683,6 +775,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    }
    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
    __syncthreads();
+   if ( CL > 1 ) cluster_sync();        /* neither CTA of a pair leaves while the other may write into it */
    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
    if ( warp == 1 )
    {
@@ -999,9 +1092,11 @@ void tc_release(TcState& t)
  * (I, J) with a pair y < x, in bands of TILE_GROUP row tiles, column by column within a band and
  * row by row within a column.  The persistent CTAs take the list round robin, so the tiles
  * running at one time lie in one band and a few columns: TILE_GROUP x-side row panels and a few
- * y-side column panels, which stay in L2 while the band's rows reuse them.  Built on the host into
- * pinned memory and copied on the stream; the copy of the previous list must be complete before
- * the host buffer is rewritten.
+ * y-side column panels, which stay in L2 while the band's rows reuse them.  With CTA pairs
+ * (KINC_TC_CLUSTER 2) the list holds units of two entries, tiles (I, J) and (I, J + 1) for even J;
+ * where J + 1 holds no pair of row tile I the second entry is the placeholder (I, -J - 1).  Built
+ * on the host into pinned memory and copied on the stream; the copy of the previous list must be
+ * complete before the host buffer is rewritten.
  */
 constexpr int TILE_GROUP = 8;
 
@@ -1014,7 +1109,7 @@ static cudaError_t tc_tile_list(TcState& t, int Ia, int Ib, int64_t xb, cudaStre
       return rowmax >= 1 ? (int)((rowmax - 1) / bn) : -1;   /* last column tile holding some y < x */
    };
    int64_t n = 0;
-   for ( int I = Ia; I <= Ib; ++I ) n += jhi(I) + 1;
+   for ( int I = Ia; I <= Ib; ++I ) n += (jhi(I) + KINC_TC_CLUSTER) / KINC_TC_CLUSTER * KINC_TC_CLUSTER;
    if ( n > INT32_MAX ) return cudaErrorInvalidValue;
    cudaError_t e;
    if ( t.tiles_ev )
@@ -1047,9 +1142,13 @@ static cudaError_t tc_tile_list(TcState& t, int Ia, int Ib, int64_t xb, cudaStre
    for ( int b0 = Ia; b0 <= Ib; b0 += TILE_GROUP )
    {
       const int b1 = std::min(Ib, b0 + TILE_GROUP - 1);
-      for ( int J = 0; J <= jhi(b1); ++J )
+      for ( int J = 0; J <= jhi(b1); J += KINC_TC_CLUSTER )
          for ( int I = b0; I <= b1; ++I )
-            if ( J <= jhi(I) ) t.h_tiles[k++] = make_int2(I, J);
+            if ( J <= jhi(I) )
+            {
+               t.h_tiles[k++] = make_int2(I, J);
+               if ( KINC_TC_CLUSTER == 2 ) t.h_tiles[k++] = make_int2(I, J + 1 <= jhi(I) ? J + 1 : -J - 1);
+            }
    }
    t.ntiles = (int)k;
    t.tiles_ia = Ia;
@@ -1059,6 +1158,46 @@ static cudaError_t tc_tile_list(TcState& t, int Ia, int Ib, int64_t xb, cudaStre
    e = cudaMemcpyAsync(t.d_tiles, t.h_tiles, (size_t)k * sizeof(int2), cudaMemcpyHostToDevice, st);
    if ( e != cudaSuccess ) return e;
    return cudaEventRecord(t.tiles_ev, st);
+}
+
+/* the persistent tensor-core kernel over the current tile list: one CTA per SM, or as many CTA
+ * pairs as can be resident at once (a pair needs two free SMs in one GPC) */
+template <int MODE>
+static cudaError_t tc_launch(const TcState& t, const TcArgs& a, cudaStream_t st)
+{
+   constexpr int CL = KINC_TC_CLUSTER;
+   static_assert(CL == 1 || CL == 2, "KINC_TC_CLUSTER is 1 or 2");
+   const int smem = Layout<MODE>::SMEM;
+   cudaError_t e = cudaFuncSetAttribute(k_pearson_tc<MODE, CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+   if ( e != cudaSuccess ) return e;
+   cudaLaunchConfig_t cfg = {};
+   cudaLaunchAttribute attr[1];
+   cfg.blockDim = dim3(TC_THREADS);
+   cfg.dynamicSmemBytes = (size_t)smem;
+   cfg.stream = st;
+   attr[0].id = cudaLaunchAttributeClusterDimension;
+   attr[0].val.clusterDim.x = CL;
+   attr[0].val.clusterDim.y = 1;
+   attr[0].val.clusterDim.z = 1;
+   cfg.attrs = attr;
+   cfg.numAttrs = CL > 1 ? 1 : 0;
+   int resident = 0;
+   if ( CL == 1 )
+   {
+      int dev = 0;
+      e = cudaGetDevice(&dev);
+      if ( e == cudaSuccess ) e = cudaDeviceGetAttribute(&resident, cudaDevAttrMultiProcessorCount, dev);
+   }
+   else
+   {
+      cfg.gridDim = dim3(CL);
+      e = cudaOccupancyMaxActiveClusters(&resident, k_pearson_tc<MODE, CL>, &cfg);
+   }
+   if ( e != cudaSuccess ) return e;
+   if ( resident < 1 ) return cudaErrorLaunchOutOfResources;
+   const int units = t.ntiles / CL;
+   cfg.gridDim = dim3((unsigned)(CL * std::max(1, std::min(resident, units))));
+   return cudaLaunchKernelEx(&cfg, k_pearson_tc<MODE, CL>, t.maps, a, (const int2*)t.d_tiles, t.ntiles);
 }
 
 /* enqueue the pairs [start, start+size): K = 1, corr[.][0] = r, NaN elsewhere */
@@ -1104,22 +1243,8 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
       const cudaError_t e = tc_tile_list(t, Ia, Ib, xb, st);
       if ( e != cudaSuccess ) return e;
       if ( t.ntiles == 0 ) return cudaGetLastError();
-      int sms = 0, dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      const int grid = std::max(1, std::min(sms, t.ntiles));
-      if ( t.mode == 1 )
-      {
-         const int smem = Layout<1>::SMEM;
-         cudaFuncSetAttribute(k_pearson_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-         k_pearson_tc<1><<<grid, TC_THREADS, smem, st>>>(t.maps, a, t.d_tiles, t.ntiles);
-      }
-      else
-      {
-         const int smem = Layout<2>::SMEM;
-         cudaFuncSetAttribute(k_pearson_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-         k_pearson_tc<2><<<grid, TC_THREADS, smem, st>>>(t.maps, a, t.d_tiles, t.ntiles);
-      }
+      const cudaError_t le = t.mode == 1 ? tc_launch<1>(t, a, st) : tc_launch<2>(t, a, st);
+      if ( le != cudaSuccess ) return le;
    }
    if ( launches ) *launches += 2;
    (void)S;
