@@ -54,6 +54,11 @@ template <int MODE> struct Cfg;
  * 5-stage ring of 64-byte rows -- were measured slower: 8.44 against 6.97 ms for the 20,000 x 2,000
  * matrix.)
  */
+#ifndef KINC_TC_PAIR
+#define KINC_TC_PAIR 0                /* 1: TF32 on CTA pairs (cta_group::2, M = 256): bit-identical
+                                         results, measured 3.5 % slower on 134M-pair blocks (4.63 vs
+                                         4.47 ms) and 20 % slower on 4M-pair blocks */
+#endif
 #ifndef KINC_TC_TF32_BK16
 #define KINC_TC_TF32_BK16 0           /* 1: TF32 K-chunks of 16 samples (64-byte rows) in a 6-stage ring:
                                          measured slower, 8.2-8.6 vs 6.6-7.0 ms per 134M-pair block */
@@ -146,17 +151,6 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
                 : "memory");
 }
 
-/* one read of the box from L2, written at shared-memory offset `dst` of every CTA in `mask` (bit r
- * = cluster rank r) and counted on the mbarrier at offset `bar` of each of them */
-__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar,
-                                               uint16_t mask)
-{
-   asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
-                " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
-                "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar), "h"(mask)
-                : "memory");
-}
-
 __device__ __forceinline__ uint32_t cluster_rank()
 {
    uint32_t r;
@@ -184,14 +178,16 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr)
    return d;
 }
 
-/* instruction descriptor: D f32, A/B format, both K-major, N columns, M = BM */
-template <int MODE, int N = Cfg<MODE>::BN>
+/* instruction descriptor: D f32, A/B format, both K-major, N columns, M rows (128 on one CTA,
+ * 256 on a CTA pair) */
+template <int MODE, int N = Cfg<MODE>::BN, int M = BM>
 __host__ __device__ constexpr uint32_t instr_desc()
 {
-   static_assert(N % 16 == 0 && N >= 16 && N <= 256, "M = 128 takes N in 16..256, a multiple of 16");
+   static_assert(N % 16 == 0 && N >= 16 && N <= 256, "M = 128 and 256 take N in 16..256, a multiple of 16");
+   static_assert(M == 128 || M == 256, "M is 128 (one CTA) or 256 (a CTA pair)");
    return (1u << 4)                                /* D format f32 */
           | (Cfg<MODE>::A_FMT << 7) | (Cfg<MODE>::B_FMT << 10)
-          | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+          | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 /*
@@ -272,12 +268,68 @@ __device__ __forceinline__ void mma_commit(uint32_t bar)
                 : "memory");
 }
 
-/* the same arrival on the mbarrier at offset `bar` of every CTA in `mask` */
-__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask)
+/* ---- CTA-pair (cta_group::2) forms */
+
+/* M = 256 TF32 MMA of a CTA pair, issued by the even CTA: A rows 0-127 and the first N/2 rows of
+ * B from its shared memory, rows 128-255 and the other N/2 rows of B from the odd CTA's (same
+ * offsets); D rows 0-127 into the even CTA's TMEM, 128-255 into the odd CTA's */
+template <int N>
+__device__ __forceinline__ void mma_pair_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate)
 {
-   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+   constexpr uint32_t idesc = instr_desc<1, N, 256>();
+   asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+                "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+/* an arrival on the mbarrier at offset `bar` of every CTA of the pair in `mask` once the pair
+ * MMAs issued so far have completed */
+__device__ __forceinline__ void commit_pair(uint32_t bar, uint16_t mask)
+{
+   asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
                 ::"r"(bar), "h"(mask)
                 : "memory");
+}
+
+/* a TMA load into this CTA's shared memory that signals the mbarrier `bar_cl` (a cluster address,
+ * possibly in the other CTA of the pair) */
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar_cl)
+{
+   asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2"
+                " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+                "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar_cl)
+                : "memory");
+}
+
+/* the cluster address of this CTA's shared-memory location `addr` in CTA `rank` */
+__device__ __forceinline__ uint32_t mapa_rank(uint32_t addr, uint32_t rank)
+{
+   uint32_t r;
+   asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+   return r;
+}
+
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cl)
+{
+   asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cl) : "memory");
+}
+
+/* mbar_wait for a barrier that threads of the other CTA arrive on */
+__device__ __forceinline__ bool mbar_wait_cluster(uint32_t bar, uint32_t parity)
+{
+   const long long t0 = clock64();
+   for ( ;; )
+   {
+      uint32_t ok;
+      asm volatile("{\n\t.reg .pred p;\n\t"
+                   "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+                   "selp.u32 %0, 1, 0, p;\n\t}"
+                   : "=r"(ok)
+                   : "r"(bar), "r"(parity)
+                   : "memory");
+      if ( ok ) return true;
+      if ( clock64() - t0 > WAIT_CYCLES ) return false;
+   }
 }
 
 /* 16 consecutive TMEM columns of this warp's 32 lanes into r (asynchronous: tmem_wait_ld before use) */
@@ -503,26 +555,11 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
  * tile's operand loads overlap this tile's epilogue, and TMEM, barriers and the ring are set up
  * once per CTA.  Every mbarrier wait is bounded: on expiry the CTA records an error, every role
  * stops, the CTA drains its own copies (bounded), frees its TMEM and returns.
- *
- * CL = 2: CTA pairs (thread-block clusters of two) take units of two list entries with the same
- * row tile and neighbouring column tiles.  Each CTA of the pair loads half of the shared x-side
- * panel, 64 of its 128 rows, with one TMA multicast into both CTAs' ring, and its own y-side
- * panel, so a K-chunk costs a CTA 2/3 of the L2-to-SM bytes (TF32: 24 + 24 of 72 KB).  A stage
- * is refilled only when both CTAs' MMAs have read it: every MMA commit arrives on the stage's
- * `empty` barrier in both CTAs (count 2).  A unit whose second column tile lies past the
- * diagonal carries a placeholder entry (column -J-1): that CTA loads and multiplies tile J again
- * to keep the pair in step and writes nothing.  Before it returns, each CTA waits until both
- * CTAs' MMAs have released every stage its copies went into, then the pair meets at a cluster
- * barrier, so neither leaves while the other can still write into it.
  */
 constexpr int EPI_WARPS = 8;
 constexpr int TC_THREADS = (2 + EPI_WARPS) * 32;
 
-#ifndef KINC_TC_CLUSTER
-#define KINC_TC_CLUSTER 1             /* CTAs sharing an x-side panel by TMA multicast (1 or 2) */
-#endif
-
-template <int MODE, int CL>
+template <int MODE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
    k_pearson_tc(const __grid_constant__ TcMaps maps, TcArgs args, const int2* __restrict__ tiles, int ntiles)
 {
@@ -530,7 +567,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    using L = Layout<MODE>;
    constexpr int BN = C::BN;
    constexpr int STAGES = C::STAGES;
-   static_assert(CL == 1 || (CL == 2 && 2 * BN == BM), "a CTA pair loads the x panel as two y-sized boxes");
    extern __shared__ __align__(1024) unsigned char smem_raw[];
    unsigned char* ring = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
    uint64_t* bars = (uint64_t*)(ring + L::RING);
@@ -538,13 +574,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    __shared__ int s_fail;
 
    /* a CTA that failed earlier in this launch stops the rest from starting (decided once, for
-    * the whole CTA; CTA pairs always start, so that both reach their cluster barriers) */
-   if ( threadIdx.x == 0 ) s_fail = CL == 1 && *(volatile int*)args.status != 0;
+    * the whole CTA) */
+   if ( threadIdx.x == 0 ) s_fail = *(volatile int*)args.status != 0;
    __syncthreads();
    if ( s_fail ) return;
-   const int rank = CL > 1 ? (int)cluster_rank() : 0;
-   const int unit0 = blockIdx.x / CL, nunit_step = gridDim.x / CL;
-   const int nunits = ntiles / CL;
    const int warp = threadIdx.x >> 5;
    const int lane = threadIdx.x & 31;
    const uint32_t full0 = smem_u32(&bars[0]);
@@ -559,7 +592,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for ( int s = 0; s < STAGES; ++s )
       {
          mbar_init(full0 + 8 * s, 1);
-         mbar_init(empty0 + 8 * s, CL);
+         mbar_init(empty0 + 8 * s, 1);
       }
       mbar_init(tfull, 1);
       mbar_init(tempty, EPI_WARPS);
@@ -573,7 +606,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    }
    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
    __syncthreads();
-   if ( CL > 1 ) cluster_sync();        /* both CTAs' barriers are initialised before either signals the other */
    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
    const uint32_t tmem = *tmem_holder;
 
@@ -584,10 +616,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if ( lane == 0 )
       {
          /* ---- producer: the chunks of every tile of this CTA, back to back */
-         for ( int u = unit0; u < nunits && !*(volatile int*)&s_fail; u += nunit_step )
+         for ( int t = blockIdx.x; t < ntiles && !*(volatile int*)&s_fail; t += gridDim.x )
          {
-            const int2 ij = tiles[u * CL + rank];
-            const int jy = ij.y >= 0 ? ij.y : -ij.y - 1;
+            const int2 ij = tiles[t];
             for ( int kc = 0; kc < K; ++kc, ++issued )
             {
                const int s = issued % STAGES;
@@ -601,26 +632,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                mbar_expect_tx(full0 + 8 * s, L::STAGE);
                for ( int m = 0; m < C::NMAT; ++m )
                {
-                  if ( CL == 1 )
-                     tma_load_2d(stage + m * L::XMAT, &maps.x[m], kc * C::BK, ij.x * BM, full0 + 8 * s);
-                  else
-                     tma_load_2d_mc(stage + m * L::XMAT + rank * L::YMAT, &maps.y[m], kc * C::BK,
-                                    ij.x * BM + rank * BN, full0 + 8 * s, (uint16_t)0x3);
+                  tma_load_2d(stage + m * L::XMAT, &maps.x[m], kc * C::BK, ij.x * BM, full0 + 8 * s);
                   tma_load_2d(stage + C::NMAT * L::XMAT + yslot<MODE>(m) * L::YMAT, &maps.y[m], kc * C::BK,
-                              jy * BN, full0 + 8 * s);
-               }
-            }
-         }
-         /* a pair: every arrival on this CTA's stages (the other CTA's copies and MMA commits)
-          * has landed once both MMAs have released the last chunks */
-         if ( CL > 1 && !*(volatile int*)&s_fail )
-         {
-            for ( int g = (issued > STAGES ? issued - STAGES : 0); g < issued; ++g )
-            {
-               if ( !mbar_wait(empty0 + 8 * (g % STAGES), (g / STAGES) & 1) )
-               {
-                  atomicExch(&s_fail, 1);
-                  break;
+                              ij.y * BN, full0 + 8 * s);
                }
             }
          }
@@ -632,7 +646,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       {
          /* ---- MMA issuer */
          int used = 0, tl = 0;
-         for ( int u = unit0; u < nunits && !*(volatile int*)&s_fail; u += nunit_step, ++tl )
+         for ( int t = blockIdx.x; t < ntiles && !*(volatile int*)&s_fail; t += gridDim.x, ++tl )
          {
             if ( tl > 0 && !mbar_wait(tempty, (tl - 1) & 1) )
             {
@@ -651,11 +665,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                }
                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                issue_chunk<MODE>(tmem, smem_u32(ring + s * L::STAGE), kc == 0);
-               /* frees the stage when these MMAs have read it (in both CTAs of a pair) */
-               if ( CL == 1 )
-                  mma_commit(empty0 + 8 * s);
-               else
-                  mma_commit_mc(empty0 + 8 * s, (uint16_t)0x3);
+               mma_commit(empty0 + 8 * s);      /* frees the stage when these MMAs have read it */
             }
             if ( !ok )
             {
@@ -679,7 +689,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int c0 = half * WCH;
       float* ebuf = (float*)(ring + L::RING + 256) + (warp - 2) * (32 * 8);
       int tl = 0;
-      for ( int u = unit0; u < nunits; u += nunit_step, ++tl )
+      for ( int t = blockIdx.x; t < ntiles; t += gridDim.x, ++tl )
       {
          /* one lane waits and the warp follows its verdict, so the warp stays converged for the
           * .sync.aligned TMEM loads */
@@ -692,11 +702,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             break;
          }
          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-         const int2 ij = tiles[u * CL + rank];
+         const int2 ij = tiles[t];
          const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
          /* r of this lane's row (TMEM lane = pair row) and the warp's columns */
          float r[WCH][16];
-         if ( ij.y >= 0 )
          {
 #pragma unroll
             for ( int w = 0; w < WCH; ++w )
@@ -732,7 +741,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
          __syncwarp();
          if ( lane == 0 ) mbar_arrive(tempty);
-         if ( ij.y < 0 ) continue;              /* the placeholder of a CTA pair: nothing to write */
          /* written through a 32 x 8 shared-memory tile so that each store covers 8 neighbouring
           * pairs of 4 rows (a lane's own row would put the warp's 32 stores in 32 rows); element
           * (row, col) sits at row * 8 + (col ^ (row / 4)), conflict-free both ways */
@@ -775,11 +783,309 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
    }
    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
    __syncthreads();
-   if ( CL > 1 ) cluster_sync();        /* neither CTA of a pair leaves while the other may write into it */
    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
    if ( warp == 1 )
    {
       asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+   }
+}
+
+/*
+ * The TF32 form on CTA pairs (thread-block clusters of two, tcgen05 cta_group::2).  A pair computes
+ * a 256 x 64 tile of pairs with M = 256 MMAs that the even CTA issues: each CTA holds the three
+ * x-side operands of its 128 rows and the three y-side operands of its 32 of the tile's 64 genes;
+ * an MMA reads A from each CTA's own shared memory and B half from each, and writes each CTA's
+ * 128 rows of D into that CTA's TMEM.  On one CTA the K-chunk traffic through shared memory -- TMA
+ * writing 72 KB per 32 samples, the MMAs reading 24 KB per 8 -- takes longer than the MMAs
+ * themselves (TF32 at M = 128, N = 128 + 64 + 192 per 8 samples); on a pair each SM writes 60 KB
+ * and reads 18 KB.
+ *
+ * D columns of an MMA whose B stacks s y-side operands: the even CTA's 32 genes of each operand,
+ * then the odd CTA's, i.e. operand k, tile column j at b + (j / 32) 32 s + 32 k + j % 32.
+ *
+ * Barriers: the even CTA's full[s] counts the copies of both CTAs (its producer arms it with the
+ * bytes of both; the odd CTA's copies signal it across the pair); each MMA commit arrives on
+ * empty[s] and, at a tile's end, on tfull in both CTAs; the epilogue warps of both CTAs arrive on
+ * the even CTA's tempty (count 16).  Every wait is bounded.  The pair meets at a cluster barrier
+ * after setting up and again before leaving; before the second, the even CTA waits for its MMAs
+ * to complete and each CTA for the last commits on its own barriers, so neither leaves while the
+ * other can still read or write its memory.
+ *
+ * Measured against the one-CTA form (KINC_TC_PAIR selects it): identical results; in ncu, on one
+ * cold 16.7M-pair launch, tensor pipe busy 61.6 % of the time against 46.6 % and 0.60 against
+ * 1.00 GB read from DRAM; timed in a loop over warm 134M-pair blocks, 4.63 against 4.47 ms.  The
+ * bytes through shared memory are not what holds either form back: the MMA warp waits for the
+ * next stage (the pair waits for the later of two SMs' copies).
+ */
+namespace pair {
+constexpr int BMP = 256;                  /* pair-tile rows, 128 per CTA */
+constexpr int BNP = 64;                   /* pair-tile columns */
+constexpr int HB = BNP / 2;               /* y-side genes per CTA */
+constexpr int STAGES = 3;
+constexpr int BK = Cfg<1>::BK;            /* 32 samples: 128-byte rows, SWIZZLE_128B */
+constexpr int XMAT = 128 * Cfg<1>::ROWB;  /* one x-side operand chunk, 16 KB */
+constexpr int YMAT = HB * Cfg<1>::ROWB;   /* one y-side operand chunk, 4 KB */
+constexpr int STAGE = 3 * (XMAT + YMAT);
+constexpr int RING = STAGES * STAGE;
+constexpr int NBAR = 2 * STAGES + 3;      /* full[], empty[], tfull, tempty, done */
+constexpr int SMEM = RING + 1024 /* alignment slack */ + 256 /* barriers */ + Layout<1>::EBUF;
+static_assert(SMEM <= 227 * 1024, "ring, barriers and epilogue tiles fit the shared memory of one CTA");
+static_assert((NBAR + 1) * 8 <= 256, "barriers and the TMEM address fit their 256 bytes");
+
+/* TMEM column of accumulator a (0 Sxy, 1 Sx, 2 Sy, 3 Sxx, 4 Syy, 5 n) for the tile's columns
+ * 32 h .. 32 h + 31: A_x.[A_y; M_y] at 0 (s = 2), A2_x.M_y at 128 (s = 1),
+ * M_x.[A2_y; A_y; M_y] at 192 (s = 3) */
+__host__ __device__ constexpr int acc_col(int a, int h)
+{
+   return a == 0 ? 64 * h : a == 1 ? 64 * h + 32 : a == 3 ? 128 + 32 * h
+        : a == 4 ? 192 + 96 * h : a == 2 ? 224 + 96 * h : 256 + 96 * h;
+}
+
+/* the pair MMAs of one K-chunk in ring stage `stage`; y-side operands in slots [A2_y][A_y][M_y] */
+__device__ __forceinline__ void issue_chunk(uint32_t tmem, uint32_t stage, bool first)
+{
+   const uint32_t ysb = stage + 3 * XMAT;
+#pragma unroll
+   for ( int ks = 0; ks < BK / Cfg<1>::UMMA_K; ++ks )
+   {
+      const uint32_t koff = ks * Cfg<1>::UMMA_K * Cfg<1>::ELEM;
+      const uint32_t acc = (!first || ks > 0) ? 1u : 0u;
+      const uint64_t xa = smem_desc<1>(stage + 0 * XMAT + koff);
+      const uint64_t xq = smem_desc<1>(stage + 1 * XMAT + koff);
+      const uint64_t xm = smem_desc<1>(stage + 2 * XMAT + koff);
+      const uint64_t y_q_a_m = smem_desc<1>(ysb + 0 * YMAT + koff);
+      const uint64_t y_a_m = smem_desc<1>(ysb + 1 * YMAT + koff);
+      const uint64_t y_m = smem_desc<1>(ysb + 2 * YMAT + koff);
+      mma_pair_tf32<2 * BNP>(tmem + 0, xa, y_a_m, acc);     /* Sxy | Sx */
+      mma_pair_tf32<BNP>(tmem + 128, xq, y_m, acc);         /* Sxx */
+      mma_pair_tf32<3 * BNP>(tmem + 192, xm, y_q_a_m, acc); /* Syy | Sy | n */
+   }
+}
+}  // namespace pair
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+   k_pearson_tc2(const __grid_constant__ TcMaps maps, TcArgs args, const int2* __restrict__ tiles, int ntiles)
+{
+   using namespace pair;
+   constexpr int S = STAGES;
+   extern __shared__ __align__(1024) unsigned char smem_raw[];
+   unsigned char* ring = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+   uint64_t* bars = (uint64_t*)(ring + RING);
+   uint32_t* tmem_holder = (uint32_t*)(bars + NBAR);
+   __shared__ int s_fail;
+   const int rank = (int)cluster_rank();
+   const bool lead = rank == 0;
+   const int unit0 = blockIdx.x >> 1, ustep = gridDim.x >> 1;
+   const int warp = threadIdx.x >> 5;
+   const int lane = threadIdx.x & 31;
+   const uint32_t full0 = smem_u32(&bars[0]);
+   const uint32_t empty0 = smem_u32(&bars[S]);
+   const uint32_t tfull = smem_u32(&bars[2 * S]);
+   const uint32_t tempty = smem_u32(&bars[2 * S + 1]);
+   const uint32_t done = smem_u32(&bars[2 * S + 2]);
+   const uint32_t full0_lead = mapa_rank(full0, 0);
+   const uint32_t tempty_lead = mapa_rank(tempty, 0);
+
+   if ( threadIdx.x == 0 )
+   {
+      s_fail = 0;
+      for ( int s = 0; s < S; ++s )
+      {
+         mbar_init(full0 + 8 * s, 1);
+         mbar_init(empty0 + 8 * s, 1);
+      }
+      mbar_init(tfull, 1);
+      mbar_init(tempty, 2 * EPI_WARPS);
+      mbar_init(done, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+   }
+   if ( warp == 1 )
+   {
+      /* one warp of each CTA: the pair's TMEM, the same columns in both */
+      asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                   "r"(TMEM_COLS));
+   }
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   cluster_sync();                      /* both CTAs' barriers are initialised before either signals the other */
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   const uint32_t tmem = *tmem_holder;
+
+   const int K = args.kchunks;
+   int issued = 0;                      /* producer: K-chunks whose copies this CTA issued */
+   if ( warp == 0 )
+   {
+      if ( lane == 0 )
+      {
+         /* ---- producer (both CTAs): this CTA's rows and genes of every chunk of the pair's tiles */
+         for ( int u = unit0; u < ntiles && !*(volatile int*)&s_fail; u += ustep )
+         {
+            const int2 ij = tiles[u];
+            for ( int kc = 0; kc < K; ++kc, ++issued )
+            {
+               const int s = issued % S;
+               if ( issued >= S && !mbar_wait(empty0 + 8 * s, ((issued / S) - 1) & 1) )
+               {
+                  atomicExch(&s_fail, 1);
+                  break;
+               }
+               if ( *(volatile int*)&s_fail ) break;
+               const uint32_t stage = smem_u32(ring + s * STAGE);
+               if ( lead ) mbar_expect_tx(full0 + 8 * s, 2 * STAGE);
+               for ( int m = 0; m < 3; ++m )
+               {
+                  tma_load_2d_pair(stage + m * XMAT, &maps.x[m], kc * BK, ij.x * BMP + rank * BM, full0_lead + 8 * s);
+                  tma_load_2d_pair(stage + 3 * XMAT + yslot<1>(m) * YMAT, &maps.y2[m], kc * BK, ij.y * BNP + rank * HB,
+                                   full0_lead + 8 * s);
+               }
+            }
+         }
+         /* the even CTA's last commits on this CTA's stages have landed */
+         if ( !*(volatile int*)&s_fail )
+         {
+            for ( int g = (issued > S ? issued - S : 0); g < issued; ++g )
+            {
+               if ( !mbar_wait(empty0 + 8 * (g % S), (g / S) & 1) )
+               {
+                  atomicExch(&s_fail, 1);
+                  break;
+               }
+            }
+         }
+      }
+   }
+   else if ( warp == 1 )
+   {
+      if ( lead && lane == 0 )
+      {
+         /* ---- MMA issuer (the even CTA) */
+         int used = 0, tl = 0;
+         for ( int u = unit0; u < ntiles && !*(volatile int*)&s_fail; u += ustep, ++tl )
+         {
+            if ( tl > 0 && !mbar_wait_cluster(tempty, (tl - 1) & 1) )
+            {
+               atomicExch(&s_fail, 1);
+               break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            bool ok = true;
+            for ( int kc = 0; kc < K; ++kc, ++used )
+            {
+               const int s = used % S;
+               if ( !mbar_wait(full0 + 8 * s, (used / S) & 1) )
+               {
+                  ok = false;
+                  break;
+               }
+               asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+               pair::issue_chunk(tmem, smem_u32(ring + s * STAGE), kc == 0);
+               commit_pair(empty0 + 8 * s, (uint16_t)0x3);   /* frees the stage in both CTAs */
+            }
+            if ( !ok )
+            {
+               atomicExch(&s_fail, 1);
+               break;
+            }
+            commit_pair(tfull, (uint16_t)0x3);               /* the tile's accumulators are final */
+         }
+         /* every MMA issued, reading both CTAs' shared memory, has completed */
+         commit_pair(done, (uint16_t)0x1);
+         if ( !mbar_wait(done, 0) ) atomicExch(&s_fail, 1);
+      }
+   }
+   else
+   {
+      /* ---- epilogue (both CTAs): warp w reads TMEM lanes 32 (w % 4) .. -- its quarter of this
+       * CTA's 128 rows -- and the tile's columns 32 h .. 32 h + 31, h = (w - 2) / 4 */
+      const int quarter = warp & 3;
+      const int h = (warp - 2) >> 2;
+      float* ebuf = (float*)(ring + RING + 256) + (warp - 2) * (32 * 8);
+      int tl = 0;
+      for ( int u = unit0; u < ntiles; u += ustep, ++tl )
+      {
+         int go = 0;
+         if ( lane == 0 ) go = !*(volatile int*)&s_fail && mbar_wait(tfull, tl & 1);
+         go = __shfl_sync(0xffffffffu, go, 0);
+         if ( !go )
+         {
+            if ( lane == 0 ) atomicExch(&s_fail, 1);
+            break;
+         }
+         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+         const int2 ij = tiles[u];
+         const uint32_t lane_base = tmem + ((uint32_t)(quarter * 32) << 16);
+         float r[2][16];
+#pragma unroll
+         for ( int w = 0; w < 2; ++w )
+         {
+            uint32_t v[NACC][16];
+#pragma unroll
+            for ( int a = 0; a < NACC; ++a ) tmem_ld16_async(lane_base + (uint32_t)acc_col(a, h) + w * 16, v[a]);
+            tmem_wait_ld();
+#pragma unroll
+            for ( int jj = 0; jj < 16; ++jj )
+            {
+               const float sxy = __uint_as_float(v[0][jj]), sx = __uint_as_float(v[1][jj]);
+               const float sy = __uint_as_float(v[2][jj]), sxx = __uint_as_float(v[3][jj]);
+               const float syy = __uint_as_float(v[4][jj]), n = __uint_as_float(v[5][jj]);
+               r[w][jj] = __int_as_float(0x7fc00000);
+               if ( n >= (float)args.min_samples && n > 0.f )
+               {
+                  const float num = diff_of_products(n, sxy, sx, sy);
+                  const float dx = diff_of_products(n, sxx, sx, sx);
+                  const float dy = diff_of_products(n, syy, sy, sy);
+                  r[w][jj] = num * rsqrtf(dx) * rsqrtf(dy);
+               }
+            }
+         }
+         /* every TMEM read of this warp is complete (tmem_wait_ld): hand TMEM back */
+         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+         __syncwarp();
+         if ( lane == 0 ) mbar_arrive_cluster(tempty_lead);
+         /* written through the warp's 32 x 8 shared-memory tile, as in the one-CTA form */
+         const int64_t x0 = (int64_t)ij.x * BMP + rank * BM + quarter * 32;
+#pragma unroll
+         for ( int g = 0; g < 4; ++g )
+         {
+            __syncwarp();
+#pragma unroll
+            for ( int j = 0; j < 8; ++j ) ebuf[lane * 8 + (j ^ (lane >> 2))] = r[g >> 1][(g & 1) * 8 + j];
+            __syncwarp();
+#pragma unroll
+            for ( int i = 0; i < 8; ++i )
+            {
+               const int rr = 4 * i + (lane >> 3), cc = lane & 7;
+               const int64_t x = x0 + rr;
+               const int64_t y = (int64_t)ij.y * BNP + h * HB + g * 8 + cc;
+               const int64_t p = x * (x - 1) / 2 + y;
+               if ( x < args.G && y < x && p >= args.start && p < args.end )
+                  args.out_corr[(p - args.start) * args.max_k] = ebuf[rr * 8 + (cc ^ i)];
+            }
+         }
+      }
+   }
+   __syncwarp();
+
+   /* ---- teardown: on failure drain the pair's copies (bounded), then meet, then free TMEM */
+   __syncthreads();
+   if ( *(volatile int*)&s_fail )
+   {
+      if ( threadIdx.x == 0 )
+      {
+         atomicCAS(args.status, 0, ST_TIMEOUT);
+         /* the even CTA's full barriers count both CTAs' copies */
+         if ( lead )
+            for ( int g = (issued > S ? issued - S : 0); g < issued; ++g ) mbar_wait(full0 + 8 * (g % S), (g / S) & 1);
+      }
+      __syncthreads();
+   }
+   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+   __syncthreads();
+   cluster_sync();                      /* neither CTA leaves while the other may use its memory */
+   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+   if ( warp == 1 )
+   {
+      asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
    }
 }
 
@@ -1012,12 +1318,19 @@ static EncodeTiledFn encode_fn()
 
 using namespace kinc_tc;
 
+/* rows of a tensor-core tile: 256 for the CTA-pair TF32 kernel, else 128 */
+static int tc_row_tile(int mode)
+{
+   return (mode == 1 && KINC_TC_PAIR) ? pair::BMP : BM;
+}
+
 /* prepare operands and tensor maps; returns a CUDA error or cudaSuccess */
 cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_expr, int mode, cudaStream_t st,
                        char* err, size_t errlen)
 {
    t.mode = mode;
-   t.Gp = (G + BM - 1) / BM * BM;
+   const int rows = tc_row_tile(mode);
+   t.Gp = (G + rows - 1) / rows * rows;
    t.Sp = (S + 63) / 64 * 64;
    const int elem = mode == 2 ? 2 : 4;
    const int nmat = mode == 2 ? 5 : 3;
@@ -1063,9 +1376,17 @@ cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_e
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
       CUresult r2 = enc(&t.maps.y[m], dt, 2, base, dims, strides, boxy, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if ( r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS )
+      CUresult r3 = CUDA_SUCCESS;
+      if ( mode == 1 )
       {
-         snprintf(err, errlen, "cuTensorMapEncodeTiled failed (%d, %d)", (int)r1, (int)r2);
+         /* the CTA-pair kernel's y-side boxes: each CTA's 32 of a tile's 64 genes */
+         const cuuint32_t boxh[2] = { (cuuint32_t)bk, (cuuint32_t)pair::HB };
+         r3 = enc(&t.maps.y2[m], dt, 2, base, dims, strides, boxh, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      }
+      if ( r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS || r3 != CUDA_SUCCESS )
+      {
+         snprintf(err, errlen, "cuTensorMapEncodeTiled failed (%d, %d, %d)", (int)r1, (int)r2, (int)r3);
          return cudaErrorInvalidValue;
       }
    }
@@ -1092,24 +1413,25 @@ void tc_release(TcState& t)
  * (I, J) with a pair y < x, in bands of TILE_GROUP row tiles, column by column within a band and
  * row by row within a column.  The persistent CTAs take the list round robin, so the tiles
  * running at one time lie in one band and a few columns: TILE_GROUP x-side row panels and a few
- * y-side column panels, which stay in L2 while the band's rows reuse them.  With CTA pairs
- * (KINC_TC_CLUSTER 2) the list holds units of two entries, tiles (I, J) and (I, J + 1) for even J;
- * where J + 1 holds no pair of row tile I the second entry is the placeholder (I, -J - 1).  Built
- * on the host into pinned memory and copied on the stream; the copy of the previous list must be
- * complete before the host buffer is rewritten.
+ * y-side column panels, which stay in L2 while the band's rows reuse them.  Built on the host into
+ * pinned memory and copied on the stream; the copy of the previous list must be complete before
+ * the host buffer is rewritten.
  */
 constexpr int TILE_GROUP = 8;
+
 
 static cudaError_t tc_tile_list(TcState& t, int Ia, int Ib, int64_t xb, cudaStream_t st)
 {
    if ( t.tiles_ia == Ia && t.tiles_ib == Ib && t.tiles_xb == xb ) return cudaSuccess;
    const int bn = t.mode == 1 ? Cfg<1>::BN : Cfg<2>::BN;
+   const int bm = tc_row_tile(t.mode);
+   const int group = TILE_GROUP * BM / bm;      /* the same 1,024 rows per band */
    auto jhi = [&](int I) {
-      const int64_t rowmax = std::min<int64_t>((int64_t)(I + 1) * BM - 1, xb);
+      const int64_t rowmax = std::min<int64_t>((int64_t)(I + 1) * bm - 1, xb);
       return rowmax >= 1 ? (int)((rowmax - 1) / bn) : -1;   /* last column tile holding some y < x */
    };
    int64_t n = 0;
-   for ( int I = Ia; I <= Ib; ++I ) n += (jhi(I) + KINC_TC_CLUSTER) / KINC_TC_CLUSTER * KINC_TC_CLUSTER;
+   for ( int I = Ia; I <= Ib; ++I ) n += jhi(I) + 1;
    if ( n > INT32_MAX ) return cudaErrorInvalidValue;
    cudaError_t e;
    if ( t.tiles_ev )
@@ -1139,16 +1461,12 @@ static cudaError_t tc_tile_list(TcState& t, int Ia, int Ib, int64_t xb, cudaStre
       t.tiles_cap = n;
    }
    int64_t k = 0;
-   for ( int b0 = Ia; b0 <= Ib; b0 += TILE_GROUP )
+   for ( int b0 = Ia; b0 <= Ib; b0 += group )
    {
-      const int b1 = std::min(Ib, b0 + TILE_GROUP - 1);
-      for ( int J = 0; J <= jhi(b1); J += KINC_TC_CLUSTER )
+      const int b1 = std::min(Ib, b0 + group - 1);
+      for ( int J = 0; J <= jhi(b1); ++J )
          for ( int I = b0; I <= b1; ++I )
-            if ( J <= jhi(I) )
-            {
-               t.h_tiles[k++] = make_int2(I, J);
-               if ( KINC_TC_CLUSTER == 2 ) t.h_tiles[k++] = make_int2(I, J + 1 <= jhi(I) ? J + 1 : -J - 1);
-            }
+            if ( J <= jhi(I) ) t.h_tiles[k++] = make_int2(I, J);
    }
    t.ntiles = (int)k;
    t.tiles_ia = Ia;
@@ -1160,44 +1478,47 @@ static cudaError_t tc_tile_list(TcState& t, int Ia, int Ib, int64_t xb, cudaStre
    return cudaEventRecord(t.tiles_ev, st);
 }
 
-/* the persistent tensor-core kernel over the current tile list: one CTA per SM, or as many CTA
- * pairs as can be resident at once (a pair needs two free SMs in one GPC) */
+/* the persistent one-CTA tensor-core kernel over the current tile list, one CTA per SM */
 template <int MODE>
 static cudaError_t tc_launch(const TcState& t, const TcArgs& a, cudaStream_t st)
 {
-   constexpr int CL = KINC_TC_CLUSTER;
-   static_assert(CL == 1 || CL == 2, "KINC_TC_CLUSTER is 1 or 2");
    const int smem = Layout<MODE>::SMEM;
-   cudaError_t e = cudaFuncSetAttribute(k_pearson_tc<MODE, CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+   cudaError_t e = cudaFuncSetAttribute(k_pearson_tc<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+   if ( e != cudaSuccess ) return e;
+   int dev = 0, sms = 0;
+   e = cudaGetDevice(&dev);
+   if ( e == cudaSuccess ) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+   if ( e != cudaSuccess ) return e;
+   const int grid = std::max(1, std::min(sms, t.ntiles));
+   k_pearson_tc<MODE><<<grid, TC_THREADS, smem, st>>>(t.maps, a, t.d_tiles, t.ntiles);
+   return cudaGetLastError();
+}
+
+/* the CTA-pair TF32 kernel: as many pairs as can be resident at once (a pair needs two free SMs
+ * of one GPC), each walking the list of 256 x 64 pair tiles */
+static cudaError_t tc_launch_pair(const TcState& t, const TcArgs& a, cudaStream_t st)
+{
+   const int smem = pair::SMEM;
+   cudaError_t e = cudaFuncSetAttribute(k_pearson_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
    if ( e != cudaSuccess ) return e;
    cudaLaunchConfig_t cfg = {};
    cudaLaunchAttribute attr[1];
+   cfg.gridDim = dim3(2);
    cfg.blockDim = dim3(TC_THREADS);
    cfg.dynamicSmemBytes = (size_t)smem;
    cfg.stream = st;
    attr[0].id = cudaLaunchAttributeClusterDimension;
-   attr[0].val.clusterDim.x = CL;
+   attr[0].val.clusterDim.x = 2;
    attr[0].val.clusterDim.y = 1;
    attr[0].val.clusterDim.z = 1;
    cfg.attrs = attr;
-   cfg.numAttrs = CL > 1 ? 1 : 0;
+   cfg.numAttrs = 1;
    int resident = 0;
-   if ( CL == 1 )
-   {
-      int dev = 0;
-      e = cudaGetDevice(&dev);
-      if ( e == cudaSuccess ) e = cudaDeviceGetAttribute(&resident, cudaDevAttrMultiProcessorCount, dev);
-   }
-   else
-   {
-      cfg.gridDim = dim3(CL);
-      e = cudaOccupancyMaxActiveClusters(&resident, k_pearson_tc<MODE, CL>, &cfg);
-   }
+   e = cudaOccupancyMaxActiveClusters(&resident, k_pearson_tc2, &cfg);
    if ( e != cudaSuccess ) return e;
    if ( resident < 1 ) return cudaErrorLaunchOutOfResources;
-   const int units = t.ntiles / CL;
-   cfg.gridDim = dim3((unsigned)(CL * std::max(1, std::min(resident, units))));
-   return cudaLaunchKernelEx(&cfg, k_pearson_tc<MODE, CL>, t.maps, a, (const int2*)t.d_tiles, t.ntiles);
+   cfg.gridDim = dim3((unsigned)(2 * std::max(1, std::min(resident, t.ntiles))));
+   return cudaLaunchKernelEx(&cfg, k_pearson_tc2, t.maps, a, (const int2*)t.d_tiles, t.ntiles);
 }
 
 /* enqueue the pairs [start, start+size): K = 1, corr[.][0] = r, NaN elsewhere */
@@ -1214,7 +1535,7 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
    };
    const int64_t xa = row_of(start);
    const int64_t xb = row_of(end - 1);
-   const int tile_x = t.mode == 3 ? SB : BM;
+   const int tile_x = t.mode == 3 ? SB : tc_row_tile(t.mode);
    const int tile_y = t.mode == 3 ? SB : t.mode == 1 ? Cfg<1>::BN : Cfg<2>::BN;
    const int Ia = (int)(xa / tile_x), Ib = (int)(xb / tile_x);
    const int Jn = (int)((xb + tile_y - 1) / tile_y);
@@ -1243,7 +1564,8 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
       const cudaError_t e = tc_tile_list(t, Ia, Ib, xb, st);
       if ( e != cudaSuccess ) return e;
       if ( t.ntiles == 0 ) return cudaGetLastError();
-      const cudaError_t le = t.mode == 1 ? tc_launch<1>(t, a, st) : tc_launch<2>(t, a, st);
+      const cudaError_t le = t.mode == 2 ? tc_launch<2>(t, a, st) : KINC_TC_PAIR ? tc_launch_pair(t, a, st)
+                                                                               : tc_launch<1>(t, a, st);
       if ( le != cudaSuccess ) return le;
    }
    if ( launches ) *launches += 2;

@@ -16,6 +16,7 @@ struct TcMaps
 {
    CUtensorMap x[5];                  /* 128-row boxes per operand plane */
    CUtensorMap y[5];                  /* 64-row boxes per operand plane */
+   CUtensorMap y2[3];                 /* 32-row boxes (TF32, the CTA-pair kernel's y-side halves) */
 };
 
 }  // namespace kinc_tc
@@ -24,7 +25,7 @@ struct TcMaps
 struct TcState
 {
    int mode = 0;                      /* 1 TF32, 2 3xBF16, 3 FP32 on the CUDA cores */
-   int Gp = 0, Sp = 0;                /* padded genes (x128) and samples (x64) */
+   int Gp = 0, Sp = 0;                /* padded genes (x128, x256 for the CTA-pair TF32 kernel) and samples (x64) */
    void* ops = nullptr;               /* operand planes [Gp][Sp] */
    kinc_tc::TcMaps maps;
    /* tensor-core tile list of the last range enqueued (row tiles tiles_ia..tiles_ib, rows to tiles_xb) */
