@@ -812,10 +812,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
  * other can still read or write its memory.
  *
  * Measured against the one-CTA form (KINC_TC_PAIR selects it): identical results; in ncu, on one
- * cold 16.7M-pair launch, tensor pipe busy 61.6 % of the time against 46.6 % and 0.60 against
- * 1.00 GB read from DRAM; timed in a loop over warm 134M-pair blocks, 4.63 against 4.47 ms.  The
- * bytes through shared memory are not what holds either form back: the MMA warp waits for the
- * next stage (the pair waits for the later of two SMs' copies).
+ * 16.7M-pair launch of the 20,000 x 2,000 matrix, 618 against 601 us, tensor pipe busy 61.6
+ * against 59.2 % of the time; timed in a loop over 134M-pair blocks, 4.63 against 4.47 ms.  So
+ * the bytes through shared memory are not what holds the one-CTA form back: its MMA warp waits
+ * for the next stage's copies, and the pair's waits for the later of two SMs' copies.
  */
 namespace pair {
 constexpr int BMP = 256;                  /* pair-tile rows, 128 per CTA */
