@@ -218,7 +218,7 @@ def run_reference(args, gem):
 def dense_leg(L, vp, check_pairs=1000000):
     """Pearson without clustering on the dense 20,000 x 2,000 workload (kinc_gb300.synthetic workload 3:
     rank-50 factors + noise, per-gene NaN rate ~U(0,0.2)): all 199,990,000 pairs with the tcgen05 tensor-core
-    form (TF32 and 3xBF16), the same contraction tiled in FP32 on the CUDA cores (the comparator
+    form (TF32, 3xBF16 and scaled FP16), the same contraction tiled in FP32 on the CUDA cores (the comparator
     for the tensor-core forms), and a 1,048,576-pair block with the plain per-pair FP32 kernel, all
     device-resident and timed with CUDA events; max |r - r_fp64| over a seeded random subset."""
     import ctypes
@@ -239,7 +239,7 @@ def dense_leg(L, vp, check_pairs=1000000):
                        "per-gene NaN rate ~U(0,0.2), pairwise-complete (semantics fixed)",
            "pairs": total, "fp64_check_pairs": int(len(idx))}
     stream = torch.cuda.Stream()
-    for prec in ("tf32", "3xbf16", "fp32tiled", "fp32"):
+    for prec in ("tf32", "3xbf16", "fp16", "fp32tiled", "fp32"):
         sim = Similarity(gem, semantics="fixed", precision=prec, maxclus=1)
         sim.initialize()
         ctx = sim._ctx
@@ -266,7 +266,7 @@ def dense_leg(L, vp, check_pairs=1000000):
             torch.cuda.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
-            reps = 3 if prec in ("tf32", "3xbf16") else 1
+            reps = 3 if prec in ("tf32", "3xbf16", "fp16") else 1
             e0.record(stream)
             for _ in range(reps):
                 run(False)
@@ -302,12 +302,15 @@ def dense_leg(L, vp, check_pairs=1000000):
     out["3xbf16"]["executed_tflops"] = 2 * out["3xbf16"]["useful_tflops"]
     out["3xbf16"]["frac_of_bf16_peak"] = out["3xbf16"]["executed_tflops"] / bf16
     out["3xbf16"]["frac_of_bf16_mma_peak"] = out["3xbf16"]["executed_tflops"] / mma["bf16"]
+    out["fp16"]["frac_of_f16_peak"] = out["fp16"]["useful_tflops"] / bf16
+    out["fp16"]["frac_of_f16_mma_peak"] = out["fp16"]["useful_tflops"] / mma["bf16"]
     out["mma_peak_tflops"] = mma
     out["peak_note"] = (f"frac_of_tf32_peak: half the measured bf16 library-GEMM burst ({bf16:.0f} TFLOP/s, "
                         "MEASURED_PEAKS.json); frac_of_*_mma_peak: the tcgen05 MMA rate measured in this run "
                         "(kinc_sim_tensor_peak, operands resident in shared memory: "
                         f"TF32 {mma['tf32']:.0f}, BF16 {mma['bf16']:.0f} TFLOP/s); 3xBF16 executes 2x the "
-                        "useful flops of the TF32 form")
+                        "useful flops of the TF32 form; FP16 (kind::f16, the BF16 rate) is compared with the "
+                        "bf16 burst and the BF16 MMA rate")
     sm_max = 2070.0
     if os.path.exists(peaks):
         with open(peaks) as fh:
@@ -318,6 +321,7 @@ def dense_leg(L, vp, check_pairs=1000000):
                                      f"sample are 6 FFMA")
     out["speedup_tf32_vs_fp32_tiled"] = out["tf32"]["pairs_per_s"] / out["fp32tiled"]["pairs_per_s"]
     out["speedup_3xbf16_vs_fp32_tiled"] = out["3xbf16"]["pairs_per_s"] / out["fp32tiled"]["pairs_per_s"]
+    out["speedup_fp16_vs_fp32_tiled"] = out["fp16"]["pairs_per_s"] / out["fp32tiled"]["pairs_per_s"]
     out["speedup_tf32_vs_fp32_per_pair"] = out["tf32"]["pairs_per_s"] / out["fp32"]["pairs_per_s"]
     out["speedup_3xbf16_vs_fp32_per_pair"] = out["3xbf16"]["pairs_per_s"] / out["fp32"]["pairs_per_s"]
     return out

@@ -68,9 +68,10 @@ typedef struct kinc_sim_params
                                 fit, BIC/ICL evaluated in float, a fit failing only on a zero
                                 covariance determinant (K-means: the LCG with the CPU path's fit) */
    int32_t precision;     /* clusmethod none + pearson + semantics 1 only: 0 per-pair FP32 (default),
-                             1 TF32 tensor cores, 2 3xBF16 tensor cores, 3 FP32 CUDA cores (the
-                             pairwise-complete Pearson as a tiled masked contraction; labels are not
-                             written) */
+                             1 TF32 tensor cores, 2 3xBF16 tensor cores, 3 FP32 CUDA cores, 4 FP16
+                             tensor cores with each gene's centred values scaled by a power of two
+                             (1-4: the pairwise-complete Pearson as a tiled masked contraction; labels
+                             are not written) */
 } kinc_sim_params;
 
 /* Fill `p` with the reference defaults. */

@@ -62,7 +62,7 @@ def _parser():
     sim.add_argument("--maxcorr", type=float, default=1.0)
     sim.add_argument("--ksize", type=int, default=4096)
     sim.add_argument("--semantics", default="reference", choices=["reference", "fixed"])
-    sim.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "3xbf16", "fp32tiled"])
+    sim.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "3xbf16", "fp32tiled", "fp16"])
     sim.add_argument("--autotune", action="store_true", help="pick the kernel launch shape by timing (cached)")
     sim.add_argument("--rand", default="glibc", choices=["glibc", "lcg"],
                      help="glibc: KINC's serial path; lcg: KINC's OpenCL worker (per-fit LCG GMM)")

@@ -107,7 +107,7 @@ int usage()
            "usage: kinc-gb300 run similarity --input EMX [--ccm CCM] [--cmx CMX] [--clusmethod none|gmm|kmeans]\n"
            "           [--corrmethod pearson|spearman|both] [--minexpr F] [--minsamp N] [--minclus N] [--maxclus N]\n"
            "           [--crit BIC|ICL] [--preout [true|false]] [--postout [true|false]] [--mincorr F] [--maxcorr F]\n"
-           "           [--ksize N] [--semantics reference|fixed] [--precision fp32|tf32|3xbf16|fp32tiled]\n"
+           "           [--ksize N] [--semantics reference|fixed] [--precision fp32|tf32|3xbf16|fp32tiled|fp16]\n"
            "           [--rand glibc|lcg] [--first-block N] [--blocks N | --world N --rank R [--by-cost]] [--resume]\n"
            "           [--autotune] [--little-endian]\n"
            "       kinc-gb300 run export-cmx --ccm CCM --cmx CMX --output TXT\n"
@@ -243,7 +243,7 @@ int run_similarity(const Args& a)
    p.corr_method = choice(a.str("corrmethod", "pearson"), { "pearson", "spearman", "both" }, "corrmethod", ok);
    p.criterion = choice(a.str("crit", "ICL"), { "BIC", "ICL" }, "crit", ok);
    p.semantics = choice(a.str("semantics", "reference"), { "reference", "fixed" }, "semantics", ok);
-   p.precision = choice(a.str("precision", "fp32"), { "fp32", "tf32", "3xbf16", "fp32tiled" }, "precision", ok);
+   p.precision = choice(a.str("precision", "fp32"), { "fp32", "tf32", "3xbf16", "fp32tiled", "fp16" }, "precision", ok);
    p.rand_mode = choice(a.str("rand", "glibc"), { "glibc", "lcg" }, "rand", ok);
    if ( !ok ) return 2;
    p.min_expr = (float)a.real("minexpr", p.min_expr);

@@ -461,10 +461,10 @@ int validate(const kinc_sim_params* p, int32_t G, int32_t S, std::string& why)
    }
    if ( p->semantics < 0 || p->semantics > 1 ) { why = "semantics must be 0 or 1"; return 0; }
    if ( p->rand_mode < 0 || p->rand_mode > 1 ) { why = "rand_mode must be 0 or 1"; return 0; }
-   if ( p->precision < 0 || p->precision > 3 ) { why = "precision must be 0, 1, 2 or 3"; return 0; }
+   if ( p->precision < 0 || p->precision > 4 ) { why = "precision must be 0, 1, 2, 3 or 4"; return 0; }
    if ( p->precision != 0 && (p->clus_method != 0 || p->corr_method != 0 || p->semantics != 1) )
    {
-      why = "precision TF32/3xBF16/FP32-tiled is the pairwise-complete Pearson contraction: it needs clus_method none, "
+      why = "precision TF32/3xBF16/FP32-tiled/FP16 is the pairwise-complete Pearson contraction: it needs clus_method none, "
             "corr_method pearson and semantics 1 (each sample's own values)";
       return 0;
    }

@@ -19,7 +19,12 @@
  * (6 x 64 of the 512 columns), and the four warps read them back with
  * tcgen05.ld and form r = (n Sxy - Sx Sy) / sqrt((n Sxx - Sx^2)(n Syy - Sy^2))
  * with error-compensated products.  3xBF16 splits a = hi + lo and sums
- * hi.hi + hi.lo + lo.hi (the mask is exact in BF16).
+ * hi.hi + hi.lo + lo.hi (the mask is exact in BF16).  FP16 (precision 4) scales each gene's
+ * centred values by a power of two so that the largest |a| is at most 1, which leaves r unchanged
+ * (r is scale invariant per gene, and a power of two scales exactly), and rounds a, a^2 and m to
+ * FP16: the same 11-bit significand as TF32, two bytes instead of four, and twice the MMA rate, so
+ * a 128-byte row of a K-chunk holds 64 samples instead of 32.  Values below 2^-14 of a gene's
+ * largest |a| (squares below 2^-14 of its largest square) keep fewer significant bits.
  *
  * The result is the mathematically pairwise-complete Pearson (each sample's own
  * values), i.e. semantics "fixed"; KINC's packed-array indexing is not a
@@ -31,6 +36,7 @@
 
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -81,6 +87,18 @@ template <> struct Cfg<1>             /* TF32: A, A2, M as fp32 rounded to tf32 
    static constexpr int NMAT = 3;
    static constexpr int UMMA_K = 8;
    static constexpr uint32_t A_FMT = 2, B_FMT = 2;   /* tf32 */
+};
+template <> struct Cfg<4>             /* FP16: A, A2, M with each gene scaled by a power of two */
+{
+   static constexpr int ELEM = 2;
+   static constexpr int BN = 64;
+   static constexpr int BK = 64;      /* 128-byte rows, SWIZZLE_128B */
+   static constexpr int ROWB = 128;
+   static constexpr int NMAT = 3;
+   static constexpr int UMMA_K = 16;
+   static constexpr int STAGES = 3;
+   static constexpr uint32_t A_FMT = 0, B_FMT = 0;   /* f16 */
+   static constexpr uint64_t LAYOUT = 2;              /* SWIZZLE_128B */
 };
 template <> struct Cfg<2>             /* 3xBF16: A_hi, A_lo, A2_hi, A2_lo, M as bf16 */
 {
@@ -191,7 +209,7 @@ __host__ __device__ constexpr uint32_t instr_desc()
 }
 
 /*
- * TF32: the six contractions share three x-side operands, so they are issued as three MMAs
+ * TF32 and FP16: the six contractions share three x-side operands, so they are issued as three MMAs
  * with the y-side operands stacked along N -- A_x.[A_y; M_y], A2_x.M_y, M_x.[A2_y; A_y; M_y]
  * (N = 128, 64, 192) -- which reads each x-side operand from shared memory once per K step
  * instead of two or three times (with N = 64 the operand reads, not the tensor pipe, bound the
@@ -216,7 +234,7 @@ __host__ __device__ constexpr uint32_t instr_desc()
 template <int MODE>
 __host__ __device__ constexpr bool merged()
 {
-   return (MODE == 1 && KINC_TC_MERGE) || (MODE == 2 && KINC_TC_MERGE_BF16);
+   return ((MODE == 1 || MODE == 4) && KINC_TC_MERGE) || (MODE == 2 && KINC_TC_MERGE_BF16);
 }
 
 /* shared-memory slot of y-side operand m (TF32: 0 A, 1 A2, 2 M; 3xBF16: 0 Ah, 1 Al, 2 Qh, 3 Ql, 4 M) */
@@ -224,7 +242,7 @@ template <int MODE>
 __host__ __device__ constexpr int yslot(int m)
 {
    return !merged<MODE>() ? m
-          : MODE == 1     ? (m == 0 ? 1 : m == 1 ? 0 : 2)
+          : MODE != 2     ? (m == 0 ? 1 : m == 1 ? 0 : 2)
                           : (m == 0 ? 2 : m == 1 ? 4 : m == 2 ? 1 : m == 3 ? 0 : 3);
 }
 
@@ -233,7 +251,7 @@ template <int MODE>
 __host__ __device__ constexpr int acc_col(int a)
 {
    return !merged<MODE>() ? a * Cfg<MODE>::BN
-          : MODE == 1     ? (a == 0 ? 0 : a == 1 ? 64 : a == 2 ? 256 : a == 3 ? 128 : a == 4 ? 192 : 320)
+          : MODE != 2     ? (a == 0 ? 0 : a == 1 ? 64 : a == 2 ? 256 : a == 3 ? 128 : a == 4 ? 192 : 320)
                           : (a == 0 ? 0 : a == 1 ? 64 : a == 2 ? 320 : a == 3 ? 192 : a == 4 ? 256 : 384);
 }
 
@@ -381,6 +399,27 @@ __global__ void k_tc_prep(const float* __restrict__ gem, int G, int S, int Gp, i
       n += __shfl_xor_sync(0xffffffffu, n, o);
    }
    const double mean = n > 0 ? sum / n : 0.0;
+   /* FP16: the power of two 2^-e with the gene's largest |a| below 2^e, so |a| 2^-e < 1 */
+   float scale = 1.f;
+   if ( MODE == 4 )
+   {
+      float amax = 0.f;
+      if ( warp < G )
+      {
+         for ( int s = lane; s < S; s += 32 )
+         {
+            const float v = gem[(size_t)warp * S + s];
+            if ( !isnan(v) && !(v < min_expr) ) amax = fmaxf(amax, fabsf((float)((double)v - mean)));
+         }
+      }
+      for ( int o = 16; o > 0; o >>= 1 ) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+      if ( amax > 0.f )
+      {
+         int e;
+         frexpf(amax, &e);                           /* amax = f 2^e, 0.5 <= f < 1 */
+         scale = ldexpf(1.f, -e);
+      }
+   }
    for ( int s = lane; s < Sp; s += 32 )
    {
       float a = 0.f, m = 0.f;
@@ -389,7 +428,7 @@ __global__ void k_tc_prep(const float* __restrict__ gem, int G, int S, int Gp, i
          const float v = gem[(size_t)warp * S + s];
          if ( !isnan(v) && !(v < min_expr) )
          {
-            a = (float)((double)v - mean);
+            a = (float)((double)v - mean) * scale;   /* exact: scale is a power of two */
             m = 1.f;
          }
       }
@@ -401,6 +440,13 @@ __global__ void k_tc_prep(const float* __restrict__ gem, int G, int S, int Gp, i
          f[o] = a;
          f[plane + o] = a2;
          f[2 * plane + o] = m;
+      }
+      else if ( MODE == 4 )
+      {
+         __half* h = (__half*)ops;
+         h[o] = __float2half_rn(a);
+         h[plane + o] = __float2half_rn(a2);
+         h[2 * plane + o] = __float2half_rn(m);
       }
       else if ( MODE == 1 )
       {
@@ -497,7 +543,7 @@ __device__ __forceinline__ void issue_chunk(uint32_t tmem, uint32_t stage, bool 
          mma<MODE, BN>(tmem + acc_col<MODE>(3), xq, y_m, acc);           /* Sxx */
          mma<MODE, 3 * BN>(tmem + acc_col<MODE>(4), xm, y_q_a_m, acc);   /* Syy | Sy | n */
       }
-      else if ( MODE == 1 )
+      else if ( MODE != 2 )
       {
          /* x side: 0 A, 1 A2, 2 M; y side likewise */
          const uint64_t xa = smem_desc<MODE>(stage + 0 * L::XMAT + koff);
@@ -1332,7 +1378,7 @@ cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_e
    const int rows = tc_row_tile(mode);
    t.Gp = (G + rows - 1) / rows * rows;
    t.Sp = (S + 63) / 64 * 64;
-   const int elem = mode == 2 ? 2 : 4;
+   const int elem = (mode == 2 || mode == 4) ? 2 : 4;
    const int nmat = mode == 2 ? 5 : 3;
    const size_t plane = (size_t)t.Gp * t.Sp * elem;
    cudaError_t e = cudaMalloc(&t.ops, plane * nmat);
@@ -1345,6 +1391,10 @@ cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_e
    else if ( mode == 2 )
    {
       k_tc_prep<2><<<blocks, 256, 0, st>>>(d_gem, G, S, t.Gp, t.Sp, min_expr, t.ops);
+   }
+   else if ( mode == 4 )
+   {
+      k_tc_prep<4><<<blocks, 256, 0, st>>>(d_gem, G, S, t.Gp, t.Sp, min_expr, t.ops);
    }
    else
    {
@@ -1359,17 +1409,19 @@ cudaError_t tc_prepare(TcState& t, const float* d_gem, int G, int S, float min_e
       snprintf(err, errlen, "cuTensorMapEncodeTiled is not available");
       return cudaErrorNotSupported;
    }
-   const int bk = mode == 1 ? Cfg<1>::BK : Cfg<2>::BK;
-   const int bn = mode == 1 ? Cfg<1>::BN : Cfg<2>::BN;
+   const int bk = mode == 1 ? Cfg<1>::BK : mode == 4 ? Cfg<4>::BK : Cfg<2>::BK;
+   const int bn = mode == 1 ? Cfg<1>::BN : mode == 4 ? Cfg<4>::BN : Cfg<2>::BN;
    for ( int m = 0; m < nmat; ++m )
    {
       char* base = (char*)t.ops + m * plane;
       const cuuint64_t dims[2] = { (cuuint64_t)t.Sp, (cuuint64_t)t.Gp };
       const cuuint64_t strides[1] = { (cuuint64_t)t.Sp * elem };
       const cuuint32_t estr[2] = { 1, 1 };
-      const CUtensorMapDataType dt = mode == 1 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-      const CUtensorMapSwizzle sw = (mode == 1 && Cfg<1>::ROWB == 128) ? CU_TENSOR_MAP_SWIZZLE_128B
-                                                                        : CU_TENSOR_MAP_SWIZZLE_64B;
+      const CUtensorMapDataType dt = mode == 1   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                     : mode == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+      const int rowb = mode == 1 ? Cfg<1>::ROWB : mode == 4 ? Cfg<4>::ROWB : Cfg<2>::ROWB;
+      const CUtensorMapSwizzle sw = rowb == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
       const cuuint32_t boxx[2] = { (cuuint32_t)bk, (cuuint32_t)BM };
       const cuuint32_t boxy[2] = { (cuuint32_t)bk, (cuuint32_t)bn };
       CUresult r1 = enc(&t.maps.x[m], dt, 2, base, dims, strides, boxx, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
@@ -1423,7 +1475,7 @@ constexpr int TILE_GROUP = 8;
 static cudaError_t tc_tile_list(TcState& t, int Ia, int Ib, int64_t xb, cudaStream_t st)
 {
    if ( t.tiles_ia == Ia && t.tiles_ib == Ib && t.tiles_xb == xb ) return cudaSuccess;
-   const int bn = t.mode == 1 ? Cfg<1>::BN : Cfg<2>::BN;
+   const int bn = t.mode == 1 ? Cfg<1>::BN : t.mode == 4 ? Cfg<4>::BN : Cfg<2>::BN;
    const int bm = tc_row_tile(t.mode);
    const int group = TILE_GROUP * BM / bm;      /* the same 1,024 rows per band */
    auto jhi = [&](int I) {
@@ -1536,7 +1588,7 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
    const int64_t xa = row_of(start);
    const int64_t xb = row_of(end - 1);
    const int tile_x = t.mode == 3 ? SB : tc_row_tile(t.mode);
-   const int tile_y = t.mode == 3 ? SB : t.mode == 1 ? Cfg<1>::BN : Cfg<2>::BN;
+   const int tile_y = t.mode == 3 ? SB : t.mode == 1 ? Cfg<1>::BN : t.mode == 4 ? Cfg<4>::BN : Cfg<2>::BN;
    const int Ia = (int)(xa / tile_x), Ib = (int)(xb / tile_x);
    const int Jn = (int)((xb + tile_y - 1) / tile_y);
    if ( Jn < 1 ) return cudaSuccess;
@@ -1551,7 +1603,7 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
    a.end = end;
    a.out_corr = d_corr;
    a.status = d_status;
-   a.kchunks = t.Sp / (t.mode == 1 ? Cfg<1>::BK : Cfg<2>::BK);   /* Sp is a multiple of 64 */
+   a.kchunks = t.Sp / (t.mode == 1 ? Cfg<1>::BK : t.mode == 4 ? Cfg<4>::BK : Cfg<2>::BK);   /* Sp: a multiple of 64 */
    if ( t.mode == 3 )
    {
       a.kchunks = t.Sp / SK;
@@ -1564,8 +1616,10 @@ cudaError_t tc_enqueue(TcState& t, int G, int S, int min_samples, int max_k, int
       const cudaError_t e = tc_tile_list(t, Ia, Ib, xb, st);
       if ( e != cudaSuccess ) return e;
       if ( t.ntiles == 0 ) return cudaGetLastError();
-      const cudaError_t le = t.mode == 2 ? tc_launch<2>(t, a, st) : KINC_TC_PAIR ? tc_launch_pair(t, a, st)
-                                                                               : tc_launch<1>(t, a, st);
+      const cudaError_t le = t.mode == 2   ? tc_launch<2>(t, a, st)
+                             : t.mode == 4 ? tc_launch<4>(t, a, st)
+                             : KINC_TC_PAIR ? tc_launch_pair(t, a, st)
+                                            : tc_launch<1>(t, a, st);
       if ( le != cudaSuccess ) return le;
    }
    if ( launches ) *launches += 2;

@@ -24,7 +24,7 @@ struct TcMaps
 /* Operand planes and tensor maps of one expression matrix. */
 struct TcState
 {
-   int mode = 0;                      /* 1 TF32, 2 3xBF16, 3 FP32 on the CUDA cores */
+   int mode = 0;                      /* 1 TF32, 2 3xBF16, 3 FP32 on the CUDA cores, 4 scaled FP16 */
    int Gp = 0, Sp = 0;                /* padded genes (x128, x256 for the CTA-pair TF32 kernel) and samples (x64) */
    void* ops = nullptr;               /* operand planes [Gp][Sp] */
    kinc_tc::TcMaps maps;

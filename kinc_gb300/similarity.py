@@ -21,7 +21,7 @@ CORRELATION_NAMES = ["pearson", "spearman", "both"]
 CRITERION_NAMES = ["BIC", "ICL"]
 SEMANTICS_NAMES = ["reference", "fixed"]
 RAND_NAMES = ["glibc", "lcg"]
-PRECISION_NAMES = ["fp32", "tf32", "3xbf16", "fp32tiled"]
+PRECISION_NAMES = ["fp32", "tf32", "3xbf16", "fp32tiled", "fp16"]
 
 
 class InvalidArgument(ValueError):

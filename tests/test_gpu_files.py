@@ -235,7 +235,7 @@ def test_sharded_command_line_runs_merge_into_the_single_run(tmp_path, by_cost):
         assert (tmp_path / f"all.{ext}").read_bytes() == (tmp_path / f"one.{ext}").read_bytes(), ext
 
 
-@pytest.mark.parametrize("precision", ["tf32", "3xbf16"])
+@pytest.mark.parametrize("precision", ["tf32", "3xbf16", "fp16"])
 def test_run_to_files_tensor_core_matches_execute(tmp_path, precision):
     """The tensor-core form through the file runner keeps exactly the correlations execute() returns
     (filtered at mincorr) -- the runner and the host process() see the same device results."""

@@ -66,7 +66,7 @@ def test_gmm_icl_both_30000x500_middle():
     sim.close()
 
 
-@pytest.mark.parametrize("precision,tol", [("tf32", 1e-4), ("3xbf16", 1e-5)])
+@pytest.mark.parametrize("precision,tol", [("tf32", 1e-4), ("3xbf16", 1e-5), ("fp16", 1e-4)])
 def test_tensor_core_20000x2000_vs_fp64(precision, tol):
     gem = synthetic.generate(3)
     sim = Similarity(gem, semantics="fixed", precision=precision)

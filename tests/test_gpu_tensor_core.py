@@ -1,4 +1,4 @@
-"""Masked-contraction Pearson (precision TF32 / 3xBF16 on the tensor cores,
+"""Masked-contraction Pearson (precision TF32 / 3xBF16 / scaled FP16 on the tensor cores,
 FP32 tiled on the CUDA cores; clusmethod none): maximum |r| error against the
 FP64 pairwise-complete oracle, and agreement with the plain per-pair FP32
 kernel on the same pairs (semantics fixed)."""
@@ -11,14 +11,14 @@ from oracle import pyoracle
 pytestmark = pytest.mark.gpu
 
 # max |r - r_fp64| allowed per precision
-TOL = {"3xbf16": 1e-4, "tf32": 2e-3, "fp32tiled": 1e-5}
+TOL = {"3xbf16": 1e-4, "tf32": 2e-3, "fp16": 2e-3, "fp32tiled": 1e-5}
 
 
 def _dense(genes, samples, seed=5):
     return synthetic.generate(3, genes=genes, samples=samples, seed=seed)
 
 
-@pytest.mark.parametrize("precision", ["tf32", "3xbf16", "fp32tiled"])
+@pytest.mark.parametrize("precision", ["tf32", "3xbf16", "fp16", "fp32tiled"])
 @pytest.mark.parametrize("shape", [(300, 500), (257, 130), (65, 33)])
 def test_tensor_core_pearson_vs_fp64(precision, shape):
     G, S = shape
@@ -38,7 +38,7 @@ def test_tensor_core_pearson_vs_fp64(precision, shape):
     assert err <= TOL[precision], f"max |dr| {err}"
 
 
-@pytest.mark.parametrize("precision", ["tf32", "3xbf16", "fp32tiled"])
+@pytest.mark.parametrize("precision", ["tf32", "3xbf16", "fp16", "fp32tiled"])
 def test_tensor_core_partial_range_matches_full(precision):
     gem = _dense(200, 96, seed=9)
     sim = Similarity(gem, semantics="fixed", precision=precision)
@@ -47,6 +47,29 @@ def test_tensor_core_partial_range_matches_full(precision):
     part = sim.execute(None, start=12345, size=4321)
     sim.close()
     assert np.array_equal(np.nan_to_num(part.corr[:, 0], nan=9), np.nan_to_num(full.corr[12345:16666, 0], nan=9))
+
+
+def test_fp16_scaling_with_outliers_vs_fp64():
+    """Scaled FP16: each gene is scaled by a power of two so that its largest centred |value| is
+    below 1; genes with one sample a thousand times the spread push the others' squares into FP16's
+    subnormal range, and r stays within the TF32 bound."""
+    gem = _dense(160, 300, seed=21)
+    rng = np.random.default_rng(22)
+    for g in rng.choice(160, size=20, replace=False):
+        s = rng.integers(300)
+        if np.isfinite(gem[g, s]):
+            gem[g, s] += 1000.0 * np.nanstd(gem[g])
+    sim = Similarity(gem, semantics="fixed", precision="fp16")
+    sim.initialize()
+    total = sim.total_pairs()
+    res = sim.execute(None, start=0, size=total)
+    sim.close()
+    x, y = pyoracle.pair_xy(np.arange(total))
+    ref = pyoracle.pearson_fp64_pairs(gem, x, y)
+    got = res.corr[:, 0].astype(np.float64)
+    both = ~np.isnan(ref)
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
+    assert np.abs(got[both] - ref[both]).max() <= TOL["fp16"]
 
 
 def test_plain_fp32_fixed_semantics_vs_fp64():
