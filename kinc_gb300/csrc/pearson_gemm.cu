@@ -53,6 +53,10 @@ constexpr long long WAIT_CYCLES = 4ll << 30;  /* ~2 s of SM clock before a wait 
 
 constexpr int ST_TIMEOUT = 10;        /* an mbarrier wait expired */
 
+/* warps of a tensor-core CTA: producer, MMA issuer, then two epilogue warps per TMEM lane quarter */
+constexpr int EPI_WARPS = 8;
+constexpr int TC_THREADS = (2 + EPI_WARPS) * 32;
+
 /* per precision: element type, elements per K-chunk row, swizzle, operands per side */
 template <int MODE> struct Cfg;
 /*
@@ -121,7 +125,7 @@ struct Layout
    static constexpr int STAGE = Cfg<MODE>::NMAT * (XMAT + YMAT);
    static constexpr int RING = Cfg<MODE>::STAGES * STAGE;
    /* the epilogue warps' transposition tiles: 32 rows x 8 columns of r each */
-   static constexpr int EBUF = 8 /* epilogue warps */ * 32 * 8 * 4;
+   static constexpr int EBUF = EPI_WARPS * 32 * 8 * 4;
    static constexpr int SMEM = RING + 1024 /* alignment slack */ + 256 /* barriers */ + EBUF;
    static_assert(SMEM <= 227 * 1024, "ring, barriers and epilogue tiles fit the shared memory of one CTA");
 };
@@ -602,8 +606,6 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
  * once per CTA.  Every mbarrier wait is bounded: on expiry the CTA records an error, every role
  * stops, the CTA drains its own copies (bounded), frees its TMEM and returns.
  */
-constexpr int EPI_WARPS = 8;
-constexpr int TC_THREADS = (2 + EPI_WARPS) * 32;
 
 template <int MODE>
 __global__ void __launch_bounds__(TC_THREADS, 1)
