@@ -1,8 +1,8 @@
 /*
  * pearson_gemm.cu -- pairwise-complete Pearson for clusmethod none as a dense
- * masked contraction on the tcgen05 tensor cores (precision TF32 or 3xBF16),
- * and the same contraction tiled on the CUDA cores in FP32 (precision 3, the
- * comparator for the tensor-core forms).
+ * masked contraction on the tcgen05 tensor cores (precision 1 TF32, 2 3xBF16,
+ * 4 scaled FP16), and the same contraction tiled on the CUDA cores in FP32
+ * (precision 3, the comparator for the tensor-core forms).
  *
  * For genes x, y with usable-sample masks m and centred values a (a = v - mean
  * over the gene's usable samples, 0 where unusable), every sum Pearson needs
@@ -12,11 +12,11 @@
  *     Sx  = A  . M^T      Sy  = M . A^T
  *     Sxx = A2 . M^T      Syy = M . A2^T       (A2 = a^2)
  * Centring by the gene mean changes no correlation (r is shift invariant per
- * gene) but removes the cancellation that would otherwise swamp TF32.  One CTA
- * computes a 128 x 64 tile of pairs: TMA streams 128-byte-swizzled K-chunks of
- * the operands into a 3-stage shared-memory ring, one thread issues the
- * tcgen05.mma instructions (M=128, N=64) into six accumulators held in TMEM
- * (6 x 64 of the 512 columns), and the four warps read them back with
+ * gene) but removes the cancellation that would otherwise swamp TF32.  A CTA
+ * computes 128 x 64 tiles of pairs: TMA streams swizzled K-chunks of the
+ * operands into a 3-stage shared-memory ring, one thread issues the
+ * tcgen05.mma instructions (M = 128) into six 64-column accumulators held in
+ * TMEM (384 of the 512 columns), and eight warps read them back with
  * tcgen05.ld and form r = (n Sxy - Sx Sy) / sqrt((n Sxx - Sx^2)(n Syy - Sy^2))
  * with error-compensated products.  3xBF16 splits a = hi + lo and sums
  * hi.hi + hi.lo + lo.hi (the mask is exact in BF16).  FP16 (precision 4) scales each gene's
