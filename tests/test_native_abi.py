@@ -41,7 +41,7 @@ def test_params_default_matches_reference_defaults(native):
 
 
 @pytest.mark.parametrize("field,value", [("min_clusters", 3), ("min_samples", 0), ("clus_method", 7),
-                                         ("max_clusters", 65), ("min_corr", 1.5)])
+                                         ("max_clusters", 65), ("min_corr", 1.5), ("precision", 5)])
 def test_create_rejects_invalid_arguments(native, field, value):
     p = _native.SimParams()
     native.kinc_sim_params_default(ctypes.byref(p))
@@ -56,6 +56,21 @@ def test_create_rejects_invalid_arguments(native, field, value):
     if field == "min_clusters":
         assert b"Minimum clusters must be less than or equal to maximum clusters." in \
             native.kinc_sim_last_error(None)
+
+
+@pytest.mark.parametrize("precision", [1, 2, 3, 4])
+def test_contraction_precisions_need_pairwise_complete_pearson(native, precision):
+    """The tensor-core and tiled precisions compute the pairwise-complete Pearson contraction only:
+    clus_method none, corr_method pearson, semantics 1 (each sample's own values)."""
+    p = _native.SimParams()
+    native.kinc_sim_params_default(ctypes.byref(p))
+    p.precision = precision
+    p.clus_method = 1
+    gem = np.zeros((4, 8), np.float32)
+    ctx = ctypes.c_void_p()
+    rc = native.kinc_sim_create(gem.ctypes.data_as(ctypes.c_void_p), 4, 8, ctypes.byref(p), ctypes.byref(ctx))
+    assert rc == _native.EINVAL
+    assert b"pairwise-complete Pearson contraction" in native.kinc_sim_last_error(None)
 
 
 def _process_native(native, p, S, start, K, labels, corr):

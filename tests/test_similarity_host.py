@@ -19,6 +19,18 @@ def test_defaults_and_choices():
         Similarity(np.zeros((10, 5), np.float32), clusmethod="dbscan")
 
 
+@pytest.mark.parametrize("name,value", [("fp32", 0), ("tf32", 1), ("3xbf16", 2), ("fp32tiled", 3), ("fp16", 4)])
+def test_precision_names_map_to_the_abi(name, value):
+    """The precision names of the Python mirror and the CLI, and the ABI's kinc_sim_params.precision."""
+    s = Similarity(np.zeros((10, 5), np.float32), semantics="fixed", precision=name)
+    assert s.params.precision == value
+
+
+def test_unknown_precision_is_rejected():
+    with pytest.raises(InvalidArgument):
+        Similarity(np.zeros((10, 5), np.float32), precision="fp8")
+
+
 def test_cluster_range_check():
     s = Similarity(np.zeros((10, 5), np.float32), minclus=4, maxclus=2)
     with pytest.raises(InvalidArgument, match="Minimum clusters"):
