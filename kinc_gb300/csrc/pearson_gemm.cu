@@ -601,9 +601,9 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar)
  * Warp 0 streams the K-chunks of its tiles through the ring without stopping at tile boundaries;
  * warp 1 issues a tile's MMAs once the epilogue has released TMEM from the previous tile and
  * signals `tfull` when the accumulators are final; warps 2..9 (two per TMEM lane quarter, each
- * half of the 64 columns) read them back, form r, write it and signal `tempty`.  So the next
- * tile's operand loads overlap this tile's epilogue, and TMEM, barriers and the ring are set up
- * once per CTA.  Every mbarrier wait is bounded: on expiry the CTA records an error, every role
+ * half of the 64 columns) read them back, form r, signal `tempty` and then write r.  So the next
+ * tile's operand loads overlap this tile's epilogue, its MMAs overlap the epilogue's writes, and
+ * TMEM, barriers and the ring are set up once per CTA.  Every mbarrier wait is bounded: on expiry the CTA records an error, every role
  * stops, the CTA drains its own copies (bounded), frees its TMEM and returns.
  */
 
