@@ -72,6 +72,39 @@ def test_fp16_scaling_with_outliers_vs_fp64():
     assert np.abs(got[both] - ref[both]).max() <= TOL["fp16"]
 
 
+@pytest.mark.parametrize("precision", ["tf32", "3xbf16", "fp16"])
+def test_one_column_results(precision):
+    """One correlation column (maxclus 1, the bench's dense form): every pair of a range starting
+    mid-row, written into device arrays that held other values, gets K = 1 and the r of the
+    five-column run."""
+    import ctypes
+
+    import torch
+
+    from kinc_gb300 import _native
+    gem = _dense(300, 500, seed=31)
+    start, size = 1234, 40000
+    full = Similarity(gem, semantics="fixed", precision=precision)
+    full.initialize()
+    want = full.execute(None, start=start, size=size)
+    full.close()
+    sim = Similarity(gem, semantics="fixed", precision=precision, maxclus=1)
+    sim.initialize()
+    L = _native.load()
+    dK = torch.full((size,), 7, dtype=torch.int8, device="cuda")
+    dC = torch.full((size, 1), 2.0, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()             # the worker runs on its own stream
+    vp = ctypes.c_void_p
+    _native.check(L.kinc_sim_execute_block_device(sim._ctx, start, size, vp(dK.data_ptr()), None,
+                                                  vp(dC.data_ptr()), None), sim._ctx)
+    _native.check(L.kinc_sim_synchronize(sim._ctx), sim._ctx)
+    torch.cuda.synchronize()
+    sim.close()
+    assert torch.all(dK == 1).item()
+    got = dC[:, 0].cpu().numpy()
+    assert np.array_equal(np.nan_to_num(got, nan=9.0), np.nan_to_num(want.corr[:, 0], nan=9.0))
+
+
 def test_plain_fp32_fixed_semantics_vs_fp64():
     gem = _dense(120, 300)
     sim = Similarity(gem, semantics="fixed")
