@@ -187,7 +187,8 @@ int32_t kinc_sim_last_launch_count(const kinc_sim_ctx* ctx);
  * (kinc_sim_autotune) rather than fixed.  Replaces the hand-set work-item
  * count of KINC's OpenCL worker (--ksize, src/core/similarity_input.cpp:241-251),
  * which this worker does not need for correctness.
- *   warps_per_cta  4, 8 or 16: warps of one CTA (the SM holds 16 warps either way)
+ *   warps_per_cta  warps of one CTA: 4, 8 or 16 (GMM: 4, 10 or 20); the SM holds
+ *                  16 warps (GMM: 20, at fewer registers each) either way
  *   rounds         1: a CTA's warps take their 32-pair tiles together, round by
  *                  round (they then run the same code region at the same time);
  *                  0: every warp takes its next tile as soon as it is done
@@ -260,7 +261,7 @@ int kinc_sim_work_counters(kinc_sim_ctx* ctx, uint64_t* out, int reset);
  * inside the library, which every GPU that loads the library holds until the
  * process exits.  Limits: samples <= 4096 and size <= 262144 pairs per call,
  * and the per-gene masks, per-pair arrays and the working space of at least
- * one 16-warp block must fit in the 64 MiB; precision must be 0 (the per-pair FP32
+ * one block of the kernel's warps (16; GMM 20) must fit in the 64 MiB; precision must be 0 (the per-pair FP32
  * path; corr_method 0, 1 or 2 as in kinc_sim_create).  Other requests are
  * rejected with KINC_SIM_EINVAL and a message from kinc_sim_last_error(NULL).
  *

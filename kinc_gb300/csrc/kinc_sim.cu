@@ -581,31 +581,35 @@ static KmPool km_pool_sizes(const kinc_sim_params& p, const SimKernel& k)
 
 /* ---------------------------------------------------------- launch shape */
 
-/* the shape measured best on the clustering workloads: 16-warp CTAs, rounds for GMM and no
- * clustering, free-running warps for K-means, the sweeps prefetching 8 samples ahead */
-static kinc_sim_launch default_launch(int clus)
+/* the shape measured best on the clustering workloads: CTAs of the kernel's full warp count (20
+ * for GMM, 16 otherwise), rounds for GMM and no clustering, free-running warps for K-means, the
+ * sweeps prefetching 8 samples ahead */
+static kinc_sim_launch default_launch(const SimKernel& k, int clus)
 {
    kinc_sim_launch l {};
-   l.warps_per_cta = WARPS_PER_BLOCK;
+   l.warps_per_cta = k.wpb;
    l.rounds = ((KINC_CTA_ROUNDS) >> clus) & 1;
    l.prefetch = 8;
    return l;
 }
 
-static bool launch_valid(const kinc_sim_launch& l)
+/* warps per CTA: 4, 8, 10, 16 or 20 that divide the kernel's warp count wpb (16: 4, 8, 16;
+ * 20: 4, 10, 20) */
+static bool launch_valid(const kinc_sim_launch& l, int wpb)
 {
-   const bool w = l.warps_per_cta == 4 || l.warps_per_cta == 8 || l.warps_per_cta == 16 ||
-                  l.warps_per_cta == WARPS_PER_BLOCK;
+   const int nw = l.warps_per_cta;
+   const bool w = (nw == 4 || nw == 8 || nw == 10 || nw == 16 || nw == 20 || nw == wpb) && nw <= wpb &&
+                  wpb % nw == 0;
    const bool r = l.rounds == 0 || l.rounds == 1;
    const bool f = l.prefetch == 0 || l.prefetch == 4 || l.prefetch == 8 || l.prefetch == 16;
-   return w && WARPS_PER_BLOCK % l.warps_per_cta == 0 && r && f;
+   return w && r && f;
 }
 
 /* the grid and shared memory of a shape: as many CTAs per SM as fit, within the warp scratch
  * slots the context holds */
 static int apply_launch(kinc_sim_ctx* ctx, const kinc_sim_launch& l)
 {
-   if ( !launch_valid(l) )
+   if ( !launch_valid(l, ctx->kern.wpb) )
       return fail(ctx, KINC_SIM_EINVAL, "launch shape warps_per_cta %d rounds %d prefetch %d not supported",
                   l.warps_per_cta, l.rounds, l.prefetch);
    const int nw = l.warps_per_cta;
@@ -715,14 +719,14 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    /* GMM parameters in shared memory take the room the sort buffers would use */
    const size_t param_bytes_warp = (KINC_GMM_PARAMS_SMEM && ctx->kern.clus == 1 && ctx->kern.ks > 0)
                                       ? (size_t)7 * ctx->kern.ks * TILE * sizeof(float) : 0;
-   ctx->smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * WARPS_PER_BLOCK <= 200 * 1024;
-   ctx->smem_bytes = (int)((ctx->smem_sort ? sort_bytes_warp : 0) + param_bytes_warp) * WARPS_PER_BLOCK;
+   const int wpb = ctx->kern.wpb;
+   ctx->smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * wpb <= 200 * 1024;
+   ctx->smem_bytes = (int)((ctx->smem_sort ? sort_bytes_warp : 0) + param_bytes_warp) * wpb;
    /* opt in whenever dynamic shared memory is used: the kernel's own static words count against 48 KB too */
    if ( ctx->smem_bytes > 0 )
       CKC(cudaFuncSetAttribute(ctx->kern.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, ctx->smem_bytes));
    int per_sm = 0;
-   CKC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ctx->kern.fn, WARPS_PER_BLOCK * 32,
-                                                     ctx->smem_bytes));
+   CKC(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ctx->kern.fn, wpb * 32, ctx->smem_bytes));
    per_sm = std::max(1, per_sm);
 
    /* scratch: per warp slot, interleaved by lane */
@@ -743,9 +747,9 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    CKC(cudaMemGetInfo(&free_b, &total_b));
    int grid = prop.multiProcessorCount * per_sm;
    const size_t scratch_cap = free_b / 4;
-   while ( grid > prop.multiProcessorCount && (size_t)grid * WARPS_PER_BLOCK * slot_bytes > scratch_cap )
+   while ( grid > prop.multiProcessorCount && (size_t)grid * wpb * slot_bytes > scratch_cap )
       grid -= prop.multiProcessorCount;
-   const size_t slots = (size_t)grid * WARPS_PER_BLOCK;
+   const size_t slots = (size_t)grid * wpb;
    ctx->sms = prop.multiProcessorCount;
    snprintf(ctx->gpu_name, sizeof ctx->gpu_name, "%s", prop.name);
    ctx->slots = (int64_t)slots;
@@ -841,7 +845,7 @@ extern "C" int kinc_sim_create(const float* gem, int32_t genes, int32_t samples,
    ctx->dd.rng0 = ctx->d_rng0;
    if ( params->precision == 0 )
    {
-      const kinc_sim_launch def = default_launch(params->clus_method);
+      const kinc_sim_launch def = default_launch(ctx->kern, params->clus_method);
       const int rc = apply_launch(ctx, def);
       if ( rc ) return bail(rc);
    }
@@ -1032,7 +1036,7 @@ std::string tune_key(const kinc_sim_ctx* ctx)
    return buf;
 }
 
-bool tune_cache_lookup(const std::string& key, kinc_sim_launch& out)
+bool tune_cache_lookup(const std::string& key, int wpb, kinc_sim_launch& out)
 {
    const std::string path = tune_cache_path();
    if ( path.empty() ) return false;
@@ -1047,7 +1051,7 @@ bool tune_cache_lookup(const std::string& key, kinc_sim_launch& out)
       *tab = 0;
       kinc_sim_launch l {};
       if ( key == line && sscanf(tab + 1, "%d %d %d", &l.warps_per_cta, &l.rounds, &l.prefetch) == 3
-           && launch_valid(l) )
+           && launch_valid(l, wpb) )
       {
          out = l;          /* the last entry for a key wins */
          found = true;
@@ -1111,7 +1115,7 @@ extern "C" int kinc_sim_autotune(kinc_sim_ctx* ctx, int64_t start, int64_t size,
    if ( size <= 0 ) return fail(ctx, KINC_SIM_EINVAL, "autotune needs at least one pair");
    const std::string key = tune_key(ctx);
    kinc_sim_launch best = ctx->launch;
-   if ( use_cache && tune_cache_lookup(key, best) )
+   if ( use_cache && tune_cache_lookup(key, ctx->kern.wpb, best) )
    {
       rc = apply_launch(ctx, best);
       if ( rc == KINC_SIM_OK && chosen ) *chosen = best;
@@ -1130,7 +1134,7 @@ extern "C" int kinc_sim_autotune(kinc_sim_ctx* ctx, int64_t start, int64_t size,
    rc = time_launch(ctx, best, start, size, best_ms);
    if ( rc ) return rc;
    record(best, best_ms);
-   const int warps_v[] = { 4, 8, 16 };
+   const int warps_v[] = { 4, 8, 10, 16, 20 };
    const int pf_v[] = { 0, 4, 8, 16 };
    for ( int pass = 0; pass < 2; ++pass )
    {
@@ -1138,7 +1142,7 @@ extern "C" int kinc_sim_autotune(kinc_sim_ctx* ctx, int64_t start, int64_t size,
       for ( int knob = 0; knob < 3; ++knob )
       {
          if ( knob == 0 && ctx->params.clus_method == 0 ) continue;   /* prefetch: the clustering sweeps only */
-         const int nv = knob == 0 ? 4 : knob == 1 ? 3 : 2;
+         const int nv = knob == 0 ? 4 : knob == 1 ? 5 : 2;
          const kinc_sim_launch base = best;
          for ( int v = 0; v < nv; ++v )
          {
@@ -1146,7 +1150,7 @@ extern "C" int kinc_sim_autotune(kinc_sim_ctx* ctx, int64_t start, int64_t size,
             if ( knob == 0 ) c.prefetch = pf_v[v];
             else if ( knob == 1 ) c.warps_per_cta = warps_v[v];
             else c.rounds = v;
-            if ( memcmp(&c, &base, sizeof c) == 0 || !launch_valid(c) ) continue;
+            if ( memcmp(&c, &base, sizeof c) == 0 || !launch_valid(c, ctx->kern.wpb) ) continue;
             double ms = 0;
             rc = time_launch(ctx, c, start, size, ms);
             if ( rc ) return rc;
@@ -1517,23 +1521,24 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    dp.gam_k = (KINC_STORE_GAMMA && params->clus_method == 1)
                  ? (params->max_clusters <= 3 ? 3 : params->max_clusters <= 5 ? 5 : 0) : 0;
    dp.ncorr = params->corr_method == 2 ? 2 : 1;
-   {
-      const kinc_sim_launch l = default_launch(params->clus_method);
-      dp.warps = l.warps_per_cta;
-      dp.rounds = l.rounds;
-      dp.prefetch = l.prefetch;
-   }
    const size_t sort_bytes_warp = (size_t)dp.sort_floats * sizeof(float);
    const SimKernel kern = params->clus_method == 0 ? sim_kernel_none()
                         : params->clus_method == 1 ? sim_kernel_gmm(params->max_clusters, params->rand_mode == 1)
                                                    : sim_kernel_kmeans(params->max_clusters);
+   const int wpb = kern.wpb;
+   {
+      const kinc_sim_launch l = default_launch(kern, params->clus_method);
+      dp.warps = l.warps_per_cta;
+      dp.rounds = l.rounds;
+      dp.prefetch = l.prefetch;
+   }
    const size_t param_bytes_warp = (KINC_GMM_PARAMS_SMEM && kern.clus == 1 && kern.ks > 0)
                                       ? (size_t)7 * kern.ks * TILE * sizeof(float) : 0;
    const KmPool km = km_pool_sizes(*params, kern);
    dp.km_dmax = km.dmax;
    dp.km_tmax = km.tmax;
-   const int smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * WARPS_PER_BLOCK <= 200 * 1024;
-   const int smem_bytes = (int)((smem_sort ? sort_bytes_warp : 0) + param_bytes_warp) * WARPS_PER_BLOCK;
+   const int smem_sort = need_sort && param_bytes_warp == 0 && sort_bytes_warp * wpb <= 200 * 1024;
+   const int smem_bytes = (int)((smem_sort ? sort_bytes_warp : 0) + param_bytes_warp) * wpb;
    if ( smem_bytes > 0 )
       CK(cudaFuncSetAttribute(kern.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes));
 
@@ -1564,11 +1569,11 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
                              + ((params->clus_method == 2 && KINC_KMEANS_LANE_MAJOR && kern.ks == 0)
                                    ? ((col * sizeof(float2) + 255) & ~(size_t)255) : 0)
                              + km.bytes;
-   if ( off >= NOALLOC_SCRATCH_BYTES || (NOALLOC_SCRATCH_BYTES - off) / slot_bytes < (size_t)WARPS_PER_BLOCK )
+   if ( off >= NOALLOC_SCRATCH_BYTES || (NOALLOC_SCRATCH_BYTES - off) / slot_bytes < (size_t)wpb )
       return fail(nullptr, KINC_SIM_EINVAL,
                   "%d genes x %d samples and %lld pairs do not fit the %zu-byte allocation-free scratch",
                   genes, samples, (long long)size, NOALLOC_SCRATCH_BYTES);
-   const size_t nslots = ((NOALLOC_SCRATCH_BYTES - off) / slot_bytes) / WARPS_PER_BLOCK * WARPS_PER_BLOCK;
+   const size_t nslots = ((NOALLOC_SCRATCH_BYTES - off) / slot_bytes) / wpb * wpb;
    unsigned char* base = nd.scratch;
    DevScratch ds {};
    {
@@ -1648,7 +1653,7 @@ extern "C" int kinc_sim_execute_block_noalloc(const float* d_gem, int32_t genes,
    B.tiles = d_tiles;
    B.status = d_status;
    B.work = d_work;
-   const int grid = (int)(nslots / WARPS_PER_BLOCK);
+   const int grid = (int)(nslots / wpb);
    cudaError_t e = kern.clus == 0 ? sim_launch_none(kern, grid, smem_bytes, st, dp, dd, ds, B, smem_sort)
                  : kern.clus == 1 ? sim_launch_gmm(kern, grid, smem_bytes, st, dp, dd, ds, B, smem_sort)
                                   : sim_launch_kmeans(kern, grid, smem_bytes, st, dp, dd, ds, B, smem_sort);

@@ -33,6 +33,26 @@ constexpr int WARPS_PER_BLOCK = KINC_WARPS_PER_BLOCK;
 #ifndef KINC_MIN_BLOCKS
 #define KINC_MIN_BLOCKS (16 / KINC_WARPS_PER_BLOCK)
 #endif
+/* GMM takes 20-warp CTAs: at 96 registers (spilling a few hundred bytes to L1) the fits' fixed-
+ * latency chains hide behind 25 % more warps, which beats 16 warps at 128 registers by 16 % */
+#ifndef KINC_GMM_WARPS_PER_BLOCK
+#define KINC_GMM_WARPS_PER_BLOCK 20
+#endif
+
+/* warps per CTA at most for clustering method CLUS (3: GMM in the OpenCL worker's form); the
+ * kernel's register budget follows from it, and the host sizes grids and scratch slots by it */
+template <int CLUS>
+__host__ __device__ constexpr int kernel_warps()
+{
+   return (CLUS == 1 || CLUS == 3) ? KINC_GMM_WARPS_PER_BLOCK : WARPS_PER_BLOCK;
+}
+
+template <int CLUS>
+__host__ __device__ constexpr int kernel_min_blocks()
+{
+   return (CLUS == 1 || CLUS == 3) ? (KINC_GMM_WARPS_PER_BLOCK <= 16 ? 16 / KINC_GMM_WARPS_PER_BLOCK : 1)
+                                   : KINC_MIN_BLOCKS;
+}
 
 /* What the reference left in its packed array at position i by pair c: the
  * i-th usable sample (0-based) of c.  Reads come with increasing i for the
@@ -247,14 +267,14 @@ __device__ int lane_cluster(const DevParams& P, const DevData& D, const float2* 
 namespace kinc {
 
 template <int CLUS, int KS>
-__global__ void __launch_bounds__(WARPS_PER_BLOCK * 32, KINC_MIN_BLOCKS)
+__global__ void __launch_bounds__(kernel_warps<CLUS>() * 32, kernel_min_blocks<CLUS>())
 k_similarity(DevParams P, DevData D, DevScratch W, DevBlock B, int smem_sort)
 {
    constexpr int CM = CLUS == 3 ? 1 : CLUS;    /* the clustering method (3: GMM, OpenCL worker's form) */
    extern __shared__ float smem[];
    const int lane = threadIdx.x & 31;
    const int warp = threadIdx.x >> 5;
-   const int nwarps = blockDim.x >> 5;          /* warps per CTA: a launch-shape choice, up to WARPS_PER_BLOCK */
+   const int nwarps = blockDim.x >> 5;          /* warps per CTA: a launch-shape choice, up to kernel_warps<CLUS>() */
    const int64_t slot = blockIdx.x * (int64_t)nwarps + warp;
    const size_t col = (size_t)P.S * TILE;
 
@@ -450,16 +470,17 @@ struct SimKernel
    int clus;
    int ks;
    bool ocl;
+   int wpb;                                     /* warps per CTA at most (kernel_warps) */
 };
 
 template <int CLUS, int KS>
 inline SimKernel sim_kernel_handle()
 {
-   return SimKernel { (const void*)&k_similarity<CLUS, KS>, CLUS == 3 ? 1 : CLUS, KS, CLUS == 3 };
+   return SimKernel { (const void*)&k_similarity<CLUS, KS>, CLUS == 3 ? 1 : CLUS, KS, CLUS == 3, kernel_warps<CLUS>() };
 }
 
-/* launch with P.warps warps per CTA (the host keeps it in 1..WARPS_PER_BLOCK and sizes grid, smem
- * and the scratch slots for it) */
+/* launch with P.warps warps per CTA (the host keeps it in 1..kernel_warps<CLUS>() and sizes grid,
+ * smem and the scratch slots for it) */
 template <int CLUS, int KS>
 inline cudaError_t sim_kernel_launch(int grid, int smem, cudaStream_t st, const DevParams& P, const DevData& D,
                                      const DevScratch& W, const DevBlock& B, int smem_sort)

@@ -8,7 +8,9 @@ from kinc_gb300 import Similarity, _native, synthetic
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(16, 1, 8), (8, 1, 0), (4, 0, 16), (16, 0, 4)]
+# warps per CTA divide the kernel's warp count: 20 for GMM, 16 otherwise
+SHAPES = {"gmm": [(20, 1, 8), (10, 1, 0), (4, 0, 16), (20, 0, 4)],
+          "kmeans": [(16, 1, 8), (8, 1, 0), (4, 0, 16), (16, 0, 4)]}
 
 
 @pytest.mark.parametrize("args", [dict(clusmethod="gmm", corrmethod="spearman", crit="BIC", preout=True,
@@ -21,7 +23,7 @@ def test_every_launch_shape_gives_the_same_bits(args):
     sim.initialize()
     total = sim.total_pairs()
     want = None
-    for w, r, p in SHAPES:
+    for w, r, p in SHAPES[args["clusmethod"]]:
         sim.set_launch(w, r, p)
         assert sim.launch() == {"warps_per_cta": w, "rounds": r, "prefetch": p}
         res = sim.execute(None, start=0, size=total)
@@ -40,6 +42,8 @@ def test_launch_shape_rejects_unsupported_values():
     sim.initialize()
     with pytest.raises(_native.SimError):
         sim.set_launch(5, 1, 8)
+    with pytest.raises(_native.SimError):
+        sim.set_launch(16, 1, 8)       # does not divide GMM's 20 warps
     with pytest.raises(_native.SimError):
         sim.set_launch(16, 2, 8)
     sim.close()

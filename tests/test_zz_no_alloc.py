@@ -77,8 +77,8 @@ def test_noalloc_rejects_sizes_beyond_its_limit():
 
 
 def test_noalloc_rejects_work_that_does_not_fit_its_array():
-    """GMM k <= 5 at 4,096 samples needs about 4.7 MB of working space per warp: one 16-warp block
-    no longer fits the 64 MiB array, so the call is refused before anything runs."""
+    """GMM k <= 5 at 4,096 samples needs about 4.7 MB of working space per warp: one block of the GMM
+    kernel's 20 warps no longer fits the 64 MiB array, so the call is refused before anything runs."""
     import torch
     gem = synthetic.generate(2, genes=40, samples=4096)
     params = Similarity(gem, clusmethod="gmm", corrmethod="spearman", maxclus=5).params
