@@ -101,6 +101,8 @@ def tune_grid(sim, args):
     import torch
     L = _native.load()
     vp = ctypes.c_void_p
+    wpb = sim.launch()["warps_per_cta"]             # the default shape: the kernel's full warp count
+    warps = [w for w in (4, 8, 10, 16, 20) if w <= wpb and wpb % w == 0]
     t0 = time.perf_counter()
     chosen, cands = sim.autotune(use_cache=False)
     tune_s = time.perf_counter() - t0
@@ -114,7 +116,7 @@ def tune_grid(sim, args):
     dC = torch.empty((size, sim.params.max_clusters * nc), dtype=torch.float32, device="cuda")
     stream = torch.cuda.Stream()
     grid = {}
-    for w in (4, 8, 16):
+    for w in warps:
         for r in (0, 1):
             for pf in (0, 4, 8, 16):
                 sim.set_launch(w, r, pf)
