@@ -220,8 +220,8 @@ int kinc_sim_set_launch(kinc_sim_ctx* ctx, const kinc_sim_launch* launch);
  * Pick the launch shape by timing: the pairs [start, start + size) (size is
  * capped at kinc_sim_max_device_block) run once per candidate on the context's
  * stream, timed with CUDA events, in a coordinate descent from the current
- * shape over prefetch (clustering only), warps_per_cta and rounds; the fastest is
- * applied.  With use_cache, the shape is first looked up -- and afterwards
+ * shape over prefetch (clustering only), warps_per_cta and rounds (not for GMM,
+ * which keeps the current shape's rounds); the fastest is applied.  With use_cache, the shape is first looked up -- and afterwards
  * stored -- in a small text cache keyed by the clustering and correlation
  * arguments, max_clusters, the sample count rounded up to a power of two and
  * the GPU (file: $KINC_TUNE_CACHE, else $XDG_CACHE_HOME/kinc_gb300/launch.txt,

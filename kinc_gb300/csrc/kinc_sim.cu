@@ -1142,6 +1142,11 @@ extern "C" int kinc_sim_autotune(kinc_sim_ctx* ctx, int64_t start, int64_t size,
       for ( int knob = 0; knob < 3; ++knob )
       {
          if ( knob == 0 && ctx->params.clus_method == 0 ) continue;   /* prefetch: the clustering sweeps only */
+         /* GMM keeps its CTA rounds: free-running warps drift into different fits as a launch grows
+          * longer than the timed sample, and their instructions then evict each other (a pick of
+          * 20 free-running warps from a 311,296-pair sample ran 1,048,576-pair blocks at 96k
+          * pairs/s against 164k in rounds) */
+         if ( knob == 2 && ctx->params.clus_method == 1 ) continue;
          const int nv = knob == 0 ? 4 : knob == 1 ? 5 : 2;
          const kinc_sim_launch base = best;
          for ( int v = 0; v < nv; ++v )
