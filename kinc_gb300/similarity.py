@@ -183,8 +183,9 @@ class Similarity:
 
     def autotune(self, start=None, size=None, use_cache=True, cap=64):
         """Pick the launch shape by timing candidates on pairs [start, start+size)
-        (kinc_sim_autotune; default: the middle of the pairs, 4 x 32 pairs per resident warp of
-        the GPU, at most one device block).  Returns (chosen shape, timed candidates)."""
+        (kinc_sim_autotune; default: 311,296 pairs from the middle -- 4 tiles of 32 pairs for each
+        warp of 16-warp CTAs on 152 SMs -- at most one device block).  Returns (chosen shape, timed
+        candidates)."""
         if self._ctx is None:
             self.initialize()
         L = _native.load()
